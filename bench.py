@@ -1,0 +1,354 @@
+"""Benchmark of the GB300 per-substep cloth step (vertex-substeps/s).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+One step = one frame = ClothSolverBase::SimulateSwift (num_substeps substeps) over the whole
+garment; the default workload is the garment-scale plain step: a 256x256 cloth (65,536 vertices)
+on the animated 6,890-vertex tube body, 20 substeps x 15 iterations, stretch + bend + LRA,
+obstacle and particle self contact.  Inputs are synthetic and seeded (xrtailor_gb300/scenes.py).
+
+Output: one JSON line (rank 0).  `value` times K frames with CUDA events on the library's stream,
+inputs resident in HBM, L2 flushed (a 512 MiB write) between frames outside the timed events;
+`e2e` times K frames through the public C ABI with host buffers (obstacle targets in, cloth
+positions out, per frame) by wall clock; `roofline` is the dominant phase's algorithmic bytes per
+launch over its CUDA-event launch time (a profiled pass after the timed region);
+`cpu_baseline` is the oracle (OpenMP CPU restatement) on the host cores on a bounded sample.
+`--impl reference` times that CPU restatement alone: the reference's own path is CUDA-only and
+cannot be built here (no glm / vcglib / GLFW sources), so the oracle port stands in for it.
+Several GPUs (torchrun) run independent replicas (the plain step does not shard).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK = 6800.0
+METRIC = "vertex-substeps/s"
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK, "fallback"
+
+
+def _workload(name):
+    from xrtailor_gb300 import scenes
+    if name == "garment":
+        return scenes.plain_garment(256)
+    if name == "small":
+        return scenes.plain_small(64)
+    if name == "heavy":
+        return scenes.plain_heavy(1024)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def _setup(solver, sc):
+    solver.add_cloth(sc.cloth, particle_diameter=sc.particle_diameter)
+    if sc.obstacle is not None:
+        solver.add_obstacle(sc.obstacle)
+    solver.start()
+
+
+def _targets(sc, frames):
+    if sc.body is None:
+        return None
+    return [sc.body.pose((f + 1) / 60.0) for f in range(frames)]
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def bytes_per_substep(s, p, has_obstacle):
+    """Algorithmic bytes of one substep (fp32, vec3 = 12 B, index = 4 B):
+    V*52 + I*[V*28 + E*24 + B*24 + L*12 + Nb*72 + C_solve] + P*C_gen, with
+    C_solve = V*32 + E*48 + V*32 and C_gen = V*24 + V*32 + E*48 per collision pass."""
+    V, E, B, L, Nb = s.num_vertices, s.num_edges, s.num_bends, s.num_lra, s.num_bindings
+    I = p.num_iterations
+    c_solve = (V * 32 + E * 48 + V * 32) if has_obstacle else 0
+    c_gen = (V * 24 + V * 32 + E * 48) if has_obstacle else 0
+    passes = p.num_collision_passes / p.num_substeps
+    return V * 52 + I * (V * 28 + E * 24 + B * 24 + L * 12 + Nb * 72 + c_solve) + passes * c_gen
+
+
+# Algorithmic bytes per processed unit of each phase's launch: records read + vertices read and
+# written (float4 = 16 B).  stretch: 16 B record + 8 B lambda r/w + 2 x 32 B vertex r/w;
+# bend: 16 B indices + 8 B (angle, compliance) + 4 x 32 B; collide: x, x0 read + x write (48 B);
+# vf_solve: x r/w + two contact records (32 B + 16 B) ; ee_apply: x read + write (32 B) + the
+# vertex's edge list entries are data dependent and not counted.
+BYTES_PER_UNIT = {"stretch": 88, "bend": 152, "collide": 48, "vf_solve": 64, "ee_apply": 32,
+                  "predict_finalize": 64, "lra": 32}
+
+
+def run_ours(args, rank, local_rank, world):
+    import torch
+    from xrtailor_gb300 import ClothSolver, build as xb, scenes
+    xb.build()
+    torch.cuda.set_device(local_rank)
+    sc = _workload(args.workload)
+    p = scenes.scene_params(sc)
+    solver = ClothSolver(p, device=local_rank)
+    _setup(solver, sc)
+    s = solver.sizes()
+    V, S = s.num_vertices, p.num_substeps
+    frames_needed = args.warmup + 2 * args.steps + 8
+    tg = _targets(sc, frames_needed)
+    dev_targets = None
+    if tg is not None:
+        dev_targets = torch.tensor(np.stack(tg), device=f"cuda:{local_rank}")
+        torch.cuda.synchronize()
+    _, _, stream_ptr = solver.device_state()
+    stream = torch.cuda.ExternalStream(stream_ptr, device=f"cuda:{local_rank}")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
+    lib = solver._lib
+    fi = 0
+
+    def set_targets_dev(k):
+        if dev_targets is not None:
+            lib.xrt_set_obstacle_targets_device(solver._h, dev_targets[k].data_ptr())
+
+    for _ in range(args.warmup):
+        set_targets_dev(fi)
+        solver.step()
+        fi += 1
+    solver.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        wall0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                set_targets_dev(fi)
+                fi += 1
+                starts[k].record(stream)
+                solver.step()
+                ends[k].record(stream)
+                flush.zero_()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    solver.synchronize()
+    frame_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    t_dev = sum(frame_ms) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_dev], device=f"cuda:{local_rank}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        t_dev = float(tt.item())
+    units = V * S * args.steps * world
+    value = units / t_dev
+
+    # end to end through the C ABI with host buffers
+    host_targets = tg
+    out = np.empty((V, 3), np.float32)
+    h2d = (host_targets[0].nbytes if host_targets is not None else 0)
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for k in range(args.steps):
+        if host_targets is not None:
+            solver.set_obstacle_targets(host_targets[fi % len(host_targets)])
+        fi += 1
+        solver.step()
+        out = solver.host_positions()
+    e2e_t = time.perf_counter() - e0
+    e2e = V * S * args.steps / e2e_t
+
+    # per-phase profile (eager frames with CUDA events around every launch)
+    solver.set_profiling(True)
+    for _ in range(3):
+        set_targets_dev(fi % frames_needed)
+        fi += 1
+        solver.step()
+    prof = solver.profile()
+    solver.set_profiling(False)
+    phases = {k: v for k, v in prof.items() if k != "frames"}
+    total_ms = sum(v["ms"] for v in phases.values())
+    dom = max((k for k in phases if k in BYTES_PER_UNIT), key=lambda k: phases[k]["ms"])
+    d = phases[dom]
+    peak, peak_src = _peaks()
+    per_launch_bytes = BYTES_PER_UNIT[dom] * d["units"] / max(d["launches"], 1)
+    per_launch_s = d["ms"] / 1e3 / max(d["launches"], 1)
+    achieved = per_launch_bytes / per_launch_s / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            tr = json.load(open(tpath)).get(args.workload, {}).get(dom)
+            if tr:
+                traffic = tr["bytes_per_unit"] * d["units"] / max(d["launches"], 1)
+        except Exception:
+            traffic = None
+    frame_bytes = bytes_per_substep(s, p, sc.obstacle is not None) * S
+    result = {
+        "metric": METRIC, "value": value, "unit": "vertex-substeps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene generators, xrtailor_gb300/scenes.py)",
+        "config": {"workload": f"plain_{args.workload}", "vertices": V, "edges": s.num_edges,
+                   "bends": s.num_bends, "lra": s.num_lra,
+                   "obstacle_triangles": s.num_obstacle_triangles, "substeps": S,
+                   "iterations": p.num_iterations, "collision_passes": p.num_collision_passes,
+                   "self_collision": bool(p.enable_self_collision),
+                   "stretch_colors": s.num_stretch_colors, "bend_colors": s.num_bend_colors,
+                   "l2": "flushed between frames (512 MiB write, outside the timed events)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": e2e, "unit": "vertex-substeps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": int(out.nbytes)},
+        "gpu_launches": int(s.launches_per_frame) * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_src, "bytes_per_launch": per_launch_bytes,
+                     "us_per_launch": per_launch_s * 1e6,
+                     "share_of_frame": d["ms"] / total_ms if total_ms else None},
+        "frame_bandwidth_gbs": frame_bytes / (t_dev / args.steps / world) / 1e9,
+        "phase_ms_per_frame": {k: round(v["ms"] / max(prof["frames"], 1), 4) for k, v in phases.items()},
+        "clocks": clocks.summary(),
+        "wall_s": wall,
+    }
+    return result
+
+
+def run_cpu(workload, frames, warmup=1, threads=0):
+    from oracle.oracle import OracleSolver, lib
+    from xrtailor_gb300 import scenes
+    sc = _workload(workload)
+    p = scenes.scene_params(sc)
+    o = OracleSolver(p, threads=threads)
+    _setup(o, sc)
+    tg = _targets(sc, warmup + frames)
+    V = o.sizes()["num_vertices"]
+    fi = 0
+    for _ in range(warmup):
+        if tg is not None:
+            o.set_obstacle_targets(tg[fi])
+        fi += 1
+        o.step()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        if tg is not None:
+            o.set_obstacle_targets(tg[fi])
+        fi += 1
+        o.step()
+    t = time.perf_counter() - t0
+    return V * p.num_substeps * frames / t, lib().orc_num_threads(), t
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="garment", choices=["garment", "small", "heavy"])
+    ap.add_argument("--cpu-frames", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        frames = max(args.steps, 1)
+        value, cores, t = run_cpu(args.workload, frames, warmup=min(args.warmup, 1))
+        line = {"metric": METRIC, "value": value, "unit": "vertex-substeps/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / frames,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded scene generators, xrtailor_gb300/scenes.py)",
+                "config": {"workload": f"plain_{args.workload}"}, "impl": "reference",
+                "cpu_baseline": {"value": value, "unit": "vertex-substeps/s", "cores": cores,
+                                 "kind": "port",
+                                 "sample": f"{frames} full frames of plain_{args.workload}"},
+                "e2e": {"value": value, "unit": "vertex-substeps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    res = run_ours(args, rank, local_rank, world)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, t = run_cpu(args.workload, args.cpu_frames)
+        res["cpu_baseline"] = {"value": v, "unit": "vertex-substeps/s", "cores": cores,
+                               "kind": "port",
+                               "sample": f"{args.cpu_frames} frames of plain_{args.workload} "
+                                         f"({t:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(res))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,319 @@
+"""TEST INFRASTRUCTURE — ctypes front end of the CPU oracle (oracle/_build/liboracle.so).
+
+The oracle restates the reference's Swift-mode frame on the CPU (see oracle_step.cpp for the
+file:line of every restated function).  Only tests/, the smoke check and bench.py's CPU-baseline
+leg may use it, and only as the checker; the product (libxrt.so) never links or calls it.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from oracle import build as _build  # noqa: E402
+from xrtailor_gb300 import _lib as L  # noqa: E402  (struct layouts of include/xrt.h only)
+from xrtailor_gb300.solver import cloth_desc, obstacle_desc  # noqa: E402
+
+_lib = None
+FP, UP, IP, P = C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.POINTER(C.c_int32), C.c_void_p
+
+_SIG = {
+    "orc_create": (P, []), "orc_destroy": (None, [P]), "orc_num_threads": (C.c_int, []),
+    "orc_set_threads": (None, [C.c_int]),
+    "orc_set_params": (None, [P, C.POINTER(L.SwiftParams)]),
+    "orc_add_cloth": (C.c_int, [P, C.POINTER(L.ClothDesc)]),
+    "orc_add_obstacle": (C.c_int, [P, C.POINTER(L.ObstacleDesc)]),
+    "orc_set_coloring": (None, [P, C.c_int, UP, C.c_uint32]),
+    "orc_set_compliance": (None, [P, C.c_int, FP, C.c_uint32]),
+    "orc_set_inv_mass": (None, [P, FP, C.c_uint32]),
+    "orc_start": (None, [P]), "orc_set_obstacle_targets": (None, [P, FP]),
+    "orc_step_frame": (None, [P]), "orc_get_sizes": (None, [P, UP]),
+    "orc_get_positions": (None, [P, FP]), "orc_get_velocities": (None, [P, FP]),
+    "orc_get_normals": (None, [P, FP]), "orc_get_obstacle_positions": (None, [P, FP]),
+    "orc_particle_diameter": (C.c_float, [P]),
+    "orc_get_edges": (None, [P, UP, FP]), "orc_get_bends": (None, [P, UP, FP]),
+    "orc_get_coloring": (None, [P, C.c_int, UP]), "orc_coloring_valid": (C.c_int, [P, C.c_int]),
+    "orc_get_lra": (None, [P, UP, UP, FP]), "orc_get_rtri": (None, [P, UP]),
+    "orc_export_obstacle_bvh": (None, [P, UP, UP, UP, FP, IP, IP]),
+    "orc_export_contacts": (None, [P, IP, FP, IP, FP, FP]),
+    "orc_export_neighbors": (None, [P, UP]), "orc_hash_now": (None, [P]),
+    "orc_lbvh_create": (P, []), "orc_lbvh_destroy": (None, [P]),
+    "orc_lbvh_build": (None, [P, FP, FP, C.c_uint32, C.c_float]),
+    "orc_lbvh_refit": (None, [P, FP, C.c_uint32]),
+    "orc_lbvh_export": (None, [P, UP, UP, UP, FP, IP, IP, IP]),
+    "orc_lbvh_query": (None, [P, C.c_int, FP, C.c_uint32, UP, UP]),
+    "orc_expand_bits": (C.c_uint32, [C.c_uint32]), "orc_morton_code": (C.c_uint32, [FP]),
+    "orc_nearest_point": (C.c_float, [FP, FP, FP, FP]),
+    "orc_ray_intersect": (C.c_float, [FP, FP, C.c_float, FP]),
+    "orc_closest_seg_seg": (C.c_float, [FP, FP, FP, FP, FP, FP]),
+    "orc_solve_cubic": (C.c_int, [C.c_float, C.c_float, C.c_float, C.c_float, FP]),
+}
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        h = C.CDLL(path)
+        for k, (r, a) in _SIG.items():
+            f = getattr(h, k)
+            f.restype = r
+            f.argtypes = a
+        _lib = h
+    return _lib
+
+
+def _f(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _u(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+class OracleSolver:
+    """CPU restatement with the same calls as xrtailor_gb300.ClothSolver."""
+
+    def __init__(self, params: L.SwiftParams, threads: int = 0):
+        self._l = lib()
+        if threads:
+            self._l.orc_set_threads(int(threads))
+        self._h = self._l.orc_create()
+        self.params = params
+        self._l.orc_set_params(self._h, C.byref(params))
+
+    def add_cloth(self, mesh, model_matrix=None, particle_diameter=0.0):
+        d, keep = cloth_desc(mesh, model_matrix, particle_diameter)
+        r = self._l.orc_add_cloth(self._h, C.byref(d))
+        del keep
+        return r
+
+    def add_obstacle(self, mesh, model_matrix=None):
+        d, keep = obstacle_desc(mesh, model_matrix)
+        r = self._l.orc_add_obstacle(self._h, C.byref(d))
+        del keep
+        return r
+
+    def set_coloring(self, kind, colors):
+        c = _u(colors)
+        self._l.orc_set_coloring(self._h, kind, c.ctypes.data_as(UP), c.size)
+
+    def set_compliance(self, kind, values):
+        v = _f(values)
+        self._l.orc_set_compliance(self._h, kind, v.ctypes.data_as(FP), v.size)
+
+    def set_inv_mass(self, w):
+        v = _f(w)
+        self._l.orc_set_inv_mass(self._h, v.ctypes.data_as(FP), v.size)
+
+    def start(self):
+        self._l.orc_start(self._h)
+
+    def set_obstacle_targets(self, pos):
+        p = _f(pos).reshape(-1)
+        self._l.orc_set_obstacle_targets(self._h, p.ctypes.data_as(FP))
+
+    def step(self, frames=1):
+        for _ in range(frames):
+            self._l.orc_step_frame(self._h)
+
+    fixed_update = step
+
+    def sizes(self):
+        s = np.zeros(8, np.uint32)
+        self._l.orc_get_sizes(self._h, s.ctypes.data_as(UP))
+        return dict(num_vertices=int(s[0]), num_edges=int(s[1]), num_triangles=int(s[2]),
+                    num_bends=int(s[3]), num_lra=int(s[4]), num_obstacle_vertices=int(s[5]),
+                    num_obstacle_triangles=int(s[6]), num_stretch_colors=int(s[7] & 0xFFFF),
+                    num_bend_colors=int(s[7] >> 16))
+
+    def _read(self, fn, n):
+        out = np.empty((n, 3), np.float32)
+        fn(self._h, out.ctypes.data_as(FP))
+        return out
+
+    def host_positions(self):
+        return self._read(self._l.orc_get_positions, self.sizes()["num_vertices"])
+
+    def host_velocities(self):
+        return self._read(self._l.orc_get_velocities, self.sizes()["num_vertices"])
+
+    def host_normals(self):
+        return self._read(self._l.orc_get_normals, self.sizes()["num_vertices"])
+
+    def obstacle_positions(self):
+        return self._read(self._l.orc_get_obstacle_positions, self.sizes()["num_obstacle_vertices"])
+
+    def particle_diameter(self):
+        return self._l.orc_particle_diameter(self._h)
+
+    def edges(self):
+        n = self.sizes()["num_edges"]
+        e, r = np.empty((n, 2), np.uint32), np.empty(n, np.float32)
+        self._l.orc_get_edges(self._h, e.ctypes.data_as(UP), r.ctypes.data_as(FP))
+        return e, r
+
+    def bends(self):
+        n = self.sizes()["num_bends"]
+        b, t = np.empty((n, 4), np.uint32), np.empty(n, np.float32)
+        self._l.orc_get_bends(self._h, b.ctypes.data_as(UP), t.ctypes.data_as(FP))
+        return b, t
+
+    def coloring(self, kind):
+        s = self.sizes()
+        n = s["num_edges"] if kind == 0 else s["num_bends"]
+        c = np.empty(n, np.uint32)
+        self._l.orc_get_coloring(self._h, kind, c.ctypes.data_as(UP))
+        return c
+
+    def coloring_valid(self, kind):
+        return bool(self._l.orc_coloring_valid(self._h, kind))
+
+    def lra(self):
+        n = self.sizes()["num_lra"]
+        s, t, r = np.empty(n, np.uint32), np.empty(n, np.uint32), np.empty(n, np.float32)
+        self._l.orc_get_lra(self._h, s.ctypes.data_as(UP), t.ctypes.data_as(UP), r.ctypes.data_as(FP))
+        return s, t, r
+
+    def obstacle_rtri(self):
+        m = np.empty(self.sizes()["num_obstacle_triangles"], np.uint32)
+        self._l.orc_get_rtri(self._h, m.ctypes.data_as(UP))
+        return m
+
+    def export_obstacle_bvh(self):
+        n = self.sizes()["num_obstacle_triangles"]
+        nn = 2 * n - 1
+        out = dict(morton=np.empty(n, np.uint32), objects=np.empty(n, np.uint32),
+                   nodes=np.empty((nn, 4), np.uint32), aabbs=np.empty((nn, 6), np.float32),
+                   iesc=np.empty(max(n - 1, 1), np.int32), eesc=np.empty(n, np.int32))
+        self._l.orc_export_obstacle_bvh(self._h, out["morton"].ctypes.data_as(UP),
+                                        out["objects"].ctypes.data_as(UP),
+                                        out["nodes"].ctypes.data_as(UP),
+                                        out["aabbs"].ctypes.data_as(FP),
+                                        out["iesc"].ctypes.data_as(IP),
+                                        out["eesc"].ctypes.data_as(IP))
+        out["iesc"] = out["iesc"][: max(n - 1, 0)]
+        return out
+
+    def export_contacts(self):
+        s = self.sizes()
+        nv, ne = s["num_vertices"], s["num_edges"]
+        out = dict(vf_index=np.empty(nv, np.int32), vf_qs=np.empty((nv, 3), np.float32),
+                   rt_index=np.empty(nv, np.int32), rt_qc=np.empty((nv, 3), np.float32),
+                   ee=np.empty((ne, 12), np.float32))
+        self._l.orc_export_contacts(self._h, out["vf_index"].ctypes.data_as(IP),
+                                    out["vf_qs"].ctypes.data_as(FP),
+                                    out["rt_index"].ctypes.data_as(IP),
+                                    out["rt_qc"].ctypes.data_as(FP), out["ee"].ctypes.data_as(FP))
+        return out
+
+    def export_neighbors(self):
+        nv = self.sizes()["num_vertices"]
+        out = np.empty(nv * self.params.max_neighbor_size, np.uint32)
+        self._l.orc_export_neighbors(self._h, out.ctypes.data_as(UP))
+        return out
+
+    def close(self):
+        if self._h:
+            self._l.orc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class OracleLbvh:
+    def __init__(self):
+        self._l = lib()
+        self._h = self._l.orc_lbvh_create()
+        self.n = 0
+
+    def build(self, prims, pred=None, scr=0.0):
+        a = _f(prims).reshape(-1)
+        b = None if pred is None else _f(pred).reshape(-1)
+        self.n = a.size // 9
+        self._l.orc_lbvh_build(self._h, a.ctypes.data_as(FP),
+                               None if b is None else b.ctypes.data_as(FP), self.n, float(scr))
+
+    def refit(self, pred):
+        b = _f(pred).reshape(-1)
+        self._l.orc_lbvh_refit(self._h, b.ctypes.data_as(FP), self.n)
+
+    def export(self):
+        n = self.n
+        nn = 2 * n - 1
+        out = dict(morton=np.empty(n, np.uint32), objects=np.empty(n, np.uint32),
+                   nodes=np.empty((nn, 4), np.uint32), aabbs=np.empty((nn, 6), np.float32),
+                   iesc=np.empty(max(n - 1, 1), np.int32), eesc=np.empty(n, np.int32))
+        u = C.c_int32()
+        self._l.orc_lbvh_export(self._h, out["morton"].ctypes.data_as(UP),
+                                out["objects"].ctypes.data_as(UP), out["nodes"].ctypes.data_as(UP),
+                                out["aabbs"].ctypes.data_as(FP), out["iesc"].ctypes.data_as(IP),
+                                out["eesc"].ctypes.data_as(IP), C.byref(u))
+        out["iesc"] = out["iesc"][: max(n - 1, 0)]
+        out["unique"] = bool(u.value)
+        return out
+
+    def query(self, kind, q):
+        qa = _f(q).reshape(-1)
+        nq = qa.size // (3 if kind == 0 else 6)
+        counts = np.empty(nq, np.uint32)
+        cands = np.empty((nq, 256), np.uint32)
+        self._l.orc_lbvh_query(self._h, kind, qa.ctypes.data_as(FP), nq, counts.ctypes.data_as(UP),
+                               cands.ctypes.data_as(UP))
+        return counts, cands
+
+    def close(self):
+        if self._h:
+            self._l.orc_lbvh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---- primitive KATs ---------------------------------------------------------------------------
+def expand_bits(v):
+    return int(lib().orc_expand_bits(int(v)))
+
+
+def morton_code(p):
+    a = _f(p)
+    return int(lib().orc_morton_code(a.ctypes.data_as(FP)))
+
+
+def nearest_point(p, tri):
+    p, t = _f(p), _f(tri).reshape(-1)
+    qs, uvw = np.empty(3, np.float32), np.empty(3, np.float32)
+    d = lib().orc_nearest_point(p.ctypes.data_as(FP), t.ctypes.data_as(FP), qs.ctypes.data_as(FP),
+                                uvw.ctypes.data_as(FP))
+    return np.float32(d), qs, uvw
+
+
+def ray_intersect(o, d, length, tri):
+    o, d, t = _f(o), _f(d), _f(tri).reshape(-1)
+    return np.float32(lib().orc_ray_intersect(o.ctypes.data_as(FP), d.ctypes.data_as(FP),
+                                              float(length), t.ctypes.data_as(FP)))
+
+
+def closest_seg_seg(p1, q1, p2, q2):
+    a = [_f(v) for v in (p1, q1, p2, q2)]
+    st, cc = np.empty(2, np.float32), np.empty(6, np.float32)
+    d = lib().orc_closest_seg_seg(*[v.ctypes.data_as(FP) for v in a], st.ctypes.data_as(FP),
+                                  cc.ctypes.data_as(FP))
+    return np.float32(d), st, cc
+
+
+def solve_cubic(a, b, c, d):
+    x = np.zeros(3, np.float32)
+    n = lib().orc_solve_cubic(float(a), float(b), float(c), float(d), x.ctypes.data_as(FP))
+    return int(n), x[:n]

@@ -1,0 +1,1176 @@
+// oracle_step.cpp — TEST INFRASTRUCTURE ONLY: CPU restatement (C++17 + OpenMP) of the
+// reference's Swift-mode cloth frame.  It is the checker for the CUDA library and the timed CPU
+// baseline; nothing in the product links or calls it.  Every function names the reference
+// file:line it restates.  Loops that the reference runs as one GPU thread per element are
+// OpenMP-parallel only where the elements write disjoint data; scatter loops (float atomics in
+// the reference) run sequentially in element order, which is the order the CUDA library's
+// gathers reproduce.
+//
+// Frame:              ClothSolverBase::SimulateSwift          src/pipeline/base/ClothSolverBase.cpp:171-261
+// predict/finalize:   PredictPositions_Kernel / Finalize_Kernel src/physics/ClothSolverHelper.cu:125-236
+// stretch/bend:       SolveStretch_Kernel / SolveBend_Kernel   src/physics/dynamics/BasicSolverHelper.cu:8-138
+// LRA:                SolveGeodesicLRA_Kernel                   src/physics/dynamics/LongRangeAttachments.cu:5-26
+// binding:            GenerateBinding_Kernel/SolveBinding_Kernel src/physics/dynamics/BindingConstraint.cu:20-99
+// obstacle contacts:  Generate*/Solve* kernels                  src/physics/pbd_collision/PBDCollision.cu:17-298
+// particle contacts:  SpatialHashGPU + CollideParticles         src/physics/broad_phase/spatial_hash/SpatialHashGPU.cu:9-198,
+//                                                               src/physics/ClothSolverHelper.cu:139-219
+// normals/interp:     PhysicsMeshHelper.cu:196-310, PhysicsMesh.cu:604-620
+// setup:              ClothSolverHelper.cpp:4-109, Geodesic.cpp:6-79, RTriangle.cu:19-84,
+//                     universal/ClothSolver.cpp:46-350, PhysicsMeshHelper.cu:131-150
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <queue>
+#include <set>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/xrt.h"
+#include "oracle_lbvh.h"
+
+using namespace orc;
+
+namespace {
+
+struct EEContact {
+  float dist;
+  V3 p2, q2;
+  float s, t;
+  V3 fn;
+};
+
+struct Binding {
+  uint32_t cloth;
+  float u, v, w;
+  uint32_t iu, iv, iw;
+  float L, stiffness;
+};
+
+struct Cloth {
+  std::vector<V3> mesh_pos;
+  std::vector<uint32_t> tri;  // local indices
+  std::vector<uint32_t> fixed, attached;
+  uint32_t offset = 0;
+};
+
+struct Oracle {
+  xrt_swift_params p{};
+  // cloth state
+  std::vector<V3> x0, x, v, n, x_init;
+  std::vector<float> w;
+  std::vector<uint32_t> tri;
+  std::vector<Cloth> cloths;
+  std::vector<uint32_t> edges;  // 2E, global indices
+  std::vector<float> rest, s_comp, s_lambda;
+  std::vector<uint32_t> s_color;
+  std::vector<uint32_t> bends;  // 4B
+  std::vector<float> theta, b_comp;
+  std::vector<uint32_t> b_color;
+  uint32_t n_s_colors = 0, n_b_colors = 0;
+  std::vector<uint32_t> lra_src, lra_tgt;
+  std::vector<float> lra_rest;
+  std::vector<Binding> bindings;
+  std::vector<uint32_t> vf_prefix, vf_list;  // cloth vertex -> faces (ascending)
+  float particle_diameter = 0.0f;
+  // obstacle
+  std::vector<V3> ox0, ox, ox1, on, on1;
+  std::vector<uint32_t> otri, ortri, ovf_prefix, ovf_list;
+  Lbvh bvh;
+  // contacts
+  std::vector<int32_t> vf_idx, rt_idx;
+  std::vector<V3> vf_qs, rt_qc;
+  std::vector<EEContact> ee;
+  std::vector<V3> deltas;
+  std::vector<int32_t> delta_counts;
+  // particle hash
+  std::vector<uint32_t> neighbors;
+  std::vector<uint32_t> cell_start, cell_end;
+  bool started = false;
+  uint32_t frame_index = 0;
+  std::vector<uint32_t> pending_colors[2];
+};
+
+// ---------------------------------------------------------------------------------------------
+// setup
+
+// Edge list (our order): first appearance scanning faces, local edges (0,1),(1,2),(2,0), oriented
+// as in that first face.  The reference takes vcglib's edge order, which is not reproducible
+// without vcglib; both sides of every parity test use this rule.
+void build_edges(const std::vector<uint32_t>& tri, uint32_t nv, std::vector<uint32_t>& e,
+                 std::vector<std::vector<uint32_t>>& ef) {
+  std::map<std::pair<uint32_t, uint32_t>, uint32_t> key;
+  const uint32_t nf = (uint32_t)tri.size() / 3;
+  for (uint32_t f = 0; f < nf; ++f) {
+    for (int k = 0; k < 3; ++k) {
+      uint32_t a = tri[f * 3 + k], b = tri[f * 3 + (k + 1) % 3];
+      auto kk = std::make_pair(std::min(a, b), std::max(a, b));
+      auto it = key.find(kk);
+      if (it == key.end()) {
+        uint32_t id = (uint32_t)(e.size() / 2);
+        key.emplace(kk, id);
+        e.push_back(a);
+        e.push_back(b);
+        ef.push_back({f});
+      } else {
+        ef[it->second].push_back(f);
+      }
+    }
+  }
+  (void)nv;
+}
+
+// GenerateBendingElements (ClothSolverHelper.cpp:4-88), including its string test for the
+// winding of f1 (":find" of "idx1,idx2" in "a,b,c,a,b,c"), kept with its false positives.
+void build_bends(const std::vector<V3>& pos, const std::vector<uint32_t>& tri,
+                 const std::vector<uint32_t>& e, const std::vector<std::vector<uint32_t>>& ef,
+                 uint32_t offset, std::vector<uint32_t>& out, std::vector<float>& angles) {
+  const uint32_t ne = (uint32_t)e.size() / 2;
+  for (uint32_t ei = 0; ei < ne; ++ei) {
+    const auto& faces = ef[ei];
+    if (faces.size() < 2) continue;  // border edge (IsB)
+    uint32_t idx1 = e[ei * 2], idx2 = e[ei * 2 + 1];
+    for (size_t i = 0; i < faces.size(); ++i) {
+      for (size_t j = i + 1; j < faces.size(); ++j) {
+        uint32_t f1 = faces[i], f2 = faces[j];
+        auto opposite = [&](uint32_t f) {
+          for (int k = 0; k < 3; ++k) {
+            uint32_t vtx = tri[f * 3 + k];
+            if (vtx != e[ei * 2] && vtx != e[ei * 2 + 1]) return vtx;
+          }
+          return tri[f * 3];
+        };
+        uint32_t idx3 = opposite(f1), idx4 = opposite(f2);
+        std::string s = std::to_string(tri[f1 * 3 + 0]) + "," + std::to_string(tri[f1 * 3 + 1]) +
+                        "," + std::to_string(tri[f1 * 3 + 2]);
+        s += "," + s;
+        const std::string common = std::to_string(idx1) + "," + std::to_string(idx2);
+        const bool right_order = s.find(common) != std::string::npos;
+        if (!right_order) std::swap(idx1, idx2);
+        V3 v1 = pos[idx1], v2 = pos[idx2], v3 = pos[idx3], v4 = pos[idx4];
+        V3 n1 = normalize(cross(v1 - v3, v2 - v3));
+        V3 n2 = normalize(cross(v2 - v4, v1 - v4));
+        float d = dot(n1, n2);
+        if (d < -1) d = -1;
+        else if (d > 1) d = 1;
+        float th = std::acos(d);
+        out.push_back(idx1 + offset);
+        out.push_back(idx2 + offset);
+        out.push_back(idx3 + offset);
+        out.push_back(idx4 + offset);
+        angles.push_back(th);
+      }
+    }
+  }
+}
+
+// Geodesic::ComputeGeodesicDistance (src/utils/Geodesic.cpp:6-79): Dijkstra on the edge graph
+// with float path lengths.
+std::vector<float> geodesic(const std::vector<V3>& pos, const std::vector<std::vector<uint32_t>>& adj,
+                            uint32_t src) {
+  std::vector<float> dist(pos.size(), FLT_MAX);
+  typedef std::pair<float, uint32_t> FP;
+  std::priority_queue<FP, std::vector<FP>, std::greater<FP>> pq;
+  dist[src] = 0;
+  pq.push(FP(0.0f, src));
+  while (!pq.empty()) {
+    uint32_t cur = pq.top().second;
+    pq.pop();
+    for (uint32_t nb : adj[cur]) {
+      float wgt = length(pos[nb] - pos[cur]);
+      if (dist[nb] > dist[cur] + wgt) {
+        dist[nb] = dist[cur] + wgt;
+        pq.push(FP(dist[nb], nb));
+      }
+    }
+  }
+  return dist;
+}
+
+// Greedy coloring in constraint order (our deterministic stand-in for GraphColoring::Paint,
+// src/physics/graph_coloring/Base.cu:163-317): smallest color unused by any earlier constraint
+// sharing a vertex.
+std::vector<uint32_t> greedy_color(const std::vector<uint32_t>& idx, int arity, uint32_t nv,
+                                   uint32_t& ncolors) {
+  const size_t n = idx.size() / arity;
+  std::vector<uint32_t> col(n);
+  std::vector<std::vector<uint32_t>> used(nv);
+  ncolors = 0;
+  for (size_t c = 0; c < n; ++c) {
+    uint32_t k = 0;
+    for (;; ++k) {
+      bool clash = false;
+      for (int a = 0; a < arity && !clash; ++a) {
+        const auto& u = used[idx[c * arity + a]];
+        clash = std::find(u.begin(), u.end(), k) != u.end();
+      }
+      if (!clash) break;
+    }
+    col[c] = k;
+    for (int a = 0; a < arity; ++a) used[idx[c * arity + a]].push_back(k);
+    ncolors = std::max(ncolors, k + 1);
+  }
+  return col;
+}
+
+bool coloring_valid(const std::vector<uint32_t>& idx, int arity, const std::vector<uint32_t>& col,
+                    uint32_t nv) {
+  std::vector<std::set<uint32_t>> used(nv);
+  const size_t n = idx.size() / arity;
+  for (size_t c = 0; c < n; ++c)
+    for (int a = 0; a < arity; ++a)
+      if (!used[idx[c * arity + a]].insert(col[c]).second) return false;
+  return true;
+}
+
+// RTriBuild_Kernel (RTriangle.cu:19-84) over sorted VF adjacency lists.
+std::vector<uint32_t> build_rtri(const std::vector<uint32_t>& tri, const std::vector<uint32_t>& pre,
+                                 const std::vector<uint32_t>& list) {
+  const uint32_t nf = (uint32_t)tri.size() / 3;
+  std::vector<uint32_t> out(nf);
+  for (uint32_t fid = 0; fid < nf; ++fid) {
+    uint32_t fv[3] = {tri[fid * 3], tri[fid * 3 + 1], tri[fid * 3 + 2]};
+    uint32_t info = 0, j_start = pre[fv[0]], j_end = pre[fv[0] + 1];
+    for (uint32_t iv = 0; iv < 3; ++iv) {
+      uint32_t off = j_start, i_end = j_end;
+      uint32_t i_f = list[off++];
+      if (i_f == fid) info |= (1u << iv);
+      uint32_t jv = (iv + 1) % 3;
+      j_start = pre[fv[jv]];
+      j_end = pre[fv[jv] + 1];
+      uint32_t of = 0xffffffffu;
+      for (uint32_t jno = j_start; jno < j_end; ++jno) {
+        if (list[jno] == i_f && fid != i_f) {
+          of = i_f;
+          break;
+        }
+      }
+      for (; off < i_end && of == 0xffffffffu; ++off) {
+        i_f = list[off];
+        for (uint32_t jno = j_start; jno < j_end; ++jno) {
+          if (list[jno] == i_f && fid != i_f) {
+            of = i_f;
+            break;
+          }
+        }
+      }
+      if (fid < of) info |= (1u << (iv + 3));
+    }
+    out[fid] = info;
+  }
+  return out;
+}
+
+void build_vf(const std::vector<uint32_t>& tri, uint32_t nv, std::vector<uint32_t>& pre,
+              std::vector<uint32_t>& list) {
+  std::vector<std::vector<uint32_t>> vf(nv);
+  for (uint32_t f = 0; f < tri.size() / 3; ++f)
+    for (int k = 0; k < 3; ++k) vf[tri[f * 3 + k]].push_back(f);
+  pre.assign(nv + 1, 0);
+  list.clear();
+  for (uint32_t i = 0; i < nv; ++i) {
+    std::sort(vf[i].begin(), vf[i].end());
+    vf[i].erase(std::unique(vf[i].begin(), vf[i].end()), vf[i].end());
+    list.insert(list.end(), vf[i].begin(), vf[i].end());
+    pre[i + 1] = (uint32_t)list.size();
+  }
+}
+
+// UpdateNodeNormals (PhysicsMeshHelper.cu:196-210, 282-295): area-weighted by 1/(|e0|^2|e1|^2),
+// summed per vertex in ascending face order, then normalized.
+void vertex_normals(const std::vector<V3>& pos, const std::vector<uint32_t>& tri,
+                    const std::vector<uint32_t>& pre, const std::vector<uint32_t>& list,
+                    std::vector<V3>& out) {
+  const long nv = (long)pos.size();
+  out.assign(nv, V3{0, 0, 0});
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < nv; ++i) {
+    V3 acc{0, 0, 0};
+    for (uint32_t k = pre[i]; k < pre[i + 1]; ++k) {
+      uint32_t f = list[k];
+      int j = 0;
+      while (tri[f * 3 + j] != (uint32_t)i) ++j;
+      V3 xi = pos[i];
+      V3 e0 = pos[tri[f * 3 + (j + 1) % 3]] - xi;
+      V3 e1 = pos[tri[f * 3 + (j + 2) % 3]] - xi;
+      V3 c = cross(e0, e1) / (dot(e0, e0) * dot(e1, e1));
+      acc.x += c.x;
+      acc.y += c.y;
+      acc.z += c.z;
+    }
+    out[i] = normalize(acc);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// particle hash (SpatialHashGPU.cu)
+
+inline int int_coord(float value, float spacing) { return (int)std::floor(value / spacing); }
+inline int hash_coords(int x, int y, int z, int table) {
+  int32_t h = (int32_t)(((uint32_t)x * 92837111u) ^ ((uint32_t)y * 689287499u) ^
+                        ((uint32_t)z * 283923481u));
+  int32_t r = h % table;
+  return r < 0 ? -r : r;
+}
+
+void hash_particles(Oracle& o) {
+  const uint32_t nv = (uint32_t)o.x.size();
+  const float spacing = o.particle_diameter * o.p.hash_cell_size;
+  const float spacing2 = spacing * spacing;
+  const float d2 = o.particle_diameter * o.particle_diameter;
+  const int table = (int)(2 * nv);
+  const uint32_t maxnb = (uint32_t)o.p.max_neighbor_size;
+  std::vector<uint32_t> hash(nv), index(nv);
+  for (uint32_t i = 0; i < nv; ++i) {
+    V3 q = o.x[i];
+    hash[i] = (uint32_t)hash_coords(int_coord(q.x, spacing), int_coord(q.y, spacing),
+                                    int_coord(q.z, spacing), table);
+    index[i] = i;
+  }
+  // cub::DeviceRadixSort::SortPairs is stable (SpatialHashGPU.cu:102-119)
+  std::stable_sort(index.begin(), index.end(),
+                   [&](uint32_t a, uint32_t b) { return hash[a] < hash[b]; });
+  std::vector<uint32_t> sorted_hash(nv);
+  for (uint32_t i = 0; i < nv; ++i) sorted_hash[i] = hash[index[i]];
+  o.cell_start.assign(table, 0xffffffffu);
+  if (o.cell_end.size() != (size_t)table) o.cell_end.assign(table, 0u);
+  for (uint32_t id = 0; id < nv; ++id) {  // FindCellStart_Kernel
+    uint32_t h = sorted_hash[id];
+    if (id == 0 || h != sorted_hash[id - 1]) {
+      o.cell_start[h] = id;
+      if (id > 0) o.cell_end[sorted_hash[id - 1]] = id;
+    }
+    if (id == nv - 1) o.cell_end[h] = id + 1;
+  }
+  if (o.neighbors.size() != (size_t)nv * maxnb) o.neighbors.assign((size_t)nv * maxnb, 0xffffffffu);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long tid = 0; tid < (long)nv; ++tid) {  // CacheNeighbors_Kernel
+    const uint32_t id = index[tid];
+    const V3 pos = o.x[id];
+    const V3 orig = o.x_init[id];
+    const int ix = int_coord(pos.x, spacing), iy = int_coord(pos.y, spacing),
+              iz = int_coord(pos.z, spacing);
+    uint64_t ni = id;
+    const uint64_t limit = (uint64_t)nv * maxnb;
+    bool full = false;
+    for (int xx = ix - 1; xx <= ix + 1 && !full; ++xx)
+      for (int yy = iy - 1; yy <= iy + 1 && !full; ++yy)
+        for (int zz = iz - 1; zz <= iz + 1 && !full; ++zz) {
+          int h = hash_coords(xx, yy, zz, table);
+          uint32_t start = o.cell_start[h];
+          if (start == 0xffffffffu) continue;
+          uint32_t end = std::min(o.cell_end[h], start + maxnb);
+          for (uint32_t i = start; i < end; ++i) {
+            uint32_t nb = index[i];
+            V3 dp = pos - o.x[nb];
+            V3 d0 = orig - o.x_init[nb];
+            if (nb != id && dot(dp, dp) < spacing2 && dot(d0, d0) > d2) {
+              o.neighbors[ni] = nb;
+              ni += nv;
+              if (ni >= limit) {
+                full = true;
+                break;
+              }
+            }
+          }
+        }
+    if (!full && ni < limit) o.neighbors[ni] = 0xffffffffu;
+  }
+}
+
+// ComputeFriction (ClothSolverHelper.cu:156-169)
+inline V3 friction_of(float mu, V3 correction, V3 rel_vel) {
+  V3 fr{0, 0, 0};
+  float cl = length(correction);
+  if (mu > 0.0f && cl > 0.0f) {
+    V3 nrm = correction / cl;
+    V3 tan_vel = rel_vel - nrm * dot(rel_vel, nrm);
+    float tl = length(tan_vel);
+    float max_tl = cl * mu;
+    fr = -tan_vel * mmin(max_tl / tl, 1.0f);
+  }
+  return fr;
+}
+
+// ApplyDeltas_Kernel (ClothSolverHelper.cu:139-148)
+void apply_deltas(Oracle& o) {
+  const long nv = (long)o.x.size();
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < nv; ++i) {
+    float count = (float)o.delta_counts[i];
+    if (count > 0.0f) {
+      o.x[i] += o.deltas[i] / count * o.p.relaxation_factor;
+      o.deltas[i] = V3{0, 0, 0};
+      o.delta_counts[i] = 0;
+    }
+  }
+}
+
+// CollideParticles_Kernel (ClothSolverHelper.cu:171-219) followed by ApplyDeltas.
+void collide_particles(Oracle& o) {
+  const uint32_t nv = (uint32_t)o.x.size();
+  const uint64_t limit = (uint64_t)nv * (uint64_t)o.p.max_neighbor_size;
+  const float dia = o.particle_diameter;
+#pragma omp parallel for schedule(static)
+  for (long id = 0; id < (long)nv; ++id) {
+    V3 pd{0, 0, 0};
+    int cnt = 0;
+    V3 pred_i = o.x[id];
+    V3 vel_i = pred_i - o.x0[id];
+    float w_i = o.w[id];
+    for (uint64_t k = (uint64_t)id; k < limit; k += nv) {
+      uint32_t j = o.neighbors[k];
+      if (j >= nv) break;  // reference: j > num_particles; j == nv never occurs
+      float w_j = o.w[j];
+      float denom = w_i + w_j;
+      if (denom <= 0) continue;
+      V3 pred_j = o.x[j];
+      V3 diff = pred_i - pred_j;
+      float distance = length(diff);
+      if (distance >= dia) continue;
+      V3 gradient = diff / (distance + kEps);
+      float lambda = (distance - dia) / denom;
+      V3 common = lambda * gradient;
+      cnt++;
+      pd -= w_i * common;
+      V3 rel = vel_i - (pred_j - o.x0[j]);
+      V3 fr = friction_of(o.p.friction, common, rel);
+      pd += w_i * fr;
+    }
+    o.deltas[id] = pd;
+    o.delta_counts[id] = cnt;
+  }
+  apply_deltas(o);
+}
+
+// ---------------------------------------------------------------------------------------------
+// constraints
+
+// SolveStretch_Kernel (BasicSolverHelper.cu:80-132)
+void solve_stretch(Oracle& o, uint32_t color, float dt, int iter) {
+  const long ne = (long)o.rest.size();
+#pragma omp parallel for schedule(static)
+  for (long id = 0; id < ne; ++id) {
+    if (o.s_color[id] != color) continue;
+    if (iter == 0) o.s_lambda[id] = 0.0f;
+    uint32_t i1 = o.edges[id * 2], i2 = o.edges[id * 2 + 1];
+    float expected = o.rest[id];
+    V3 diff = o.x[i1] - o.x[i2];
+    float distance = length(diff);
+    float w1 = o.w[i1], w2 = o.w[i2];
+    if (distance != expected && w1 + w2 > 0.0f) {
+      V3 gradient = diff / (distance + kEps);
+      float alpha_tilde = o.s_comp[id] / (dt * dt);
+      float constraint = distance - expected;
+      float dl = (-constraint - alpha_tilde * o.s_lambda[id]) / (w1 + w2 + alpha_tilde);
+      V3 corr = dl * gradient;
+      o.s_lambda[id] = o.s_lambda[id] + dl;
+      V3 c1 = corr * w1;
+      V3 c2 = -corr * w2;
+      o.x[i1] += c1;
+      o.x[i2] += c2;
+    }
+  }
+}
+
+// SolveBend_Kernel (BasicSolverHelper.cu:8-72)
+void solve_bend(Oracle& o, uint32_t color, float dt) {
+  const long nb = (long)o.theta.size();
+#pragma omp parallel for schedule(static)
+  for (long id = 0; id < nb; ++id) {
+    if (o.b_color[id] != color) continue;
+    uint32_t i1 = o.bends[id * 4], i2 = o.bends[id * 4 + 1], i3 = o.bends[id * 4 + 2],
+             i4 = o.bends[id * 4 + 3];
+    float expected = o.theta[id];
+    float w1 = o.w[i1], w2 = o.w[i2], w3 = o.w[i3], w4 = o.w[i4];
+    V3 p1 = o.x[i1];
+    V3 p2 = o.x[i2] - p1;
+    V3 p3 = o.x[i3] - p1;
+    V3 p4 = o.x[i4] - p1;
+    V3 n1 = normalize(cross(p2, p3));
+    V3 n2 = normalize(cross(p2, p4));
+    float d = clampf(dot(n1, n2), 0.0f, 1.0f);
+    float angle = std::acos(d);
+    if (angle < kEps || std::isnan(d)) continue;
+    V3 q3 = (cross(p2, n2) + cross(n1, p2) * d) / (length(cross(p2, p3)) + kEps);
+    V3 q4 = (cross(p2, n1) + cross(n2, p2) * d) / (length(cross(p2, p4)) + kEps);
+    V3 q2 = -(cross(p3, n2) + cross(n1, p3) * d) / (length(cross(p2, p3)) + kEps) -
+            (cross(p4, n1) + cross(n2, p4) * d) / (length(cross(p2, p4)) + kEps);
+    V3 q1 = -q2 - q3 - q4;
+    float xpbd_bend = o.b_comp[id] / dt / dt;
+    float denom = xpbd_bend + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) +
+                               w4 * dot(q4, q4));
+    if (denom < kEps) continue;
+    float lambda = std::sqrt(1.0f - d * d) * (angle - expected) / denom;
+    float scaling = 1.0f;
+    V3 c1 = scaling * w1 * lambda * q1;
+    V3 c2 = scaling * w2 * lambda * q2;
+    V3 c3 = scaling * w3 * lambda * q3;
+    V3 c4 = scaling * w4 * lambda * q4;
+    o.x[i1] += c1;
+    o.x[i2] += c2;
+    o.x[i3] += c3;
+    o.x[i4] += c4;
+  }
+}
+
+// SolveGeodesicLRA_Kernel (LongRangeAttachments.cu:5-26).  Constraints are applied in list order
+// (slot-major); the reference's concurrent "+=" of several slots on one vertex is a race whose
+// sequential order we fix.
+void solve_lra(Oracle& o) {
+  const size_t n = o.lra_rest.size();
+  const float s = o.p.long_range_stretchiness;
+  for (size_t c = 0; c < n; ++c) {
+    uint32_t src = o.lra_src[c], tgt = o.lra_tgt[c];
+    float target = o.lra_rest[c] * s;
+    if (o.w[tgt] < kEps && target > 0) continue;
+    V3 diff = o.x[tgt] - o.x[src];
+    float dist = length(diff);
+    if (dist > target) o.x[tgt] += -diff + diff / dist * target;
+  }
+}
+
+// SolveBinding_Kernel (BindingConstraint.cu:56-92)
+void solve_binding(Oracle& o) {
+  for (const Binding& b : o.bindings) {
+    V3 pc = o.x[b.cloth];
+    float im = o.w[b.cloth];
+    if (im < kEps) continue;
+    V3 pu = o.ox[b.iu], pv = o.ox[b.iv], pw = o.ox[b.iw];
+    V3 pob = b.u * pu + b.v * pv + b.w * pw;
+    float C = length(pc - pob) - b.L;
+    V3 nn = normalize(pc - pob);
+    float s = im;
+    s = C / s;
+    if (C < 0.0f) continue;
+    s *= b.stiffness;
+    V3 dc = -s * im * nn;
+    o.x[b.cloth] += dc;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// obstacle
+
+// BVH::UpdateData (BVH.cu:382-421, 565-573) with ccd=false, then Construct(scr=0).
+void rebuild_obstacle_bvh(Oracle& o, float tol) {
+  const uint32_t nf = (uint32_t)o.otri.size() / 3;
+  o.bvh.objects.resize(nf);
+  for (uint32_t f = 0; f < nf; ++f) {
+    uint32_t a = o.otri[f * 3], b = o.otri[f * 3 + 1], c = o.otri[f * 3 + 2];
+    Prim& pr = o.bvh.objects[f];
+    pr.idx1 = a;
+    pr.idx2 = b;
+    pr.idx3 = c;
+    pr.v1 = o.ox0[a] + tol * o.on[a];
+    pr.v2 = o.ox0[b] + tol * o.on[b];
+    pr.v3 = o.ox0[c] + tol * o.on[c];
+    pr.pred1 = pr.v1;
+    pr.pred2 = pr.v2;
+    pr.pred3 = pr.v3;
+  }
+  o.bvh.construct(0.0f);
+}
+
+// PhysicsMesh::Interpolate (PhysicsMesh.cu:610-620), UpdateMidstepNormals
+// (PhysicsMeshHelper.cu:212-225, 297-310), BVH::RefitMidstep (BVH.cu:770-818).
+void obstacle_pass(Oracle& o, int step, int num_steps) {
+  const long nv = (long)o.ox.size();
+  float alpha = ((float)step + 1.0f) / (float)num_steps;
+  for (long i = 0; i < nv; ++i) o.ox1[i] = (1.0f - alpha) * o.ox0[i] + alpha * o.ox[i];
+  vertex_normals(o.ox1, o.otri, o.ovf_prefix, o.ovf_list, o.on1);
+  if (!o.bvh.active) return;
+  const uint32_t n = o.bvh.num_objects(), ni = n - 1;
+  const float tol = o.p.bvh_tolerance;
+  for (uint32_t i = 0; i < n; ++i) {
+    uint32_t k = ni + i;
+    uint32_t obj = o.bvh.nodes[k].object;
+    Prim& pr = o.bvh.objects[obj];
+    uint32_t a = o.otri[obj * 3], b = o.otri[obj * 3 + 1], c = o.otri[obj * 3 + 2];
+    pr.pred1 = o.ox1[a] + tol * o.on1[a];
+    pr.pred2 = o.ox1[b] + tol * o.on1[b];
+    pr.pred3 = o.ox1[c] + tol * o.on1[c];
+    Box& bx = o.bvh.aabbs[k];
+    bx = box_merge_point(bx, pr.pred1);
+    bx = box_merge_point(bx, pr.pred2);
+    bx = box_merge_point(bx, pr.pred3);
+  }
+  o.bvh.merge_internal_cas();
+}
+
+// GenerateVF_DCD_Kernel, GenerateVFCCD_Kernel, GenerateEE_DCD_Kernel (PBDCollision.cu)
+void generate_contacts(Oracle& o) {
+  const long nv = (long)o.x.size();
+  const long ne = (long)o.rest.size();
+  const Lbvh& bvh = o.bvh;
+#pragma omp parallel for schedule(dynamic, 128)
+  for (long i = 0; i < nv; ++i) {
+    uint32_t buf[kMaxBuffer];
+    // VF DCD
+    {
+      V3 pred = o.x[i];
+      uint32_t nf = bvh.query_point(pred, buf);
+      float hit = kScalarMax;
+      int hit_idx = -1;
+      V3 hit_qs{0, 0, 0};
+      for (uint32_t k = 0; k < nf; ++k) {
+        const Prim& pr = bvh.objects[buf[k]];
+        V3 qs;
+        float u, v, ww;
+        float dist = nearest_point(pred, pr.pred1, pr.pred2, pr.pred3, qs, u, v, ww);
+        if (dist < hit) {
+          hit = dist;
+          hit_qs = qs;
+          hit_idx = (int)buf[k];
+        }
+      }
+      o.vf_idx[i] = hit_idx;
+      o.vf_qs[i] = hit_qs;
+    }
+    // VF CCD
+    {
+      o.rt_idx[i] = -1;
+      o.rt_qc[i] = V3{0, 0, 0};
+      V3 p1 = o.x0[i], p2 = o.x[i];
+      V3 d = p2 - p1;
+      const float len = length(d);
+      if (!(len < kEps)) {
+        d = d / len;
+        uint32_t nf = bvh.query_segment(p1, p2, buf);
+        float hit = kScalarMax;
+        int hit_idx = -1;
+        V3 qc{0, 0, 0};
+        for (uint32_t k = 0; k < nf; ++k) {
+          const Prim& pr = bvh.objects[buf[k]];
+          float dist = ray_intersect(p1, d, len, pr.pred1, pr.pred2, pr.pred3);
+          if (dist < hit) {
+            qc = p1 + dist * d;
+            hit = dist;
+            hit_idx = (int)buf[k];
+          }
+        }
+        o.rt_idx[i] = hit_idx;
+        o.rt_qc[i] = qc;
+      }
+    }
+  }
+#pragma omp parallel for schedule(dynamic, 128)
+  for (long e = 0; e < ne; ++e) {
+    uint32_t buf[kMaxBuffer];
+    uint32_t i1 = o.edges[e * 2], i2 = o.edges[e * 2 + 1];
+    V3 pc = o.x[i1], qc = o.x[i2];
+    uint32_t nf = bvh.query_segment(pc, qc, buf);
+    float s = 0, t = 0;
+    V3 p2{0, 0, 0}, q2{0, 0, 0}, fn{0, 0, 0};
+    float min_dist = kScalarMax;
+    for (uint32_t k = 0; k < nf; ++k) {
+      uint32_t f = buf[k];
+      const Prim& pr = bvh.objects[f];
+      uint32_t info = o.ortri[f];
+      V3 ov[3] = {pr.pred1, pr.pred2, pr.pred3};
+      for (uint32_t a = 0; a < 3; ++a) {
+        if ((info >> (a + 3u)) & 1u) {
+          float _s, _t;
+          V3 c1, c2;
+          uint32_t b = (a + 1) % 3;
+          if (closest_pt_segment_segment(pc, qc, ov[a], ov[b], _s, _t, c1, c2) != 0.0f) {
+            V3 dd = c1 - c2;
+            float dist = length(dd);
+            if (dist < min_dist) {
+              min_dist = dist;
+              p2 = ov[a];
+              q2 = ov[b];
+              s = _s;
+              t = _t;
+              fn = face_normal(ov[0], ov[1], ov[2]);
+            }
+          }
+        }
+      }
+    }
+    o.ee[e] = EEContact{min_dist, p2, q2, s, t, fn};
+  }
+}
+
+// SolveVFCCD_Kernel (PBDCollision.cu:279-298), SolveVFDCD_Kernel (:57-80),
+// SolveEEDCD_Kernel (:163-212), ApplyDeltas.
+void solve_contacts(Oracle& o) {
+  const long nv = (long)o.x.size();
+  const long ne = (long)o.rest.size();
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < nv; ++i) {
+    if (o.rt_idx[i] == -1) continue;
+    const Prim& pr = o.bvh.objects[o.rt_idx[i]];
+    V3 nc = face_normal(pr.pred1, pr.pred2, pr.pred3);
+    float lambda = dot(nc, o.x[i] - o.rt_qc[i]);
+    if (lambda < 0) {
+      V3 corr = -lambda * nc;
+      o.x[i] += corr;
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < nv; ++i) {
+    if (o.vf_idx[i] == -1) continue;
+    const Prim& pr = o.bvh.objects[o.vf_idx[i]];
+    V3 ns = face_normal(pr.pred1, pr.pred2, pr.pred3);
+    float lambda = dot(ns, o.x[i] - o.vf_qs[i]) - 1e-3f;
+    if (lambda < 0) {
+      V3 corr = -lambda * ns;
+      o.x[i] += corr;
+    }
+  }
+  for (long e = 0; e < ne; ++e) {
+    const EEContact& c = o.ee[e];
+    if (c.dist > 1e6f) continue;
+    uint32_t i1 = o.edges[e * 2], i2 = o.edges[e * 2 + 1];
+    V3 p1 = o.x[i1], q1 = o.x[i2];
+    float s = c.s, t = c.t;
+    V3 c1 = (1 - s) * p1 + s * q1;
+    V3 c2 = (1 - t) * c.p2 + t * c.q2;
+    V3 d = c1 - c2;
+    float len = length(d);
+    if (len < kEps) continue;
+    float proj = dot(d, c.fn) - 1e-3f;
+    float lambda = proj;
+    if (lambda > 0) continue;
+    V3 corr1 = -(1 - s) * lambda * c.fn;
+    V3 corr2 = -(s)*lambda * c.fn;
+    o.deltas[i1] += corr1;
+    o.deltas[i2] += corr2;
+    o.delta_counts[i1] += 1;
+    o.delta_counts[i2] += 1;
+  }
+  apply_deltas(o);
+}
+
+// ---------------------------------------------------------------------------------------------
+// frame — ClothSolverBase::SimulateSwift (ClothSolverBase.cpp:171-261)
+
+void step_frame(Oracle& o) {
+  const xrt_swift_params& p = o.p;
+  const float substep_time = p.frame_time / (float)p.num_substeps;
+  const long nv = (long)o.x.size();
+  const bool obstacle_updated = p.update_obstacle_animation && !o.otri.empty();
+  if (obstacle_updated) rebuild_obstacle_bvh(o, 0.0f);
+  const bool has_obstacle = o.bvh.active;
+  const int frequency = (p.num_substeps * p.num_iterations) / p.num_collision_passes;
+  int cnt = 0;
+  for (int substep = 0; substep < p.num_substeps; ++substep) {
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < nv; ++i) {  // PredictPositions_Kernel
+      if (o.w[i] > kEps) o.v[i] += V3{p.gravity[0], p.gravity[1], p.gravity[2]} * substep_time;
+      o.x[i] = o.x0[i] + o.v[i] * substep_time;
+    }
+    if (p.enable_self_collision && substep % p.inter_leaved_hash == 0) hash_particles(o);
+    for (int it = 0; it < p.num_iterations; ++it) {
+      if (p.enable_self_collision) collide_particles(o);
+      int current = substep * p.num_iterations + it;
+      if (current % frequency == 0) {
+        if (obstacle_updated) obstacle_pass(o, cnt, p.num_collision_passes);
+        if (has_obstacle) generate_contacts(o);
+        cnt++;
+      }
+      for (uint32_t c = 0; c < o.n_s_colors; ++c) solve_stretch(o, c, substep_time, it);
+      if (p.solve_bending)
+        for (uint32_t c = 0; c < o.n_b_colors; ++c) solve_bend(o, c, substep_time);
+      if (p.geodesic_lra) solve_lra(o);
+      if (has_obstacle) {
+        solve_contacts(o);
+      } else {
+        apply_deltas(o);
+      }
+      if (!o.otri.empty()) solve_binding(o);
+    }
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < nv; ++i) {  // Finalize_Kernel
+      V3 np = o.x[i];
+      V3 raw = (np - o.x0[i]) / substep_time;
+      o.v[i] = raw * (1 - p.damping * substep_time);
+      o.x0[i] = np;
+    }
+  }
+  if (!o.otri.empty()) {
+    o.ox0 = o.ox;  // PredictedToPositions
+    vertex_normals(o.ox0, o.otri, o.ovf_prefix, o.ovf_list, o.on);
+  }
+  vertex_normals(o.x0, o.tri, o.vf_prefix, o.vf_list, o.n);
+  o.frame_index++;
+}
+
+void start(Oracle& o) {
+  const uint32_t nv = (uint32_t)o.x0.size();
+  // coloring
+  for (int kind = 0; kind < 2; ++kind) {
+    const std::vector<uint32_t>& idx = kind == 0 ? o.edges : o.bends;
+    const int arity = kind == 0 ? 2 : 4;
+    std::vector<uint32_t>& col = kind == 0 ? o.s_color : o.b_color;
+    uint32_t& nc = kind == 0 ? o.n_s_colors : o.n_b_colors;
+    if (!o.pending_colors[kind].empty()) {
+      col = o.pending_colors[kind];
+      nc = 0;
+      for (uint32_t c : col) nc = std::max(nc, c + 1);
+    } else {
+      col = greedy_color(idx, arity, nv, nc);
+    }
+  }
+  o.s_lambda.assign(o.rest.size(), 0.0f);
+  build_vf(o.tri, nv, o.vf_prefix, o.vf_list);
+  vertex_normals(o.x0, o.tri, o.vf_prefix, o.vf_list, o.n);
+  o.x_init = o.x0;  // SpatialHashGPU::SetInitialPositions (universal/ClothSolver.cpp:88)
+  o.deltas.assign(nv, V3{0, 0, 0});
+  o.delta_counts.assign(nv, 0);
+  o.vf_idx.assign(nv, -1);
+  o.rt_idx.assign(nv, -1);
+  o.vf_qs.assign(nv, V3{0, 0, 0});
+  o.rt_qc.assign(nv, V3{0, 0, 0});
+  o.ee.assign(o.rest.size(), EEContact{kScalarMax, {0, 0, 0}, {0, 0, 0}, 0, 0, {0, 0, 0}});
+  if (!o.otri.empty()) {
+    const uint32_t onv = (uint32_t)o.ox0.size();
+    build_vf(o.otri, onv, o.ovf_prefix, o.ovf_list);
+    vertex_normals(o.ox0, o.otri, o.ovf_prefix, o.ovf_list, o.on);
+    o.on1 = o.on;
+    o.ox1 = o.ox0;
+    rebuild_obstacle_bvh(o, 0.0f);  // ClothSolverUniversal::Start (ClothSolver.cpp:60-61)
+    o.ortri = build_rtri(o.otri, o.ovf_prefix, o.ovf_list);
+  }
+  // bindings: GenerateBinding_Kernel (BindingConstraint.cu:20-44) from x0 of both meshes
+  for (Binding& b : o.bindings) {
+    V3 pcl = o.x0[b.cloth];
+    V3 pb = b.u * o.ox0[b.iu] + b.v * o.ox0[b.iv] + b.w * o.ox0[b.iw];
+    if (b.L < kEps) b.L = length(pcl - pb);
+  }
+  o.started = true;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// C API of the oracle (test infrastructure)
+
+extern "C" {
+
+void* orc_create() { return new Oracle(); }
+void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
+int orc_num_threads() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+void orc_set_params(void* h, const xrt_swift_params* p) { static_cast<Oracle*>(h)->p = *p; }
+
+int orc_add_cloth(void* h, const xrt_cloth_desc* d) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  Cloth c;
+  c.offset = (uint32_t)o.x0.size();
+  c.mesh_pos.resize(d->num_vertices);
+  for (uint32_t i = 0; i < d->num_vertices; ++i)
+    c.mesh_pos[i] = V3{d->positions[i * 3], d->positions[i * 3 + 1], d->positions[i * 3 + 2]};
+  c.tri.assign(d->triangles, d->triangles + 3 * (size_t)d->num_triangles);
+  for (uint32_t i = 0; i < d->num_vertices; ++i) {
+    V3 q = c.mesh_pos[i];
+    if (d->model_matrix) q = transform_point(d->model_matrix, q);
+    o.x0.push_back(q);
+    o.x.push_back(c.mesh_pos[i]);
+    o.v.push_back(V3{0, 0, 0});
+    o.w.push_back(1.0f);
+  }
+  for (uint32_t k = 0; k < 3 * d->num_triangles; ++k) o.tri.push_back(d->triangles[k] + c.offset);
+  for (uint32_t i = 0; i < d->num_fixed; ++i) o.w[c.offset + d->fixed_indices[i]] = 0.0f;
+  // edges / stretch (PrepareBasicStretchData, ClothSolverHelper.cpp:90-109)
+  std::vector<uint32_t> e;
+  std::vector<std::vector<uint32_t>> ef;
+  build_edges(c.tri, d->num_vertices, e, ef);
+  for (size_t k = 0; k < e.size() / 2; ++k) {
+    o.edges.push_back(e[k * 2] + c.offset);
+    o.edges.push_back(e[k * 2 + 1] + c.offset);
+    o.rest.push_back(length(c.mesh_pos[e[k * 2]] - c.mesh_pos[e[k * 2 + 1]]));
+    o.s_comp.push_back(o.p.stretch_compliance);
+  }
+  if (o.p.solve_bending) {
+    std::vector<uint32_t> b;
+    std::vector<float> th;
+    build_bends(c.mesh_pos, c.tri, e, ef, c.offset, b, th);
+    o.bends.insert(o.bends.end(), b.begin(), b.end());
+    o.theta.insert(o.theta.end(), th.begin(), th.end());
+    o.b_comp.insert(o.b_comp.end(), th.size(), o.p.bend_compliance);
+  }
+  // geodesic LRA (ClothObjectBase.cpp:79-93)
+  if (d->num_attached > 0 && o.p.geodesic_lra) {
+    std::vector<std::vector<uint32_t>> adj(d->num_vertices);
+    for (size_t k = 0; k < e.size() / 2; ++k) {
+      adj[e[k * 2]].push_back(e[k * 2 + 1]);
+      adj[e[k * 2 + 1]].push_back(e[k * 2]);
+    }
+    for (auto& a : adj) std::sort(a.begin(), a.end());
+    for (uint32_t s = 0; s < d->num_attached; ++s) {
+      uint32_t slot = d->attached_indices[s];
+      std::vector<float> dist = geodesic(c.mesh_pos, adj, slot);
+      for (uint32_t vtx = 0; vtx < d->num_vertices; ++vtx) {
+        o.lra_src.push_back(slot + c.offset);
+        o.lra_tgt.push_back(vtx + c.offset);
+        o.lra_rest.push_back(dist[vtx]);
+      }
+    }
+  }
+  for (uint32_t i = 0; i < d->num_binded; ++i) {
+    Binding b;
+    b.cloth = d->binded_indices[i] + c.offset;
+    b.iu = d->bind_obstacle_tri[i * 3];
+    b.iv = d->bind_obstacle_tri[i * 3 + 1];
+    b.iw = d->bind_obstacle_tri[i * 3 + 2];
+    b.u = d->bind_barycentric[i * 3];
+    b.v = d->bind_barycentric[i * 3 + 1];
+    b.w = d->bind_barycentric[i * 3 + 2];
+    b.L = d->bind_distances ? d->bind_distances[i] : 0.0f;
+    b.stiffness = d->bind_stiffnesses ? d->bind_stiffnesses[i] : 1.0f;
+    o.bindings.push_back(b);
+  }
+  // particle diameter (universal/ClothObject.hpp:36-37): the last cloth added wins
+  if (d->particle_diameter > 0.0f) {
+    o.particle_diameter = d->particle_diameter;
+  } else {
+    o.particle_diameter =
+        length(c.mesh_pos[c.tri[0]] - c.mesh_pos[c.tri[1]]) * o.p.particle_diameter;
+  }
+  o.cloths.push_back(std::move(c));
+  return (int)o.cloths.back().offset;
+}
+
+int orc_add_obstacle(void* h, const xrt_obstacle_desc* d) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  uint32_t off = (uint32_t)o.ox0.size();
+  for (uint32_t i = 0; i < d->num_vertices; ++i) {
+    V3 q{d->positions[i * 3], d->positions[i * 3 + 1], d->positions[i * 3 + 2]};
+    if (d->model_matrix) q = transform_point(d->model_matrix, q);
+    o.ox0.push_back(q);
+    o.ox.push_back(q);
+  }
+  for (uint32_t k = 0; k < 3 * d->num_triangles; ++k) o.otri.push_back(d->triangles[k] + off);
+  return (int)off;
+}
+
+void orc_set_coloring(void* h, int kind, const uint32_t* colors, uint32_t n) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  o.pending_colors[kind & 1].assign(colors, colors + n);
+}
+void orc_set_compliance(void* h, int kind, const float* c, uint32_t n) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  (kind == 0 ? o.s_comp : o.b_comp).assign(c, c + n);
+}
+void orc_set_inv_mass(void* h, const float* w, uint32_t n) {
+  static_cast<Oracle*>(h)->w.assign(w, w + n);
+}
+void orc_start(void* h) { start(*static_cast<Oracle*>(h)); }
+void orc_set_obstacle_targets(void* h, const float* pos) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  for (size_t i = 0; i < o.ox.size(); ++i) o.ox[i] = V3{pos[i * 3], pos[i * 3 + 1], pos[i * 3 + 2]};
+}
+void orc_step_frame(void* h) { step_frame(*static_cast<Oracle*>(h)); }
+
+static void put3(const std::vector<V3>& v, float* out) {
+  for (size_t i = 0; i < v.size(); ++i) {
+    out[i * 3] = v[i].x;
+    out[i * 3 + 1] = v[i].y;
+    out[i * 3 + 2] = v[i].z;
+  }
+}
+void orc_get_sizes(void* h, uint32_t* out8) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  out8[0] = (uint32_t)o.x0.size();
+  out8[1] = (uint32_t)o.rest.size();
+  out8[2] = (uint32_t)o.tri.size() / 3;
+  out8[3] = (uint32_t)o.theta.size();
+  out8[4] = (uint32_t)o.lra_rest.size();
+  out8[5] = (uint32_t)o.ox0.size();
+  out8[6] = (uint32_t)o.otri.size() / 3;
+  out8[7] = o.n_s_colors | (o.n_b_colors << 16);
+}
+void orc_get_positions(void* h, float* out) { put3(static_cast<Oracle*>(h)->x0, out); }
+void orc_get_velocities(void* h, float* out) { put3(static_cast<Oracle*>(h)->v, out); }
+void orc_get_normals(void* h, float* out) { put3(static_cast<Oracle*>(h)->n, out); }
+void orc_get_obstacle_positions(void* h, float* out) { put3(static_cast<Oracle*>(h)->ox0, out); }
+float orc_particle_diameter(void* h) { return static_cast<Oracle*>(h)->particle_diameter; }
+void orc_get_edges(void* h, uint32_t* e, float* rest) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  std::copy(o.edges.begin(), o.edges.end(), e);
+  std::copy(o.rest.begin(), o.rest.end(), rest);
+}
+void orc_get_bends(void* h, uint32_t* b, float* th) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  std::copy(o.bends.begin(), o.bends.end(), b);
+  std::copy(o.theta.begin(), o.theta.end(), th);
+}
+void orc_get_coloring(void* h, int kind, uint32_t* out) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  const auto& c = kind == 0 ? o.s_color : o.b_color;
+  std::copy(c.begin(), c.end(), out);
+}
+int orc_coloring_valid(void* h, int kind) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  return kind == 0 ? coloring_valid(o.edges, 2, o.s_color, (uint32_t)o.x0.size())
+                   : coloring_valid(o.bends, 4, o.b_color, (uint32_t)o.x0.size());
+}
+void orc_get_lra(void* h, uint32_t* src, uint32_t* tgt, float* rest) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  std::copy(o.lra_src.begin(), o.lra_src.end(), src);
+  std::copy(o.lra_tgt.begin(), o.lra_tgt.end(), tgt);
+  std::copy(o.lra_rest.begin(), o.lra_rest.end(), rest);
+}
+void orc_get_rtri(void* h, uint32_t* out) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  std::copy(o.ortri.begin(), o.ortri.end(), out);
+}
+static void export_bvh(const Lbvh& b, uint32_t* morton, uint32_t* objs, uint32_t* nodes,
+                       float* aabbs, int32_t* iesc, int32_t* eesc) {
+  const size_t n = b.num_objects();
+  if (morton) std::copy(b.sorted_morton.begin(), b.sorted_morton.end(), morton);
+  if (objs) std::copy(b.sorted_objects.begin(), b.sorted_objects.end(), objs);
+  for (size_t k = 0; k < b.nodes.size(); ++k) {
+    if (nodes) {
+      nodes[k * 4] = b.nodes[k].parent;
+      nodes[k * 4 + 1] = b.nodes[k].left;
+      nodes[k * 4 + 2] = b.nodes[k].right;
+      nodes[k * 4 + 3] = b.nodes[k].object;
+    }
+    if (aabbs) {
+      const Box& bx = b.aabbs[k];
+      float* a = aabbs + k * 6;
+      a[0] = bx.lo.x; a[1] = bx.lo.y; a[2] = bx.lo.z;
+      a[3] = bx.hi.x; a[4] = bx.hi.y; a[5] = bx.hi.z;
+    }
+  }
+  if (iesc && n > 1) std::copy(b.iesc.begin(), b.iesc.begin() + (n - 1), iesc);
+  if (eesc) std::copy(b.eesc.begin(), b.eesc.end(), eesc);
+}
+void orc_export_obstacle_bvh(void* h, uint32_t* morton, uint32_t* objs, uint32_t* nodes,
+                             float* aabbs, int32_t* iesc, int32_t* eesc) {
+  export_bvh(static_cast<Oracle*>(h)->bvh, morton, objs, nodes, aabbs, iesc, eesc);
+}
+void orc_export_contacts(void* h, int32_t* vf_index, float* vf_qs, int32_t* rt_index, float* rt_qc,
+                         float* ee) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  if (vf_index) std::copy(o.vf_idx.begin(), o.vf_idx.end(), vf_index);
+  if (vf_qs) put3(o.vf_qs, vf_qs);
+  if (rt_index) std::copy(o.rt_idx.begin(), o.rt_idx.end(), rt_index);
+  if (rt_qc) put3(o.rt_qc, rt_qc);
+  if (ee) {
+    for (size_t k = 0; k < o.ee.size(); ++k) {
+      const EEContact& c = o.ee[k];
+      float* r = ee + k * 12;
+      r[0] = c.dist;
+      r[1] = c.p2.x; r[2] = c.p2.y; r[3] = c.p2.z;
+      r[4] = c.q2.x; r[5] = c.q2.y; r[6] = c.q2.z;
+      r[7] = c.s; r[8] = c.t;
+      r[9] = c.fn.x; r[10] = c.fn.y; r[11] = c.fn.z;
+    }
+  }
+}
+void orc_export_neighbors(void* h, uint32_t* out) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  std::copy(o.neighbors.begin(), o.neighbors.end(), out);
+}
+void orc_hash_now(void* h) {  // run SpatialHashGPU::Hash on the current predicted positions
+  Oracle& o = *static_cast<Oracle*>(h);
+  hash_particles(o);
+}
+
+// ---- standalone LBVH -------------------------------------------------------------------------
+void* orc_lbvh_create() { return new Lbvh(); }
+void orc_lbvh_destroy(void* h) { delete static_cast<Lbvh*>(h); }
+void orc_lbvh_build(void* h, const float* prims, const float* pred, uint32_t n, float scr) {
+  Lbvh& b = *static_cast<Lbvh*>(h);
+  b.objects.resize(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    const float* q = prims + (size_t)i * 9;
+    const float* r = pred ? pred + (size_t)i * 9 : q;
+    Prim& pr = b.objects[i];
+    pr.v1 = V3{q[0], q[1], q[2]};
+    pr.v2 = V3{q[3], q[4], q[5]};
+    pr.v3 = V3{q[6], q[7], q[8]};
+    pr.pred1 = V3{r[0], r[1], r[2]};
+    pr.pred2 = V3{r[3], r[4], r[5]};
+    pr.pred3 = V3{r[6], r[7], r[8]};
+    pr.idx1 = i * 3;
+    pr.idx2 = i * 3 + 1;
+    pr.idx3 = i * 3 + 2;
+  }
+  b.construct(scr);
+}
+void orc_lbvh_refit(void* h, const float* pred, uint32_t n) {
+  Lbvh& b = *static_cast<Lbvh*>(h);
+  std::vector<V3> p3((size_t)n * 3);
+  for (size_t k = 0; k < (size_t)n * 3; ++k) p3[k] = V3{pred[k * 3], pred[k * 3 + 1], pred[k * 3 + 2]};
+  b.refit_pred(p3);
+}
+void orc_lbvh_export(void* h, uint32_t* morton, uint32_t* objs, uint32_t* nodes, float* aabbs,
+                     int32_t* iesc, int32_t* eesc, int32_t* unique) {
+  Lbvh& b = *static_cast<Lbvh*>(h);
+  export_bvh(b, morton, objs, nodes, aabbs, iesc, eesc);
+  if (unique) *unique = b.morton_unique ? 1 : 0;
+}
+void orc_lbvh_query(void* h, int kind, const float* q, uint32_t n, uint32_t* counts,
+                    uint32_t* cands) {
+  Lbvh& b = *static_cast<Lbvh*>(h);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (long i = 0; i < (long)n; ++i) {
+    uint32_t* out = cands + (size_t)i * kMaxBuffer;
+    uint32_t c = 0;
+    if (kind == 0) {
+      c = b.query_point(V3{q[i * 3], q[i * 3 + 1], q[i * 3 + 2]}, out);
+    } else if (kind == 1) {
+      const float* s = q + (size_t)i * 6;
+      c = b.query_segment(V3{s[0], s[1], s[2]}, V3{s[3], s[4], s[5]}, out);
+    } else {
+      const float* s = q + (size_t)i * 6;
+      Box bx;
+      bx.lo = V3{s[0], s[1], s[2]};
+      bx.hi = V3{s[3], s[4], s[5]};
+      c = b.query_box(bx, out);
+    }
+    counts[i] = c;
+  }
+}
+
+// ---- primitive KATs ----------------------------------------------------------------------------
+uint32_t orc_expand_bits(uint32_t v) { return expand_bits(v); }
+uint32_t orc_morton_code(const float* p) { return morton_code(V3{p[0], p[1], p[2]}); }
+float orc_nearest_point(const float* p, const float* tri, float* qs, float* uvw) {
+  V3 q;
+  float u, v, w;
+  float d = nearest_point(V3{p[0], p[1], p[2]}, V3{tri[0], tri[1], tri[2]},
+                          V3{tri[3], tri[4], tri[5]}, V3{tri[6], tri[7], tri[8]}, q, u, v, w);
+  qs[0] = q.x; qs[1] = q.y; qs[2] = q.z;
+  uvw[0] = u; uvw[1] = v; uvw[2] = w;
+  return d;
+}
+float orc_ray_intersect(const float* o, const float* d, float len, const float* tri) {
+  return ray_intersect(V3{o[0], o[1], o[2]}, V3{d[0], d[1], d[2]}, len, V3{tri[0], tri[1], tri[2]},
+                       V3{tri[3], tri[4], tri[5]}, V3{tri[6], tri[7], tri[8]});
+}
+float orc_closest_seg_seg(const float* p1, const float* q1, const float* p2, const float* q2,
+                          float* st, float* c1c2) {
+  V3 c1, c2;
+  float s, t;
+  float d = closest_pt_segment_segment(V3{p1[0], p1[1], p1[2]}, V3{q1[0], q1[1], q1[2]},
+                                       V3{p2[0], p2[1], p2[2]}, V3{q2[0], q2[1], q2[2]}, s, t, c1,
+                                       c2);
+  st[0] = s; st[1] = t;
+  c1c2[0] = c1.x; c1c2[1] = c1.y; c1c2[2] = c1.z;
+  c1c2[3] = c2.x; c1c2[4] = c2.y; c1c2[5] = c2.z;
+  return d;
+}
+int orc_solve_cubic(float a, float b, float c, float d, float* x) { return solve_cubic(a, b, c, d, x); }
+
+}  // extern "C"

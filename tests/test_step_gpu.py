@@ -1,0 +1,201 @@
+"""Parity of the Swift frame on the GPU against the CPU oracle.
+
+Tolerance (north-star): positions after a frame within 1e-4 of the cloth's bounding-box diagonal.
+Without bending every operation on the path is an IEEE +,-,*,/,sqrt or floor in the same order on
+both sides, so those frames must match bit for bit; with bending the device acosf and the host
+acosf may differ in the last place, so those frames are held to the tolerance."""
+import numpy as np
+import pytest
+
+from tests.helpers import bits, diag, make_pair, small_scene, tube_mesh
+from xrtailor_gb300 import ClothSolver, XrtError, scenes
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+def _params(**kw):
+    base = dict(num_substeps=4, num_iterations=5, stretch_compliance=1e-8, bend_compliance=1e-6,
+                num_collision_passes=4)
+    base.update(kw)
+    return scenes._params(**base)
+
+
+def _close(g, o, exact):
+    xg, xo = g.host_positions(), o.host_positions()
+    assert np.isfinite(xg).all()
+    if exact:
+        np.testing.assert_array_equal(bits(xg), bits(xo))
+    err = np.abs(xg.astype(np.float64) - xo).max()
+    assert err <= TOL * diag(xo), (err, diag(xo))
+    return err
+
+
+def test_setup_exports_match_oracle(xrt):
+    cloth, obs = small_scene(20, attached=[0, 19, 210])
+    g, o = make_pair(_params(), [cloth], [obs], colors_from_gpu=False)
+    e1, r1 = g.edges()
+    e2, r2 = o.edges()
+    np.testing.assert_array_equal(e1, e2)
+    np.testing.assert_array_equal(bits(r1), bits(r2))
+    b1, t1 = g.bends()
+    b2, t2 = o.bends()
+    np.testing.assert_array_equal(b1, b2)
+    np.testing.assert_array_equal(bits(t1), bits(t2))
+    for k in (0, 1):  # both sides color greedily in constraint order
+        np.testing.assert_array_equal(g.coloring(k), o.coloring(k))
+        assert o.coloring_valid(k)
+    for a, b in zip(g.lra(), o.lra()):
+        np.testing.assert_array_equal(np.asarray(a).view(np.uint32), np.asarray(b).view(np.uint32))
+    np.testing.assert_array_equal(g.obstacle_rtri(), o.obstacle_rtri())
+    s = g.sizes()
+    assert (s.num_edges, s.num_bends, s.num_lra) == (len(e2), len(b2), 3 * 400)
+    assert abs(s.particle_diameter - o.particle_diameter()) == 0
+
+
+@pytest.mark.parametrize("self_collision", [0, 1])
+def test_frame_bit_exact_without_bending(xrt, self_collision):
+    cloth, obs = small_scene(16)
+    p = _params(solve_bending=0, enable_self_collision=self_collision)
+    g, o = make_pair(p, [cloth], [obs], particle_diameter=0.02)
+    for f in range(3):
+        g.step()
+        o.step()
+        _close(g, o, exact=True)
+    np.testing.assert_array_equal(bits(g.host_velocities()), bits(o.host_velocities()))
+    np.testing.assert_array_equal(bits(g.host_normals()), bits(o.host_normals()))
+    g.synchronize()
+
+
+def test_contacts_and_bvh_match_oracle(xrt):
+    cloth, obs = small_scene(24)
+    p = _params(solve_bending=0, enable_self_collision=1, num_substeps=2, num_iterations=3)
+    g, o = make_pair(p, [cloth], [obs], particle_diameter=0.02)
+    for _ in range(8):  # fall onto the sphere
+        g.step()
+        o.step()
+    _close(g, o, exact=True)
+    cg, co = g.export_contacts(), o.export_contacts()
+    for k in ("vf_index", "rt_index"):
+        np.testing.assert_array_equal(cg[k], co[k])
+    for k in ("vf_qs", "rt_qc", "ee"):
+        np.testing.assert_array_equal(bits(cg[k]), bits(co[k]))
+    assert (cg["vf_index"] >= 0).sum() > 0
+    bg, bo = g.export_obstacle_bvh(), o.export_obstacle_bvh()
+    for k in ("morton", "objects", "nodes", "iesc", "eesc"):
+        np.testing.assert_array_equal(bg[k], bo[k])
+    np.testing.assert_array_equal(bits(bg["aabbs"]), bits(bo["aabbs"]))
+    np.testing.assert_array_equal(g.export_neighbors(), o.export_neighbors())
+
+
+def test_frame_with_bending_within_tolerance(xrt):
+    cloth, obs = small_scene(16)
+    g, o = make_pair(_params(), [cloth], [obs], particle_diameter=0.02)
+    for _ in range(2):
+        g.step()
+        o.step()
+        _close(g, o, exact=False)
+
+
+def test_small_config_one_frame(xrt):
+    sc = scenes.plain_small(64)
+    p = scenes.scene_params(sc)
+    g, o = make_pair(p, [sc.cloth], [sc.obstacle], particle_diameter=sc.particle_diameter)
+    g.step()
+    o.step()
+    _close(g, o, exact=False)
+
+
+@pytest.mark.parametrize("pinned_slots", [True, False])
+def test_long_range_attachments(xrt, pinned_slots):
+    cloth, obs = small_scene(16, attached=[0, 15], pins=pinned_slots)
+    p = _params(solve_bending=0, enable_self_collision=0, long_range_stretchiness=1.02)
+    g, o = make_pair(p, [cloth], [obs])
+    for _ in range(3):
+        g.step()
+        o.step()
+        _close(g, o, exact=True)
+
+
+def test_moving_obstacle_and_bindings(xrt):
+    body = tube_mesh()
+    cloth, _ = small_scene(12)
+    # bind four cloth vertices to body triangles
+    tris = body.triangles[:4]
+    cloth.binded_indices = np.array([30, 40, 50, 60], np.uint32)
+    cloth.bind_obstacle_tri = tris.astype(np.uint32)
+    cloth.bind_barycentric = np.tile(np.array([[0.2, 0.3, 0.5]], np.float32), (4, 1))
+    cloth.bind_stiffnesses = np.full(4, 0.5, np.float32)
+    cloth.bind_distances = np.zeros(4, np.float32)
+    p = _params(solve_bending=0, enable_self_collision=1)
+    g, o = make_pair(p, [cloth], [body.mesh], particle_diameter=0.02)
+    for f in range(4):
+        tgt = body.pose((f + 1) / 60.0)
+        g.set_obstacle_targets(tgt)
+        o.set_obstacle_targets(tgt)
+        g.step()
+        o.step()
+        _close(g, o, exact=True)
+    np.testing.assert_array_equal(bits(g.obstacle_positions()), bits(o.obstacle_positions()))
+
+
+def test_multiple_cloths_and_obstacles(xrt):
+    c1, o1 = small_scene(10, seed=3)
+    c2, _ = small_scene(8, seed=4, size=0.6)
+    o2 = scenes.ground_plane(6, 2.0, height=-0.5, center=(0.5, 0.5))
+    p = _params(solve_bending=0)
+    g, o = make_pair(p, [c1, c2], [o1, o2], particle_diameter=0.02)
+    for _ in range(2):
+        g.step()
+        o.step()
+        _close(g, o, exact=True)
+
+
+def test_no_obstacle(xrt):
+    cloth, _ = small_scene(16, obstacle=None)
+    p = _params(solve_bending=0, enable_self_collision=0)
+    g, o = make_pair(p, [cloth], [])
+    for _ in range(3):
+        g.step()
+        o.step()
+        _close(g, o, exact=True)
+
+
+def test_graph_replay_equals_eager(xrt):
+    cloth, obs = small_scene(16)
+    p = _params(enable_self_collision=1)
+    a = ClothSolver(p)
+    b = ClothSolver(p)
+    for s in (a, b):
+        s.add_cloth(cloth, particle_diameter=0.02)
+        s.add_obstacle(obs)
+        s.start()
+    b.set_graph_mode(False)
+    for _ in range(3):
+        a.step()
+        b.step()
+    np.testing.assert_array_equal(bits(a.host_positions()), bits(b.host_positions()))
+    assert a.sizes().launches_per_frame > 0
+
+
+def test_invalid_inputs_are_rejected(xrt):
+    cloth, obs = small_scene(8)
+    bad = _params(num_substeps=1, num_iterations=2, num_collision_passes=3)
+    with pytest.raises(XrtError):
+        ClothSolver(bad)
+    s = ClothSolver(_params())
+    broken = scenes.grid_cloth(4, 1.0)
+    broken.triangles = broken.triangles.copy()
+    broken.triangles[0, 0] = 99
+    with pytest.raises(XrtError):
+        s.add_cloth(broken)
+    s.add_cloth(cloth)
+    e, _ = s.edges()
+    s.set_coloring(0, np.zeros(len(e), np.uint32))  # every edge the same color: not independent
+    with pytest.raises(XrtError):
+        s.start()
+    t = ClothSolver(_params())
+    t.add_cloth(cloth)
+    t.start()
+    with pytest.raises(XrtError):
+        t.add_obstacle(obs)

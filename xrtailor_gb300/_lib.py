@@ -1,0 +1,213 @@
+"""ctypes bindings of libxrt.so (the C ABI declared in include/xrt.h).
+
+The structs below mirror include/xrt.h field for field.  Loading fails loudly when the library
+has not been built: there is no Python or CPU fallback for any product entry point.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libxrt.so")
+
+XRT_OK = 0
+XRT_ERR_INVALID_CONFIG = 1001
+XRT_ERR_INVALID_MESH = 1002
+XRT_ERR_INVALID_ARGUMENT = 1003
+XRT_ERR_STATE = 1004
+XRT_ERR_CUDA = 8000
+XRT_ERR_NODE_CAPACITY = 8001
+XRT_ERR_EDGE_CAPACITY = 8003
+XRT_ERR_FACE_CAPACITY = 8004
+XRT_ERR_DEVICE_FLAG = 8100
+XRT_ERR_NO_DEVICE = 8200
+XRT_ERR_COLORING = 8300
+
+
+class SwiftParams(C.Structure):
+    _fields_ = [
+        ("num_substeps", C.c_int32),
+        ("num_iterations", C.c_int32),
+        ("max_speed", C.c_float),
+        ("gravity", C.c_float * 3),
+        ("damping", C.c_float),
+        ("stretch_compliance", C.c_float),
+        ("bend_compliance", C.c_float),
+        ("relaxation_factor", C.c_float),
+        ("long_range_stretchiness", C.c_float),
+        ("geodesic_lra", C.c_int32),
+        ("solve_bending", C.c_int32),
+        ("num_collision_passes", C.c_int32),
+        ("sdf_collision_margin", C.c_float),
+        ("bvh_tolerance", C.c_float),
+        ("friction", C.c_float),
+        ("max_neighbor_size", C.c_int32),
+        ("inter_leaved_hash", C.c_int32),
+        ("enable_self_collision", C.c_int32),
+        ("particle_diameter", C.c_float),
+        ("hash_cell_size", C.c_float),
+        ("frame_time", C.c_float),
+        ("update_obstacle_animation", C.c_int32),
+        ("reserved", C.c_int32 * 8),
+    ]
+
+
+class ClothDesc(C.Structure):
+    _fields_ = [
+        ("positions", C.POINTER(C.c_float)),
+        ("num_vertices", C.c_uint32),
+        ("triangles", C.POINTER(C.c_uint32)),
+        ("num_triangles", C.c_uint32),
+        ("model_matrix", C.POINTER(C.c_float)),
+        ("fixed_indices", C.POINTER(C.c_uint32)),
+        ("num_fixed", C.c_uint32),
+        ("attached_indices", C.POINTER(C.c_uint32)),
+        ("num_attached", C.c_uint32),
+        ("binded_indices", C.POINTER(C.c_uint32)),
+        ("bind_stiffnesses", C.POINTER(C.c_float)),
+        ("bind_distances", C.POINTER(C.c_float)),
+        ("bind_obstacle_tri", C.POINTER(C.c_uint32)),
+        ("bind_barycentric", C.POINTER(C.c_float)),
+        ("num_binded", C.c_uint32),
+        ("particle_diameter", C.c_float),
+    ]
+
+
+class ObstacleDesc(C.Structure):
+    _fields_ = [
+        ("positions", C.POINTER(C.c_float)),
+        ("num_vertices", C.c_uint32),
+        ("triangles", C.POINTER(C.c_uint32)),
+        ("num_triangles", C.c_uint32),
+        ("model_matrix", C.POINTER(C.c_float)),
+    ]
+
+
+class Sizes(C.Structure):
+    _fields_ = [
+        ("num_vertices", C.c_uint32), ("num_edges", C.c_uint32), ("num_triangles", C.c_uint32),
+        ("num_bends", C.c_uint32), ("num_lra", C.c_uint32), ("num_bindings", C.c_uint32),
+        ("num_obstacle_vertices", C.c_uint32), ("num_obstacle_triangles", C.c_uint32),
+        ("num_stretch_colors", C.c_uint32), ("num_bend_colors", C.c_uint32),
+        ("launches_per_frame", C.c_uint32), ("frame_index", C.c_uint32),
+        ("particle_diameter", C.c_float), ("reserved", C.c_uint32 * 7),
+    ]
+
+
+class Profile(C.Structure):
+    _fields_ = [("ms", C.c_double * 16), ("launches", C.c_uint64 * 16), ("units", C.c_uint64 * 16),
+                ("frames", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+
+
+PHASES = ["predict_finalize", "hash", "collide", "bvh_build", "obstacle_pass", "generate",
+          "stretch", "bend", "lra", "vf_solve", "ee_apply", "obstacle_commit"]
+
+# name -> (restype, argtypes); every symbol declared in include/xrt.h
+P = C.c_void_p
+FP = C.POINTER(C.c_float)
+UP = C.POINTER(C.c_uint32)
+IP = C.POINTER(C.c_int32)
+SIGNATURES = {
+    "xrt_get_version": (C.c_int32, [IP]),
+    "xrt_default_params": (C.c_int32, [C.POINTER(SwiftParams)]),
+    "xrt_create": (C.c_int32, [C.POINTER(P), C.c_int32]),
+    "xrt_destroy": (C.c_int32, [P]),
+    "xrt_last_error": (C.c_char_p, [P]),
+    "xrt_set_params": (C.c_int32, [P, C.POINTER(SwiftParams)]),
+    "xrt_add_cloth": (C.c_int32, [P, C.POINTER(ClothDesc), IP]),
+    "xrt_add_obstacle": (C.c_int32, [P, C.POINTER(ObstacleDesc), IP]),
+    "xrt_set_coloring": (C.c_int32, [P, C.c_int32, UP, C.c_uint32]),
+    "xrt_set_compliance": (C.c_int32, [P, C.c_int32, FP, C.c_uint32]),
+    "xrt_set_inv_mass": (C.c_int32, [P, FP, C.c_uint32]),
+    "xrt_start": (C.c_int32, [P]),
+    "xrt_set_obstacle_targets": (C.c_int32, [P, FP]),
+    "xrt_set_obstacle_targets_device": (C.c_int32, [P, P]),
+    "xrt_step_frame": (C.c_int32, [P]),
+    "xrt_step_frames": (C.c_int32, [P, C.c_int32]),
+    "xrt_synchronize": (C.c_int32, [P]),
+    "xrt_set_graph_mode": (C.c_int32, [P, C.c_int32]),
+    "xrt_get_sizes": (C.c_int32, [P, C.POINTER(Sizes)]),
+    "xrt_set_profiling": (C.c_int32, [P, C.c_int32]),
+    "xrt_get_profile": (C.c_int32, [P, C.POINTER(Profile)]),
+    "xrt_phase_name": (C.c_char_p, [C.c_int32]),
+    "xrt_get_positions": (C.c_int32, [P, FP]),
+    "xrt_get_velocities": (C.c_int32, [P, FP]),
+    "xrt_get_normals": (C.c_int32, [P, FP]),
+    "xrt_get_obstacle_positions": (C.c_int32, [P, FP]),
+    "xrt_get_obstacle_normals": (C.c_int32, [P, FP]),
+    "xrt_set_state": (C.c_int32, [P, FP, FP]),
+    "xrt_get_device_state": (C.c_int32, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
+    "xrt_get_edges": (C.c_int32, [P, UP, FP]),
+    "xrt_get_bends": (C.c_int32, [P, UP, FP]),
+    "xrt_get_coloring": (C.c_int32, [P, C.c_int32, UP]),
+    "xrt_get_lra": (C.c_int32, [P, UP, UP, FP]),
+    "xrt_get_obstacle_rtri": (C.c_int32, [P, UP]),
+    "xrt_export_obstacle_bvh": (C.c_int32, [P, UP, UP, UP, FP, IP, IP]),
+    "xrt_export_contacts": (C.c_int32, [P, IP, FP, IP, FP, FP]),
+    "xrt_export_neighbors": (C.c_int32, [P, UP]),
+    "xrt_lbvh_create": (C.c_int32, [C.POINTER(P), C.c_int32]),
+    "xrt_lbvh_destroy": (C.c_int32, [P]),
+    "xrt_lbvh_build": (C.c_int32, [P, FP, FP, C.c_uint32, C.c_float]),
+    "xrt_lbvh_build_device": (C.c_int32, [P, P, P, C.c_uint32, C.c_float, P]),
+    "xrt_lbvh_refit": (C.c_int32, [P, FP, C.c_uint32]),
+    "xrt_lbvh_refit_device": (C.c_int32, [P, P, C.c_uint32, P]),
+    "xrt_lbvh_export": (C.c_int32, [P, UP, UP, UP, FP, IP, IP, IP]),
+    "xrt_lbvh_query": (C.c_int32, [P, C.c_int32, FP, C.c_uint32, UP, UP]),
+    "xrt_lbvh_sizes": (C.c_int32, [P, UP]),
+}
+
+_lib = None
+
+
+def load():
+    """Loads libxrt.so; raises if it was not built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with "
+                           "`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class XrtError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"xrt status {code}: {msg}")
+        self.code = code
+
+
+def check(code, ctx=None, what=""):
+    if code != XRT_OK:
+        msg = ""
+        if ctx:
+            raw = load().xrt_last_error(ctx)
+            msg = raw.decode() if raw else ""
+        raise XrtError(code, f"{what}: {msg}")
+
+
+def fptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(FP)
+
+
+def uptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.uint32 and a.flags.c_contiguous
+    return a.ctypes.data_as(UP)
+
+
+def iptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(IP)

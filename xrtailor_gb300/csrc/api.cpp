@@ -1,0 +1,1273 @@
+// api.cpp — the C ABI (include/xrt.h): setup, the per-frame launch sequence of
+// ClothSolverBase::SimulateSwift (src/pipeline/base/ClothSolverBase.cpp:171-261), CUDA-graph
+// replay of frames, state and parity exports, and the standalone LBVH.
+//
+// Every entry point returns a status and never exits; CUDA failures become XRT_ERR_CUDA with the
+// CUDA message in xrt_last_error.  The product path has no CPU fallback: without a device of the
+// architecture this library was compiled for, xrt_create fails with XRT_ERR_NO_DEVICE.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/xrt.h"
+#include "context.h"
+#include "setup.h"
+
+using xrt::ColorRange;
+using xrt::Context;
+using xrt::DBuf;
+
+struct xrt_ctx {
+  Context c;
+};
+
+struct xrt_lbvh {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  xrt::Lbvh b;
+  DBuf<float> staging;
+  DBuf<uint32_t> err;
+  std::string last_error;
+};
+
+namespace {
+
+#define XRT_CUDA(ctxp, expr)                                                          \
+  do {                                                                                \
+    cudaError_t e_ = (expr);                                                          \
+    if (e_ != cudaSuccess) {                                                          \
+      (ctxp)->set_error(std::string(#expr) + ": " + cudaGetErrorString(e_));          \
+      return XRT_ERR_CUDA;                                                            \
+    }                                                                                 \
+  } while (0)
+
+xrt_status check_device(int device, std::string& why) {
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    why = std::string("no CUDA device: ") + cudaGetErrorString(e);
+    return XRT_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= count) {
+    why = "device index out of range";
+    return XRT_ERR_NO_DEVICE;
+  }
+  cudaFuncAttributes attr;
+  (void)attr;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+    why = "cudaGetDeviceProperties failed";
+    return XRT_ERR_NO_DEVICE;
+  }
+  if (prop.major != 10 || prop.minor != 3) {
+    why = "this library is built for sm_103a (GB300); device is sm_" + std::to_string(prop.major) +
+          std::to_string(prop.minor);
+    return XRT_ERR_NO_DEVICE;
+  }
+  return XRT_OK;
+}
+
+template <typename T>
+cudaError_t upload(DBuf<T>& d, const std::vector<T>& h, cudaStream_t s) {
+  cudaError_t e = d.reserve(h.empty() ? 1 : h.size());
+  if (e != cudaSuccess || h.empty()) return e;
+  return cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+std::vector<float4> to_f4(const std::vector<float>& xyz, const std::vector<float>* w) {
+  const size_t n = xyz.size() / 3;
+  std::vector<float4> out(n);
+  for (size_t i = 0; i < n; ++i)
+    out[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], w ? (*w)[i] : 0.0f);
+  return out;
+}
+
+xrt_status validate_params(const xrt_swift_params& p, std::string& why) {
+  if (p.num_substeps < 1) why = "num_substeps must be >= 1";
+  else if (p.num_iterations < 1) why = "num_iterations must be >= 1";
+  else if (p.num_collision_passes < 1) why = "num_collision_passes must be >= 1";
+  else if (p.num_collision_passes > p.num_substeps * p.num_iterations)
+    why = "num_collision_passes exceeds num_substeps * num_iterations (the reference divides by zero)";
+  else if (p.inter_leaved_hash < 1) why = "inter_leaved_hash must be >= 1";
+  else if (p.max_neighbor_size < 1) why = "max_neighbor_size must be >= 1";
+  else if (!(p.frame_time > 0.0f)) why = "frame_time must be > 0";
+  else if (!(p.hash_cell_size > 0.0f)) why = "hash_cell_size must be > 0";
+  else return XRT_OK;
+  return XRT_ERR_INVALID_CONFIG;
+}
+
+xrt::FrameConst frame_const(const Context& c) {
+  const xrt_swift_params& p = c.params;
+  xrt::FrameConst k;
+  k.dt = p.frame_time / (float)p.num_substeps;
+  k.gx = p.gravity[0];
+  k.gy = p.gravity[1];
+  k.gz = p.gravity[2];
+  k.damping = p.damping;
+  k.relaxation = p.relaxation_factor;
+  k.lra_stretch = p.long_range_stretchiness;
+  k.friction = p.friction;
+  k.particle_diameter = c.particle_diameter;
+  return k;
+}
+
+enum Phase {
+  kPredict = 0, kHash, kCollide, kBvhBuild, kObstaclePass, kGenerate, kStretch, kBend, kLra,
+  kVfSolve, kEeApply, kObstacleCommit
+};
+const char* const kPhaseNames[XRT_NUM_PHASES] = {
+    "predict_finalize", "hash", "collide", "bvh_build", "obstacle_pass", "generate",
+    "stretch", "bend", "lra", "vf_solve", "ee_apply", "obstacle_commit"};
+
+// CUDA-event pair around one launch group when profiling (eager frames only).
+struct Timed {
+  Context& c;
+  size_t idx = (size_t)-1;
+  Timed(Context& ctx, int phase, uint32_t kernels, uint64_t units) : c(ctx) {
+    if (!c.profiling) return;
+    if (c.prof_used == c.prof_events.size()) {
+      Context::ProfEvent e{};
+      cudaEventCreate(&e.a);
+      cudaEventCreate(&e.b);
+      c.prof_events.push_back(e);
+    }
+    idx = c.prof_used++;
+    Context::ProfEvent& e = c.prof_events[idx];
+    e.phase = phase;
+    e.kernels = kernels;
+    e.units = units;
+    cudaEventRecord(e.a, c.stream);
+  }
+  ~Timed() {
+    if (idx != (size_t)-1) cudaEventRecord(c.prof_events[idx].b, c.stream);
+  }
+};
+
+void collect_profile(Context& c) {
+  if (!c.profiling) return;
+  cudaStreamSynchronize(c.stream);
+  for (size_t i = 0; i < c.prof_used; ++i) {
+    const Context::ProfEvent& e = c.prof_events[i];
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e.a, e.b);
+    c.prof_ms[e.phase] += ms;
+    c.prof_launches[e.phase] += e.kernels;
+    c.prof_units[e.phase] += e.units;
+  }
+  c.prof_used = 0;
+  c.prof_frames++;
+}
+
+// The launch sequence of one frame (ClothSolverBase::SimulateSwift, ClothSolverBase.cpp:171-261).
+void record_frame(Context& c) {
+  const xrt_swift_params& p = c.params;
+  const xrt::FrameConst k = frame_const(c);
+  float4* const x_start = c.x.p;
+  int swaps = 0;
+  auto swap_x = [&]() {
+    std::swap(c.x.p, c.x_alt.p);
+    ++swaps;
+  };
+  const bool obstacle_updated = p.update_obstacle_animation && c.onf > 0;
+  if (obstacle_updated) {  // UpdateObstacleAnimationFrame: UpdateData(tol 0) + Construct()
+    Timed t(c, kBvhBuild, 19, c.onf);
+    xrt::launch_prims_obstacle(c, 0.0f);
+    c.bvh.construct(0.0f, c.stream, c.err.p);
+  }
+  const bool has_obstacle = c.onf > 0;
+  const bool bindings = c.nbind > 0;
+  const int frequency = (p.num_substeps * p.num_iterations) / p.num_collision_passes;
+  int cnt = 0;
+  for (int s = 0; s < p.num_substeps; ++s) {
+    if (s == 0) {
+      Timed t(c, kPredict, 1, c.nv);
+      xrt::launch_predict(c, k);
+    }
+    if (p.enable_self_collision && s % p.inter_leaved_hash == 0) {
+      Timed t(c, kHash, 13, c.nv);
+      xrt::launch_hash(c);
+    }
+    for (int it = 0; it < p.num_iterations; ++it) {
+      if (p.enable_self_collision) {
+        {
+          Timed t(c, kCollide, 1, c.nv);
+          xrt::launch_collide(c, k);
+        }
+        swap_x();
+      }
+      const int current = s * p.num_iterations + it;
+      if (current % frequency == 0) {
+        if (obstacle_updated) {
+          Timed t(c, kObstaclePass, 2, c.onv);
+          xrt::launch_obstacle_pass(c, cnt, p.num_collision_passes);
+        }
+        if (has_obstacle) {
+          Timed t(c, kGenerate, 2, c.nv + c.ne);
+          xrt::launch_generate_contacts(c);
+        }
+        cnt++;
+      }
+      for (const ColorRange& r : c.s_ranges) {
+        Timed t(c, kStretch, 1, r.end - r.begin);
+        xrt::launch_stretch(c, k, r, it == 0);
+      }
+      if (p.solve_bending)
+        for (const ColorRange& r : c.b_ranges) {
+          Timed t(c, kBend, 1, r.end - r.begin);
+          xrt::launch_bend(c, k, r);
+        }
+      if (p.geodesic_lra && c.nl) {
+        Timed t(c, kLra, c.lra_by_target ? 1 : (uint32_t)c.lra_blocks.size(), c.nl);
+        xrt::launch_lra(c, k);
+      }
+      if (has_obstacle) {
+        Timed t(c, kVfSolve, 1, c.nv);
+        xrt::launch_vf_solve(c);
+      }
+      if (has_obstacle || bindings) {
+        {
+          Timed t(c, kEeApply, 1, c.nv);
+          xrt::launch_ee_apply(c, k, has_obstacle, bindings);
+        }
+        swap_x();
+      }
+    }
+    const bool last = s + 1 == p.num_substeps;
+    Timed t(c, kPredict, 1, c.nv);
+    xrt::launch_finalize_predict(c, k, !last, last);
+  }
+  if (c.onv > 0) {
+    Timed t(c, kObstacleCommit, 1, c.onv);
+    xrt::launch_obstacle_commit(c);
+  }
+  if (swaps & 1) {  // keep the frame's state in the buffer a replayed graph starts from
+    cudaMemcpyAsync(x_start, c.x.p, sizeof(float4) * c.nv, cudaMemcpyDeviceToDevice, c.stream);
+    std::swap(c.x.p, c.x_alt.p);
+  }
+}
+
+xrt_status capture_frame(Context& c) {
+  if (c.graph_exec) {
+    cudaGraphExecDestroy(c.graph_exec);
+    c.graph_exec = nullptr;
+  }
+  cudaGraph_t graph = nullptr;
+  XRT_CUDA(&c, cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+  record_frame(c);
+  cudaError_t e = cudaStreamEndCapture(c.stream, &graph);
+  if (e != cudaSuccess) {
+    c.set_error(std::string("frame capture failed: ") + cudaGetErrorString(e));
+    return XRT_ERR_CUDA;
+  }
+  size_t num_nodes = 0;
+  cudaGraphGetNodes(graph, nullptr, &num_nodes);
+  std::vector<cudaGraphNode_t> nodes(num_nodes);
+  if (num_nodes) cudaGraphGetNodes(graph, nodes.data(), &num_nodes);
+  uint32_t kernels = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
+  }
+  c.launches_per_frame = kernels;
+  e = cudaGraphInstantiate(&c.graph_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    c.set_error(std::string("graph instantiate failed: ") + cudaGetErrorString(e));
+    c.graph_exec = nullptr;
+    return XRT_ERR_CUDA;
+  }
+  c.graph_dirty = false;
+  return XRT_OK;
+}
+
+xrt_status require_started(Context& c) {
+  if (!c.started) {
+    c.set_error("call xrt_start first");
+    return XRT_ERR_STATE;
+  }
+  return XRT_OK;
+}
+
+xrt_status read_f4(Context& c, const DBuf<float4>& d, uint32_t n, float* out) {
+  if (!out) {
+    c.set_error("null output pointer");
+    return XRT_ERR_INVALID_ARGUMENT;
+  }
+  std::vector<float4> h(n);
+  if (n) {
+    XRT_CUDA(&c, cudaMemcpyAsync(h.data(), d.p, n * sizeof(float4), cudaMemcpyDeviceToHost, c.stream));
+    XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  }
+  for (uint32_t i = 0; i < n; ++i) {
+    out[3 * i] = h[i].x;
+    out[3 * i + 1] = h[i].y;
+    out[3 * i + 2] = h[i].z;
+  }
+  return XRT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+xrt_status xrt_get_version(int32_t* v) {
+  if (!v) return XRT_ERR_INVALID_ARGUMENT;
+  *v = XRT_API_VERSION;
+  return XRT_OK;
+}
+
+xrt_status xrt_default_params(xrt_swift_params* p) {
+  if (!p) return XRT_ERR_INVALID_ARGUMENT;
+  std::memset(p, 0, sizeof(*p));
+  p->num_substeps = 1;
+  p->num_iterations = 200;
+  p->max_speed = 1e6f;
+  p->gravity[0] = 0.0f;
+  p->gravity[1] = -9.8f;
+  p->gravity[2] = 0.0f;
+  p->damping = 0.98f;
+  p->stretch_compliance = 0.0f;
+  p->bend_compliance = 1e2f;
+  p->relaxation_factor = 0.25f;
+  p->long_range_stretchiness = 1.1f;
+  p->geodesic_lra = 1;
+  p->solve_bending = 1;
+  p->num_collision_passes = 10;
+  p->sdf_collision_margin = 1e-2f;
+  p->bvh_tolerance = 0.003f;
+  p->friction = 0.1f;
+  p->max_neighbor_size = 64;
+  p->inter_leaved_hash = 3;
+  p->enable_self_collision = 1;
+  p->particle_diameter = 1.3f;
+  p->hash_cell_size = 1.5f;
+  p->frame_time = 1.0f / 60.0f;
+  p->update_obstacle_animation = 1;
+  return XRT_OK;
+}
+
+xrt_status xrt_create(xrt_ctx** out, int32_t device) {
+  if (!out) return XRT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  std::string why;
+  xrt_status st = check_device(device, why);
+  if (st != XRT_OK) return st;
+  xrt_ctx* h = new xrt_ctx();
+  Context& c = h->c;
+  c.device = device;
+  xrt_default_params(&c.params);
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess ||
+      c.err.reserve(1) != cudaSuccess || cudaMemset(c.err.p, 0, sizeof(uint32_t)) != cudaSuccess) {
+    delete h;
+    return XRT_ERR_CUDA;
+  }
+  *out = h;
+  return XRT_OK;
+}
+
+xrt_status xrt_destroy(xrt_ctx* h) {
+  if (!h) return XRT_OK;
+  Context& c = h->c;
+  cudaSetDevice(c.device);
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+  for (auto& e : c.prof_events) {
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  DBuf<float4>* f4[] = {&c.x, &c.x_alt, &c.x0, &c.v, &c.n, &c.x_init, &c.bind_a, &c.vf_qs,
+                        &c.rt_qc, &c.ee_a, &c.ee_b, &c.ee_c, &c.ox0, &c.ox, &c.ox1, &c.on, &c.on1};
+  for (auto* b : f4) b->release();
+  DBuf<uint32_t>* u[] = {&c.vf_ptr, &c.vf_list, &c.lra_ptr, &c.lra_src, &c.lra_l_src, &c.lra_l_tgt,
+                         &c.bind_ptr, &c.ve_ptr, &c.ve_list, &c.hash_key, &c.hash_val,
+                         &c.cell_start, &c.cell_end, &c.neighbors, &c.ovf_ptr, &c.ovf_list, &c.err};
+  for (auto* b : u) b->release();
+  c.tri.release(); c.s_con.release(); c.b_idx.release(); c.bind_b.release(); c.otri.release();
+  c.s_lambda.release(); c.lra_rest.release(); c.lra_l_rest.release(); c.b_tc.release();
+  c.edge.release(); c.vf_idx.release(); c.rt_idx.release();
+  c.hash_sorter.keys_tmp.release(); c.hash_sorter.vals_tmp.release(); c.hash_sorter.hist.release();
+  c.bvh.release();
+  if (c.stream) cudaStreamDestroy(c.stream);
+  delete h;
+  return XRT_OK;
+}
+
+const char* xrt_last_error(const xrt_ctx* h) { return h ? h->c.last_error.c_str() : "null context"; }
+
+xrt_status xrt_set_params(xrt_ctx* h, const xrt_swift_params* p) {
+  if (!h || !p) return XRT_ERR_INVALID_ARGUMENT;
+  std::string why;
+  if (validate_params(*p, why) != XRT_OK) {
+    h->c.set_error(why);
+    return XRT_ERR_INVALID_CONFIG;
+  }
+  h->c.params = *p;
+  h->c.graph_dirty = true;
+  return XRT_OK;
+}
+
+xrt_status xrt_add_cloth(xrt_ctx* h, const xrt_cloth_desc* d, int32_t* out_offset) {
+  if (!h || !d || !d->positions || !d->triangles) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (c.started) {
+    c.set_error("xrt_add_cloth after xrt_start");
+    return XRT_ERR_STATE;
+  }
+  if (d->num_vertices == 0 || d->num_triangles == 0) {
+    c.set_error("empty cloth mesh");
+    return XRT_ERR_INVALID_MESH;
+  }
+  const uint64_t total = (uint64_t)c.h_w.size() + d->num_vertices;
+  if (total >= (1ull << 30)) {
+    c.set_error("vertex count exceeds 2^30");
+    return XRT_ERR_NODE_CAPACITY;
+  }
+  for (uint64_t k = 0; k < 3ull * d->num_triangles; ++k)
+    if (d->triangles[k] >= d->num_vertices) {
+      c.set_error("triangle index out of range");
+      return XRT_ERR_INVALID_MESH;
+    }
+  auto check_list = [&](const uint32_t* l, uint32_t n, const char* what) {
+    if (n && !l) return std::string(what) + " pointer is null";
+    for (uint32_t i = 0; i < n; ++i)
+      if (l[i] >= d->num_vertices) return std::string(what) + " index out of range";
+    return std::string();
+  };
+  std::string why = check_list(d->fixed_indices, d->num_fixed, "fixed");
+  if (why.empty()) why = check_list(d->attached_indices, d->num_attached, "attached");
+  if (why.empty()) why = check_list(d->binded_indices, d->num_binded, "binded");
+  if (why.empty() && d->num_binded && (!d->bind_obstacle_tri || !d->bind_barycentric))
+    why = "binding needs bind_obstacle_tri and bind_barycentric";
+  if (!why.empty()) {
+    c.set_error(why);
+    return XRT_ERR_INVALID_MESH;
+  }
+  Context::HostCloth cl;
+  cl.offset = (uint32_t)c.h_w.size();
+  cl.mesh_pos.assign(d->positions, d->positions + 3 * (size_t)d->num_vertices);
+  cl.tri.assign(d->triangles, d->triangles + 3 * (size_t)d->num_triangles);
+  std::vector<xrt::setup::V3> pos(d->num_vertices);
+  for (uint32_t i = 0; i < d->num_vertices; ++i)
+    pos[i] = xrt::setup::V3{d->positions[3 * i], d->positions[3 * i + 1], d->positions[3 * i + 2]};
+  // InitializePositions (ClothSolverHelper.cu:113-123): x0 = model * p
+  for (uint32_t i = 0; i < d->num_vertices; ++i) {
+    xrt::setup::V3 q = pos[i];
+    if (d->model_matrix) q = xrt::setup::transform_point(d->model_matrix, q);
+    c.h_x0.push_back(q.x);
+    c.h_x0.push_back(q.y);
+    c.h_x0.push_back(q.z);
+    c.h_w.push_back(1.0f);  // PhysicsMeshHelper.cu:139: free nodes have inverse mass 1
+  }
+  for (uint32_t k = 0; k < 3 * d->num_triangles; ++k) c.h_tri.push_back(d->triangles[k] + cl.offset);
+  for (uint32_t i = 0; i < d->num_fixed; ++i) c.h_w[cl.offset + d->fixed_indices[i]] = 0.0f;
+  std::vector<uint32_t> e;
+  std::vector<std::vector<uint32_t>> ef;
+  xrt::setup::build_edges(cl.tri, e, ef);
+  for (size_t k = 0; k < e.size() / 2; ++k) {
+    c.h_edges.push_back(e[2 * k] + cl.offset);
+    c.h_edges.push_back(e[2 * k + 1] + cl.offset);
+    c.h_rest.push_back(xrt::setup::length(xrt::setup::sub(pos[e[2 * k]], pos[e[2 * k + 1]])));
+    c.h_scomp.push_back(c.params.stretch_compliance);
+  }
+  if (c.params.solve_bending) {
+    std::vector<uint32_t> b;
+    std::vector<float> th;
+    xrt::setup::build_bends(pos, cl.tri, e, ef, cl.offset, b, th);
+    c.h_bends.insert(c.h_bends.end(), b.begin(), b.end());
+    c.h_theta.insert(c.h_theta.end(), th.begin(), th.end());
+    c.h_bcomp.insert(c.h_bcomp.end(), th.size(), c.params.bend_compliance);
+  }
+  if (d->num_attached > 0 && c.params.geodesic_lra) {  // ClothObjectBase.cpp:79-93
+    std::vector<std::vector<uint32_t>> adj(d->num_vertices);
+    for (size_t k = 0; k < e.size() / 2; ++k) {
+      adj[e[2 * k]].push_back(e[2 * k + 1]);
+      adj[e[2 * k + 1]].push_back(e[2 * k]);
+    }
+    for (auto& a : adj) std::sort(a.begin(), a.end());
+    for (uint32_t s = 0; s < d->num_attached; ++s) {
+      const uint32_t slot = d->attached_indices[s];
+      const std::vector<float> dist = xrt::setup::geodesic(pos, adj, slot);
+      for (uint32_t v = 0; v < d->num_vertices; ++v) {
+        c.h_lra_src.push_back(slot + cl.offset);
+        c.h_lra_tgt.push_back(v + cl.offset);
+        c.h_lra_rest.push_back(dist[v]);
+      }
+    }
+  }
+  for (uint32_t i = 0; i < d->num_binded; ++i) {
+    Context::HostBinding b;
+    b.cloth = d->binded_indices[i] + cl.offset;
+    b.iu = d->bind_obstacle_tri[3 * i];
+    b.iv = d->bind_obstacle_tri[3 * i + 1];
+    b.iw = d->bind_obstacle_tri[3 * i + 2];
+    b.u = d->bind_barycentric[3 * i];
+    b.v = d->bind_barycentric[3 * i + 1];
+    b.w = d->bind_barycentric[3 * i + 2];
+    b.L = d->bind_distances ? d->bind_distances[i] : 0.0f;
+    b.stiffness = d->bind_stiffnesses ? d->bind_stiffnesses[i] : 1.0f;
+    c.h_bind.push_back(b);
+  }
+  // universal/ClothObject.hpp:36-37: first edge length x PARTICLE_DIAMETER; the last cloth wins
+  if (d->particle_diameter > 0.0f)
+    c.particle_diameter = d->particle_diameter;
+  else
+    c.particle_diameter =
+        xrt::setup::length(xrt::setup::sub(pos[cl.tri[0]], pos[cl.tri[1]])) * c.params.particle_diameter;
+  if (out_offset) *out_offset = (int32_t)cl.offset;
+  c.cloths.push_back(std::move(cl));
+  return XRT_OK;
+}
+
+xrt_status xrt_add_obstacle(xrt_ctx* h, const xrt_obstacle_desc* d, int32_t* out_offset) {
+  if (!h || !d || !d->positions || !d->triangles) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (c.started) {
+    c.set_error("xrt_add_obstacle after xrt_start");
+    return XRT_ERR_STATE;
+  }
+  for (uint64_t k = 0; k < 3ull * d->num_triangles; ++k)
+    if (d->triangles[k] >= d->num_vertices) {
+      c.set_error("obstacle triangle index out of range");
+      return XRT_ERR_INVALID_MESH;
+    }
+  const uint32_t off = (uint32_t)(c.h_ox0.size() / 3);
+  for (uint32_t i = 0; i < d->num_vertices; ++i) {
+    xrt::setup::V3 q{d->positions[3 * i], d->positions[3 * i + 1], d->positions[3 * i + 2]};
+    if (d->model_matrix) q = xrt::setup::transform_point(d->model_matrix, q);
+    c.h_ox0.push_back(q.x);
+    c.h_ox0.push_back(q.y);
+    c.h_ox0.push_back(q.z);
+  }
+  for (uint64_t k = 0; k < 3ull * d->num_triangles; ++k) c.h_otri.push_back(d->triangles[k] + off);
+  if (out_offset) *out_offset = (int32_t)off;
+  return XRT_OK;
+}
+
+xrt_status xrt_set_coloring(xrt_ctx* h, int32_t kind, const uint32_t* colors, uint32_t n) {
+  if (!h || (n && !colors) || (kind != 0 && kind != 1)) return XRT_ERR_INVALID_ARGUMENT;
+  if (h->c.started) {
+    h->c.set_error("xrt_set_coloring after xrt_start");
+    return XRT_ERR_STATE;
+  }
+  h->c.pending_colors[kind].assign(colors, colors + n);
+  return XRT_OK;
+}
+
+static xrt_status upload_constraints(Context& c);
+
+xrt_status xrt_set_compliance(xrt_ctx* h, int32_t kind, const float* comp, uint32_t n) {
+  if (!h || !comp || (kind != 0 && kind != 1)) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  std::vector<float>& dst = kind == 0 ? c.h_scomp : c.h_bcomp;
+  if (n != dst.size()) {
+    c.set_error("compliance count does not match the constraint count");
+    return XRT_ERR_INVALID_ARGUMENT;
+  }
+  dst.assign(comp, comp + n);
+  if (c.started) {
+    cudaSetDevice(c.device);
+    return upload_constraints(c);
+  }
+  return XRT_OK;
+}
+
+xrt_status xrt_set_inv_mass(xrt_ctx* h, const float* w, uint32_t n) {
+  if (!h || !w) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (n != c.h_w.size()) {
+    c.set_error("inverse-mass count does not match the vertex count");
+    return XRT_ERR_INVALID_ARGUMENT;
+  }
+  if (c.started) {
+    c.set_error("xrt_set_inv_mass after xrt_start");
+    return XRT_ERR_STATE;
+  }
+  c.h_w.assign(w, w + n);
+  return XRT_OK;
+}
+
+// Constraint arrays sorted by color (stable within a color).
+static xrt_status upload_constraints(Context& c) {
+  std::vector<int4> scon(c.ne);
+  for (uint32_t j = 0; j < c.ne; ++j) {
+    const uint32_t o = c.s_perm[j];
+    int4 v;
+    v.x = (int)c.h_edges[2 * o];
+    v.y = (int)c.h_edges[2 * o + 1];
+    std::memcpy(&v.z, &c.h_rest[o], 4);
+    std::memcpy(&v.w, &c.h_scomp[o], 4);
+    scon[j] = v;
+  }
+  std::vector<int4> bidx(c.nb);
+  std::vector<float2> btc(c.nb);
+  for (uint32_t j = 0; j < c.nb; ++j) {
+    const uint32_t o = c.b_perm[j];
+    bidx[j] = make_int4((int)c.h_bends[4 * o], (int)c.h_bends[4 * o + 1], (int)c.h_bends[4 * o + 2],
+                        (int)c.h_bends[4 * o + 3]);
+    btc[j] = make_float2(c.h_theta[o], c.h_bcomp[o]);
+  }
+  XRT_CUDA(&c, upload(c.s_con, scon, c.stream));
+  XRT_CUDA(&c, upload(c.b_idx, bidx, c.stream));
+  XRT_CUDA(&c, upload(c.b_tc, btc, c.stream));
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  return XRT_OK;
+}
+
+static void sort_by_color(const std::vector<uint32_t>& col, uint32_t ncolors,
+                          std::vector<uint32_t>& perm, std::vector<ColorRange>& ranges) {
+  perm.resize(col.size());
+  std::iota(perm.begin(), perm.end(), 0u);
+  std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) { return col[a] < col[b]; });
+  ranges.assign(ncolors, ColorRange{0, 0});
+  uint32_t j = 0;
+  for (uint32_t k = 0; k < ncolors; ++k) {
+    ranges[k].begin = j;
+    while (j < perm.size() && col[perm[j]] == k) ++j;
+    ranges[k].end = j;
+  }
+}
+
+xrt_status xrt_start(xrt_ctx* h) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (c.started) {
+    c.set_error("xrt_start called twice");
+    return XRT_ERR_STATE;
+  }
+  if (c.h_w.empty()) {
+    c.set_error("no cloth added");
+    return XRT_ERR_STATE;
+  }
+  cudaSetDevice(c.device);
+  c.nv = (uint32_t)c.h_w.size();
+  c.ne = (uint32_t)c.h_rest.size();
+  c.nf = (uint32_t)(c.h_tri.size() / 3);
+  c.nb = (uint32_t)c.h_theta.size();
+  c.nl = (uint32_t)c.h_lra_rest.size();
+  c.nbind = (uint32_t)c.h_bind.size();
+  c.onv = (uint32_t)(c.h_ox0.size() / 3);
+  c.onf = (uint32_t)(c.h_otri.size() / 3);
+  for (const auto& b : c.h_bind)
+    if (c.onv == 0 || b.iu >= c.onv || b.iv >= c.onv || b.iw >= c.onv) {
+      c.set_error("binding refers to a missing obstacle vertex");
+      return XRT_ERR_INVALID_MESH;
+    }
+  // coloring
+  for (int kind = 0; kind < 2; ++kind) {
+    const std::vector<uint32_t>& idx = kind == 0 ? c.h_edges : c.h_bends;
+    const int arity = kind == 0 ? 2 : 4;
+    std::vector<uint32_t>& col = kind == 0 ? c.h_scolor : c.h_bcolor;
+    uint32_t& nc = kind == 0 ? c.n_scolors : c.n_bcolors;
+    if (!c.pending_colors[kind].empty()) {
+      std::string why;
+      if (!xrt::setup::coloring_valid(idx, arity, c.pending_colors[kind], c.nv, why)) {
+        c.set_error("invalid coloring: " + why);
+        return XRT_ERR_COLORING;
+      }
+      col = c.pending_colors[kind];
+      nc = 0;
+      for (uint32_t v : col) nc = std::max(nc, v + 1);
+    } else {
+      col = xrt::setup::greedy_color(idx, arity, c.nv, nc);
+    }
+  }
+  sort_by_color(c.h_scolor, c.n_scolors, c.s_perm, c.s_ranges);
+  sort_by_color(c.h_bcolor, c.n_bcolors, c.b_perm, c.b_ranges);
+  xrt_status st = upload_constraints(c);
+  if (st != XRT_OK) return st;
+  XRT_CUDA(&c, c.s_lambda.reserve(std::max(c.ne, 1u)));
+  XRT_CUDA(&c, cudaMemsetAsync(c.s_lambda.p, 0, sizeof(float) * std::max(c.ne, 1u), c.stream));
+  // state
+  const std::vector<float4> x0 = to_f4(c.h_x0, &c.h_w);
+  std::vector<float4> x0_plain = to_f4(c.h_x0, nullptr);
+  XRT_CUDA(&c, upload(c.x, x0, c.stream));
+  XRT_CUDA(&c, upload(c.x_alt, x0, c.stream));
+  XRT_CUDA(&c, upload(c.x0, x0_plain, c.stream));
+  XRT_CUDA(&c, upload(c.x_init, x0_plain, c.stream));  // SpatialHashGPU::SetInitialPositions
+  XRT_CUDA(&c, c.v.reserve(c.nv));
+  XRT_CUDA(&c, cudaMemsetAsync(c.v.p, 0, sizeof(float4) * c.nv, c.stream));
+  XRT_CUDA(&c, c.n.reserve(c.nv));
+  // topology
+  std::vector<int4> tri(c.nf);
+  for (uint32_t f = 0; f < c.nf; ++f)
+    tri[f] = make_int4((int)c.h_tri[3 * f], (int)c.h_tri[3 * f + 1], (int)c.h_tri[3 * f + 2], 0);
+  XRT_CUDA(&c, upload(c.tri, tri, c.stream));
+  std::vector<uint32_t> ptr, list;
+  xrt::setup::build_vf(c.h_tri, c.nv, ptr, list);
+  XRT_CUDA(&c, upload(c.vf_ptr, ptr, c.stream));
+  XRT_CUDA(&c, upload(c.vf_list, list, c.stream));
+  std::vector<uint2> edge(c.ne);
+  for (uint32_t e = 0; e < c.ne; ++e) edge[e] = make_uint2(c.h_edges[2 * e], c.h_edges[2 * e + 1]);
+  XRT_CUDA(&c, upload(c.edge, edge, c.stream));
+  xrt::setup::build_ve(c.h_edges, c.nv, ptr, list);
+  XRT_CUDA(&c, upload(c.ve_ptr, ptr, c.stream));
+  XRT_CUDA(&c, upload(c.ve_list, list, c.stream));
+  xrt::launch_vertex_normals(c.x0.p, c.tri.p, c.vf_ptr.p, c.vf_list.p, c.n.p, c.nv, c.stream);
+  // LRA: by target when every slot vertex is pinned, else slot-major blocks
+  {
+    c.lra_by_target = true;
+    for (uint32_t k = 0; k < c.nl; ++k)
+      if (c.h_w[c.h_lra_src[k]] > 0.0f) c.lra_by_target = false;
+    std::vector<uint32_t> lptr(c.nv + 1, 0), lsrc(c.nl);
+    std::vector<float> lrest(c.nl);
+    for (uint32_t k = 0; k < c.nl; ++k) lptr[c.h_lra_tgt[k] + 1]++;
+    for (uint32_t i = 0; i < c.nv; ++i) lptr[i + 1] += lptr[i];
+    std::vector<uint32_t> fill(lptr.begin(), lptr.end() - 1);
+    for (uint32_t k = 0; k < c.nl; ++k) {
+      const uint32_t pos = fill[c.h_lra_tgt[k]]++;
+      lsrc[pos] = c.h_lra_src[k];
+      lrest[pos] = c.h_lra_rest[k];
+    }
+    XRT_CUDA(&c, upload(c.lra_ptr, lptr, c.stream));
+    XRT_CUDA(&c, upload(c.lra_src, lsrc, c.stream));
+    XRT_CUDA(&c, upload(c.lra_rest, lrest, c.stream));
+    c.lra_blocks.clear();
+    if (!c.lra_by_target) {
+      XRT_CUDA(&c, upload(c.lra_l_src, c.h_lra_src, c.stream));
+      XRT_CUDA(&c, upload(c.lra_l_tgt, c.h_lra_tgt, c.stream));
+      XRT_CUDA(&c, upload(c.lra_l_rest, c.h_lra_rest, c.stream));
+      uint32_t k = 0;
+      while (k < c.nl) {  // maximal runs of one source slot, in list order
+        uint32_t e = k;
+        while (e < c.nl && c.h_lra_src[e] == c.h_lra_src[k]) ++e;
+        c.lra_blocks.push_back(ColorRange{k, e});
+        k = e;
+      }
+    }
+  }
+  // contacts
+  XRT_CUDA(&c, c.vf_idx.reserve(c.nv));
+  XRT_CUDA(&c, c.rt_idx.reserve(c.nv));
+  XRT_CUDA(&c, c.vf_qs.reserve(c.nv));
+  XRT_CUDA(&c, c.rt_qc.reserve(c.nv));
+  XRT_CUDA(&c, c.ee_a.reserve(std::max(c.ne, 1u)));
+  XRT_CUDA(&c, c.ee_b.reserve(std::max(c.ne, 1u)));
+  XRT_CUDA(&c, c.ee_c.reserve(std::max(c.ne, 1u)));
+  XRT_CUDA(&c, cudaMemsetAsync(c.vf_idx.p, 0xFF, sizeof(int) * c.nv, c.stream));
+  XRT_CUDA(&c, cudaMemsetAsync(c.rt_idx.p, 0xFF, sizeof(int) * c.nv, c.stream));
+  XRT_CUDA(&c, cudaMemsetAsync(c.vf_qs.p, 0, sizeof(float4) * c.nv, c.stream));
+  XRT_CUDA(&c, cudaMemsetAsync(c.rt_qc.p, 0, sizeof(float4) * c.nv, c.stream));
+  {
+    std::vector<float4> ea(std::max(c.ne, 1u), make_float4(xrt::kScalarMaxHost, 0, 0, 0));
+    std::vector<float4> zero(std::max(c.ne, 1u), make_float4(0, 0, 0, 0));
+    XRT_CUDA(&c, upload(c.ee_a, ea, c.stream));
+    XRT_CUDA(&c, upload(c.ee_b, zero, c.stream));
+    XRT_CUDA(&c, upload(c.ee_c, zero, c.stream));
+  }
+  // particle hash
+  {
+    const uint32_t table = 2 * c.nv;
+    const size_t nbs = (size_t)c.nv * (size_t)c.params.max_neighbor_size;
+    XRT_CUDA(&c, c.hash_key.reserve(c.nv));
+    XRT_CUDA(&c, c.hash_val.reserve(c.nv));
+    XRT_CUDA(&c, c.cell_start.reserve(table));
+    XRT_CUDA(&c, c.cell_end.reserve(table));
+    XRT_CUDA(&c, c.neighbors.reserve(nbs));
+    XRT_CUDA(&c, cudaMemsetAsync(c.cell_end.p, 0, sizeof(uint32_t) * table, c.stream));
+    XRT_CUDA(&c, cudaMemsetAsync(c.neighbors.p, 0, sizeof(uint32_t) * nbs, c.stream));
+    XRT_CUDA(&c, c.hash_sorter.reserve(c.nv));
+  }
+  // bindings: GenerateBinding_Kernel (BindingConstraint.cu:20-44) rest lengths from x0
+  {
+    std::vector<uint32_t> bptr(c.nv + 1, 0);
+    for (auto& b : c.h_bind) {
+      if (b.L < 1e-6f) {
+        const float* po = c.h_ox0.data();
+        auto P = [&](uint32_t i) { return xrt::setup::V3{po[3 * i], po[3 * i + 1], po[3 * i + 2]}; };
+        const xrt::setup::V3 pu = P(b.iu), pv = P(b.iv), pw = P(b.iw);
+        const xrt::setup::V3 pb{(b.u * pu.x + b.v * pv.x) + b.w * pw.x,
+                                (b.u * pu.y + b.v * pv.y) + b.w * pw.y,
+                                (b.u * pu.z + b.v * pv.z) + b.w * pw.z};
+        const xrt::setup::V3 pc{c.h_x0[3 * b.cloth], c.h_x0[3 * b.cloth + 1], c.h_x0[3 * b.cloth + 2]};
+        b.L = xrt::setup::length(xrt::setup::sub(pc, pb));
+      }
+      bptr[b.cloth + 1]++;
+    }
+    for (uint32_t i = 0; i < c.nv; ++i) bptr[i + 1] += bptr[i];
+    std::vector<uint32_t> fill(bptr.begin(), bptr.end() - 1);
+    std::vector<float4> ba(std::max<size_t>(c.nbind, 1));
+    std::vector<int4> bb(std::max<size_t>(c.nbind, 1));
+    for (const auto& b : c.h_bind) {
+      const uint32_t pos = fill[b.cloth]++;
+      ba[pos] = make_float4(b.u, b.v, b.w, b.L);
+      int sbits;
+      std::memcpy(&sbits, &b.stiffness, 4);
+      bb[pos] = make_int4((int)b.iu, (int)b.iv, (int)b.iw, sbits);
+    }
+    XRT_CUDA(&c, upload(c.bind_ptr, bptr, c.stream));
+    XRT_CUDA(&c, upload(c.bind_a, ba, c.stream));
+    XRT_CUDA(&c, upload(c.bind_b, bb, c.stream));
+  }
+  // obstacle
+  if (c.onv > 0) {
+    const std::vector<float4> ox = to_f4(c.h_ox0, nullptr);
+    XRT_CUDA(&c, upload(c.ox0, ox, c.stream));
+    XRT_CUDA(&c, upload(c.ox, ox, c.stream));
+    XRT_CUDA(&c, upload(c.ox1, ox, c.stream));
+    XRT_CUDA(&c, c.on.reserve(c.onv));
+    XRT_CUDA(&c, c.on1.reserve(c.onv));
+    c.h_ortri = xrt::setup::build_rtri(c.h_otri, c.onv);
+    std::vector<int4> ot(std::max(c.onf, 1u));
+    for (uint32_t f = 0; f < c.onf; ++f)
+      ot[f] = make_int4((int)c.h_otri[3 * f], (int)c.h_otri[3 * f + 1], (int)c.h_otri[3 * f + 2],
+                        (int)c.h_ortri[f]);
+    XRT_CUDA(&c, upload(c.otri, ot, c.stream));
+    xrt::setup::build_vf(c.h_otri, c.onv, ptr, list);
+    XRT_CUDA(&c, upload(c.ovf_ptr, ptr, c.stream));
+    XRT_CUDA(&c, upload(c.ovf_list, list, c.stream));
+    xrt::launch_vertex_normals(c.ox0.p, c.otri.p, c.ovf_ptr.p, c.ovf_list.p, c.on.p, c.onv, c.stream);
+    XRT_CUDA(&c, cudaMemcpyAsync(c.on1.p, c.on.p, sizeof(float4) * c.onv, cudaMemcpyDeviceToDevice,
+                                 c.stream));
+    if (c.onf > 0) {
+      XRT_CUDA(&c, c.bvh.reserve(c.onf));
+      c.bvh.n = c.onf;
+      xrt::launch_prims_obstacle(c, 0.0f);  // ClothSolverUniversal::Start: UpdateData(0) + Construct
+      c.bvh.construct(0.0f, c.stream, c.err.p);
+    }
+  }
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  XRT_CUDA(&c, cudaGetLastError());
+  c.started = true;
+  c.graph_dirty = true;
+  return XRT_OK;
+}
+
+xrt_status xrt_set_obstacle_targets(xrt_ctx* h, const float* pos) {
+  if (!h || !pos) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (require_started(c) != XRT_OK) return XRT_ERR_STATE;
+  if (c.onv == 0) {
+    c.set_error("no obstacle");
+    return XRT_ERR_STATE;
+  }
+  cudaSetDevice(c.device);
+  std::vector<float4> t(c.onv);
+  for (uint32_t i = 0; i < c.onv; ++i) t[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0);
+  XRT_CUDA(&c, cudaMemcpyAsync(c.ox.p, t.data(), sizeof(float4) * c.onv, cudaMemcpyHostToDevice, c.stream));
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  return XRT_OK;
+}
+
+xrt_status xrt_set_obstacle_targets_device(xrt_ctx* h, const float* d_pos) {
+  if (!h || !d_pos) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (require_started(c) != XRT_OK) return XRT_ERR_STATE;
+  cudaSetDevice(c.device);
+  // 3 floats -> float4 with a strided 2D copy (pitch 12 B in, 16 B out)
+  XRT_CUDA(&c, cudaMemcpy2DAsync(c.ox.p, sizeof(float4), d_pos, 3 * sizeof(float), 3 * sizeof(float),
+                                 c.onv, cudaMemcpyDeviceToDevice, c.stream));
+  return XRT_OK;
+}
+
+xrt_status xrt_step_frame(xrt_ctx* h) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (require_started(c) != XRT_OK) return XRT_ERR_STATE;
+  cudaSetDevice(c.device);
+  if (c.profiling) {
+    record_frame(c);
+    XRT_CUDA(&c, cudaGetLastError());
+    collect_profile(c);
+  } else if (c.graph_enabled) {
+    if (c.graph_dirty || !c.graph_exec) {
+      xrt_status st = capture_frame(c);
+      if (st != XRT_OK) return st;
+    }
+    XRT_CUDA(&c, cudaGraphLaunch(c.graph_exec, c.stream));
+  } else {
+    record_frame(c);
+    XRT_CUDA(&c, cudaGetLastError());
+  }
+  c.frame_index++;
+  return XRT_OK;
+}
+
+xrt_status xrt_step_frames(xrt_ctx* h, int32_t n) {
+  for (int32_t i = 0; i < n; ++i) {
+    xrt_status st = xrt_step_frame(h);
+    if (st != XRT_OK) return st;
+  }
+  return XRT_OK;
+}
+
+xrt_status xrt_synchronize(xrt_ctx* h) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  cudaSetDevice(c.device);
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  uint32_t err = 0;
+  XRT_CUDA(&c, cudaMemcpy(&err, c.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  if (err) {
+    c.set_error("device error word 0x" + std::to_string(err) +
+                " (1: traversal bound, 2: tree-walk bound, 4: index range)");
+    return XRT_ERR_DEVICE_FLAG;
+  }
+  return XRT_OK;
+}
+
+xrt_status xrt_set_graph_mode(xrt_ctx* h, int32_t enabled) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  h->c.graph_enabled = enabled != 0;
+  h->c.graph_dirty = true;
+  return XRT_OK;
+}
+
+xrt_status xrt_set_profiling(xrt_ctx* h, int32_t enabled) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  cudaSetDevice(c.device);
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  c.profiling = enabled != 0;
+  c.prof_used = 0;
+  c.prof_frames = 0;
+  for (int i = 0; i < 16; ++i) {
+    c.prof_ms[i] = 0.0;
+    c.prof_launches[i] = 0;
+    c.prof_units[i] = 0;
+  }
+  return XRT_OK;
+}
+
+xrt_status xrt_get_profile(xrt_ctx* h, xrt_profile* out) {
+  if (!h || !out) return XRT_ERR_INVALID_ARGUMENT;
+  const Context& c = h->c;
+  std::memset(out, 0, sizeof(*out));
+  for (int i = 0; i < 16; ++i) {
+    out->ms[i] = c.prof_ms[i];
+    out->launches[i] = c.prof_launches[i];
+    out->units[i] = c.prof_units[i];
+  }
+  out->frames = c.prof_frames;
+  return XRT_OK;
+}
+
+const char* xrt_phase_name(int32_t phase) {
+  return (phase >= 0 && phase < XRT_NUM_PHASES) ? kPhaseNames[phase] : "";
+}
+
+xrt_status xrt_get_sizes(const xrt_ctx* h, xrt_sizes* out) {
+  if (!h || !out) return XRT_ERR_INVALID_ARGUMENT;
+  const Context& c = h->c;
+  std::memset(out, 0, sizeof(*out));
+  out->num_vertices = (uint32_t)c.h_w.size();
+  out->num_edges = (uint32_t)c.h_rest.size();
+  out->num_triangles = (uint32_t)(c.h_tri.size() / 3);
+  out->num_bends = (uint32_t)c.h_theta.size();
+  out->num_lra = (uint32_t)c.h_lra_rest.size();
+  out->num_bindings = (uint32_t)c.h_bind.size();
+  out->num_obstacle_vertices = (uint32_t)(c.h_ox0.size() / 3);
+  out->num_obstacle_triangles = (uint32_t)(c.h_otri.size() / 3);
+  out->num_stretch_colors = c.n_scolors;
+  out->num_bend_colors = c.n_bcolors;
+  out->launches_per_frame = c.launches_per_frame;
+  out->frame_index = c.frame_index;
+  out->particle_diameter = c.particle_diameter;
+  return XRT_OK;
+}
+
+xrt_status xrt_get_positions(xrt_ctx* h, float* out) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  if (require_started(h->c) != XRT_OK) return XRT_ERR_STATE;
+  cudaSetDevice(h->c.device);
+  return read_f4(h->c, h->c.x0, h->c.nv, out);
+}
+xrt_status xrt_get_velocities(xrt_ctx* h, float* out) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  if (require_started(h->c) != XRT_OK) return XRT_ERR_STATE;
+  cudaSetDevice(h->c.device);
+  return read_f4(h->c, h->c.v, h->c.nv, out);
+}
+xrt_status xrt_get_normals(xrt_ctx* h, float* out) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  if (require_started(h->c) != XRT_OK) return XRT_ERR_STATE;
+  cudaSetDevice(h->c.device);
+  return read_f4(h->c, h->c.n, h->c.nv, out);
+}
+xrt_status xrt_get_obstacle_positions(xrt_ctx* h, float* out) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  if (require_started(h->c) != XRT_OK) return XRT_ERR_STATE;
+  cudaSetDevice(h->c.device);
+  return read_f4(h->c, h->c.ox0, h->c.onv, out);
+}
+xrt_status xrt_get_obstacle_normals(xrt_ctx* h, float* out) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  if (require_started(h->c) != XRT_OK) return XRT_ERR_STATE;
+  cudaSetDevice(h->c.device);
+  return read_f4(h->c, h->c.on, h->c.onv, out);
+}
+
+xrt_status xrt_set_state(xrt_ctx* h, const float* pos, const float* vel) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (require_started(c) != XRT_OK) return XRT_ERR_STATE;
+  cudaSetDevice(c.device);
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  if (pos) {
+    std::vector<float> p(pos, pos + 3 * (size_t)c.nv);
+    const std::vector<float4> a = to_f4(p, &c.h_w), b = to_f4(p, nullptr);
+    XRT_CUDA(&c, cudaMemcpy(c.x.p, a.data(), sizeof(float4) * c.nv, cudaMemcpyHostToDevice));
+    XRT_CUDA(&c, cudaMemcpy(c.x_alt.p, a.data(), sizeof(float4) * c.nv, cudaMemcpyHostToDevice));
+    XRT_CUDA(&c, cudaMemcpy(c.x0.p, b.data(), sizeof(float4) * c.nv, cudaMemcpyHostToDevice));
+  }
+  if (vel) {
+    std::vector<float> p(vel, vel + 3 * (size_t)c.nv);
+    const std::vector<float4> b = to_f4(p, nullptr);
+    XRT_CUDA(&c, cudaMemcpy(c.v.p, b.data(), sizeof(float4) * c.nv, cudaMemcpyHostToDevice));
+  }
+  return XRT_OK;
+}
+
+xrt_status xrt_get_device_state(xrt_ctx* h, void** dx, void** dv, void** stream) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  if (require_started(h->c) != XRT_OK) return XRT_ERR_STATE;
+  if (dx) *dx = h->c.x0.p;
+  if (dv) *dv = h->c.v.p;
+  if (stream) *stream = (void*)h->c.stream;
+  return XRT_OK;
+}
+
+xrt_status xrt_get_edges(const xrt_ctx* h, uint32_t* out2, float* rest) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  if (out2) std::copy(h->c.h_edges.begin(), h->c.h_edges.end(), out2);
+  if (rest) std::copy(h->c.h_rest.begin(), h->c.h_rest.end(), rest);
+  return XRT_OK;
+}
+xrt_status xrt_get_bends(const xrt_ctx* h, uint32_t* out4, float* th) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  if (out4) std::copy(h->c.h_bends.begin(), h->c.h_bends.end(), out4);
+  if (th) std::copy(h->c.h_theta.begin(), h->c.h_theta.end(), th);
+  return XRT_OK;
+}
+xrt_status xrt_get_coloring(const xrt_ctx* h, int32_t kind, uint32_t* colors) {
+  if (!h || !colors || (kind != 0 && kind != 1)) return XRT_ERR_INVALID_ARGUMENT;
+  const auto& col = kind == 0 ? h->c.h_scolor : h->c.h_bcolor;
+  std::copy(col.begin(), col.end(), colors);
+  return XRT_OK;
+}
+xrt_status xrt_get_lra(const xrt_ctx* h, uint32_t* src, uint32_t* tgt, float* rest) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  if (src) std::copy(h->c.h_lra_src.begin(), h->c.h_lra_src.end(), src);
+  if (tgt) std::copy(h->c.h_lra_tgt.begin(), h->c.h_lra_tgt.end(), tgt);
+  if (rest) std::copy(h->c.h_lra_rest.begin(), h->c.h_lra_rest.end(), rest);
+  return XRT_OK;
+}
+xrt_status xrt_get_obstacle_rtri(const xrt_ctx* h, uint32_t* masks) {
+  if (!h || !masks) return XRT_ERR_INVALID_ARGUMENT;
+  std::copy(h->c.h_ortri.begin(), h->c.h_ortri.end(), masks);
+  return XRT_OK;
+}
+
+static xrt_status export_lbvh(xrt::Lbvh& b, cudaStream_t s, std::string& err, uint32_t* morton,
+                              uint32_t* objs, uint32_t* nodes, float* aabbs, int32_t* iesc,
+                              int32_t* eesc, int32_t* unique) {
+  const uint32_t n = b.n;
+  if (!b.active || n == 0) {
+    err = "LBVH not built";
+    return XRT_ERR_STATE;
+  }
+  const uint32_t nn = 2 * n - 1;
+  auto fail = [&](cudaError_t e) {
+    err = cudaGetErrorString(e);
+    return XRT_ERR_CUDA;
+  };
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(e);
+  if (morton && (e = cudaMemcpy(morton, b.sorted_morton, 4 * n, cudaMemcpyDeviceToHost))) return fail(e);
+  if (objs && (e = cudaMemcpy(objs, b.sorted_index, 4 * n, cudaMemcpyDeviceToHost))) return fail(e);
+  if (nodes && (e = cudaMemcpy(nodes, b.node.p, 16 * (size_t)nn, cudaMemcpyDeviceToHost))) return fail(e);
+  if (aabbs) {
+    std::vector<float4> lo(nn), hi(nn);
+    if ((e = cudaMemcpy(lo.data(), b.lo.p, 16 * (size_t)nn, cudaMemcpyDeviceToHost))) return fail(e);
+    if ((e = cudaMemcpy(hi.data(), b.hi.p, 16 * (size_t)nn, cudaMemcpyDeviceToHost))) return fail(e);
+    for (uint32_t k = 0; k < nn; ++k) {
+      float* a = aabbs + 6 * (size_t)k;
+      a[0] = lo[k].x; a[1] = lo[k].y; a[2] = lo[k].z;
+      a[3] = hi[k].x; a[4] = hi[k].y; a[5] = hi[k].z;
+    }
+  }
+  if (iesc && n > 1 && (e = cudaMemcpy(iesc, b.iesc.p, 4 * (n - 1), cudaMemcpyDeviceToHost))) return fail(e);
+  if (eesc && (e = cudaMemcpy(eesc, b.eesc.p, 4 * n, cudaMemcpyDeviceToHost))) return fail(e);
+  if (unique) {
+    uint32_t dup = 0;
+    if ((e = cudaMemcpy(&dup, b.dup.p, 4, cudaMemcpyDeviceToHost))) return fail(e);
+    *unique = dup == 0 ? 1 : 0;
+  }
+  return XRT_OK;
+}
+
+xrt_status xrt_export_obstacle_bvh(xrt_ctx* h, uint32_t* morton, uint32_t* objs, uint32_t* nodes,
+                                   float* aabbs, int32_t* iesc, int32_t* eesc) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(h->c.device);
+  std::string err;
+  xrt_status st = export_lbvh(h->c.bvh, h->c.stream, err, morton, objs, nodes, aabbs, iesc, eesc, nullptr);
+  if (st != XRT_OK) h->c.set_error(err);
+  return st;
+}
+
+xrt_status xrt_export_contacts(xrt_ctx* h, int32_t* vf_index, float* vf_qs, int32_t* rt_index,
+                               float* rt_qc, float* ee) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (require_started(c) != XRT_OK) return XRT_ERR_STATE;
+  cudaSetDevice(c.device);
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  if (vf_index) XRT_CUDA(&c, cudaMemcpy(vf_index, c.vf_idx.p, 4 * c.nv, cudaMemcpyDeviceToHost));
+  if (rt_index) XRT_CUDA(&c, cudaMemcpy(rt_index, c.rt_idx.p, 4 * c.nv, cudaMemcpyDeviceToHost));
+  if (vf_qs && read_f4(c, c.vf_qs, c.nv, vf_qs) != XRT_OK) return XRT_ERR_CUDA;
+  if (rt_qc && read_f4(c, c.rt_qc, c.nv, rt_qc) != XRT_OK) return XRT_ERR_CUDA;
+  if (ee && c.ne) {
+    std::vector<float4> a(c.ne), b(c.ne), d(c.ne);
+    XRT_CUDA(&c, cudaMemcpy(a.data(), c.ee_a.p, 16 * (size_t)c.ne, cudaMemcpyDeviceToHost));
+    XRT_CUDA(&c, cudaMemcpy(b.data(), c.ee_b.p, 16 * (size_t)c.ne, cudaMemcpyDeviceToHost));
+    XRT_CUDA(&c, cudaMemcpy(d.data(), c.ee_c.p, 16 * (size_t)c.ne, cudaMemcpyDeviceToHost));
+    for (uint32_t e = 0; e < c.ne; ++e) {
+      float* r = ee + 12 * (size_t)e;
+      r[0] = a[e].x; r[1] = a[e].y; r[2] = a[e].z; r[3] = a[e].w;
+      r[4] = b[e].x; r[5] = b[e].y; r[6] = b[e].z;
+      r[7] = b[e].w; r[8] = d[e].w;
+      r[9] = d[e].x; r[10] = d[e].y; r[11] = d[e].z;
+    }
+  }
+  return XRT_OK;
+}
+
+xrt_status xrt_export_neighbors(xrt_ctx* h, uint32_t* out) {
+  if (!h || !out) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (require_started(c) != XRT_OK) return XRT_ERR_STATE;
+  cudaSetDevice(c.device);
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  XRT_CUDA(&c, cudaMemcpy(out, c.neighbors.p, 4 * (size_t)c.nv * c.params.max_neighbor_size,
+                          cudaMemcpyDeviceToHost));
+  return XRT_OK;
+}
+
+// ---- standalone LBVH ---------------------------------------------------------------------------
+
+xrt_status xrt_lbvh_create(xrt_lbvh** out, int32_t device) {
+  if (!out) return XRT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  std::string why;
+  xrt_status st = check_device(device, why);
+  if (st != XRT_OK) return st;
+  xrt_lbvh* b = new xrt_lbvh();
+  b->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      b->err.reserve(1) != cudaSuccess || cudaMemset(b->err.p, 0, 4) != cudaSuccess) {
+    delete b;
+    return XRT_ERR_CUDA;
+  }
+  *out = b;
+  return XRT_OK;
+}
+
+xrt_status xrt_lbvh_destroy(xrt_lbvh* b) {
+  if (!b) return XRT_OK;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  b->b.release();
+  b->staging.release();
+  b->err.release();
+  cudaStreamDestroy(b->stream);
+  delete b;
+  return XRT_OK;
+}
+
+xrt_status xrt_lbvh_build_device(xrt_lbvh* b, const float* d_prims, const float* d_pred, uint32_t n,
+                                 float scr, void* stream) {
+  if (!b || (n && !d_prims)) return XRT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(b->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+  if (b->b.reserve(n) != cudaSuccess) return XRT_ERR_CUDA;
+  b->b.n = n;
+  xrt::launch_float9_to_float4(d_prims, b->b.v.p, n, s);
+  xrt::launch_float9_to_float4(d_pred ? d_pred : d_prims, b->b.pred.p, n, s);
+  b->b.construct(scr, s, b->err.p);
+  return cudaGetLastError() == cudaSuccess ? XRT_OK : XRT_ERR_CUDA;
+}
+
+xrt_status xrt_lbvh_build(xrt_lbvh* b, const float* prims, const float* pred, uint32_t n, float scr) {
+  if (!b || (n && !prims)) return XRT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(b->device);
+  if (b->staging.reserve(18 * (size_t)std::max(n, 1u)) != cudaSuccess) return XRT_ERR_CUDA;
+  if (n) {
+    if (cudaMemcpy(b->staging.p, prims, 36 * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess)
+      return XRT_ERR_CUDA;
+    if (pred && cudaMemcpy(b->staging.p + 9 * (size_t)n, pred, 36 * (size_t)n,
+                           cudaMemcpyHostToDevice) != cudaSuccess)
+      return XRT_ERR_CUDA;
+  }
+  xrt_status st = xrt_lbvh_build_device(b, b->staging.p, pred ? b->staging.p + 9 * (size_t)n : nullptr,
+                                        n, scr, nullptr);
+  if (st != XRT_OK) return st;
+  return cudaStreamSynchronize(b->stream) == cudaSuccess ? XRT_OK : XRT_ERR_CUDA;
+}
+
+xrt_status xrt_lbvh_refit_device(xrt_lbvh* b, const float* d_pred, uint32_t n, void* stream) {
+  if (!b || !d_pred || n != b->b.n) return XRT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(b->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+  xrt::launch_float9_to_float4(d_pred, b->b.pred.p, n, s);
+  b->b.refit_from_pred(s, b->err.p);
+  return cudaGetLastError() == cudaSuccess ? XRT_OK : XRT_ERR_CUDA;
+}
+
+xrt_status xrt_lbvh_refit(xrt_lbvh* b, const float* pred, uint32_t n) {
+  if (!b || !pred || n != b->b.n) return XRT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(b->device);
+  if (b->staging.reserve(9 * (size_t)std::max(n, 1u)) != cudaSuccess) return XRT_ERR_CUDA;
+  if (cudaMemcpy(b->staging.p, pred, 36 * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess)
+    return XRT_ERR_CUDA;
+  xrt_status st = xrt_lbvh_refit_device(b, b->staging.p, n, nullptr);
+  if (st != XRT_OK) return st;
+  return cudaStreamSynchronize(b->stream) == cudaSuccess ? XRT_OK : XRT_ERR_CUDA;
+}
+
+xrt_status xrt_lbvh_export(xrt_lbvh* b, uint32_t* morton, uint32_t* objs, uint32_t* nodes, float* aabbs,
+                           int32_t* iesc, int32_t* eesc, int32_t* unique) {
+  if (!b) return XRT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(b->device);
+  return export_lbvh(b->b, b->stream, b->last_error, morton, objs, nodes, aabbs, iesc, eesc, unique);
+}
+
+xrt_status xrt_lbvh_query(xrt_lbvh* b, int32_t kind, const float* q, uint32_t nq, uint32_t* counts,
+                          uint32_t* cands) {
+  if (!b || (nq && (!q || !counts || !cands)) || kind < 0 || kind > 2) return XRT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(b->device);
+  if (nq == 0) return XRT_OK;
+  if (!b->b.active) return XRT_ERR_STATE;
+  const size_t per = kind == 0 ? 3 : 6;
+  DBuf<float> dq;
+  DBuf<uint32_t> dcount, dcand;
+  if (dq.reserve(per * nq) || dcount.reserve(nq) || dcand.reserve((size_t)nq * xrt::kMaxCandidatesHost))
+    return XRT_ERR_CUDA;
+  xrt_status st = XRT_OK;
+  if (cudaMemcpy(dq.p, q, per * 4 * nq, cudaMemcpyHostToDevice) != cudaSuccess) st = XRT_ERR_CUDA;
+  if (st == XRT_OK) {
+    xrt::launch_lbvh_query(b->b, kind, dq.p, nq, dcount.p, dcand.p, b->stream, b->err.p);
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess ||
+        cudaMemcpy(counts, dcount.p, 4 * (size_t)nq, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(cands, dcand.p, 4 * (size_t)nq * xrt::kMaxCandidatesHost, cudaMemcpyDeviceToHost) !=
+            cudaSuccess)
+      st = XRT_ERR_CUDA;
+  }
+  dq.release();
+  dcount.release();
+  dcand.release();
+  return st;
+}
+
+xrt_status xrt_lbvh_sizes(const xrt_lbvh* b, uint32_t* n) {
+  if (!b || !n) return XRT_ERR_INVALID_ARGUMENT;
+  *n = b->b.n;
+  return XRT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,63 @@
+// common.cuh — device vector math and launch helpers of the GB300 cloth step.
+//
+// Vector operations keep glm's evaluation order (dot = (x*x' + y*y') + z*z', cross, length =
+// sqrt(dot), normalize = v * (1/sqrt(dot))) and the library is compiled with --fmad=false and
+// IEEE division / square root, so every float the kernels produce is reproducible on the host.
+// That is what lets Morton codes, LBVH topology and candidate lists match the CPU restatement
+// bit-for-bit (xrtailor/src/physics/broad_phase/lbvh/BVH.cu:22-46 feeds integer codes from float
+// box centres; one ulp moves a code across a cell boundary).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define XRT_HD __host__ __device__ __forceinline__
+
+namespace xrt {
+
+struct f3 {
+  float x, y, z;
+};
+XRT_HD f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+XRT_HD f3 mk3(float4 v) { return f3{v.x, v.y, v.z}; }
+XRT_HD float4 mk4(f3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
+XRT_HD f3 operator+(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+XRT_HD f3 operator-(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+XRT_HD f3 operator-(f3 a) { return f3{-a.x, -a.y, -a.z}; }
+XRT_HD f3 operator*(f3 a, float s) { return f3{a.x * s, a.y * s, a.z * s}; }
+XRT_HD f3 operator*(float s, f3 a) { return f3{s * a.x, s * a.y, s * a.z}; }
+XRT_HD f3 operator/(f3 a, float s) { return f3{a.x / s, a.y / s, a.z / s}; }
+XRT_HD float dot(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+XRT_HD f3 cross(f3 a, f3 b) {
+  return f3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+}
+XRT_HD float length(f3 v) { return sqrtf(dot(v, v)); }
+XRT_HD f3 normalize(f3 v) { return v * (1.0f / sqrtf(dot(v, v))); }
+XRT_HD float comp(f3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+template <typename T> XRT_HD T tmin(T a, T b) { return a < b ? a : b; }
+template <typename T> XRT_HD T tmax(T a, T b) { return a > b ? a : b; }
+template <typename T> XRT_HD T tclamp(T x, T a, T b) { return x < a ? a : (x > b ? b : x); }
+template <typename T> XRT_HD T tabs(T x) { return x < T(0) ? -x : x; }
+
+// MathFunctions::FaceNormal (src/math/MathFunctions.cu:14-20)
+XRT_HD f3 face_normal(f3 a, f3 b, f3 c) { return normalize(cross(b - a, c - a)); }
+
+constexpr float kEps = 1e-6f;             // EPSILON (core/Scalar.hpp:39)
+constexpr float kScalarMax = 3.402823466e+38f;  // SCALAR_MAX = FLT_MAX (core/Scalar.cuh:10)
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr uint32_t kMaxCandidates = 256;  // LBVH_MAX_BUFFER_SIZE (core/Common.cuh:23)
+constexpr int kBlock = 256;
+
+// Bits of the sticky device error word.
+enum : uint32_t {
+  kErrTraversal = 1u << 0,  // a traversal exceeded its visit bound
+  kErrTreeWalk = 1u << 1,   // a bottom-up / escape walk exceeded its depth bound
+  kErrIndex = 1u << 2,      // an index was out of range
+};
+
+__device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit) { atomicOr(err, bit); }
+
+inline unsigned grid_for(uint32_t n, int block = kBlock) {
+  return (unsigned)((n + (uint32_t)block - 1) / (uint32_t)block);
+}
+
+}  // namespace xrt

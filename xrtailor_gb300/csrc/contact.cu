@@ -1,0 +1,228 @@
+// contact.cu — obstacle motion within a frame and Swift obstacle-contact generation.
+//
+//   Interpolate_Kernel .............. xrtailor/src/physics/PhysicsMesh.cu:610-620
+//   UpdateNodeMidstepNormals ........ xrtailor/src/physics/PhysicsMeshHelper.cu:212-225, 297-310
+//   GenerateVF_DCD_Kernel ........... xrtailor/src/physics/pbd_collision/PBDCollision.cu:17-46
+//   GenerateVFCCD_Kernel ............ PBDCollision.cu:236-267
+//   GenerateEE_DCD_Kernel ........... PBDCollision.cu:100-151 (R-triangle edge filter RTriangle.cu:12-17)
+//   PredictedToPositions/UpdateNormals PhysicsMesh.cu:604-608, PhysicsMeshHelper.cu:196-210
+//
+// Vertex normals are gathered per vertex over its faces in ascending face order (the reference
+// scatters them with float atomics); the interpolated midstep position x1 of a neighbor is
+// recomputed from x0 and x inside the gather, so interpolation and normals are one kernel.
+#include "common.cuh"
+#include "context.h"
+#include "lbvh_dev.cuh"
+#include "prim_tests.cuh"
+
+namespace xrt {
+namespace {
+
+__device__ __forceinline__ f3 lerp_pos(const float4* __restrict__ x0, const float4* __restrict__ x,
+                                       int i, float alpha) {
+  return (1.0f - alpha) * mk3(x0[i]) + alpha * mk3(x[i]);
+}
+
+__global__ void k_obstacle_pass(const float4* __restrict__ x0, const float4* __restrict__ x,
+                                float4* __restrict__ x1, float4* __restrict__ n1,
+                                const int4* __restrict__ tri, const uint32_t* __restrict__ ptr,
+                                const uint32_t* __restrict__ list, uint32_t nv, float alpha) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  const f3 xi = lerp_pos(x0, x, i, alpha);
+  f3 acc = mk3(0, 0, 0);
+  for (uint32_t k = ptr[i]; k < ptr[i + 1]; ++k) {
+    const uint32_t fc = list[k];
+    const int4 t = tri[fc >> 2];
+    const int id[3] = {t.x, t.y, t.z};
+    const int j = (int)(fc & 3u);
+    const f3 e0 = lerp_pos(x0, x, id[(j + 1) % 3], alpha) - xi;
+    const f3 e1 = lerp_pos(x0, x, id[(j + 2) % 3], alpha) - xi;
+    acc = acc + cross(e0, e1) / (dot(e0, e0) * dot(e1, e1));
+  }
+  x1[i] = mk4(xi, 0.0f);
+  n1[i] = mk4(normalize(acc), 0.0f);
+}
+
+__global__ void k_vertex_normals(const float4* __restrict__ x, const int4* __restrict__ tri,
+                                 const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ list,
+                                 float4* __restrict__ out, uint32_t nv) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  const f3 xi = mk3(x[i]);
+  f3 acc = mk3(0, 0, 0);
+  for (uint32_t k = ptr[i]; k < ptr[i + 1]; ++k) {
+    const uint32_t fc = list[k];
+    const int4 t = tri[fc >> 2];
+    const int id[3] = {t.x, t.y, t.z};
+    const int j = (int)(fc & 3u);
+    const f3 e0 = mk3(x[id[(j + 1) % 3]]) - xi;
+    const f3 e1 = mk3(x[id[(j + 2) % 3]]) - xi;
+    acc = acc + cross(e0, e1) / (dot(e0, e0) * dot(e1, e1));
+  }
+  out[i] = mk4(normalize(acc), 0.0f);
+}
+
+// Frame end: x0 = x, then normals of the new x0 (computed from x, which is the same data).
+__global__ void k_obstacle_commit(const float4* __restrict__ x, float4* __restrict__ x0,
+                                  float4* __restrict__ nrm, const int4* __restrict__ tri,
+                                  const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ list,
+                                  uint32_t nv) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  const f3 xi = mk3(x[i]);
+  f3 acc = mk3(0, 0, 0);
+  for (uint32_t k = ptr[i]; k < ptr[i + 1]; ++k) {
+    const uint32_t fc = list[k];
+    const int4 t = tri[fc >> 2];
+    const int id[3] = {t.x, t.y, t.z};
+    const int j = (int)(fc & 3u);
+    const f3 e0 = mk3(x[id[(j + 1) % 3]]) - xi;
+    const f3 e1 = mk3(x[id[(j + 2) % 3]]) - xi;
+    acc = acc + cross(e0, e1) / (dot(e0, e0) * dot(e1, e1));
+  }
+  x0[i] = mk4(xi, 0.0f);
+  nrm[i] = mk4(normalize(acc), 0.0f);
+}
+
+// VF-DCD (nearest obstacle point of the predicted vertex) and VF-CCD (first hit of the segment
+// x0 -> x), one thread per cloth vertex.
+__global__ void __launch_bounds__(kBlock) k_generate_vf(LbvhView b, const float4* __restrict__ x,
+                                                        const float4* __restrict__ x0, uint32_t nv,
+                                                        int* __restrict__ vf_idx,
+                                                        float4* __restrict__ vf_qs,
+                                                        int* __restrict__ rt_idx,
+                                                        float4* __restrict__ rt_qc, uint32_t* err) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  const f3 pred = mk3(x[i]);
+  {
+    float hit = kScalarMax;
+    int hit_idx = -1;
+    f3 hit_qs = mk3(0, 0, 0);
+    lbvh_traverse(
+        b, [&](float4 l, float4 h) { return overlap_point(l, h, pred); },
+        [&](uint32_t f) {
+          f3 qs;
+          const float dist = nearest_point(pred, mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]),
+                                           mk3(b.pred[3 * f + 2]), qs);
+          if (dist < hit) {
+            hit = dist;
+            hit_qs = qs;
+            hit_idx = (int)f;
+          }
+        },
+        err);
+    vf_idx[i] = hit_idx;
+    vf_qs[i] = mk4(hit_qs, 0.0f);
+  }
+  {
+    const f3 p1 = mk3(x0[i]), p2 = pred;
+    f3 d = p2 - p1;
+    const float len = length(d);
+    int hit_idx = -1;
+    f3 qc = mk3(0, 0, 0);
+    if (!(len < kEps)) {
+      d = d / len;
+      float hit = kScalarMax;
+      lbvh_traverse(
+          b, [&](float4 l, float4 h) { return overlap_segment(l, h, p1, p2); },
+          [&](uint32_t f) {
+            const float dist = ray_intersect(p1, d, len, mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]),
+                                             mk3(b.pred[3 * f + 2]));
+            if (dist < hit) {
+              qc = p1 + dist * d;
+              hit = dist;
+              hit_idx = (int)f;
+            }
+          },
+          err);
+    }
+    rt_idx[i] = hit_idx;
+    rt_qc[i] = mk4(qc, 0.0f);
+  }
+}
+
+// EE-DCD: closest R-triangle-owned obstacle edge to each cloth edge.
+__global__ void __launch_bounds__(kBlock) k_generate_ee(LbvhView b, const float4* __restrict__ x,
+                                                        const uint2* __restrict__ edge, uint32_t ne,
+                                                        const int4* __restrict__ otri,
+                                                        float4* __restrict__ ee_a,
+                                                        float4* __restrict__ ee_b,
+                                                        float4* __restrict__ ee_c, uint32_t* err) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const uint2 ed = edge[e];
+  const f3 pc = mk3(x[ed.x]), qc = mk3(x[ed.y]);
+  float s = 0, t = 0;
+  f3 p2 = mk3(0, 0, 0), q2 = mk3(0, 0, 0), fn = mk3(0, 0, 0);
+  float min_dist = kScalarMax;
+  lbvh_traverse(
+      b, [&](float4 l, float4 h) { return overlap_segment(l, h, pc, qc); },
+      [&](uint32_t f) {
+        const uint32_t info = (uint32_t)otri[f].w;
+        const f3 ov[3] = {mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]), mk3(b.pred[3 * f + 2])};
+#pragma unroll
+        for (uint32_t a = 0; a < 3; ++a) {
+          if ((info >> (a + 3u)) & 1u) {
+            float _s, _t;
+            f3 c1, c2;
+            const uint32_t bb = (a + 1u) % 3u;
+            if (closest_seg_seg(pc, qc, ov[a], ov[bb], _s, _t, c1, c2) != 0.0f) {
+              const float dist = length(c1 - c2);
+              if (dist < min_dist) {
+                min_dist = dist;
+                p2 = ov[a];
+                q2 = ov[bb];
+                s = _s;
+                t = _t;
+                fn = face_normal(ov[0], ov[1], ov[2]);
+              }
+            }
+          }
+        }
+      },
+      err);
+  ee_a[e] = make_float4(min_dist, p2.x, p2.y, p2.z);
+  ee_b[e] = make_float4(q2.x, q2.y, q2.z, s);
+  ee_c[e] = make_float4(fn.x, fn.y, fn.z, t);
+}
+
+}  // namespace
+
+void launch_obstacle_pass(Context& c, int step, int num_steps) {
+  if (c.onv == 0) return;
+  const float alpha = ((float)step + 1.0f) / (float)num_steps;
+  k_obstacle_pass<<<grid_for(c.onv), kBlock, 0, c.stream>>>(c.ox0.p, c.ox.p, c.ox1.p, c.on1.p,
+                                                            c.otri.p, c.ovf_ptr.p, c.ovf_list.p,
+                                                            c.onv, alpha);
+  launch_refit_midstep(c.bvh, c.ox1.p, c.on1.p, c.otri.p, c.params.bvh_tolerance, c.stream, c.err.p);
+}
+
+void launch_generate_contacts(Context& c) {
+  if (!c.bvh.active) return;
+  k_generate_vf<<<grid_for(c.nv), kBlock, 0, c.stream>>>(c.bvh.view(), c.x.p, c.x0.p, c.nv,
+                                                         c.vf_idx.p, c.vf_qs.p, c.rt_idx.p,
+                                                         c.rt_qc.p, c.err.p);
+  k_generate_ee<<<grid_for(c.ne), kBlock, 0, c.stream>>>(c.bvh.view(), c.x.p, c.edge.p, c.ne,
+                                                         c.otri.p, c.ee_a.p, c.ee_b.p, c.ee_c.p,
+                                                         c.err.p);
+}
+
+void launch_obstacle_commit(Context& c) {
+  if (c.onv == 0) return;
+  k_obstacle_commit<<<grid_for(c.onv), kBlock, 0, c.stream>>>(c.ox.p, c.ox0.p, c.on.p, c.otri.p,
+                                                              c.ovf_ptr.p, c.ovf_list.p, c.onv);
+}
+
+void launch_vertex_normals(const float4* x, const int4* tri, const uint32_t* ptr,
+                           const uint32_t* list, float4* out, uint32_t nv, cudaStream_t s) {
+  if (nv == 0) return;
+  k_vertex_normals<<<grid_for(nv), kBlock, 0, s>>>(x, tri, ptr, list, out, nv);
+}
+
+void launch_prims_obstacle(Context& c, float tol) {
+  launch_prims_from_mesh(c.bvh, c.ox0.p, c.on.p, c.otri.p, c.onf, tol, c.stream);
+}
+
+}  // namespace xrt

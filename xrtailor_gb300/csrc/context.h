@@ -1,0 +1,226 @@
+// context.h — host-side context of the GB300 cloth step: device buffers and the launchers that
+// the C ABI (api.cpp) sequences.  One context = one CUDA stream; no globals.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/xrt.h"
+
+namespace xrt {
+
+constexpr uint32_t kMaxCandidatesHost = 256;         // LBVH_MAX_BUFFER_SIZE
+constexpr float kScalarMaxHost = 3.402823466e+38f;   // SCALAR_MAX
+
+// Growable device buffer (cudaMalloc / cudaFree only at setup or on growth, never per frame).
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t reserve(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// ---- radix sort (radix.cu) --------------------------------------------------------------------
+struct RadixSort {
+  DBuf<uint32_t> keys_tmp, vals_tmp, hist;
+  cudaError_t reserve(uint32_t n);
+  // Stable LSD sort of (keys, vals) by the low `bits` bits of keys.  The result is left in
+  // (keys, vals) if the number of 8-bit passes is even, else in the tmp buffers; returns the
+  // buffers that hold it.
+  void sort(uint32_t* keys, uint32_t* vals, uint32_t n, int bits, cudaStream_t s,
+            uint32_t** out_keys, uint32_t** out_vals);
+};
+
+// ---- LBVH (lbvh.cu) ---------------------------------------------------------------------------
+struct LbvhView {
+  uint32_t n;          // primitives
+  const float4* pred;  // 3 per primitive (pred1..3), original order
+  const float4* lo;    // 2n-1 nodes; xyz = lower, w = left child (internal) / object (leaf)
+  const float4* hi;    // 2n-1 nodes; xyz = upper, w = escape index (-1 = end)
+};
+
+struct Lbvh {
+  uint32_t n = 0;
+  bool active = false;
+  DBuf<float4> v, pred;            // 3 per primitive
+  DBuf<float4> leaf_lo, leaf_hi;   // per primitive (original order) before sorting
+  DBuf<float4> lo, hi;             // per node
+  DBuf<int4> node;                 // parent, left, right, object
+  DBuf<uint32_t> morton, index;    // sort inputs
+  DBuf<unsigned long long> key64;
+  DBuf<uint32_t> flags;            // arrival counters of the bottom-up merge (parity)
+  DBuf<int32_t> iesc, eesc;
+  DBuf<float> root;                // 6 floats
+  DBuf<uint32_t> dup;              // number of equal adjacent Morton codes
+  uint32_t* sorted_morton = nullptr;
+  uint32_t* sorted_index = nullptr;
+  RadixSort sorter;
+
+  cudaError_t reserve(uint32_t n_prims);
+  // BVH::Construct(scr) on v / pred already in device memory (BVH.cu:618-722).
+  void construct(float scr, cudaStream_t s, uint32_t* d_err);
+  // Leaves grow by pred (already updated), internal boxes recomputed bottom-up.
+  void refit_from_pred(cudaStream_t s, uint32_t* d_err);
+  LbvhView view() const { return LbvhView{n, pred.p, lo.p, hi.p}; }
+  void release();
+};
+
+// prims from a mesh: v_k = x[idx_k] + tol * n[idx_k], pred = v (BVH::UpdateData, ccd = false)
+void launch_prims_from_mesh(Lbvh& b, const float4* x, const float4* nrm, const int4* tri,
+                            uint32_t nf, float tol, cudaStream_t s);
+// RefitMidstep: pred_k = x1[idx_k] + tol * n1[idx_k], leaves grow, internal merge.
+void launch_refit_midstep(Lbvh& b, const float4* x1, const float4* n1, const int4* tri, float tol,
+                          cudaStream_t s, uint32_t* d_err);
+// Standalone query kernel: candidates of points (kind 0), segments (1), boxes (2).
+void launch_lbvh_query(const Lbvh& b, int kind, const float* d_q, uint32_t nq, uint32_t* d_counts,
+                       uint32_t* d_cands, cudaStream_t s, uint32_t* d_err);
+void launch_float9_to_float4(const float* d_in, float4* d_out, uint32_t n_prims, cudaStream_t s);
+
+// ---- cloth state --------------------------------------------------------------------------------
+struct ColorRange {
+  uint32_t begin, end;
+};
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  xrt_swift_params params{};
+  bool started = false;
+  bool graph_enabled = true;
+  cudaGraphExec_t graph_exec = nullptr;
+  bool graph_dirty = true;
+  uint32_t frame_index = 0;
+  uint32_t launches_per_frame = 0;
+  bool targets_pending = false;
+
+  // host copies (setup)
+  struct HostCloth {
+    std::vector<float> mesh_pos;    // 3 per vertex, mesh space
+    std::vector<uint32_t> tri;      // local
+    uint32_t offset = 0;
+  };
+  std::vector<HostCloth> cloths;
+  std::vector<float> h_x0;          // 3 per vertex, world
+  std::vector<float> h_w;           // inverse mass
+  std::vector<uint32_t> h_tri;      // global
+  std::vector<uint32_t> h_edges;    // 2 per edge
+  std::vector<float> h_rest, h_scomp;
+  std::vector<uint32_t> h_bends;    // 4 per bend
+  std::vector<float> h_theta, h_bcomp;
+  std::vector<uint32_t> h_scolor, h_bcolor;
+  std::vector<uint32_t> pending_colors[2];
+  std::vector<uint32_t> h_lra_src, h_lra_tgt;
+  std::vector<float> h_lra_rest;
+  struct HostBinding {
+    uint32_t cloth, iu, iv, iw;
+    float u, v, w, L, stiffness;
+  };
+  std::vector<HostBinding> h_bind;
+  float particle_diameter = 0.0f;
+  std::vector<float> h_ox0;         // obstacle world positions
+  std::vector<uint32_t> h_otri;
+  std::vector<uint32_t> h_ortri;
+  uint32_t n_scolors = 0, n_bcolors = 0;
+  std::vector<ColorRange> s_ranges, b_ranges;
+  std::vector<uint32_t> s_perm, b_perm;  // sorted slot -> original constraint index
+
+  // sizes
+  uint32_t nv = 0, ne = 0, nf = 0, nb = 0, nl = 0, nbind = 0, onv = 0, onf = 0;
+
+  // device: cloth
+  DBuf<float4> x, x_alt, x0, v, n, x_init;
+  DBuf<int4> tri;                    // a, b, c, 0
+  DBuf<uint32_t> vf_ptr, vf_list;    // vertex -> (face << 2 | corner), ascending faces
+  DBuf<int4> s_con;                  // sorted by color: i0, i1, rest bits, compliance bits
+  DBuf<float> s_lambda;
+  DBuf<int4> b_idx;                  // sorted by color
+  DBuf<float2> b_tc;                 // theta, compliance
+  DBuf<uint32_t> lra_ptr, lra_src;   // per target vertex, slot order
+  DBuf<float> lra_rest;
+  DBuf<uint32_t> lra_l_src, lra_l_tgt;  // list order (slot-major), used when a slot is free
+  DBuf<float> lra_l_rest;
+  std::vector<ColorRange> lra_blocks;   // list range of each slot
+  bool lra_by_target = true;
+  DBuf<uint32_t> bind_ptr;           // per cloth vertex -> bindings
+  DBuf<float4> bind_a;               // u, v, w, L
+  DBuf<int4> bind_b;                 // iu, iv, iw, stiffness bits
+  DBuf<uint2> edge;                  // original edge order (EE contacts)
+  DBuf<uint32_t> ve_ptr, ve_list;    // vertex -> (edge << 1 | side), ascending edges
+  // contacts
+  DBuf<int> vf_idx, rt_idx;
+  DBuf<float4> vf_qs, rt_qc;
+  DBuf<float4> ee_a, ee_b, ee_c;     // {dist, p2}, {q2, s}, {fn, t}
+  // particle hash
+  DBuf<uint32_t> hash_key, hash_val, cell_start, cell_end, neighbors;
+  RadixSort hash_sorter;
+  // obstacle
+  DBuf<float4> ox0, ox, ox1, on, on1;
+  DBuf<int4> otri;                   // a, b, c, r-triangle mask
+  DBuf<uint32_t> ovf_ptr, ovf_list;
+  Lbvh bvh;
+  // error word
+  DBuf<uint32_t> err;
+  // per-phase profiling (eager frames only)
+  struct ProfEvent {
+    cudaEvent_t a, b;
+    int phase;
+    uint32_t kernels;
+    uint64_t units;
+  };
+  bool profiling = false;
+  std::vector<ProfEvent> prof_events;
+  size_t prof_used = 0;
+  double prof_ms[16] = {};
+  uint64_t prof_launches[16] = {};
+  uint64_t prof_units[16] = {};
+  uint32_t prof_frames = 0;
+
+  void set_error(const std::string& m) { last_error = m; }
+};
+
+// ---- kernels (solver.cu / contact.cu / hash.cu) ---------------------------------------------------
+struct FrameConst {
+  float dt;
+  float gx, gy, gz;
+  float damping;
+  float relaxation;
+  float lra_stretch;
+  float friction;
+  float particle_diameter;
+};
+
+void launch_predict(Context& c, const FrameConst& k);
+void launch_finalize_predict(Context& c, const FrameConst& k, bool predict_next, bool normals);
+void launch_stretch(Context& c, const FrameConst& k, ColorRange r, bool reset_lambda);
+void launch_bend(Context& c, const FrameConst& k, ColorRange r);
+void launch_lra(Context& c, const FrameConst& k);
+void launch_vf_solve(Context& c);
+// EE solve + ApplyDeltas + binding: reads x, writes x_alt; caller swaps.
+void launch_ee_apply(Context& c, const FrameConst& k, bool contacts, bool bindings);
+void launch_obstacle_pass(Context& c, int step, int num_steps);
+void launch_generate_contacts(Context& c);
+void launch_obstacle_commit(Context& c);
+void launch_vertex_normals(const float4* x, const int4* tri, const uint32_t* ptr,
+                           const uint32_t* list, float4* out, uint32_t nv, cudaStream_t s);
+void launch_hash(Context& c);
+void launch_collide(Context& c, const FrameConst& k);  // reads x, writes x_alt; caller swaps
+void launch_prims_obstacle(Context& c, float tol);
+
+}  // namespace xrt

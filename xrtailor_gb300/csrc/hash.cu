@@ -1,0 +1,163 @@
+// hash.cu — Swift particle self-collision: uniform-grid hash, stable sort, cell ranges,
+// neighbor cache and the Jacobi push-out with friction.
+//
+//   ComputeIntCoord/HashCoords ...... xrtailor/src/physics/broad_phase/spatial_hash/SpatialHashGPU.cu:9-25
+//   FindCellStart_Kernel ............ SpatialHashGPU.cu:27-54
+//   CacheNeighbors_Kernel ........... SpatialHashGPU.cu:56-99
+//   HashObjects ..................... SpatialHashGPU.cu:128-160 (cub radix sort -> radix.cu)
+//   CollideParticles_Kernel ......... xrtailor/src/physics/ClothSolverHelper.cu:171-219
+//   ComputeFriction / ApplyDeltas ... ClothSolverHelper.cu:139-169
+//
+// The push-out reads positions from one buffer and writes the relaxed result to the other (the
+// caller swaps them), which is the reference's deltas + ApplyDeltas pair in one launch.
+#include "common.cuh"
+#include "context.h"
+
+namespace xrt {
+namespace {
+
+__device__ __forceinline__ int int_coord(float value, float spacing) {
+  return (int)floorf(value / spacing);
+}
+__device__ __forceinline__ int hash_coords(int x, int y, int z, int table) {
+  const int h = (int)(((uint32_t)x * 92837111u) ^ ((uint32_t)y * 689287499u) ^
+                      ((uint32_t)z * 283923481u));
+  return abs(h % table);
+}
+
+__global__ void k_hash(const float4* __restrict__ x, uint32_t nv, float spacing, int table,
+                       uint32_t* __restrict__ key, uint32_t* __restrict__ val) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  const float4 p = x[i];
+  key[i] = (uint32_t)hash_coords(int_coord(p.x, spacing), int_coord(p.y, spacing),
+                                 int_coord(p.z, spacing), table);
+  val[i] = i;
+}
+
+__global__ void k_cell_bounds(const uint32_t* __restrict__ skey, uint32_t nv,
+                              uint32_t* __restrict__ cell_start, uint32_t* __restrict__ cell_end) {
+  const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= nv) return;
+  const uint32_t h = skey[id];
+  if (id == 0 || h != skey[id - 1]) {
+    cell_start[h] = id;
+    if (id > 0) cell_end[skey[id - 1]] = id;
+  }
+  if (id == nv - 1) cell_end[h] = id + 1;
+}
+
+__global__ void k_cache_neighbors(const uint32_t* __restrict__ sidx,
+                                  const uint32_t* __restrict__ cell_start,
+                                  const uint32_t* __restrict__ cell_end,
+                                  const float4* __restrict__ x, const float4* __restrict__ x_init,
+                                  uint32_t nv, float spacing, float spacing2, float d2, int table,
+                                  uint32_t maxnb, uint32_t* __restrict__ neighbors) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= nv) return;
+  const uint32_t id = sidx[tid];
+  const f3 pos = mk3(x[id]);
+  const f3 orig = mk3(x_init[id]);
+  const int ix = int_coord(pos.x, spacing), iy = int_coord(pos.y, spacing),
+            iz = int_coord(pos.z, spacing);
+  uint64_t ni = id;
+  const uint64_t limit = (uint64_t)nv * maxnb;
+  for (int xx = ix - 1; xx <= ix + 1; ++xx)
+    for (int yy = iy - 1; yy <= iy + 1; ++yy)
+      for (int zz = iz - 1; zz <= iz + 1; ++zz) {
+        const int h = hash_coords(xx, yy, zz, table);
+        const uint32_t start = cell_start[h];
+        if (start == kNone) continue;
+        const uint32_t end = min(cell_end[h], start + maxnb);
+        for (uint32_t k = start; k < end; ++k) {
+          const uint32_t nb = sidx[k];
+          const f3 dp = pos - mk3(x[nb]);
+          const f3 d0 = orig - mk3(x_init[nb]);
+          if (nb != id && dot(dp, dp) < spacing2 && dot(d0, d0) > d2) {
+            neighbors[ni] = nb;
+            ni += nv;
+            if (ni >= limit) return;
+          }
+        }
+      }
+  if (ni < limit) neighbors[ni] = kNone;
+}
+
+__device__ __forceinline__ f3 friction_of(float mu, f3 correction, f3 rel_vel) {
+  f3 fr = mk3(0, 0, 0);
+  const float cl = length(correction);
+  if (mu > 0.0f && cl > 0.0f) {
+    const f3 nrm = correction / cl;
+    const f3 tan_vel = rel_vel - nrm * dot(rel_vel, nrm);
+    const float tl = length(tan_vel);
+    const float max_tl = cl * mu;
+    fr = -tan_vel * tmin(max_tl / tl, 1.0f);
+  }
+  return fr;
+}
+
+__global__ void k_collide(const float4* __restrict__ x_in, float4* __restrict__ x_out,
+                          const float4* __restrict__ x0, const uint32_t* __restrict__ neighbors,
+                          uint32_t nv, uint32_t maxnb, float diameter, float mu, float relaxation) {
+  const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= nv) return;
+  const float4 pi = x_in[id];
+  const f3 pred_i = mk3(pi);
+  const f3 vel_i = pred_i - mk3(x0[id]);
+  const float w_i = pi.w;
+  f3 pd = mk3(0, 0, 0);
+  int cnt = 0;
+  const uint64_t limit = (uint64_t)nv * maxnb;
+  for (uint64_t k = id; k < limit; k += nv) {
+    const uint32_t j = neighbors[k];
+    if (j >= nv) break;  // reference: j > num_particles; j == nv never occurs
+    const float4 pj = x_in[j];
+    const float denom = w_i + pj.w;
+    if (denom <= 0) continue;
+    const f3 pred_j = mk3(pj);
+    const f3 diff = pred_i - pred_j;
+    const float distance = length(diff);
+    if (distance >= diameter) continue;
+    const f3 gradient = diff / (distance + kEps);
+    const float lambda = (distance - diameter) / denom;
+    const f3 common = lambda * gradient;
+    ++cnt;
+    pd = pd - w_i * common;
+    const f3 rel = vel_i - (pred_j - mk3(x0[j]));
+    pd = pd + w_i * friction_of(mu, common, rel);
+  }
+  f3 q = pred_i;
+  const float count = (float)cnt;
+  if (count > 0.0f) q = q + pd / count * relaxation;
+  x_out[id] = mk4(q, w_i);
+}
+
+}  // namespace
+
+void launch_hash(Context& c) {
+  const uint32_t nv = c.nv;
+  if (nv == 0) return;
+  const float spacing = c.particle_diameter * c.params.hash_cell_size;
+  const float spacing2 = spacing * spacing;
+  const float d2 = c.particle_diameter * c.particle_diameter;
+  const int table = (int)(2 * nv);
+  int bits = 0;
+  while ((1u << bits) < (uint32_t)table) ++bits;
+  k_hash<<<grid_for(nv), kBlock, 0, c.stream>>>(c.x.p, nv, spacing, table, c.hash_key.p,
+                                                c.hash_val.p);
+  uint32_t *skey = nullptr, *sidx = nullptr;
+  c.hash_sorter.sort(c.hash_key.p, c.hash_val.p, nv, bits, c.stream, &skey, &sidx);
+  cudaMemsetAsync(c.cell_start.p, 0xFF, sizeof(uint32_t) * table, c.stream);
+  k_cell_bounds<<<grid_for(nv), kBlock, 0, c.stream>>>(skey, nv, c.cell_start.p, c.cell_end.p);
+  k_cache_neighbors<<<grid_for(nv), kBlock, 0, c.stream>>>(
+      sidx, c.cell_start.p, c.cell_end.p, c.x.p, c.x_init.p, nv, spacing, spacing2, d2, table,
+      (uint32_t)c.params.max_neighbor_size, c.neighbors.p);
+}
+
+void launch_collide(Context& c, const FrameConst& k) {
+  k_collide<<<grid_for(c.nv), kBlock, 0, c.stream>>>(
+      c.x.p, c.x_alt.p, c.x0.p, c.neighbors.p, c.nv, (uint32_t)c.params.max_neighbor_size,
+      k.particle_diameter, k.friction, k.relaxation);
+}
+
+}  // namespace xrt

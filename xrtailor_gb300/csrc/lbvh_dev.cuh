@@ -1,0 +1,85 @@
+// lbvh_dev.cuh — device-side LBVH box tests and the stackless traversal shared by the query,
+// contact-generation and self-contact kernels.
+//
+// Box tests restate Bounds::Overlap (xrtailor/src/physics/broad_phase/Bounds.cu:115-191);
+// the traversal restates QueryDeviceStackless (xrtailor/src/physics/broad_phase/lbvh/BVH.cu:957-1055):
+// left-first, escape indices instead of a stack, at most LBVH_MAX_BUFFER_SIZE (256) hits.
+// Candidates are handed to a visitor in traversal order instead of a 1 KB per-thread buffer, so
+// the narrow phase runs inline with identical first-minimum semantics.
+#pragma once
+#include "common.cuh"
+#include "context.h"
+
+namespace xrt {
+
+__device__ __forceinline__ bool overlap_point(float4 l, float4 h, f3 p) {
+  return p.x > l.x && p.x < h.x && p.y > l.y && p.y < h.y && p.z > l.z && p.z < h.z;
+}
+
+__device__ __forceinline__ int seg_intersection(float d1, float d2, f3 p1, f3 p2, f3& hit) {
+  if ((d1 * d2) >= 0.0f) return 0;
+  if (d1 == d2) return 0;
+  hit = p1 + (p2 - p1) * (-d1 / (d2 - d1));
+  return 1;
+}
+__device__ __forceinline__ int seg_in_box(f3 q, float4 l, float4 h, int axis) {
+  if (axis == 1 && q.z > l.z && q.z < h.z && q.y > l.y && q.y < h.y) return 1;
+  if (axis == 2 && q.z > l.z && q.z < h.z && q.x > l.x && q.x < h.x) return 1;
+  if (axis == 3 && q.x > l.x && q.x < h.x && q.y > l.y && q.y < h.y) return 1;
+  return 0;
+}
+
+__device__ __forceinline__ bool overlap_segment(float4 l, float4 h, f3 p1, f3 p2) {
+  if (p2.x < l.x && p1.x < l.x) return false;
+  if (p2.x > h.x && p1.x > h.x) return false;
+  if (p2.y < l.y && p1.y < l.y) return false;
+  if (p2.y > h.y && p1.y > h.y) return false;
+  if (p2.z < l.z && p1.z < l.z) return false;
+  if (p2.z > h.z && p1.z > h.z) return false;
+  if (p1.x > l.x && p1.x < h.x && p1.y > l.y && p1.y < h.y && p1.z > l.z && p1.z < h.z) return true;
+  f3 hit = mk3(0, 0, 0);
+  if ((seg_intersection(p1.x - l.x, p2.x - l.x, p1, p2, hit) && seg_in_box(hit, l, h, 1)) ||
+      (seg_intersection(p1.y - l.y, p2.y - l.y, p1, p2, hit) && seg_in_box(hit, l, h, 2)) ||
+      (seg_intersection(p1.z - l.z, p2.z - l.z, p1, p2, hit) && seg_in_box(hit, l, h, 3)) ||
+      (seg_intersection(p1.x - h.x, p2.x - h.x, p1, p2, hit) && seg_in_box(hit, l, h, 1)) ||
+      (seg_intersection(p1.y - h.y, p2.y - h.y, p1, p2, hit) && seg_in_box(hit, l, h, 2)) ||
+      (seg_intersection(p1.z - h.z, p2.z - h.z, p1, p2, hit) && seg_in_box(hit, l, h, 3)))
+    return true;
+  return false;
+}
+
+__device__ __forceinline__ bool overlap_box(float4 l, float4 h, f3 qlo, f3 qhi) {
+  return !(l.x > qhi.x || h.x < qlo.x || l.y > qhi.y || h.y < qlo.y || l.z > qhi.z || h.z < qlo.z);
+}
+
+// Stackless traversal; `ov(lo, hi)` tests a node box, `visit(object)` receives each hit.
+template <class Overlap, class Visit>
+__device__ __forceinline__ uint32_t lbvh_traverse(const LbvhView& b, Overlap ov, Visit visit,
+                                                  uint32_t* err) {
+  const uint32_t ni = b.n - 1;
+  int nodei = 0;
+  uint32_t found = 0, guard = 0;
+  const uint32_t limit = 2 * b.n + 2;
+  while (nodei != -1) {
+    if (found >= kMaxCandidates) break;
+    if (++guard > limit) {
+      raise_error(err, kErrTraversal);
+      break;
+    }
+    const float4 l = b.lo[nodei], h = b.hi[nodei];
+    if (ov(l, h)) {
+      if ((uint32_t)nodei >= ni) {
+        visit((uint32_t)__float_as_int(l.w));
+        ++found;
+        nodei = __float_as_int(h.w);
+      } else {
+        nodei = __float_as_int(l.w);
+      }
+    } else {
+      nodei = __float_as_int(h.w);
+    }
+  }
+  return found;
+}
+
+}  // namespace xrt

@@ -1,0 +1,260 @@
+// setup.cpp — host-side setup of the cloth step (runs once per xrt_start / xrt_add_cloth).
+//
+// Rest data follow the reference's setup code with glm's float evaluation order (this file is
+// compiled without FMA contraction):
+//   stretch rest lengths ....... PrepareBasicStretchData (src/physics/ClothSolverHelper.cpp:90-109)
+//   bend elements / rest angles  GenerateBendingElements (ClothSolverHelper.cpp:4-88), including the
+//                                string test for the winding of the first face
+//   geodesic LRA lengths ....... Geodesic::ComputeGeodesicDistance (src/utils/Geodesic.cpp:6-79)
+//   representative triangles ... RTriBuild_Kernel (src/physics/representative_triangle/RTriangle.cu:19-84)
+// The reference takes edge order from vcglib; here edges are numbered by first appearance over
+// the faces, and the graph coloring (randomized in the reference, GraphColoring::Paint,
+// src/physics/graph_coloring/Base.cu:163-317) is a deterministic greedy coloring unless the
+// caller supplies one.
+#include "setup.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <map>
+#include <queue>
+#include <set>
+
+namespace xrt {
+namespace setup {
+
+static inline V3 add(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+V3 sub(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+static inline V3 mul(V3 a, float s) { return V3{a.x * s, a.y * s, a.z * s}; }
+static inline float dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+static inline V3 cross(V3 a, V3 b) {
+  return V3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+}
+float length(V3 a) { return std::sqrt(dot(a, a)); }
+static inline V3 normalize(V3 a) { return mul(a, 1.0f / std::sqrt(dot(a, a))); }
+
+V3 transform_point(const float* m, V3 p) {
+  float r[3];
+  for (int k = 0; k < 3; ++k) {
+    const float a0 = m[0 + k] * p.x, a1 = m[4 + k] * p.y, a2 = m[8 + k] * p.z, a3 = m[12 + k] * 1.0f;
+    r[k] = (a0 + a1) + (a2 + a3);
+  }
+  return V3{r[0], r[1], r[2]};
+}
+
+void build_edges(const std::vector<uint32_t>& tri, std::vector<uint32_t>& e,
+                 std::vector<std::vector<uint32_t>>& ef) {
+  std::map<uint64_t, uint32_t> seen;
+  const uint32_t nf = (uint32_t)(tri.size() / 3);
+  for (uint32_t f = 0; f < nf; ++f) {
+    for (int k = 0; k < 3; ++k) {
+      const uint32_t a = tri[f * 3 + k], b = tri[f * 3 + (k + 1) % 3];
+      const uint64_t key = ((uint64_t)std::min(a, b) << 32) | std::max(a, b);
+      auto it = seen.find(key);
+      if (it == seen.end()) {
+        seen.emplace(key, (uint32_t)(e.size() / 2));
+        e.push_back(a);
+        e.push_back(b);
+        ef.push_back(std::vector<uint32_t>{f});
+      } else {
+        ef[it->second].push_back(f);
+      }
+    }
+  }
+}
+
+void build_bends(const std::vector<V3>& pos, const std::vector<uint32_t>& tri,
+                 const std::vector<uint32_t>& e, const std::vector<std::vector<uint32_t>>& ef,
+                 uint32_t offset, std::vector<uint32_t>& out, std::vector<float>& angles) {
+  const size_t ne = e.size() / 2;
+  for (size_t ei = 0; ei < ne; ++ei) {
+    const std::vector<uint32_t>& faces = ef[ei];
+    if (faces.size() < 2) continue;
+    const uint32_t ea = e[ei * 2], eb = e[ei * 2 + 1];
+    uint32_t idx1 = ea, idx2 = eb;
+    for (size_t i = 0; i < faces.size(); ++i) {
+      for (size_t j = i + 1; j < faces.size(); ++j) {
+        const uint32_t f1 = faces[i], f2 = faces[j];
+        auto opposite = [&](uint32_t f) {
+          for (int k = 0; k < 3; ++k) {
+            const uint32_t q = tri[f * 3 + k];
+            if (q != ea && q != eb) return q;
+          }
+          return tri[f * 3];
+        };
+        const uint32_t idx3 = opposite(f1), idx4 = opposite(f2);
+        std::string f1s = std::to_string(tri[f1 * 3]) + "," + std::to_string(tri[f1 * 3 + 1]) + "," +
+                          std::to_string(tri[f1 * 3 + 2]);
+        f1s += "," + f1s;
+        const std::string common = std::to_string(idx1) + "," + std::to_string(idx2);
+        if (f1s.find(common) == std::string::npos) std::swap(idx1, idx2);
+        const V3 v1 = pos[idx1], v2 = pos[idx2], v3 = pos[idx3], v4 = pos[idx4];
+        const V3 n1 = normalize(cross(sub(v1, v3), sub(v2, v3)));
+        const V3 n2 = normalize(cross(sub(v2, v4), sub(v1, v4)));
+        float d = dot(n1, n2);
+        if (d < -1) d = -1;
+        else if (d > 1) d = 1;
+        out.push_back(idx1 + offset);
+        out.push_back(idx2 + offset);
+        out.push_back(idx3 + offset);
+        out.push_back(idx4 + offset);
+        angles.push_back(std::acos(d));
+      }
+    }
+  }
+}
+
+std::vector<float> geodesic(const std::vector<V3>& pos,
+                            const std::vector<std::vector<uint32_t>>& adj, uint32_t src) {
+  std::vector<float> dist(pos.size(), FLT_MAX);
+  typedef std::pair<float, uint32_t> Item;
+  std::priority_queue<Item, std::vector<Item>, std::greater<Item>> pq;
+  dist[src] = 0.0f;
+  pq.push(Item(0.0f, src));
+  while (!pq.empty()) {
+    const uint32_t cur = pq.top().second;
+    pq.pop();
+    for (uint32_t nb : adj[cur]) {
+      const float w = length(sub(pos[nb], pos[cur]));
+      if (dist[nb] > dist[cur] + w) {
+        dist[nb] = dist[cur] + w;
+        pq.push(Item(dist[nb], nb));
+      }
+    }
+  }
+  return dist;
+}
+
+std::vector<uint32_t> greedy_color(const std::vector<uint32_t>& idx, int arity, uint32_t nv,
+                                   uint32_t& ncolors) {
+  const size_t n = idx.size() / arity;
+  std::vector<uint32_t> col(n);
+  // per vertex: bit mask of the first 64 colors, overflow list beyond
+  std::vector<uint64_t> mask(nv, 0);
+  std::vector<std::vector<uint32_t>> over(nv);
+  ncolors = 0;
+  for (size_t c = 0; c < n; ++c) {
+    uint64_t used = 0;
+    for (int a = 0; a < arity; ++a) used |= mask[idx[c * arity + a]];
+    uint32_t k;
+    if (~used) {
+      k = (uint32_t)__builtin_ctzll(~used);
+    } else {
+      k = 64;
+      for (;; ++k) {
+        bool clash = false;
+        for (int a = 0; a < arity && !clash; ++a) {
+          const auto& o = over[idx[c * arity + a]];
+          clash = std::find(o.begin(), o.end(), k) != o.end();
+        }
+        if (!clash) break;
+      }
+    }
+    col[c] = k;
+    for (int a = 0; a < arity; ++a) {
+      if (k < 64) mask[idx[c * arity + a]] |= (1ull << k);
+      else over[idx[c * arity + a]].push_back(k);
+    }
+    ncolors = std::max(ncolors, k + 1);
+  }
+  return col;
+}
+
+bool coloring_valid(const std::vector<uint32_t>& idx, int arity, const std::vector<uint32_t>& col,
+                    uint32_t nv, std::string& why) {
+  const size_t n = idx.size() / arity;
+  if (col.size() != n) {
+    why = "coloring has " + std::to_string(col.size()) + " entries, expected " + std::to_string(n);
+    return false;
+  }
+  std::vector<std::set<uint32_t>> used(nv);
+  for (size_t c = 0; c < n; ++c)
+    for (int a = 0; a < arity; ++a)
+      if (!used[idx[c * arity + a]].insert(col[c]).second) {
+        why = "constraints sharing vertex " + std::to_string(idx[c * arity + a]) + " have color " +
+              std::to_string(col[c]);
+        return false;
+      }
+  return true;
+}
+
+void build_vf(const std::vector<uint32_t>& tri, uint32_t nv, std::vector<uint32_t>& ptr,
+              std::vector<uint32_t>& list) {
+  ptr.assign(nv + 1, 0);
+  const uint32_t nf = (uint32_t)(tri.size() / 3);
+  for (uint32_t f = 0; f < nf; ++f)
+    for (int k = 0; k < 3; ++k) ptr[tri[f * 3 + k] + 1]++;
+  for (uint32_t i = 0; i < nv; ++i) ptr[i + 1] += ptr[i];
+  list.assign(ptr[nv], 0);
+  std::vector<uint32_t> fill(ptr.begin(), ptr.end() - 1);
+  for (uint32_t f = 0; f < nf; ++f)  // ascending f keeps every list sorted
+    for (uint32_t k = 0; k < 3; ++k) list[fill[tri[f * 3 + k]]++] = (f << 2) | k;
+}
+
+void build_ve(const std::vector<uint32_t>& edges, uint32_t nv, std::vector<uint32_t>& ptr,
+              std::vector<uint32_t>& list) {
+  ptr.assign(nv + 1, 0);
+  const uint32_t ne = (uint32_t)(edges.size() / 2);
+  for (uint32_t e = 0; e < ne; ++e) {
+    ptr[edges[2 * e] + 1]++;
+    ptr[edges[2 * e + 1] + 1]++;
+  }
+  for (uint32_t i = 0; i < nv; ++i) ptr[i + 1] += ptr[i];
+  list.assign(ptr[nv], 0);
+  std::vector<uint32_t> fill(ptr.begin(), ptr.end() - 1);
+  for (uint32_t e = 0; e < ne; ++e) {
+    list[fill[edges[2 * e]]++] = (e << 1) | 0u;
+    list[fill[edges[2 * e + 1]]++] = (e << 1) | 1u;
+  }
+}
+
+std::vector<uint32_t> build_rtri(const std::vector<uint32_t>& tri, uint32_t nv) {
+  // sorted, de-duplicated vertex -> face lists (the reference's std::set per vertex)
+  std::vector<std::vector<uint32_t>> vf(nv);
+  const uint32_t nf = (uint32_t)(tri.size() / 3);
+  for (uint32_t f = 0; f < nf; ++f)
+    for (int k = 0; k < 3; ++k) vf[tri[f * 3 + k]].push_back(f);
+  std::vector<uint32_t> pre(nv + 1, 0), lst;
+  for (uint32_t i = 0; i < nv; ++i) {
+    auto& l = vf[i];
+    std::sort(l.begin(), l.end());
+    l.erase(std::unique(l.begin(), l.end()), l.end());
+    lst.insert(lst.end(), l.begin(), l.end());
+    pre[i + 1] = (uint32_t)lst.size();
+  }
+  std::vector<uint32_t> out(nf, 0);
+  for (uint32_t fid = 0; fid < nf; ++fid) {
+    const uint32_t fv[3] = {tri[fid * 3], tri[fid * 3 + 1], tri[fid * 3 + 2]};
+    uint32_t info = 0;
+    uint32_t j_start = pre[fv[0]], j_end = pre[fv[0] + 1];
+    for (uint32_t iv = 0; iv < 3; ++iv) {
+      uint32_t off = j_start;
+      const uint32_t i_end = j_end;
+      uint32_t i_f = lst[off++];
+      if (i_f == fid) info |= 1u << iv;
+      const uint32_t jv = (iv + 1) % 3;
+      j_start = pre[fv[jv]];
+      j_end = pre[fv[jv] + 1];
+      uint32_t of = 0xFFFFFFFFu;
+      for (uint32_t jno = j_start; jno < j_end; ++jno)
+        if (lst[jno] == i_f && fid != i_f) {
+          of = i_f;
+          break;
+        }
+      for (; off < i_end && of == 0xFFFFFFFFu; ++off) {
+        i_f = lst[off];
+        for (uint32_t jno = j_start; jno < j_end; ++jno)
+          if (lst[jno] == i_f && fid != i_f) {
+            of = i_f;
+            break;
+          }
+      }
+      if (fid < of) info |= 1u << (iv + 3);
+    }
+    out[fid] = info;
+  }
+  return out;
+}
+
+}  // namespace setup
+}  // namespace xrt

@@ -1,0 +1,228 @@
+"""Seeded synthetic scenes for the cloth step (no dataset or asset files are involved).
+
+The reference ships demo scenes (examples/) and relies on SMPL body models that are not part of
+it; these generators stand in with the shapes and sizes of the benchmark configurations:
+  * grid cloth: n x n vertices over a square, two triangles per quad, 2n(n-1)+(n-1)^2 edges,
+    seeded per-coordinate jitter;
+  * icosphere obstacle (subdivision 3: 642 vertices / 1,280 triangles);
+  * tube body with the SMPL mesh's counts (82 rings x 84 slices + 2 poles = 6,890 vertices,
+    13,776 triangles), skinned rigidly to a chain of 24 bones whose joint angles are sums of 3
+    seeded sinusoids (amplitude <= 0.4 rad in total per joint, 0.2-1.5 Hz);
+  * tessellated ground plane.
+"""
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from .solver import Mesh
+
+
+def grid_cloth(n: int, size: float = 1.0, origin=(0.0, 0.0, 0.0), jitter: float = 1e-3,
+               seed: int = 1) -> Mesh:
+    """n x n grid in the xz plane at height origin[1]; normal +y; vertex (i, j) = i * n + j."""
+    rng = np.random.default_rng(seed)
+    h = size / (n - 1)
+    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    pos = np.stack([origin[0] + j * h, np.full_like(i, origin[1], dtype=np.float64),
+                    origin[2] + i * h], axis=-1).reshape(-1, 3)
+    if jitter > 0:
+        pos = pos + rng.uniform(-jitter, jitter, size=pos.shape)
+    a = (i[:-1, :-1] * n + j[:-1, :-1]).reshape(-1)
+    b = a + 1
+    c = a + n
+    d = c + 1
+    tri = np.empty((a.size * 2, 3), np.uint32)
+    tri[0::2] = np.stack([a, c, b], -1)
+    tri[1::2] = np.stack([b, c, d], -1)
+    return Mesh(positions=pos.astype(np.float32), triangles=tri)
+
+
+def icosphere(subdiv: int = 3, radius: float = 0.3, center=(0.0, 0.0, 0.0)) -> Mesh:
+    t = (1.0 + 5 ** 0.5) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t),
+             (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+             (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8),
+             (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(v, np.float64) / np.linalg.norm(v) for v in verts]
+    for _ in range(subdiv):
+        cache = {}
+        new_faces = []
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            new_faces += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = new_faces
+    pos = np.array(verts) * radius + np.asarray(center)
+    return Mesh(positions=pos.astype(np.float32), triangles=np.array(faces, np.uint32))
+
+
+def ground_plane(n: int = 64, size: float = 4.0, height: float = 0.0, center=(0.0, 0.0)) -> Mesh:
+    m = grid_cloth(n, size, origin=(center[0] - size / 2, height, center[1] - size / 2), jitter=0.0)
+    return m
+
+
+@dataclass
+class TubeBody:
+    """Tube body with SMPL counts, rigidly skinned to a 24-bone chain along +y."""
+    rings: int = 82
+    slices: int = 84
+    height: float = 1.2
+    radius: float = 0.16
+    bones: int = 24
+    seed: int = 2
+    base: tuple = (0.0, 0.0, 0.0)
+    rest: np.ndarray = field(init=False)
+    triangles: np.ndarray = field(init=False)
+    bone_of: np.ndarray = field(init=False)
+
+    def __post_init__(self):
+        R, S = self.rings, self.slices
+        ys = np.linspace(0.08 * self.height, 0.92 * self.height, R)
+        phi = np.linspace(0, 2 * np.pi, S, endpoint=False)
+        prof = self.radius * (1.0 + 0.15 * np.sin(ys / self.height * 3 * np.pi))
+        ring = np.stack([np.cos(phi)[None, :] * prof[:, None],
+                         np.repeat(ys[:, None], S, 1),
+                         np.sin(phi)[None, :] * prof[:, None]], -1).reshape(-1, 3)
+        bottom = np.array([[0.0, 0.0, 0.0]])
+        top = np.array([[0.0, self.height, 0.0]])
+        self.rest = np.concatenate([ring, bottom, top]) + np.asarray(self.base)
+        tris = []
+        for r in range(R - 1):
+            for s in range(S):
+                a = r * S + s
+                b = r * S + (s + 1) % S
+                c = a + S
+                d = b + S
+                tris += [(a, c, b), (b, c, d)]
+        nb, nt = R * S, R * S + 1
+        for s in range(S):
+            tris.append((nb, s, (s + 1) % S))
+            a = (R - 1) * S + s
+            b = (R - 1) * S + (s + 1) % S
+            tris.append((nt, b, a))
+        self.triangles = np.array(tris, np.uint32)
+        yl = self.rest[:, 1] - self.base[1]
+        self.bone_of = np.clip((yl / self.height * self.bones).astype(int), 0, self.bones - 1)
+        rng = np.random.default_rng(self.seed)
+        self.amp = rng.uniform(0, 0.4 / 3, size=(self.bones, 3))
+        self.freq = rng.uniform(0.2, 1.5, size=(self.bones, 3))
+        self.phase = rng.uniform(0, 2 * np.pi, size=(self.bones, 3))
+        self.axis = np.where(np.arange(self.bones)[:, None] % 2 == 0, [[1.0, 0.0, 0.0]],
+                             [[0.0, 0.0, 1.0]])
+
+    @property
+    def mesh(self) -> Mesh:
+        return Mesh(positions=self.rest.astype(np.float32), triangles=self.triangles)
+
+    def joint_angles(self, t: float) -> np.ndarray:
+        return (self.amp * np.sin(2 * np.pi * self.freq * t + self.phase)).sum(1)
+
+    def pose(self, t: float) -> np.ndarray:
+        """World positions at time t: bone b rotates by angle_b / 6 relative to bone b-1."""
+        L = self.height / self.bones
+        ang = self.joint_angles(t) / 6.0
+        Rs, bases = [], []
+        Rcur = np.eye(3)
+        base = np.asarray(self.base, np.float64)
+        for b in range(self.bones):
+            ax = self.axis[b]
+            c, s = np.cos(ang[b]), np.sin(ang[b])
+            K = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+            Rrel = np.eye(3) + s * K + (1 - c) * K @ K
+            if b > 0:
+                base = base + Rcur @ np.array([0.0, L, 0.0])
+            Rcur = Rcur @ Rrel
+            Rs.append(Rcur.copy())
+            bases.append(base.copy())
+        Rs, bases = np.array(Rs), np.array(bases)
+        local = self.rest - np.asarray(self.base) - np.stack(
+            [np.zeros(len(self.rest)), self.bone_of * L, np.zeros(len(self.rest))], -1)
+        out = np.einsum("vij,vj->vi", Rs[self.bone_of], local) + bases[self.bone_of]
+        return out.astype(np.float32)
+
+
+def two_corner_pins(n: int) -> np.ndarray:
+    """Pins the two corners of the edge i = 0 (vertices 0 and n-1)."""
+    return np.array([0, n - 1], np.uint32)
+
+
+@dataclass
+class Scene:
+    name: str
+    cloth: Mesh
+    obstacle: Optional[Mesh]
+    params: dict
+    particle_diameter: float = 0.0
+    body: Optional[TubeBody] = None
+    frames: int = 1
+
+
+def _params(**kw):
+    from . import _lib as L
+    import ctypes as C
+    p = L.SwiftParams()
+    L.load().xrt_default_params(C.byref(p))
+    for k, v in kw.items():
+        if k == "gravity":
+            for i in range(3):
+                p.gravity[i] = v[i]
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def plain_small(n: int = 64, frames: int = 120) -> Scene:
+    """64x64 cloth (1 m, jitter +-1e-3, two corners pinned) onto an icosphere r = 0.3 m;
+    stretch 1e-8, bend 1e-6, 10 substeps x 10 iterations, self-contact thickness 2 mm."""
+    cloth = grid_cloth(n, 1.0, origin=(0.0, 0.4, 0.0), jitter=1e-3, seed=1)
+    cloth.fixed_indices = two_corner_pins(n)
+    sphere = icosphere(3, 0.3, center=(0.5, 0.0, 0.5))
+    return Scene("plain_small", cloth, sphere,
+                 dict(num_substeps=10, num_iterations=10, stretch_compliance=1e-8,
+                      bend_compliance=1e-6), particle_diameter=2e-3, frames=frames)
+
+
+def plain_garment(n: int = 256, frames: int = 240) -> Scene:
+    """256x256 cloth draped over the animated 6,890-vertex tube body; stretch, bend and LRA
+    (slots = the two pinned corners) with obstacle and self contact; 20 substeps x 15 iterations."""
+    body = TubeBody(seed=2)
+    top = body.height
+    cloth = grid_cloth(n, 1.0, origin=(-0.5, top + 0.05, -0.5), jitter=1e-3, seed=2)
+    cloth.fixed_indices = two_corner_pins(n)
+    cloth.attached_indices = two_corner_pins(n)
+    return Scene("plain_garment", cloth, body.mesh,
+                 dict(num_substeps=20, num_iterations=15, stretch_compliance=1e-8,
+                      bend_compliance=1e-6), body=body, frames=frames)
+
+
+def plain_heavy(n: int = 1024, frames: int = 180, seed: int = 3) -> Scene:
+    """1024x1024 cloth dropped diagonally with seeded folds onto a tessellated ground plane;
+    self contact 1 mm; 10 substeps x 10 iterations."""
+    rng = np.random.default_rng(seed)
+    cloth = grid_cloth(n, 2.0, origin=(-1.0, 0.0, -1.0), jitter=1e-4, seed=seed)
+    p = cloth.positions.astype(np.float64)
+    k = rng.uniform(2, 6, size=2)
+    ph = rng.uniform(0, 2 * np.pi, size=2)
+    p[:, 1] = 0.25 + 0.6 * (p[:, 0] + 1.0) / 2.0 + 0.05 * np.sin(k[0] * p[:, 0] + ph[0]) * np.sin(
+        k[1] * p[:, 2] + ph[1])
+    cloth.positions = p.astype(np.float32)
+    ground = ground_plane(64, 6.0, height=0.0)
+    return Scene("plain_heavy", cloth, ground,
+                 dict(num_substeps=10, num_iterations=10, stretch_compliance=1e-8,
+                      bend_compliance=1e-6), particle_diameter=1e-3, frames=frames)
+
+
+def scene_params(scene: Scene, **overrides):
+    kw = dict(scene.params)
+    kw.update(overrides)
+    return _params(**kw)
