@@ -196,6 +196,7 @@ def run_ours(args, rank, local_rank, world):
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
     solver.synchronize()
+    s = solver.sizes()  # launches_per_frame is known once the frame graph exists
     frame_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     t_dev = sum(frame_ms) / 1e3
     if world > 1:

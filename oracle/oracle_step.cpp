@@ -344,7 +344,8 @@ void hash_particles(Oracle& o) {
     }
     if (id == nv - 1) o.cell_end[h] = id + 1;
   }
-  if (o.neighbors.size() != (size_t)nv * maxnb) o.neighbors.assign((size_t)nv * maxnb, 0xffffffffu);
+  // thrust::device_vector::resize value-initialises the table (SpatialHashGPU.cu:173)
+  if (o.neighbors.size() != (size_t)nv * maxnb) o.neighbors.assign((size_t)nv * maxnb, 0u);
 #pragma omp parallel for schedule(dynamic, 256)
   for (long tid = 0; tid < (long)nv; ++tid) {  // CacheNeighbors_Kernel
     const uint32_t id = index[tid];
