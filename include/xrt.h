@@ -241,6 +241,23 @@ xrt_status xrt_lbvh_query(xrt_lbvh* bvh, int32_t kind, const float* queries, uin
 /* Wall-clock-free timing helper for benchmarks: the build's kernels on the given stream. */
 xrt_status xrt_lbvh_sizes(const xrt_lbvh* bvh, uint32_t* num_objects);
 
+/* LBVH build that allocates no memory.  No counterpart in the reference.
+ * For callers that may not allocate GPU memory: applications that host the solver inside their
+ * own frame loop (engines, DCC plugins) and forbid allocation after start-up, because
+ * cudaMalloc / cudaFree can synchronise the device mid-frame or fail under memory pressure.
+ * Same result as xrt_lbvh_build_device + xrt_lbvh_export, written to the caller's device
+ * buffers: sorted_morton / sorted_objects (n), nodes (4 x (2n-1) uint32), aabbs (6 x (2n-1)
+ * float), i_esc (n-1), e_esc (n).  d_pred may be NULL (= d_prims).  Asynchronous on `stream`.
+ * Working memory is one fixed ~17 MiB device array per GPU (held from first use until exit):
+ * at most 65,536 primitives (larger n -> XRT_ERR_FACE_CAPACITY).  All calls on a GPU share that
+ * array; calls whose device work overlaps race, so order them on one stream.  The first call on
+ * each GPU looks up the array's device address (cudaGetSymbolAddress) with that GPU current;
+ * make it before any stream capture starts. */
+xrt_status xrt_lbvh_build_noalloc(const float* d_prims, const float* d_pred, uint32_t n, float scr,
+                                  uint32_t* d_sorted_morton, uint32_t* d_sorted_objects,
+                                  uint32_t* d_nodes, float* d_aabbs, int32_t* d_i_esc,
+                                  int32_t* d_e_esc, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -155,6 +155,7 @@ SIGNATURES = {
     "xrt_lbvh_export": (C.c_int32, [P, UP, UP, UP, FP, IP, IP, IP]),
     "xrt_lbvh_query": (C.c_int32, [P, C.c_int32, FP, C.c_uint32, UP, UP]),
     "xrt_lbvh_sizes": (C.c_int32, [P, UP]),
+    "xrt_lbvh_build_noalloc": (C.c_int32, [P, P, C.c_uint32, C.c_float, P, P, P, P, P, P, P]),
 }
 
 _lib = None
