@@ -72,7 +72,15 @@ typedef struct xrt_swift_params {
   float hash_cell_size;            /* COLLISION.PARTICLE.HASH_CELL_SIZE (1.5, x particle diameter) */
   float frame_time;                /* Timer fixed_delta_time_ (1/60) */
   int32_t update_obstacle_animation; /* SimParams.update_obstacle_animation (1) */
-  int32_t reserved[8];
+  /* Quality-mode PBD repulsion inside the Swift frame (0 = off, the reference's Swift step).
+   * When on, each frame builds the cloth LBVH and Update(ccd)s the obstacle LBVH, and every
+   * iteration starts with SolveNoProximity, preceded every 10 iterations by UpdatePairs with
+   * thickness 1e-6 (ClothSolverBase.cpp:276-308).  Frames then run eagerly (pair counts are
+   * read back), not as a replayed graph. */
+  int32_t pbd_repulsion;
+  float pbd_thickness;             /* REPULSION.PBD_THICKNESS (1e-4) */
+  float repulsion_relaxation;      /* REPULSION.RELAXATION_RATE (0.25) */
+  int32_t reserved[5];
 } xrt_swift_params;
 
 /* Cloth registration, mirrors ClothSolverUniversal::AddCloth(mesh, model_matrix, particle_diameter)

@@ -40,6 +40,14 @@ _SIG = {
     "orc_export_obstacle_bvh": (None, [P, UP, UP, UP, FP, IP, IP]),
     "orc_export_contacts": (None, [P, IP, FP, IP, FP, FP]),
     "orc_export_neighbors": (None, [P, UP]), "orc_hash_now": (None, [P]),
+    "orc_cloth_bvh_build": (None, [P]), "orc_obstacle_bvh_update_ccd": (None, [P]),
+    "orc_update_pairs": (C.c_uint32, [P, C.c_float]),
+    "orc_solve_repulsion": (None, [P, C.c_float, C.c_float]),
+    "orc_check_impacts": (None, [P, C.c_float]),
+    "orc_get_pairs": (C.c_uint32, [P, UP]),
+    "orc_get_impacts": (None, [P, FP, FP, FP, UP, IP]),
+    "orc_set_positions_predicted": (None, [P, FP]), "orc_get_positions_predicted": (None, [P, FP]),
+    "orc_export_cloth_bvh": (None, [P, UP, UP, UP, FP, IP, IP]),
     "orc_lbvh_create": (P, []), "orc_lbvh_destroy": (None, [P]),
     "orc_lbvh_build": (None, [P, FP, FP, C.c_uint32, C.c_float]),
     "orc_lbvh_refit": (None, [P, FP, C.c_uint32]),
@@ -50,6 +58,7 @@ _SIG = {
     "orc_ray_intersect": (C.c_float, [FP, FP, C.c_float, FP]),
     "orc_closest_seg_seg": (C.c_float, [FP, FP, FP, FP, FP, FP]),
     "orc_solve_cubic": (C.c_int, [C.c_float, C.c_float, C.c_float, C.c_float, FP]),
+    "orc_acos_as": (C.c_float, [C.c_float]),
 }
 
 
@@ -216,6 +225,59 @@ class OracleSolver:
         self._l.orc_export_neighbors(self._h, out.ctypes.data_as(UP))
         return out
 
+    # -- Quality-mode self contact --------------------------------------------------------
+    def cloth_bvh_build(self):
+        self._l.orc_cloth_bvh_build(self._h)
+
+    def obstacle_bvh_update_ccd(self):
+        self._l.orc_obstacle_bvh_update_ccd(self._h)
+
+    def update_pairs(self, thickness):
+        return int(self._l.orc_update_pairs(self._h, float(thickness)))
+
+    def proximity_solve(self, thickness, relaxation):
+        self._l.orc_solve_repulsion(self._h, float(thickness), float(relaxation))
+
+    def check_impacts(self, thickness):
+        self._l.orc_check_impacts(self._h, float(thickness))
+
+    def pairs(self):
+        n = self._l.orc_get_pairs(self._h, None)
+        out = np.empty((n, 2), np.uint32)
+        self._l.orc_get_pairs(self._h, out.ctypes.data_as(UP))
+        return out
+
+    def impacts(self):
+        n = 15 * self._l.orc_get_pairs(self._h, None)
+        out = dict(t=np.empty(n, np.float32), w=np.empty((n, 4), np.float32),
+                   n=np.empty((n, 3), np.float32), nodes=np.empty((n, 4), np.uint32),
+                   is_vf=np.empty(n, np.int32))
+        self._l.orc_get_impacts(self._h, out["t"].ctypes.data_as(FP), out["w"].ctypes.data_as(FP),
+                                out["n"].ctypes.data_as(FP), out["nodes"].ctypes.data_as(UP),
+                                out["is_vf"].ctypes.data_as(IP))
+        return out
+
+    def set_predicted(self, x):
+        a = _f(x).reshape(-1)
+        self._l.orc_set_positions_predicted(self._h, a.ctypes.data_as(FP))
+
+    def predicted(self):
+        return self._read(self._l.orc_get_positions_predicted, self.sizes()["num_vertices"])
+
+    def export_cloth_bvh(self):
+        n = self.sizes()["num_triangles"]
+        nn = 2 * n - 1
+        out = dict(morton=np.empty(n, np.uint32), objects=np.empty(n, np.uint32),
+                   nodes=np.empty((nn, 4), np.uint32), aabbs=np.empty((nn, 6), np.float32),
+                   iesc=np.empty(max(n - 1, 1), np.int32), eesc=np.empty(n, np.int32))
+        self._l.orc_export_cloth_bvh(self._h, out["morton"].ctypes.data_as(UP),
+                                     out["objects"].ctypes.data_as(UP),
+                                     out["nodes"].ctypes.data_as(UP),
+                                     out["aabbs"].ctypes.data_as(FP),
+                                     out["iesc"].ctypes.data_as(IP), out["eesc"].ctypes.data_as(IP))
+        out["iesc"] = out["iesc"][: max(n - 1, 0)]
+        return out
+
     def close(self):
         if self._h:
             self._l.orc_destroy(self._h)
@@ -311,6 +373,10 @@ def closest_seg_seg(p1, q1, p2, q2):
     d = lib().orc_closest_seg_seg(*[v.ctypes.data_as(FP) for v in a], st.ctypes.data_as(FP),
                                   cc.ctypes.data_as(FP))
     return np.float32(d), st, cc
+
+
+def acos_as(x):
+    return float(lib().orc_acos_as(float(x)))
 
 
 def solve_cubic(a, b, c, d):

@@ -47,6 +47,20 @@ template <typename T> static inline T mabs(T x) { return x < T(0) ? -x : x; }
 static const float kEps = 1e-6f;       // EPSILON, core/Scalar.hpp:39
 static const float kScalarMax = FLT_MAX;  // SCALAR_MAX, core/Scalar.cuh:10
 
+// arccos on [0, 1]: Abramowitz & Stegun 4.4.46, |error| <= 2e-8 (the CUDA library evaluates the
+// same polynomial in its bend kernel, so both sides round identically).
+static inline float acos_as(float x) {
+  float p = -0.0012624911f;
+  p = p * x + 0.0066700901f;
+  p = p * x + -0.0170881256f;
+  p = p * x + 0.0308918810f;
+  p = p * x + -0.0501743046f;
+  p = p * x + 0.0889789874f;
+  p = p * x + -0.2145988016f;
+  p = p * x + 1.5707963050f;
+  return std::sqrt(1.0f - x) * p;
+}
+
 // MathFunctions::FaceNormal (src/math/MathFunctions.cu:14-20)
 static inline V3 face_normal(V3 a, V3 b, V3 c) { return normalize(cross(b - a, c - a)); }
 

@@ -91,6 +91,27 @@ struct Oracle {
   bool started = false;
   uint32_t frame_index = 0;
   std::vector<uint32_t> pending_colors[2];
+  // Quality-mode proximity repulsion / CCD impacts.  Unified numbering: cloth nodes, faces and
+  // edges first, then the obstacle's (the reference addresses both through Node*/Face*/Edge*).
+  std::vector<uint8_t> cfree;             // Node::is_free of cloth nodes (false when pinned)
+  std::vector<V3> cmesh_pos, omesh_pos;   // registration-time positions (Face::n is set from them)
+  std::vector<uint32_t> cface_edges, oface_edges;  // 3 per face: edge of (v_i, v_{i+1})
+  std::vector<int32_t> cedge_adj, oedge_adj;       // 4 per edge: adjacent faces, -1 = none
+  std::vector<uint32_t> crtri;
+  std::vector<V3> cface_n0, oface_n0;
+  std::vector<uint32_t> oedges;
+  Lbvh cloth_bvh;
+  std::vector<uint32_t> pairs;            // 2 per face pair (unified face ids)
+  std::vector<V3> rep_deltas;
+  std::vector<int32_t> rep_counts;
+  struct Impact {
+    float t;
+    float w[4];
+    V3 n;
+    uint32_t nodes[4];
+    int32_t is_vf;
+  };
+  std::vector<Impact> impacts;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -493,7 +514,7 @@ void solve_bend(Oracle& o, uint32_t color, float dt) {
     V3 n1 = normalize(cross(p2, p3));
     V3 n2 = normalize(cross(p2, p4));
     float d = clampf(dot(n1, n2), 0.0f, 1.0f);
-    float angle = std::acos(d);
+    float angle = acos_as(d);  // the reference calls acos; see oracle_math.h
     if (angle < kEps || std::isnan(d)) continue;
     V3 q3 = (cross(p2, n2) + cross(n1, p2) * d) / (length(cross(p2, p3)) + kEps);
     V3 q4 = (cross(p2, n1) + cross(n2, p2) * d) / (length(cross(p2, p4)) + kEps);
@@ -747,6 +768,448 @@ void solve_contacts(Oracle& o) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// Quality-mode proximity repulsion and CCD impacts
+//   UpdatePairs / Traverse ........ src/physics/repulsion/PBDRepulsion.cu:22-32,
+//                                   src/physics/broad_phase/lbvh/BVH.cu:1149-1227, 1315-1340
+//   BVH::Update(ccd) .............. BVH.cu:820-852
+//   EvaluateRep / ApplyPBDImpulse . PBDRepulsion.cu:264-313, 329-515
+//   Proximity ctor ................ src/physics/repulsion/Proximity.cu:10-37
+//   signed distances / InEdge ..... src/math/BasicPrimitiveTests.cu:286-301, 369-436
+//   CheckImpact(s) ................ src/physics/impact_zone/ImpactHelper.cu:34-177
+
+struct UNodes {  // unified node view: cloth then obstacle
+  const Oracle& o;
+  uint32_t V;
+  explicit UNodes(const Oracle& oo) : o(oo), V((uint32_t)oo.x.size()) {}
+  V3 x(uint32_t i) const { return i < V ? o.x[i] : o.ox[i - V]; }
+  V3 x0(uint32_t i) const { return i < V ? o.x0[i] : o.ox0[i - V]; }
+  float w(uint32_t i) const { return i < V ? o.w[i] : 1.0f / 1e3f; }  // PhysicsMeshHelper.cu:148
+  bool free_(uint32_t i) const { return i < V ? o.cfree[i] != 0 : false; }
+  uint32_t F() const { return (uint32_t)o.tri.size() / 3; }
+  uint32_t E() const { return (uint32_t)o.edges.size() / 2; }
+  uint32_t fnode(uint32_t f, int k) const {
+    return f < F() ? o.tri[f * 3 + k] : V + o.otri[(f - F()) * 3 + k];
+  }
+  uint32_t fedge(uint32_t f, int k) const {
+    return f < F() ? o.cface_edges[f * 3 + k] : E() + o.oface_edges[(f - F()) * 3 + k];
+  }
+  uint32_t frtri(uint32_t f) const { return f < F() ? o.crtri[f] : o.ortri[f - F()]; }
+  V3 fn0(uint32_t f) const { return f < F() ? o.cface_n0[f] : o.oface_n0[f - F()]; }
+  bool ffree(uint32_t f) const { return free_(fnode(f, 0)) && free_(fnode(f, 1)) && free_(fnode(f, 2)); }
+  uint32_t enode(uint32_t e, int k) const {
+    return e < E() ? o.edges[e * 2 + k] : V + o.oedges[(e - E()) * 2 + k];
+  }
+  int32_t eadj(uint32_t e, int k) const {
+    if (e < E()) return o.cedge_adj[e * 4 + k];
+    int32_t a = o.oedge_adj[(e - E()) * 4 + k];
+    return a < 0 ? -1 : (int32_t)(F() + (uint32_t)a);
+  }
+  bool efree(uint32_t e) const { return free_(enode(e, 0)) && free_(enode(e, 1)); }
+};
+
+inline float mixed(V3 a, V3 b, V3 c) { return dot(a, cross(b, c)); }
+
+// SignedVertexFaceDistance (BasicPrimitiveTests.cu:369-386).  On a degenerate face the reference
+// returns before writing w; here w stays at the caller's zeros.
+float signed_vf_distance(V3 x, V3 y0, V3 y1, V3 y2, V3& n, float* w) {
+  n = cross(normalize(y1 - y0), normalize(y2 - y0));
+  if (dot(n, n) < 1e-6f) return std::numeric_limits<float>::infinity();
+  n = normalize(n);
+  float h = dot(x - y0, n);
+  float b0 = mixed(y1 - x, y2 - x, n);
+  float b1 = mixed(y2 - x, y0 - x, n);
+  float b2 = mixed(y0 - x, y1 - x, n);
+  w[0] = 1.0f;
+  w[1] = -b0 / (b0 + b1 + b2);
+  w[2] = -b1 / (b0 + b1 + b2);
+  w[3] = -b2 / (b0 + b1 + b2);
+  return h;
+}
+
+// SignedEdgeEdgeDistance (BasicPrimitiveTests.cu:420-436); its glm::normalize(n) result is
+// discarded in the reference, so n stays unnormalized.
+float signed_ee_distance(V3 x0, V3 x1, V3 y0, V3 y1, V3& n, float* w) {
+  n = cross(normalize(x1 - x0), normalize(y1 - y0));
+  if (dot(n, n) < 1e-6f) return std::numeric_limits<float>::infinity();
+  float h = dot(x0 - y0, n);
+  float a0 = mixed(y1 - x1, y0 - x1, n);
+  float a1 = mixed(y0 - x0, y1 - x0, n);
+  float b0 = mixed(x0 - y1, x1 - y1, n);
+  float b1 = mixed(x1 - y0, x0 - y0, n);
+  w[0] = a0 / (a0 + a1);
+  w[1] = a1 / (a0 + a1);
+  w[2] = -b0 / (b0 + b1);
+  w[3] = -b1 / (b0 + b1);
+  return h;
+}
+
+// InEdge (BasicPrimitiveTests.cu:286-301): Face::n is the normal set at registration.
+bool in_edge(const UNodes& u, float wt, uint32_t e0, uint32_t e1) {
+  V3 xx = (1 - wt) * u.x(u.enode(e0, 0)) + wt * u.x(u.enode(e0, 1));
+  bool in = true;
+  for (int k = 0; k < 4; ++k) {
+    int32_t f = u.eadj(e1, k);
+    if (f < 0) continue;
+    V3 e = u.x(u.enode(e1, 1)) - u.x(u.enode(e1, 0));
+    V3 nn = u.fn0((uint32_t)f);
+    V3 r = xx - u.x(u.enode(e1, 0));
+    in &= (mixed(e, nn, r) >= 0);
+  }
+  return in;
+}
+
+// Edge::ComputeNormal (src/memory/Edge.cu:42-59)
+V3 edge_normal(const UNodes& u, uint32_t e) {
+  V3 ans{0, 0, 0};
+  int cnt = 0;
+  for (int k = 0; k < 4; ++k) {
+    int32_t f = u.eadj(e, k);
+    if (f < 0) break;
+    ans += face_normal(u.x(u.fnode(f, 0)), u.x(u.fnode(f, 1)), u.x(u.fnode(f, 2)));
+    cnt++;
+  }
+  if (cnt == 0) return ans;
+  return ans / (float)cnt;
+}
+
+struct Impulse {
+  uint32_t nodes[4];
+  V3 corr[4];
+};
+
+// EvaluateVFProximity (PBDRepulsion.cu:329-409) with the Proximity(node, face) normal rule.
+bool evaluate_vf(const UNodes& u, uint32_t node, uint32_t face, float h, Impulse& imp) {
+  const uint32_t f0 = u.fnode(face, 0), f1 = u.fnode(face, 1), f2 = u.fnode(face, 2);
+  if (node == f0 || node == f1 || node == f2) return false;
+  const uint32_t nd[4] = {node, f0, f1, f2};
+  V3 pn;
+  float pw[4] = {0, 0, 0, 0};
+  float d0 = signed_vf_distance(u.x0(nd[0]), u.x0(nd[1]), u.x0(nd[2]), u.x0(nd[3]), pn, pw);
+  if (d0 < 0.0f && u.ffree(face)) pn = -pn;
+  V3 fn;
+  float w[4] = {0, 0, 0, 0};
+  signed_vf_distance(u.x(nd[0]), u.x(nd[1]), u.x(nd[2]), u.x(nd[3]), fn, w);
+  bool inside = mmin(-w[1], mmin(-w[2], -w[3])) >= 1e-6f;
+  if (!inside) return false;
+  V3 n = face_normal(u.x(nd[1]), u.x(nd[2]), u.x(nd[3]));
+  float side = dot(n, pn) > 0.0f ? 1.0f : -1.0f;
+  V3 q = u.x(nd[0]), p1 = u.x(nd[1]), p2 = u.x(nd[2]), p3 = u.x(nd[3]);
+  q = q - p1;
+  p2 = p2 - p1;
+  p3 = p3 - p1;
+  n = side * cross(p2, p3);
+  float c23 = length(n);
+  n = normalize(n);
+  float C = dot(q, n) - h;
+  if (C > 0) return false;
+  V3 dcq = n;
+  V3 dcp2 = (cross(p3, q) + cross(n, p3) * dot(n, q)) / c23;
+  V3 dcp3 = -(cross(p2, q) + cross(n, p2) * dot(n, q)) / c23;
+  V3 dcp1 = -dcq - dcp2 - dcp3;
+  float denom = u.w(nd[0]) * dot(dcq, dcq) + u.w(nd[1]) * dot(dcp1, dcp1) +
+                u.w(nd[2]) * dot(dcp2, dcp2) + u.w(nd[3]) * dot(dcp3, dcp3);
+  if (denom < kEps) return false;
+  float s = C / denom;
+  imp.corr[0] = -u.w(nd[0]) * s * dcq;
+  imp.corr[1] = -u.w(nd[1]) * s * dcp1;
+  imp.corr[2] = -u.w(nd[2]) * s * dcp2;
+  imp.corr[3] = -u.w(nd[3]) * s * dcp3;
+  for (int k = 0; k < 4; ++k) imp.nodes[k] = nd[k];
+  return true;
+}
+
+// EvaluateEEProximity (PBDRepulsion.cu:411-468) with the Proximity(edge, edge) normal rule.
+bool evaluate_ee(const UNodes& u, uint32_t e0, uint32_t e1, float h, Impulse& imp) {
+  const uint32_t nd[4] = {u.enode(e0, 0), u.enode(e0, 1), u.enode(e1, 0), u.enode(e1, 1)};
+  if (nd[0] == nd[2] || nd[0] == nd[3] || nd[1] == nd[2] || nd[1] == nd[3]) return false;
+  V3 pn;
+  float pw[4] = {0, 0, 0, 0};
+  float d0 = signed_ee_distance(u.x0(nd[0]), u.x0(nd[1]), u.x0(nd[2]), u.x0(nd[3]), pn, pw);
+  if (!u.efree(e1)) {
+    pn = edge_normal(u, e1);
+  } else if (d0 < 0.0f) {
+    pn = -pn;
+  }
+  V3 ln;
+  float b[4] = {0, 0, 0, 0};
+  signed_ee_distance(u.x(nd[0]), u.x(nd[1]), u.x(nd[2]), u.x(nd[3]), ln, b);
+  bool inside = mmin(mmin(b[0], b[1]), mmin(-b[2], -b[3])) >= 1e-6f && in_edge(u, b[1], e0, e1) &&
+                in_edge(u, -b[3], e1, e0);
+  if (!inside) return false;
+  V3 d{0, 0, 0};
+  for (int k = 0; k < 4; ++k) d += b[k] * u.x(nd[k]);
+  V3 n = pn;
+  float C = dot(d, n) - h;
+  if (C > 0) return false;
+  b[2] *= -1;
+  b[3] *= -1;
+  V3 grads[4] = {b[0] * n, b[1] * n, -b[2] * n, -b[3] * n};
+  float denom = 0;
+  for (int k = 0; k < 4; ++k) denom += u.w(nd[k]) * b[k] * b[k];
+  if (denom < kEps) return false;
+  float s = C / denom;
+  for (int k = 0; k < 4; ++k) {
+    imp.nodes[k] = nd[k];
+    imp.corr[k] = -s * u.w(nd[k]) * grads[k];
+  }
+  return true;
+}
+
+// BVH::UpdateData(faces, 0, false) + Construct() of the cloth (ClothSolverBase.cpp:277-278).
+void build_cloth_bvh(Oracle& o) {
+  const uint32_t nf = (uint32_t)o.tri.size() / 3;
+  o.cloth_bvh.objects.resize(nf);
+  for (uint32_t f = 0; f < nf; ++f) {
+    Prim& pr = o.cloth_bvh.objects[f];
+    uint32_t a = o.tri[f * 3], b = o.tri[f * 3 + 1], c = o.tri[f * 3 + 2];
+    pr.idx1 = a; pr.idx2 = b; pr.idx3 = c;
+    pr.v1 = o.x0[a] + 0.0f * o.n[a];
+    pr.v2 = o.x0[b] + 0.0f * o.n[b];
+    pr.v3 = o.x0[c] + 0.0f * o.n[c];
+    pr.pred1 = pr.v1; pr.pred2 = pr.v2; pr.pred3 = pr.v3;
+  }
+  o.cloth_bvh.construct(0.0f);
+}
+
+// BVH::Update(faces, ccd = true) (BVH.cu:820-852): pred = x, leaves grow by the x/x0 bounds of
+// their face, internal boxes become the union of their leaves.
+void update_bvh_ccd(Lbvh& b, const std::vector<V3>& x, const std::vector<V3>& x0,
+                    const std::vector<uint32_t>& tri) {
+  if (!b.active) return;
+  const uint32_t n = b.num_objects(), ni = n - 1;
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t k = ni + i, obj = b.nodes[k].object;
+    const uint32_t id[3] = {tri[obj * 3], tri[obj * 3 + 1], tri[obj * 3 + 2]};
+    Prim& pr = b.objects[obj];
+    pr.pred1 = x[id[0]];
+    pr.pred2 = x[id[1]];
+    pr.pred3 = x[id[2]];
+    Box fb;  // Face::ComputeBounds(true)
+    for (int c = 0; c < 3; ++c) {
+      fb = box_merge_point(fb, x[id[c]]);
+      fb = box_merge_point(fb, x0[id[c]]);
+    }
+    b.aabbs[k] = box_merge(b.aabbs[k], fb);
+  }
+  b.merge_internal_cas();
+}
+
+// CountPairs_Kernel + inclusive scan + FindPairs_Kernel (BVH.cu:1149-1227, 1315-1340): pairs of
+// one query are written back to front.
+void traverse_pairs(const Lbvh& lhs, const Lbvh& rhs, uint32_t lhs_face_base,
+                    uint32_t rhs_face_base, float thickness, std::vector<uint32_t>& out) {
+  if (!lhs.active || !rhs.active) return;
+  const uint32_t nq = lhs.num_objects(), nil = nq - 1, nir = rhs.num_objects() - 1;
+  std::vector<std::vector<uint32_t>> hits(nq);
+  for (uint32_t id = 0; id < nq; ++id) {
+    Box q = lhs.aabbs[nil + id];
+    for (int i = 0; i < 3; ++i) {  // Bounds::Dilate
+      set(q.lo, i, get(q.lo, i) - thickness);
+      set(q.hi, i, get(q.hi, i) + thickness);
+    }
+    int node = 0;
+    while (node != -1) {
+      const BVNode& nd = rhs.nodes[node];
+      if (box_overlap_box(rhs.aabbs[node], q)) {
+        if (nd.object != kNone) {
+          hits[id].push_back(nd.object);
+          node = rhs.eesc[node - nir];
+        } else {
+          node = (int)nd.left;
+        }
+      } else {
+        node = nd.object != kNone ? rhs.eesc[node - nir] : rhs.iesc[node];
+      }
+    }
+  }
+  for (uint32_t id = 0; id < nq; ++id) {
+    const uint32_t obj = lhs.nodes[nil + id].object;
+    for (size_t k = hits[id].size(); k-- > 0;) {
+      out.push_back(lhs_face_base + obj);
+      out.push_back(rhs_face_base + hits[id][k]);
+    }
+  }
+}
+
+// PBDRepulsionSolver::UpdatePairs (PBDRepulsion.cu:22-32)
+void update_pairs(Oracle& o, float thickness) {
+  update_bvh_ccd(o.cloth_bvh, o.x, o.x0, o.tri);
+  o.pairs.clear();
+  const uint32_t F = (uint32_t)o.tri.size() / 3;
+  traverse_pairs(o.cloth_bvh, o.bvh, 0, F, thickness, o.pairs);
+  traverse_pairs(o.cloth_bvh, o.cloth_bvh, 0, 0, thickness, o.pairs);
+}
+
+// EvaluateRep_Kernel + ApplyPBDImpulse_Kernel (PBDRepulsion.cu:470-515, 299-313); the deltas
+// are summed in pair order (float atomics in the reference).
+void solve_repulsion(Oracle& o, float h, float relaxation) {
+  UNodes u(o);
+  const uint32_t V = u.V;
+  o.rep_deltas.assign(V, V3{0, 0, 0});
+  o.rep_counts.assign(V, 0);
+  auto accumulate = [&](const Impulse& imp) {
+    for (int k = 0; k < 4; ++k) {
+      if (length(imp.corr[k]) < kEps) continue;
+      if (!u.free_(imp.nodes[k])) continue;
+      o.rep_deltas[imp.nodes[k]] += imp.corr[k];
+      o.rep_counts[imp.nodes[k]] += 1;
+    }
+  };
+  const size_t np = o.pairs.size() / 2;
+  for (size_t p = 0; p < np; ++p) {
+    const uint32_t f0 = o.pairs[2 * p], f1 = o.pairs[2 * p + 1];
+    const uint32_t r0 = u.frtri(f0), r1 = u.frtri(f1);
+    for (int i = 0; i < 3; ++i) {
+      if (!((r0 >> i) & 1u)) continue;
+      Impulse imp;
+      if (evaluate_vf(u, u.fnode(f0, i), f1, h, imp)) accumulate(imp);
+    }
+    for (int i = 0; i < 3; ++i) {
+      if (!((r0 >> (i + 3)) & 1u)) continue;
+      for (int j = 0; j < 3; ++j) {
+        if (!((r1 >> (j + 3)) & 1u)) continue;
+        Impulse imp;
+        if (evaluate_ee(u, u.fedge(f0, i), u.fedge(f1, j), h, imp)) accumulate(imp);
+      }
+    }
+  }
+  for (uint32_t i = 0; i < V; ++i) {
+    float count = (float)o.rep_counts[i];
+    if (count <= kEps) continue;
+    V3 dx = o.rep_deltas[i] / count * relaxation;
+    o.x[i] = o.x[i] + dx;
+  }
+}
+
+// CheckImpact (ImpactHelper.cu:34-87)
+bool check_impact(const UNodes& u, bool vf, const uint32_t* nd, Oracle::Impact& im) {
+  for (int k = 0; k < 4; ++k) im.nodes[k] = nd[k];
+  V3 x0 = u.x0(nd[0]);
+  V3 v0 = u.x(nd[0]) - x0;
+  V3 x1 = u.x0(nd[1]) - x0, x2 = u.x0(nd[2]) - x0, x3 = u.x0(nd[3]) - x0;
+  V3 v1 = (u.x(nd[1]) - u.x0(nd[1])) - v0;
+  V3 v2 = (u.x(nd[2]) - u.x0(nd[2])) - v0;
+  V3 v3 = (u.x(nd[3]) - u.x0(nd[3])) - v0;
+  float a0 = mixed(x1, x2, x3);
+  float a1 = mixed(v1, x2, x3) + mixed(x1, v2, x3) + mixed(x1, x2, v3);
+  float a2 = mixed(x1, v2, v3) + mixed(v1, x2, v3) + mixed(v1, v2, x3);
+  float a3 = mixed(v1, v2, v3);
+  float t[3];
+  int ns = solve_cubic(a3, a2, a1, a0, t);
+  for (int i = 0; i < ns; ++i) {
+    if (t[i] < 0 || t[i] > 1) continue;
+    im.t = t[i];
+    auto pos = [&](uint32_t id) { return u.x0(id) + t[i] * (u.x(id) - u.x0(id)); };
+    V3 p0 = pos(nd[0]), p1 = pos(nd[1]), p2 = pos(nd[2]), p3 = pos(nd[3]);
+    float d;
+    bool inside;
+    if (vf) {
+      d = signed_vf_distance(p0, p1, p2, p3, im.n, im.w);
+      inside = mmin(-im.w[1], mmin(-im.w[2], -im.w[3])) >= -1e-6f;
+    } else {
+      d = signed_ee_distance(p0, p1, p2, p3, im.n, im.w);
+      inside = mmin(mmin(im.w[0], im.w[1]), mmin(-im.w[2], -im.w[3])) >= -1e-6f;
+    }
+    if (dot(im.n, im.w[1] * v1 + im.w[2] * v2 + im.w[3] * v3) > 0) im.n = -im.n;
+    if (mabs(d) < 1e-6f && inside) return true;
+  }
+  return false;
+}
+
+Box node_bounds(const UNodes& u, const uint32_t* ids, int count) {  // ComputeBounds(ccd = true)
+  Box b;
+  for (int k = 0; k < count; ++k) {
+    b = box_merge_point(b, u.x(ids[k]));
+    b = box_merge_point(b, u.x0(ids[k]));
+  }
+  return b;
+}
+
+bool overlap_dilated(const Box& a, const Box& b, float thickness) {  // Bounds::Overlap(b, h)
+  Box d = b;
+  for (int i = 0; i < 3; ++i) {
+    set(d.lo, i, get(d.lo, i) - thickness);
+    set(d.hi, i, get(d.hi, i) + thickness);
+  }
+  return box_overlap_box(a, d);
+}
+
+// CheckImpacts_Kernel (ImpactHelper.cu:116-171): 6 vertex-face and 9 edge-edge tests per pair.
+void check_impacts(Oracle& o, float thickness) {
+  UNodes u(o);
+  const size_t np = o.pairs.size() / 2;
+  o.impacts.assign(np * 15, Oracle::Impact{});
+  for (size_t p = 0; p < np; ++p) {
+    const uint32_t fa = o.pairs[2 * p], fb = o.pairs[2 * p + 1];
+    size_t index = 15 * p;
+    for (int side = 0; side < 2; ++side) {
+      const uint32_t f0 = side == 0 ? fa : fb, f1 = side == 0 ? fb : fa;
+      for (int i = 0; i < 3; ++i) {
+        Oracle::Impact& im = o.impacts[index++];
+        im.is_vf = 1;
+        const uint32_t nd[4] = {u.fnode(f0, i), u.fnode(f1, 0), u.fnode(f1, 1), u.fnode(f1, 2)};
+        for (int k = 0; k < 4; ++k) {
+          im.nodes[k] = nd[k];
+          im.w[k] = 0;
+        }
+        bool ok = false;
+        if (!(nd[0] == nd[1] || nd[0] == nd[2] || nd[0] == nd[3])) {
+          const uint32_t fn3[3] = {nd[1], nd[2], nd[3]};
+          if (overlap_dilated(node_bounds(u, nd, 1), node_bounds(u, fn3, 3), thickness))
+            ok = check_impact(u, true, nd, im);
+        }
+        if (!ok) im.t = -1;
+      }
+    }
+    for (int i = 0; i < 3; ++i) {
+      for (int j = 0; j < 3; ++j) {
+        Oracle::Impact& im = o.impacts[index++];
+        im.is_vf = 0;
+        const uint32_t ea = u.fedge(fa, i), eb = u.fedge(fb, j);
+        const uint32_t nd[4] = {u.enode(ea, 0), u.enode(ea, 1), u.enode(eb, 0), u.enode(eb, 1)};
+        for (int k = 0; k < 4; ++k) {
+          im.nodes[k] = nd[k];
+          im.w[k] = 0;
+        }
+        bool ok = false;
+        if (!(nd[0] == nd[2] || nd[0] == nd[3] || nd[1] == nd[2] || nd[1] == nd[3])) {
+          if (overlap_dilated(node_bounds(u, nd, 2), node_bounds(u, nd + 2, 2), thickness))
+            ok = check_impact(u, false, nd, im);
+        }
+        if (!ok) im.t = -1;
+      }
+    }
+  }
+}
+
+// Face edges, edge adjacency and registration-time face normals (Face::SetEdge, Face::Update,
+// PhysicsMeshHelper.cu:118-123) of a triangle list.
+void face_topology(const std::vector<uint32_t>& tri, const std::vector<uint32_t>& edges,
+                   const std::vector<V3>& reg_pos, std::vector<uint32_t>& face_edges,
+                   std::vector<int32_t>& edge_adj, std::vector<V3>& face_n0) {
+  std::map<std::pair<uint32_t, uint32_t>, uint32_t> key;
+  for (uint32_t e = 0; e < edges.size() / 2; ++e)
+    key[std::make_pair(std::min(edges[2 * e], edges[2 * e + 1]),
+                       std::max(edges[2 * e], edges[2 * e + 1]))] = e;
+  const uint32_t nf = (uint32_t)tri.size() / 3;
+  face_edges.assign(3 * (size_t)nf, 0);
+  edge_adj.assign(2 * edges.size(), -1);
+  std::vector<int> fill(edges.size() / 2, 0);
+  face_n0.resize(nf);
+  for (uint32_t f = 0; f < nf; ++f) {
+    for (int k = 0; k < 3; ++k) {
+      uint32_t a = tri[f * 3 + k], b = tri[f * 3 + (k + 1) % 3];
+      uint32_t e = key[std::make_pair(std::min(a, b), std::max(a, b))];
+      face_edges[f * 3 + k] = e;
+      if (fill[e] < 4) edge_adj[e * 4 + fill[e]++] = (int32_t)f;
+    }
+    V3 d1 = reg_pos[tri[f * 3 + 1]] - reg_pos[tri[f * 3]];
+    V3 d2 = reg_pos[tri[f * 3 + 2]] - reg_pos[tri[f * 3]];
+    face_n0[f] = normalize(cross(d1, d2));
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
 // frame — ClothSolverBase::SimulateSwift (ClothSolverBase.cpp:171-261)
 
 void step_frame(Oracle& o) {
@@ -756,6 +1219,11 @@ void step_frame(Oracle& o) {
   const bool obstacle_updated = p.update_obstacle_animation && !o.otri.empty();
   if (obstacle_updated) rebuild_obstacle_bvh(o, 0.0f);
   const bool has_obstacle = o.bvh.active;
+  const bool repulsion = p.pbd_repulsion != 0;
+  if (repulsion) {  // SimulateQuality (ClothSolverBase.cpp:276-293)
+    if (!o.otri.empty()) update_bvh_ccd(o.bvh, o.ox, o.ox0, o.otri);
+    build_cloth_bvh(o);
+  }
   const int frequency = (p.num_substeps * p.num_iterations) / p.num_collision_passes;
   int cnt = 0;
   for (int substep = 0; substep < p.num_substeps; ++substep) {
@@ -766,6 +1234,10 @@ void step_frame(Oracle& o) {
     }
     if (p.enable_self_collision && substep % p.inter_leaved_hash == 0) hash_particles(o);
     for (int it = 0; it < p.num_iterations; ++it) {
+      if (repulsion) {  // ClothSolverBase.cpp:303-313
+        if (it % 10 == 0) update_pairs(o, 1e-6f);
+        solve_repulsion(o, p.pbd_thickness, p.repulsion_relaxation);
+      }
       if (p.enable_self_collision) collide_particles(o);
       int current = substep * p.num_iterations + it;
       if (current % frequency == 0) {
@@ -836,6 +1308,15 @@ void start(Oracle& o) {
     rebuild_obstacle_bvh(o, 0.0f);  // ClothSolverUniversal::Start (ClothSolver.cpp:60-61)
     o.ortri = build_rtri(o.otri, o.ovf_prefix, o.ovf_list);
   }
+  // proximity topology: face edges, edge adjacency, registration normals, cloth R-triangles
+  face_topology(o.tri, o.edges, o.cmesh_pos, o.cface_edges, o.cedge_adj, o.cface_n0);
+  o.crtri = build_rtri(o.tri, o.vf_prefix, o.vf_list);
+  if (!o.otri.empty()) {
+    std::vector<std::vector<uint32_t>> oef;
+    o.oedges.clear();
+    build_edges(o.otri, (uint32_t)o.ox0.size(), o.oedges, oef);
+    face_topology(o.otri, o.oedges, o.omesh_pos, o.oface_edges, o.oedge_adj, o.oface_n0);
+  }
   // bindings: GenerateBinding_Kernel (BindingConstraint.cu:20-44) from x0 of both meshes
   for (Binding& b : o.bindings) {
     V3 pcl = o.x0[b.cloth];
@@ -888,7 +1369,12 @@ int orc_add_cloth(void* h, const xrt_cloth_desc* d) {
     o.w.push_back(1.0f);
   }
   for (uint32_t k = 0; k < 3 * d->num_triangles; ++k) o.tri.push_back(d->triangles[k] + c.offset);
-  for (uint32_t i = 0; i < d->num_fixed; ++i) o.w[c.offset + d->fixed_indices[i]] = 0.0f;
+  o.cfree.resize(o.x0.size(), 1);
+  for (uint32_t i = 0; i < d->num_fixed; ++i) {
+    o.w[c.offset + d->fixed_indices[i]] = 0.0f;  // SetInvMass(0) + SetFree(false)
+    o.cfree[c.offset + d->fixed_indices[i]] = 0;
+  }
+  o.cmesh_pos.insert(o.cmesh_pos.end(), c.mesh_pos.begin(), c.mesh_pos.end());
   // edges / stretch (PrepareBasicStretchData, ClothSolverHelper.cpp:90-109)
   std::vector<uint32_t> e;
   std::vector<std::vector<uint32_t>> ef;
@@ -954,6 +1440,7 @@ int orc_add_obstacle(void* h, const xrt_obstacle_desc* d) {
   uint32_t off = (uint32_t)o.ox0.size();
   for (uint32_t i = 0; i < d->num_vertices; ++i) {
     V3 q{d->positions[i * 3], d->positions[i * 3 + 1], d->positions[i * 3 + 2]};
+    o.omesh_pos.push_back(q);
     if (d->model_matrix) q = transform_point(d->model_matrix, q);
     o.ox0.push_back(q);
     o.ox.push_back(q);
@@ -1087,6 +1574,53 @@ void orc_hash_now(void* h) {  // run SpatialHashGPU::Hash on the current predict
   hash_particles(o);
 }
 
+// ---- Quality-mode proximity repulsion and CCD impacts ------------------------------------------
+void orc_cloth_bvh_build(void* h) { build_cloth_bvh(*static_cast<Oracle*>(h)); }
+void orc_obstacle_bvh_update_ccd(void* h) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  update_bvh_ccd(o.bvh, o.ox, o.ox0, o.otri);
+}
+uint32_t orc_update_pairs(void* h, float thickness) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  update_pairs(o, thickness);
+  return (uint32_t)(o.pairs.size() / 2);
+}
+void orc_solve_repulsion(void* h, float thickness, float relaxation) {
+  solve_repulsion(*static_cast<Oracle*>(h), thickness, relaxation);
+}
+void orc_check_impacts(void* h, float thickness) { check_impacts(*static_cast<Oracle*>(h), thickness); }
+uint32_t orc_get_pairs(void* h, uint32_t* out) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  if (out) std::copy(o.pairs.begin(), o.pairs.end(), out);
+  return (uint32_t)(o.pairs.size() / 2);
+}
+void orc_get_impacts(void* h, float* t, float* w, float* n, uint32_t* nodes, int32_t* is_vf) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  for (size_t k = 0; k < o.impacts.size(); ++k) {
+    const Oracle::Impact& im = o.impacts[k];
+    if (t) t[k] = im.t;
+    for (int j = 0; j < 4; ++j) {
+      if (w) w[k * 4 + j] = im.w[j];
+      if (nodes) nodes[k * 4 + j] = im.nodes[j];
+    }
+    if (n) {
+      n[k * 3] = im.n.x;
+      n[k * 3 + 1] = im.n.y;
+      n[k * 3 + 2] = im.n.z;
+    }
+    if (is_vf) is_vf[k] = im.is_vf;
+  }
+}
+void orc_set_positions_predicted(void* h, const float* x) {  // cloth x (predicted) only
+  Oracle& o = *static_cast<Oracle*>(h);
+  for (size_t i = 0; i < o.x.size(); ++i) o.x[i] = V3{x[i * 3], x[i * 3 + 1], x[i * 3 + 2]};
+}
+void orc_get_positions_predicted(void* h, float* out) { put3(static_cast<Oracle*>(h)->x, out); }
+void orc_export_cloth_bvh(void* h, uint32_t* morton, uint32_t* objs, uint32_t* nodes, float* aabbs,
+                          int32_t* iesc, int32_t* eesc) {
+  export_bvh(static_cast<Oracle*>(h)->cloth_bvh, morton, objs, nodes, aabbs, iesc, eesc);
+}
+
 // ---- standalone LBVH -------------------------------------------------------------------------
 void* orc_lbvh_create() { return new Lbvh(); }
 void orc_lbvh_destroy(void* h) { delete static_cast<Lbvh*>(h); }
@@ -1173,5 +1707,6 @@ float orc_closest_seg_seg(const float* p1, const float* q1, const float* p2, con
   return d;
 }
 int orc_solve_cubic(float a, float b, float c, float d, float* x) { return solve_cubic(a, b, c, d, x); }
+float orc_acos_as(float x) { return acos_as(x); }
 
 }  // extern "C"

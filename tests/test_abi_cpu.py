@@ -13,9 +13,13 @@ HEADER = os.path.join(ROOT, "include", "xrt.h")
 
 
 def declared_symbols():
-    text = open(HEADER).read()
-    return sorted(set(re.findall(r"^(?:xrt_status|const char\*)\s+(xrt_[a-z0-9_]+)\s*\(", text,
-                                 flags=re.M)))
+    import glob
+    syms = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        syms |= set(re.findall(r"^(?:xrt_status|const char\*)\s+(xrt_[a-z0-9_]+)\s*\(", text,
+                               flags=re.M))
+    return sorted(syms)
 
 
 def test_every_declared_symbol_is_exported(xrt):

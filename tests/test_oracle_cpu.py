@@ -83,6 +83,14 @@ def test_closest_segment_segment_known_answers(oracle_lib):
     assert d == np.float32(1.0) and st[1] == 0
 
 
+def test_arccos_polynomial_error_bound(oracle_lib):
+    """A&S 4.4.46 as evaluated in float by the oracle and the bend kernel."""
+    x = np.linspace(0.0, 1.0, 200001, dtype=np.float32)
+    got = np.array([orc.acos_as(float(v)) for v in x[::97]], np.float64)
+    ref = np.arccos(x[::97].astype(np.float64))
+    assert np.abs(got - ref).max() < 3e-7  # 2e-8 formula error + float evaluation
+
+
 def test_solve_cubic_roots(oracle_lib):
     # (x-0.2)(x-0.5)(x-0.8) = x^3 - 1.5x^2 + 0.66x - 0.08
     n, x = orc.solve_cubic(1.0, -1.5, 0.66, -0.08)

@@ -49,7 +49,10 @@ class SwiftParams(C.Structure):
         ("hash_cell_size", C.c_float),
         ("frame_time", C.c_float),
         ("update_obstacle_animation", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("pbd_repulsion", C.c_int32),
+        ("pbd_thickness", C.c_float),
+        ("repulsion_relaxation", C.c_float),
+        ("reserved", C.c_int32 * 5),
     ]
 
 
@@ -156,6 +159,17 @@ SIGNATURES = {
     "xrt_lbvh_query": (C.c_int32, [P, C.c_int32, FP, C.c_uint32, UP, UP]),
     "xrt_lbvh_sizes": (C.c_int32, [P, UP]),
     "xrt_lbvh_build_noalloc": (C.c_int32, [P, P, C.c_uint32, C.c_float, P, P, P, P, P, P, P]),
+    # include/xrt_contact.h
+    "xrt_cloth_bvh_build": (C.c_int32, [P]),
+    "xrt_obstacle_bvh_update_ccd": (C.c_int32, [P]),
+    "xrt_proximity_update_pairs": (C.c_int32, [P, C.c_float, UP]),
+    "xrt_proximity_solve": (C.c_int32, [P, C.c_float, C.c_float]),
+    "xrt_impacts_check": (C.c_int32, [P, C.c_float, UP]),
+    "xrt_export_pairs": (C.c_int32, [P, UP]),
+    "xrt_export_impacts": (C.c_int32, [P, FP, FP, FP, UP, IP]),
+    "xrt_export_cloth_bvh": (C.c_int32, [P, UP, UP, UP, FP, IP, IP]),
+    "xrt_get_predicted": (C.c_int32, [P, FP]),
+    "xrt_set_predicted": (C.c_int32, [P, FP]),
 }
 
 _lib = None

@@ -21,9 +21,6 @@ using xrt::ColorRange;
 using xrt::Context;
 using xrt::DBuf;
 
-struct xrt_ctx {
-  Context c;
-};
 
 struct xrt_lbvh {
   int device = 0;
@@ -180,6 +177,11 @@ void record_frame(Context& c) {
   }
   const bool has_obstacle = c.onf > 0;
   const bool bindings = c.nbind > 0;
+  const bool repulsion = p.pbd_repulsion != 0;
+  if (repulsion) {  // SimulateQuality: cloth LBVH per frame, obstacle Update(ccd) (:276-293)
+    if (has_obstacle) xrt::launch_update_ccd(c.bvh, c.ox.p, c.ox0.p, c.otri.p, c.stream, c.err.p);
+    xrt::launch_cloth_bvh_build(c);
+  }
   const int frequency = (p.num_substeps * p.num_iterations) / p.num_collision_passes;
   int cnt = 0;
   for (int s = 0; s < p.num_substeps; ++s) {
@@ -192,6 +194,10 @@ void record_frame(Context& c) {
       xrt::launch_hash(c);
     }
     for (int it = 0; it < p.num_iterations; ++it) {
+      if (repulsion) {  // PBD repulsion at the start of the iteration (ClothSolverBase.cpp:303-313)
+        if (it % 10 == 0) xrt::prox_update_pairs(c, 1e-6f);
+        xrt::prox_solve(c, p.pbd_thickness, p.repulsion_relaxation);
+      }
       if (p.enable_self_collision) {
         {
           Timed t(c, kCollide, 1, c.nv);
@@ -211,15 +217,30 @@ void record_frame(Context& c) {
         }
         cnt++;
       }
-      for (const ColorRange& r : c.s_ranges) {
-        Timed t(c, kStretch, 1, r.end - r.begin);
-        xrt::launch_stretch(c, k, r, it == 0);
-      }
-      if (p.solve_bending)
-        for (const ColorRange& r : c.b_ranges) {
-          Timed t(c, kBend, 1, r.end - r.begin);
-          xrt::launch_bend(c, k, r);
+      if (c.s_tiles.on) {
+        for (size_t tc = 0; tc < c.s_tiles.tile_colors.size(); ++tc) {
+          Timed t(c, kStretch, 1, c.s_tiles.tile_color_cons[tc]);
+          xrt::launch_stretch_tiles(c, k, c.s_tiles.tile_colors[tc], it == 0);
         }
+      } else {
+        for (const ColorRange& r : c.s_ranges) {
+          Timed t(c, kStretch, 1, r.end - r.begin);
+          xrt::launch_stretch(c, k, r, it == 0);
+        }
+      }
+      if (p.solve_bending) {
+        if (c.b_tiles.on) {
+          for (size_t tc = 0; tc < c.b_tiles.tile_colors.size(); ++tc) {
+            Timed t(c, kBend, 1, c.b_tiles.tile_color_cons[tc]);
+            xrt::launch_bend_tiles(c, k, c.b_tiles.tile_colors[tc]);
+          }
+        } else {
+          for (const ColorRange& r : c.b_ranges) {
+            Timed t(c, kBend, 1, r.end - r.begin);
+            xrt::launch_bend(c, k, r);
+          }
+        }
+      }
       if (p.geodesic_lra && c.nl) {
         Timed t(c, kLra, c.lra_by_target ? 1 : (uint32_t)c.lra_blocks.size(), c.nl);
         xrt::launch_lra(c, k);
@@ -347,6 +368,9 @@ xrt_status xrt_default_params(xrt_swift_params* p) {
   p->hash_cell_size = 1.5f;
   p->frame_time = 1.0f / 60.0f;
   p->update_obstacle_animation = 1;
+  p->pbd_repulsion = 0;
+  p->pbd_thickness = 1e-4f;         // RepulsionSettings (config/Base.hpp:102-108)
+  p->repulsion_relaxation = 0.25f;
   return XRT_OK;
 }
 
@@ -392,6 +416,17 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   c.edge.release(); c.vf_idx.release(); c.rt_idx.release();
   c.hash_sorter.keys_tmp.release(); c.hash_sorter.vals_tmp.release(); c.hash_sorter.hist.release();
   c.bvh.release();
+  for (xrt::TiledSet* t : {&c.s_tiles, &c.b_tiles}) {
+    t->foot.release();
+    t->foot_ptr.release();
+    t->lc_ptr.release();
+  }
+  xrt::ProximityState& P = c.prox;
+  P.cbvh.release();
+  P.face.release(); P.fedge.release(); P.fn0.release(); P.edge.release(); P.eadj.release();
+  P.cfree.release(); P.counts.release(); P.incl.release(); P.total.release(); P.pairs.release();
+  P.deltas.release(); P.rcounts.release(); P.imp_t.release(); P.imp_w.release(); P.imp_n.release();
+  P.imp_nodes.release();
   if (c.stream) cudaStreamDestroy(c.stream);
   delete h;
   return XRT_OK;
@@ -464,7 +499,11 @@ xrt_status xrt_add_cloth(xrt_ctx* h, const xrt_cloth_desc* d, int32_t* out_offse
     c.h_w.push_back(1.0f);  // PhysicsMeshHelper.cu:139: free nodes have inverse mass 1
   }
   for (uint32_t k = 0; k < 3 * d->num_triangles; ++k) c.h_tri.push_back(d->triangles[k] + cl.offset);
-  for (uint32_t i = 0; i < d->num_fixed; ++i) c.h_w[cl.offset + d->fixed_indices[i]] = 0.0f;
+  c.h_cfree.resize(c.h_w.size(), 1);
+  for (uint32_t i = 0; i < d->num_fixed; ++i) {  // SetInvMass(0) + SetFree(false)
+    c.h_w[cl.offset + d->fixed_indices[i]] = 0.0f;
+    c.h_cfree[cl.offset + d->fixed_indices[i]] = 0;
+  }
   std::vector<uint32_t> e;
   std::vector<std::vector<uint32_t>> ef;
   xrt::setup::build_edges(cl.tri, e, ef);
@@ -538,6 +577,9 @@ xrt_status xrt_add_obstacle(xrt_ctx* h, const xrt_obstacle_desc* d, int32_t* out
   const uint32_t off = (uint32_t)(c.h_ox0.size() / 3);
   for (uint32_t i = 0; i < d->num_vertices; ++i) {
     xrt::setup::V3 q{d->positions[3 * i], d->positions[3 * i + 1], d->positions[3 * i + 2]};
+    c.h_omesh.push_back(q.x);
+    c.h_omesh.push_back(q.y);
+    c.h_omesh.push_back(q.z);
     if (d->model_matrix) q = xrt::setup::transform_point(d->model_matrix, q);
     c.h_ox0.push_back(q.x);
     c.h_ox0.push_back(q.y);
@@ -597,8 +639,9 @@ static xrt_status upload_constraints(Context& c) {
   for (uint32_t j = 0; j < c.ne; ++j) {
     const uint32_t o = c.s_perm[j];
     int4 v;
-    v.x = (int)c.h_edges[2 * o];
-    v.y = (int)c.h_edges[2 * o + 1];
+    const bool tiled = c.s_tiles.on;
+    v.x = (int)(tiled ? c.s_local[2 * j] : c.h_edges[2 * o]);
+    v.y = (int)(tiled ? c.s_local[2 * j + 1] : c.h_edges[2 * o + 1]);
     std::memcpy(&v.z, &c.h_rest[o], 4);
     std::memcpy(&v.w, &c.h_scomp[o], 4);
     scon[j] = v;
@@ -607,8 +650,12 @@ static xrt_status upload_constraints(Context& c) {
   std::vector<float2> btc(c.nb);
   for (uint32_t j = 0; j < c.nb; ++j) {
     const uint32_t o = c.b_perm[j];
-    bidx[j] = make_int4((int)c.h_bends[4 * o], (int)c.h_bends[4 * o + 1], (int)c.h_bends[4 * o + 2],
-                        (int)c.h_bends[4 * o + 3]);
+    if (c.b_tiles.on)
+      bidx[j] = make_int4((int)c.b_local[4 * j], (int)c.b_local[4 * j + 1], (int)c.b_local[4 * j + 2],
+                          (int)c.b_local[4 * j + 3]);
+    else
+      bidx[j] = make_int4((int)c.h_bends[4 * o], (int)c.h_bends[4 * o + 1],
+                          (int)c.h_bends[4 * o + 2], (int)c.h_bends[4 * o + 3]);
     btc[j] = make_float2(c.h_theta[o], c.h_bcomp[o]);
   }
   XRT_CUDA(&c, upload(c.s_con, scon, c.stream));
@@ -672,12 +719,55 @@ xrt_status xrt_start(xrt_ctx* h) {
       col = c.pending_colors[kind];
       nc = 0;
       for (uint32_t v : col) nc = std::max(nc, v + 1);
+    } else if (c.tile_vertices > 0 && !idx.empty() &&
+               [&] {
+                 uint32_t tv = c.tile_vertices;
+                 c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv);
+                 while (c.tmp_schedule.max_footprint > 4096 && tv > 32) {  // <= 64 KB of smem
+                   tv /= 2;
+                   c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv);
+                 }
+                 return c.tmp_schedule.num_tile_colors > 0 && c.tmp_schedule.max_footprint <= 4096;
+               }()) {
+      // tile-local Gauss-Seidel schedule (a coloring; see setup::TileSchedule)
+      xrt::TiledSet& T = kind == 0 ? c.s_tiles : c.b_tiles;
+      const xrt::setup::TileSchedule& S = c.tmp_schedule;
+      col = S.color;
+      nc = S.num_tile_colors * S.num_local;
+      T.on = true;
+      T.num_local = S.num_local;
+      T.max_foot = S.max_footprint;
+      T.max_cons = 0;
+      for (size_t tt = 0; tt + 1 < S.foot_ptr.size(); ++tt)
+        T.max_cons = std::max(T.max_cons, S.lc_ptr[(tt + 1) * S.num_local] - S.lc_ptr[tt * S.num_local]);
+      T.tile_colors.clear();
+      T.tile_color_cons.clear();
+      for (uint32_t k = 0; k < S.num_tile_colors; ++k) {
+        T.tile_colors.push_back(ColorRange{S.tile_color_ptr[k], S.tile_color_ptr[k + 1]});
+        T.tile_color_cons.push_back(S.lc_ptr[S.tile_color_ptr[k + 1] * S.num_local] -
+                                    S.lc_ptr[S.tile_color_ptr[k] * S.num_local]);
+      }
+      XRT_CUDA(&c, upload(T.foot, S.foot, c.stream));
+      XRT_CUDA(&c, upload(T.foot_ptr, S.foot_ptr, c.stream));
+      XRT_CUDA(&c, upload(T.lc_ptr, S.lc_ptr, c.stream));
+      (kind == 0 ? c.s_perm : c.b_perm) = S.order;
+      (kind == 0 ? c.s_local : c.b_local) = S.local_slot;
+      continue;
     } else {
       col = xrt::setup::greedy_color(idx, arity, c.nv, nc);
     }
+    if (kind == 0) sort_by_color(c.h_scolor, c.n_scolors, c.s_perm, c.s_ranges);
+    else sort_by_color(c.h_bcolor, c.n_bcolors, c.b_perm, c.b_ranges);
   }
-  sort_by_color(c.h_scolor, c.n_scolors, c.s_perm, c.s_ranges);
-  sort_by_color(c.h_bcolor, c.n_bcolors, c.b_perm, c.b_ranges);
+  if (c.s_tiles.on || c.b_tiles.on) {
+    const size_t smem = std::max(xrt::tile_smem_bytes(c.s_tiles, sizeof(int4) + sizeof(float)),
+                                 xrt::tile_smem_bytes(c.b_tiles, sizeof(int4) + sizeof(float2)));
+    if (smem > 200 * 1024) {
+      c.set_error("tile schedule needs more shared memory than a block has");
+      return XRT_ERR_INVALID_MESH;
+    }
+    XRT_CUDA(&c, xrt::configure_tile_kernels(std::max<size_t>(smem, 16)));
+  }
   xrt_status st = upload_constraints(c);
   if (st != XRT_OK) return st;
   XRT_CUDA(&c, c.s_lambda.reserve(std::max(c.ne, 1u)));
@@ -869,11 +959,15 @@ xrt_status xrt_step_frame(xrt_ctx* h) {
   Context& c = h->c;
   if (require_started(c) != XRT_OK) return XRT_ERR_STATE;
   cudaSetDevice(c.device);
+  if (c.params.pbd_repulsion) {
+    xrt_status st = xrt::prox_prepare(c);
+    if (st != XRT_OK) return st;
+  }
   if (c.profiling) {
     record_frame(c);
     XRT_CUDA(&c, cudaGetLastError());
     collect_profile(c);
-  } else if (c.graph_enabled) {
+  } else if (c.graph_enabled && !c.params.pbd_repulsion) {
     if (c.graph_dirty || !c.graph_exec) {
       xrt_status st = capture_frame(c);
       if (st != XRT_OK) return st;
@@ -1062,7 +1156,9 @@ xrt_status xrt_get_obstacle_rtri(const xrt_ctx* h, uint32_t* masks) {
   return XRT_OK;
 }
 
-static xrt_status export_lbvh(xrt::Lbvh& b, cudaStream_t s, std::string& err, uint32_t* morton,
+}  // extern "C"
+
+xrt_status xrt::export_lbvh(xrt::Lbvh& b, cudaStream_t s, std::string& err, uint32_t* morton,
                               uint32_t* objs, uint32_t* nodes, float* aabbs, int32_t* iesc,
                               int32_t* eesc, int32_t* unique) {
   const uint32_t n = b.n;
@@ -1099,6 +1195,8 @@ static xrt_status export_lbvh(xrt::Lbvh& b, cudaStream_t s, std::string& err, ui
   }
   return XRT_OK;
 }
+
+extern "C" {
 
 xrt_status xrt_export_obstacle_bvh(xrt_ctx* h, uint32_t* morton, uint32_t* objs, uint32_t* nodes,
                                    float* aabbs, int32_t* iesc, int32_t* eesc) {

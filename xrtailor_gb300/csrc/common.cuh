@@ -38,6 +38,22 @@ template <typename T> XRT_HD T tmax(T a, T b) { return a > b ? a : b; }
 template <typename T> XRT_HD T tclamp(T x, T a, T b) { return x < a ? a : (x > b ? b : x); }
 template <typename T> XRT_HD T tabs(T x) { return x < T(0) ? -x : x; }
 
+// arccos on [0, 1] by Abramowitz & Stegun, Handbook of Mathematical Functions, formula 4.4.46:
+// acos(x) = sqrt(1 - x) * (a0 + a1 x + ... + a7 x^7), |error| <= 2e-8.  The same expression is
+// compiled for the device and for the CPU oracle, so bend projections agree bit for bit (the two
+// platforms' acosf differ in the last place, and the bend solve amplifies that).
+XRT_HD float acos_as(float x) {
+  float p = -0.0012624911f;
+  p = p * x + 0.0066700901f;
+  p = p * x + -0.0170881256f;
+  p = p * x + 0.0308918810f;
+  p = p * x + -0.0501743046f;
+  p = p * x + 0.0889789874f;
+  p = p * x + -0.2145988016f;
+  p = p * x + 1.5707963050f;
+  return sqrtf(1.0f - x) * p;
+}
+
 // MathFunctions::FaceNormal (src/math/MathFunctions.cu:14-20)
 XRT_HD f3 face_normal(f3 a, f3 b, f3 c) { return normalize(cross(b - a, c - a)); }
 

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/xrt.h"
+#include "setup.h"
 
 namespace xrt {
 
@@ -97,6 +98,39 @@ struct ColorRange {
   uint32_t begin, end;
 };
 
+// Tile-local Gauss-Seidel schedule of one constraint kind on the device (setup::TileSchedule):
+// one launch per tile color, one block per tile, local colors in shared memory.
+struct TiledSet {
+  bool on = false;
+  uint32_t num_local = 0;
+  uint32_t max_foot = 0;
+  uint32_t max_cons = 0;                // most constraints in one tile
+  std::vector<ColorRange> tile_colors;  // ranges of executed tiles per tile color
+  std::vector<uint32_t> tile_color_cons;  // constraints per tile color (profiling units)
+  DBuf<uint32_t> foot, foot_ptr, lc_ptr;
+};
+
+// Quality-mode self contact (proximity.cu): unified numbering, cloth first then obstacle.
+struct ProximityState {
+  bool ready = false;
+  Lbvh cbvh;                       // cloth LBVH
+  DBuf<int4> face;                 // nodes (unified) + r-triangle mask
+  DBuf<int4> fedge;                // unified edge of (v_i, v_i+1)
+  DBuf<float4> fn0;                // registration-time face normals
+  DBuf<uint2> edge;                // unified nodes of each edge
+  DBuf<int4> eadj;                 // adjacent unified faces, -1 = none
+  DBuf<uint8_t> cfree;             // Node::is_free of cloth nodes
+  DBuf<uint32_t> counts, incl, total;
+  DBuf<uint2> pairs;
+  uint32_t npairs = 0;
+  DBuf<float> deltas;              // 3 per cloth node
+  DBuf<int> rcounts;
+  DBuf<float> imp_t;
+  DBuf<float4> imp_w, imp_n;
+  DBuf<uint4> imp_nodes;
+  uint32_t nimpacts = 0;
+};
+
 struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -109,6 +143,7 @@ struct Context {
   uint32_t frame_index = 0;
   uint32_t launches_per_frame = 0;
   bool targets_pending = false;
+  uint32_t tile_vertices = 512;  // 0: plain per-color launches of a greedy coloring
 
   // host copies (setup)
   struct HostCloth {
@@ -134,12 +169,16 @@ struct Context {
   };
   std::vector<HostBinding> h_bind;
   float particle_diameter = 0.0f;
+  std::vector<uint8_t> h_cfree;     // Node::is_free (false for pinned vertices)
+  std::vector<float> h_omesh;       // obstacle positions at registration (mesh space)
   std::vector<float> h_ox0;         // obstacle world positions
   std::vector<uint32_t> h_otri;
   std::vector<uint32_t> h_ortri;
   uint32_t n_scolors = 0, n_bcolors = 0;
   std::vector<ColorRange> s_ranges, b_ranges;
-  std::vector<uint32_t> s_perm, b_perm;  // sorted slot -> original constraint index
+  std::vector<uint32_t> s_perm, b_perm;  // execution slot -> original constraint index
+  std::vector<uint32_t> s_local, b_local;  // footprint-local vertex slots (tiled schedules)
+  setup::TileSchedule tmp_schedule;        // scratch of xrt_start
 
   // sizes
   uint32_t nv = 0, ne = 0, nf = 0, nb = 0, nl = 0, nbind = 0, onv = 0, onf = 0;
@@ -148,10 +187,11 @@ struct Context {
   DBuf<float4> x, x_alt, x0, v, n, x_init;
   DBuf<int4> tri;                    // a, b, c, 0
   DBuf<uint32_t> vf_ptr, vf_list;    // vertex -> (face << 2 | corner), ascending faces
-  DBuf<int4> s_con;                  // sorted by color: i0, i1, rest bits, compliance bits
+  DBuf<int4> s_con;                  // execution order: i0, i1, rest bits, compliance bits
   DBuf<float> s_lambda;
-  DBuf<int4> b_idx;                  // sorted by color
+  DBuf<int4> b_idx;                  // execution order
   DBuf<float2> b_tc;                 // theta, compliance
+  TiledSet s_tiles, b_tiles;         // when on, s_con / b_idx hold footprint-local slots
   DBuf<uint32_t> lra_ptr, lra_src;   // per target vertex, slot order
   DBuf<float> lra_rest;
   DBuf<uint32_t> lra_l_src, lra_l_tgt;  // list order (slot-major), used when a slot is free
@@ -175,6 +215,7 @@ struct Context {
   DBuf<int4> otri;                   // a, b, c, r-triangle mask
   DBuf<uint32_t> ovf_ptr, ovf_list;
   Lbvh bvh;
+  ProximityState prox;
   // error word
   DBuf<uint32_t> err;
   // per-phase profiling (eager frames only)
@@ -210,6 +251,11 @@ void launch_predict(Context& c, const FrameConst& k);
 void launch_finalize_predict(Context& c, const FrameConst& k, bool predict_next, bool normals);
 void launch_stretch(Context& c, const FrameConst& k, ColorRange r, bool reset_lambda);
 void launch_bend(Context& c, const FrameConst& k, ColorRange r);
+cudaError_t configure_tile_kernels(size_t max_smem_bytes);
+size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes);
+// tile-local Gauss-Seidel: all tiles of one tile color (range of executed tiles)
+void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, bool reset_lambda);
+void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles);
 void launch_lra(Context& c, const FrameConst& k);
 void launch_vf_solve(Context& c);
 // EE solve + ApplyDeltas + binding: reads x, writes x_alt; caller swaps.
@@ -223,4 +269,22 @@ void launch_hash(Context& c);
 void launch_collide(Context& c, const FrameConst& k);  // reads x, writes x_alt; caller swaps
 void launch_prims_obstacle(Context& c, float tol);
 
+// Copies a built LBVH to host arrays in the export layout of include/xrt.h (api.cpp).
+xrt_status export_lbvh(Lbvh& b, cudaStream_t s, std::string& err, uint32_t* morton, uint32_t* objs,
+                       uint32_t* nodes, float* aabbs, int32_t* iesc, int32_t* eesc, int32_t* unique);
+
+// ---- Quality-mode self contact (proximity.cu) ----------------------------------------------------
+xrt_status prox_prepare(Context& c);  // uploads the unified topology once (api_contact.cpp)
+void launch_cloth_bvh_build(Context& c);
+void launch_update_ccd(Lbvh& b, const float4* x, const float4* x0, const int4* tri, cudaStream_t s,
+                       uint32_t* err);
+cudaError_t prox_update_pairs(Context& c, float thickness);
+void prox_solve(Context& c, float thickness, float relaxation);
+cudaError_t prox_check_impacts(Context& c, float thickness);
+
 }  // namespace xrt
+
+// The opaque handle of include/xrt.h.
+struct xrt_ctx {
+  xrt::Context c;
+};

@@ -211,31 +211,9 @@ __global__ void k_internal(const unsigned long long* __restrict__ code, uint32_t
   lo[idx].w = __int_as_float((int)left);
 }
 
-// Bottom-up merge.  Each leaf walks towards the root; at every internal node the first arrival
-// stops and the second merges both children (AssignAABBCAS_Kernel).  The arrival counters are
-// never reset: every walk adds exactly two arrivals per internal node, so the parity of the
-// counter tells first from second.  Walks are bounded by the tree height (<= n).
-__device__ void merge_upwards(uint32_t leaf_node, uint32_t n, float4* lo, float4* hi,
-                              const int4* node, uint32_t* flags, uint32_t* err) {
-  int parent = node[leaf_node].x;
-  uint32_t steps = 0;
-  while (parent >= 0) {
-    if (++steps > n) {
-      raise_error(err, kErrTreeWalk);
-      return;
-    }
-    __threadfence();
-    const uint32_t old = atomicAdd(&flags[parent], 1u);
-    if ((old & 1u) == 0u) return;  // first arrival
-    __threadfence();
-    const int4 nd = node[parent];
-    const float4 la = __ldcg(&lo[nd.y]), ha = __ldcg(&hi[nd.y]);
-    const float4 lb = __ldcg(&lo[nd.z]), hb = __ldcg(&hi[nd.z]);
-    const float4 ol = __ldcg(&lo[parent]), oh = __ldcg(&hi[parent]);
-    __stcg(&lo[parent], make_float4(fminf(la.x, lb.x), fminf(la.y, lb.y), fminf(la.z, lb.z), ol.w));
-    __stcg(&hi[parent], make_float4(fmaxf(ha.x, hb.x), fmaxf(ha.y, hb.y), fmaxf(ha.z, hb.z), oh.w));
-    parent = nd.x;
-  }
+__device__ __forceinline__ void merge_upwards(uint32_t leaf_node, uint32_t n, float4* lo, float4* hi,
+                                              const int4* node, uint32_t* flags, uint32_t* err) {
+  lbvh_merge_upwards(leaf_node, n, lo, hi, node, flags, err);
 }
 
 __global__ void k_build_internal_boxes(uint32_t n, float4* lo, float4* hi, const int4* node,

@@ -52,6 +52,34 @@ __device__ __forceinline__ bool overlap_box(float4 l, float4 h, f3 qlo, f3 qhi) 
   return !(l.x > qhi.x || h.x < qlo.x || l.y > qhi.y || h.y < qlo.y || l.z > qhi.z || h.z < qlo.z);
 }
 
+// Bottom-up merge (AssignAABBCAS_Kernel, BVH.cu:515-538).  Each leaf walks towards the root; at
+// every internal node the first arrival stops and the second merges both children.  The arrival
+// counters are never reset: every walk adds exactly two arrivals per internal node, so the parity
+// of the counter tells first from second.  Walks are bounded by the tree height (<= n).
+__device__ __forceinline__ void lbvh_merge_upwards(uint32_t leaf_node, uint32_t n, float4* lo,
+                                                   float4* hi, const int4* node, uint32_t* flags,
+                                                   uint32_t* err) {
+  int parent = node[leaf_node].x;
+  uint32_t steps = 0;
+  while (parent >= 0) {
+    if (++steps > n) {
+      raise_error(err, kErrTreeWalk);
+      return;
+    }
+    __threadfence();
+    const uint32_t old = atomicAdd(&flags[parent], 1u);
+    if ((old & 1u) == 0u) return;  // first arrival
+    __threadfence();
+    const int4 nd = node[parent];
+    const float4 la = __ldcg(&lo[nd.y]), ha = __ldcg(&hi[nd.y]);
+    const float4 lb = __ldcg(&lo[nd.z]), hb = __ldcg(&hi[nd.z]);
+    const float4 ol = __ldcg(&lo[parent]), oh = __ldcg(&hi[parent]);
+    __stcg(&lo[parent], make_float4(fminf(la.x, lb.x), fminf(la.y, lb.y), fminf(la.z, lb.z), ol.w));
+    __stcg(&hi[parent], make_float4(fmaxf(ha.x, hb.x), fmaxf(ha.y, hb.y), fmaxf(ha.z, hb.z), oh.w));
+    parent = nd.x;
+  }
+}
+
 // Stackless traversal; `ov(lo, hi)` tests a node box, `visit(object)` receives each hit.
 template <class Overlap, class Visit>
 __device__ __forceinline__ uint32_t lbvh_traverse(const LbvhView& b, Overlap ov, Visit visit,

@@ -256,5 +256,106 @@ std::vector<uint32_t> build_rtri(const std::vector<uint32_t>& tri, uint32_t nv) 
   return out;
 }
 
+TileSchedule build_tiles(const std::vector<uint32_t>& idx, int arity, uint32_t nv,
+                         uint32_t tile_vertices, const std::vector<uint32_t>& segments) {
+  TileSchedule S;
+  const size_t n = idx.size() / arity;
+  // vertex -> tile: tiles are cut inside each segment from its first vertex
+  std::vector<uint32_t> seg = segments.empty() ? std::vector<uint32_t>{0u} : segments;
+  seg.push_back(nv);
+  std::vector<uint32_t> seg_tile(seg.size(), 0);
+  for (size_t s = 0; s + 1 < seg.size(); ++s)
+    seg_tile[s + 1] = seg_tile[s] + std::max(1u, (seg[s + 1] - seg[s] + tile_vertices - 1) / tile_vertices);
+  const uint32_t ntiles = seg_tile.back();
+  auto tile_of = [&](uint32_t v) {
+    const size_t s = (size_t)(std::upper_bound(seg.begin(), seg.end() - 1, v) - seg.begin()) - 1;
+    return seg_tile[s] + (v - seg[s]) / tile_vertices;
+  };
+  // constraint -> tile of its smallest vertex
+  std::vector<std::vector<uint32_t>> members(ntiles);
+  std::vector<uint32_t> ctile(n);
+  for (size_t c = 0; c < n; ++c) {
+    uint32_t m = idx[c * arity];
+    for (int a = 1; a < arity; ++a) m = std::min(m, idx[c * arity + a]);
+    ctile[c] = tile_of(m);
+    members[ctile[c]].push_back((uint32_t)c);
+  }
+  // footprints
+  std::vector<std::vector<uint32_t>> foot(ntiles);
+  for (uint32_t t = 0; t < ntiles; ++t) {
+    auto& f = foot[t];
+    for (uint32_t c : members[t])
+      for (int a = 0; a < arity; ++a) f.push_back(idx[c * arity + a]);
+    std::sort(f.begin(), f.end());
+    f.erase(std::unique(f.begin(), f.end()), f.end());
+  }
+  // tile colors: greedy over tiles in order; conflict = shared footprint vertex
+  std::vector<uint32_t> tcolor(ntiles, 0);
+  std::vector<uint64_t> vmask(nv, 0);  // tile colors (< 64) already touching a vertex
+  for (uint32_t t = 0; t < ntiles; ++t) {
+    uint64_t used = 0;
+    for (uint32_t v : foot[t]) used |= vmask[v];
+    if (~used == 0) return TileSchedule{};  // more than 64 tile colors: caller falls back
+    const uint32_t k = (uint32_t)__builtin_ctzll(~used);
+    tcolor[t] = k;
+    for (uint32_t v : foot[t]) vmask[v] |= 1ull << k;
+    S.num_tile_colors = std::max(S.num_tile_colors, k + 1);
+  }
+  // local colors inside each tile (constraint order)
+  std::vector<uint32_t> lcolor(n, 0);
+  std::vector<std::vector<uint32_t>> by_local(ntiles);
+  for (uint32_t t = 0; t < ntiles; ++t) {
+    std::vector<uint32_t> sub;
+    sub.reserve(members[t].size() * arity);
+    for (uint32_t c : members[t])
+      for (int a = 0; a < arity; ++a) sub.push_back(idx[c * arity + a]);
+    // greedy on the tile's constraints with vertex masks keyed by footprint position
+    std::vector<uint64_t> m(foot[t].size(), 0);
+    for (size_t j = 0; j < members[t].size(); ++j) {
+      uint64_t used = 0;
+      uint32_t slot[4];
+      for (int a = 0; a < arity; ++a) {
+        slot[a] = (uint32_t)(std::lower_bound(foot[t].begin(), foot[t].end(), sub[j * arity + a]) -
+                             foot[t].begin());
+        used |= m[slot[a]];
+      }
+      if (~used == 0) return TileSchedule{};  // more than 64 local colors
+      const uint32_t k = (uint32_t)__builtin_ctzll(~used);
+      lcolor[members[t][j]] = k;
+      for (int a = 0; a < arity; ++a) m[slot[a]] |= 1ull << k;
+      S.num_local = std::max(S.num_local, k + 1);
+    }
+  }
+  S.color.resize(n);
+  for (size_t c = 0; c < n; ++c) S.color[c] = tcolor[ctile[c]] * S.num_local + lcolor[c];
+  // execution order: tile color, tile, local color, constraint order
+  S.tile_color_ptr.assign(1, 0);
+  S.foot_ptr.assign(1, 0);
+  S.lc_ptr.clear();
+  for (uint32_t k = 0; k < S.num_tile_colors; ++k) {
+    for (uint32_t t = 0; t < ntiles; ++t) {
+      if (tcolor[t] != k || members[t].empty()) continue;
+      S.tiles.push_back(t);
+      S.foot.insert(S.foot.end(), foot[t].begin(), foot[t].end());
+      S.foot_ptr.push_back((uint32_t)S.foot.size());
+      S.max_footprint = std::max(S.max_footprint, (uint32_t)foot[t].size());
+      for (uint32_t l = 0; l < S.num_local; ++l) {
+        S.lc_ptr.push_back((uint32_t)S.order.size());
+        for (uint32_t c : members[t]) {
+          if (lcolor[c] != l) continue;
+          S.order.push_back(c);
+          for (int a = 0; a < arity; ++a)
+            S.local_slot.push_back((uint32_t)(std::lower_bound(foot[t].begin(), foot[t].end(),
+                                                               idx[c * arity + a]) -
+                                              foot[t].begin()));
+        }
+      }
+    }
+    S.tile_color_ptr.push_back((uint32_t)S.tiles.size());
+  }
+  S.lc_ptr.push_back((uint32_t)S.order.size());
+  return S;
+}
+
 }  // namespace setup
 }  // namespace xrt

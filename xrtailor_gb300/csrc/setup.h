@@ -46,5 +46,28 @@ std::vector<uint32_t> build_rtri(const std::vector<uint32_t>& tri, uint32_t nv);
 float length(V3 a);
 V3 sub(V3 a, V3 b);
 
+// Tile schedule of a constraint set for tile-local Gauss-Seidel.  Vertices are cut into
+// contiguous tiles; a constraint belongs to the tile of its smallest vertex; tiles whose
+// footprints (vertices their constraints touch) intersect get different tile colors; inside a
+// tile the constraints get local colors.  Processing tile color by tile color, local color by
+// local color, is a coloring of the whole set: global color = tile_color * num_local + local.
+struct TileSchedule {
+  uint32_t num_tile_colors = 0, num_local = 0;
+  std::vector<uint32_t> color;          // global color per constraint (input order)
+  std::vector<uint32_t> order;          // constraints in execution order
+  std::vector<uint32_t> local_slot;     // per execution slot and arity: footprint-local index
+  std::vector<uint32_t> tiles;          // tiles in execution order (grouped by tile color)
+  std::vector<uint32_t> tile_color_ptr; // num_tile_colors + 1 offsets into `tiles`
+  std::vector<uint32_t> foot_ptr;       // per executed tile: footprint range into `foot`
+  std::vector<uint32_t> foot;           // footprint vertices (ascending)
+  std::vector<uint32_t> lc_ptr;         // per executed tile: num_local + 1 offsets into `order`
+  uint32_t max_footprint = 0;
+};
+// `segments`: ascending first vertex of each independent mesh (instance); tiles never cross a
+// segment and are numbered inside it exactly as for that mesh alone, so a batch of meshes gets
+// the schedule every mesh would get on its own.  Empty = one segment.
+TileSchedule build_tiles(const std::vector<uint32_t>& idx, int arity, uint32_t nv,
+                         uint32_t tile_vertices, const std::vector<uint32_t>& segments = {});
+
 }  // namespace setup
 }  // namespace xrt

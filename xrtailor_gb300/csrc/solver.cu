@@ -68,6 +68,26 @@ __global__ void k_finalize(float4* __restrict__ x, float4* __restrict__ x0, floa
   }
 }
 
+// XPBD distance constraint on two vertices; returns true when it moved them (lam updated).
+__device__ __forceinline__ bool stretch_project(float4& a, float4& b, float rest, float compliance,
+                                                float dt, float& lam) {
+  const f3 diff = mk3(a) - mk3(b);
+  const float distance = length(diff);
+  const float w1 = a.w, w2 = b.w;
+  if (!(distance != rest && w1 + w2 > 0.0f)) return false;
+  const f3 gradient = diff / (distance + kEps);
+  const float alpha_tilde = compliance / (dt * dt);
+  const float constraint = distance - rest;
+  const float dl = (-constraint - alpha_tilde * lam) / (w1 + w2 + alpha_tilde);
+  const f3 corr = dl * gradient;
+  lam = lam + dl;
+  const f3 c1 = corr * w1;
+  const f3 c2 = -corr * w2;
+  a = make_float4(a.x + c1.x, a.y + c1.y, a.z + c1.z, a.w);
+  b = make_float4(b.x + c2.x, b.y + c2.y, b.z + c2.z, b.w);
+  return true;
+}
+
 template <bool RESET>
 __global__ void k_stretch(const int4* __restrict__ con, float* __restrict__ lambda,
                           float4* __restrict__ x, uint32_t begin, uint32_t end, float dt) {
@@ -75,27 +95,63 @@ __global__ void k_stretch(const int4* __restrict__ con, float* __restrict__ lamb
   if (j >= end) return;
   const int4 c = __ldg(&con[j]);
   float lam = RESET ? 0.0f : lambda[j];
-  const float4 a = x[c.x], b = x[c.y];
-  const float rest = __int_as_float(c.z), compliance = __int_as_float(c.w);
-  const f3 diff = mk3(a) - mk3(b);
-  const float distance = length(diff);
-  const float w1 = a.w, w2 = b.w;
-  if (distance != rest && w1 + w2 > 0.0f) {
-    const f3 gradient = diff / (distance + kEps);
-    const float alpha_tilde = compliance / (dt * dt);
-    const float constraint = distance - rest;
-    const float dl = (-constraint - alpha_tilde * lam) / (w1 + w2 + alpha_tilde);
-    const f3 corr = dl * gradient;
-    lam = lam + dl;
-    const f3 c1 = corr * w1;
-    const f3 c2 = -corr * w2;
-    x[c.x] = make_float4(a.x + c1.x, a.y + c1.y, a.z + c1.z, a.w);
-    x[c.y] = make_float4(b.x + c2.x, b.y + c2.y, b.z + c2.z, b.w);
+  float4 a = x[c.x], b = x[c.y];
+  if (stretch_project(a, b, __int_as_float(c.z), __int_as_float(c.w), dt, lam)) {
+    x[c.x] = a;
+    x[c.y] = b;
     lambda[j] = lam;
   } else if (RESET) {
     lambda[j] = 0.0f;
   }
 }
+
+// Tile-local Gauss-Seidel: block = one tile of the launched tile color.  The tile's footprint is
+// staged in shared memory, its local colors run in order with a block barrier between them, and
+// the footprint is written back.  Tiles of one tile color have disjoint footprints.
+// Shared memory of a tile launch: footprint positions, then the tile's constraint records (and,
+// for stretch, the multipliers).  Everything global is read once, up front, in coalesced sweeps,
+// so the chain of local colors touches only shared memory.
+template <bool RESET>
+__global__ void __launch_bounds__(kBlock) k_stretch_tiles(
+    const int4* __restrict__ con, float* __restrict__ lambda, float4* __restrict__ x,
+    const uint32_t* __restrict__ foot, const uint32_t* __restrict__ foot_ptr,
+    const uint32_t* __restrict__ lc_ptr, uint32_t tile_begin, uint32_t num_local,
+    uint32_t max_foot, uint32_t max_cons, float dt) {
+  extern __shared__ float4 smem[];
+  float4* sx = smem;
+  int4* sc = reinterpret_cast<int4*>(sx + max_foot);
+  float* sl = reinterpret_cast<float*>(sc + max_cons);
+  const uint32_t t = tile_begin + blockIdx.x;
+  const uint32_t fb = foot_ptr[t], fe = foot_ptr[t + 1];
+  const uint32_t* lp = lc_ptr + (size_t)t * num_local;
+  const uint32_t c0 = lp[0], c1 = lp[num_local];
+  for (uint32_t k = fb + threadIdx.x; k < fe; k += blockDim.x) sx[k - fb] = x[foot[k]];
+  for (uint32_t j = c0 + threadIdx.x; j < c1; j += blockDim.x) {
+    sc[j - c0] = __ldg(&con[j]);
+    sl[j - c0] = RESET ? 0.0f : lambda[j];
+  }
+  __syncthreads();
+  for (uint32_t l = 0; l < num_local; ++l) {
+    const uint32_t cb = lp[l] - c0, ce = lp[l + 1] - c0;
+    for (uint32_t j = cb + threadIdx.x; j < ce; j += blockDim.x) {
+      const int4 c = sc[j];
+      float lam = sl[j];
+      float4 a = sx[c.x], b = sx[c.y];
+      if (stretch_project(a, b, __int_as_float(c.z), __int_as_float(c.w), dt, lam)) {
+        sx[c.x] = a;
+        sx[c.y] = b;
+        sl[j] = lam;
+      }
+    }
+    __syncthreads();
+  }
+  for (uint32_t k = fb + threadIdx.x; k < fe; k += blockDim.x) x[foot[k]] = sx[k - fb];
+  for (uint32_t j = c0 + threadIdx.x; j < c1; j += blockDim.x) lambda[j] = sl[j - c0];
+}
+
+// Dihedral bend projection of SolveBend_Kernel on four vertices.
+__device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3, float4& a4,
+                                             float theta, float compliance, float dt);
 
 __global__ void k_bend(const int4* __restrict__ idx, const float2* __restrict__ tc,
                        float4* __restrict__ x, uint32_t begin, uint32_t end, float dt) {
@@ -103,7 +159,52 @@ __global__ void k_bend(const int4* __restrict__ idx, const float2* __restrict__ 
   if (j >= end) return;
   const int4 b = __ldg(&idx[j]);
   const float2 th = __ldg(&tc[j]);
-  const float4 a1 = x[b.x], a2 = x[b.y], a3 = x[b.z], a4 = x[b.w];
+  float4 a1 = x[b.x], a2 = x[b.y], a3 = x[b.z], a4 = x[b.w];
+  bend_project(a1, a2, a3, a4, th.x, th.y, dt);
+  x[b.x] = a1;  // unchanged values when the constraint is inactive; a color is independent
+  x[b.y] = a2;
+  x[b.z] = a3;
+  x[b.w] = a4;
+}
+
+__global__ void __launch_bounds__(kBlock) k_bend_tiles(
+    const int4* __restrict__ idx, const float2* __restrict__ tc, float4* __restrict__ x,
+    const uint32_t* __restrict__ foot, const uint32_t* __restrict__ foot_ptr,
+    const uint32_t* __restrict__ lc_ptr, uint32_t tile_begin, uint32_t num_local,
+    uint32_t max_foot, uint32_t max_cons, float dt) {
+  extern __shared__ float4 smem[];
+  float4* sx = smem;
+  int4* sc = reinterpret_cast<int4*>(sx + max_foot);
+  float2* st = reinterpret_cast<float2*>(sc + max_cons);
+  const uint32_t t = tile_begin + blockIdx.x;
+  const uint32_t fb = foot_ptr[t], fe = foot_ptr[t + 1];
+  const uint32_t* lp = lc_ptr + (size_t)t * num_local;
+  const uint32_t c0 = lp[0], c1 = lp[num_local];
+  for (uint32_t k = fb + threadIdx.x; k < fe; k += blockDim.x) sx[k - fb] = x[foot[k]];
+  for (uint32_t j = c0 + threadIdx.x; j < c1; j += blockDim.x) {
+    sc[j - c0] = __ldg(&idx[j]);
+    st[j - c0] = __ldg(&tc[j]);
+  }
+  __syncthreads();
+  for (uint32_t l = 0; l < num_local; ++l) {
+    const uint32_t cb = lp[l] - c0, ce = lp[l + 1] - c0;
+    for (uint32_t j = cb + threadIdx.x; j < ce; j += blockDim.x) {
+      const int4 b = sc[j];
+      const float2 th = st[j];
+      float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
+      bend_project(a1, a2, a3, a4, th.x, th.y, dt);
+      sx[b.x] = a1;
+      sx[b.y] = a2;
+      sx[b.z] = a3;
+      sx[b.w] = a4;
+    }
+    __syncthreads();
+  }
+  for (uint32_t k = fb + threadIdx.x; k < fe; k += blockDim.x) x[foot[k]] = sx[k - fb];
+}
+
+__device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3, float4& a4,
+                                             float theta, float compliance, float dt) {
   const float w1 = a1.w, w2 = a2.w, w3 = a3.w, w4 = a4.w;
   const f3 p1 = mk3(a1);
   const f3 p2 = mk3(a2) - p1;
@@ -112,27 +213,27 @@ __global__ void k_bend(const int4* __restrict__ idx, const float2* __restrict__ 
   const f3 n1 = normalize(cross(p2, p3));
   const f3 n2 = normalize(cross(p2, p4));
   const float d = tclamp(dot(n1, n2), 0.0f, 1.0f);
-  const float angle = acosf(d);
+  const float angle = acos_as(d);  // d in [0, 1] (or NaN, rejected below)
   if (angle < kEps || isnan(d)) return;
   const f3 q3 = (cross(p2, n2) + cross(n1, p2) * d) / (length(cross(p2, p3)) + kEps);
   const f3 q4 = (cross(p2, n1) + cross(n2, p2) * d) / (length(cross(p2, p4)) + kEps);
   const f3 q2 = -(cross(p3, n2) + cross(n1, p3) * d) / (length(cross(p2, p3)) + kEps) -
                 (cross(p4, n1) + cross(n2, p4) * d) / (length(cross(p2, p4)) + kEps);
   const f3 q1 = -q2 - q3 - q4;
-  const float xpbd_bend = th.y / dt / dt;
+  const float xpbd_bend = compliance / dt / dt;
   const float denom =
       xpbd_bend + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) + w4 * dot(q4, q4));
   if (denom < kEps) return;
-  const float lambda = sqrtf(1.0f - d * d) * (angle - th.x) / denom;
+  const float lambda = sqrtf(1.0f - d * d) * (angle - theta) / denom;
   const float scaling = 1.0f;
   const f3 c1 = scaling * w1 * lambda * q1;
   const f3 c2 = scaling * w2 * lambda * q2;
   const f3 c3 = scaling * w3 * lambda * q3;
   const f3 c4 = scaling * w4 * lambda * q4;
-  x[b.x] = make_float4(a1.x + c1.x, a1.y + c1.y, a1.z + c1.z, w1);
-  x[b.y] = make_float4(a2.x + c2.x, a2.y + c2.y, a2.z + c2.z, w2);
-  x[b.z] = make_float4(a3.x + c3.x, a3.y + c3.y, a3.z + c3.z, w3);
-  x[b.w] = make_float4(a4.x + c4.x, a4.y + c4.y, a4.z + c4.z, w4);
+  a1 = make_float4(a1.x + c1.x, a1.y + c1.y, a1.z + c1.z, w1);
+  a2 = make_float4(a2.x + c2.x, a2.y + c2.y, a2.z + c2.z, w2);
+  a3 = make_float4(a3.x + c3.x, a3.y + c3.y, a3.z + c3.z, w3);
+  a4 = make_float4(a4.x + c4.x, a4.y + c4.y, a4.z + c4.z, w4);
 }
 
 __device__ __forceinline__ f3 lra_project(f3 xt, f3 xs, float w_t, float rest, float stretch) {
@@ -294,6 +395,47 @@ void launch_bend(Context& c, const FrameConst& k, ColorRange r) {
   const uint32_t n = r.end - r.begin;
   if (n == 0) return;
   k_bend<<<grid_for(n), kBlock, 0, c.stream>>>(c.b_idx.p, c.b_tc.p, c.x.p, r.begin, r.end, k.dt);
+}
+
+cudaError_t configure_tile_kernels(size_t max_smem_bytes) {
+  const int bytes = (int)max_smem_bytes;
+  cudaError_t e = cudaFuncSetAttribute(k_stretch_tiles<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_stretch_tiles<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_bend_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return e;
+}
+
+size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes) {
+  return sizeof(float4) * T.max_foot + record_bytes * T.max_cons;
+}
+
+void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, bool reset_lambda) {
+  const uint32_t nt = tiles.end - tiles.begin;
+  if (nt == 0) return;
+  const TiledSet& T = c.s_tiles;
+  const size_t smem = tile_smem_bytes(T, sizeof(int4) + sizeof(float));
+  if (reset_lambda)
+    k_stretch_tiles<true><<<nt, kBlock, smem, c.stream>>>(c.s_con.p, c.s_lambda.p, c.x.p, T.foot.p,
+                                                          T.foot_ptr.p, T.lc_ptr.p, tiles.begin,
+                                                          T.num_local, T.max_foot, T.max_cons,
+                                                          k.dt);
+  else
+    k_stretch_tiles<false><<<nt, kBlock, smem, c.stream>>>(
+        c.s_con.p, c.s_lambda.p, c.x.p, T.foot.p, T.foot_ptr.p, T.lc_ptr.p, tiles.begin,
+        T.num_local, T.max_foot, T.max_cons, k.dt);
+}
+
+void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles) {
+  const uint32_t nt = tiles.end - tiles.begin;
+  if (nt == 0) return;
+  const TiledSet& T = c.b_tiles;
+  k_bend_tiles<<<nt, kBlock, tile_smem_bytes(T, sizeof(int4) + sizeof(float2)), c.stream>>>(
+      c.b_idx.p, c.b_tc.p, c.x.p, T.foot.p, T.foot_ptr.p, T.lc_ptr.p, tiles.begin, T.num_local,
+      T.max_foot, T.max_cons, k.dt);
 }
 
 // LRA phase: one per-target launch when every slot vertex is pinned (slot positions are then

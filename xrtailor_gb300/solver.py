@@ -373,6 +373,65 @@ class ClothSolver:
         L.check(self._lib.xrt_export_neighbors(self._h, L.uptr(out)), self._h, "neighbors")
         return out
 
+    # -- Quality-mode self contact (include/xrt_contact.h) --------------------------------
+    def cloth_bvh_build(self):
+        L.check(self._lib.xrt_cloth_bvh_build(self._h), self._h, "cloth bvh")
+
+    def obstacle_bvh_update_ccd(self):
+        L.check(self._lib.xrt_obstacle_bvh_update_ccd(self._h), self._h, "obstacle bvh ccd")
+
+    def update_pairs(self, thickness: float) -> int:
+        n = C.c_uint32()
+        L.check(self._lib.xrt_proximity_update_pairs(self._h, float(thickness), C.byref(n)),
+                self._h, "update pairs")
+        self._npairs = n.value
+        return n.value
+
+    def proximity_solve(self, thickness: float, relaxation: float):
+        L.check(self._lib.xrt_proximity_solve(self._h, float(thickness), float(relaxation)),
+                self._h, "proximity solve")
+
+    def check_impacts(self, thickness: float) -> int:
+        n = C.c_uint32()
+        L.check(self._lib.xrt_impacts_check(self._h, float(thickness), C.byref(n)), self._h,
+                "impacts")
+        self._nimpacts = n.value
+        return n.value
+
+    def pairs(self):
+        out = np.empty((getattr(self, "_npairs", 0), 2), np.uint32)
+        L.check(self._lib.xrt_export_pairs(self._h, L.uptr(out)), self._h, "pairs")
+        return out
+
+    def impacts(self):
+        n = getattr(self, "_nimpacts", 0)
+        out = dict(t=np.empty(n, np.float32), w=np.empty((n, 4), np.float32),
+                   n=np.empty((n, 3), np.float32), nodes=np.empty((n, 4), np.uint32),
+                   is_vf=np.empty(n, np.int32))
+        L.check(self._lib.xrt_export_impacts(self._h, L.fptr(out["t"]), L.fptr(out["w"]),
+                                             L.fptr(out["n"]), L.uptr(out["nodes"]),
+                                             L.iptr(out["is_vf"])), self._h, "impacts")
+        return out
+
+    def export_cloth_bvh(self):
+        n = self.sizes().num_triangles
+        nn = 2 * n - 1
+        out = dict(morton=np.empty(n, np.uint32), objects=np.empty(n, np.uint32),
+                   nodes=np.empty((nn, 4), np.uint32), aabbs=np.empty((nn, 6), np.float32),
+                   iesc=np.empty(max(n - 1, 1), np.int32), eesc=np.empty(n, np.int32))
+        L.check(self._lib.xrt_export_cloth_bvh(
+            self._h, L.uptr(out["morton"]), L.uptr(out["objects"]), L.uptr(out["nodes"]),
+            L.fptr(out["aabbs"]), L.iptr(out["iesc"]), L.iptr(out["eesc"])), self._h, "cloth bvh")
+        out["iesc"] = out["iesc"][: max(n - 1, 0)]
+        return out
+
+    def predicted(self):
+        return self._read(self._lib.xrt_get_predicted, self.sizes().num_vertices)
+
+    def set_predicted(self, x):
+        a = _f32(x).reshape(-1)
+        L.check(self._lib.xrt_set_predicted(self._h, L.fptr(a)), self._h, "set predicted")
+
     def close(self):
         if self._h:
             self._lib.xrt_destroy(self._h)
