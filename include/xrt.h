@@ -173,6 +173,16 @@ xrt_status xrt_step_frames(xrt_ctx* ctx, int32_t num_frames);
 xrt_status xrt_synchronize(xrt_ctx* ctx);
 /* Enables (1) / disables (0) CUDA-graph replay of frames (default 1). */
 xrt_status xrt_set_graph_mode(xrt_ctx* ctx, int32_t enabled);
+/* Enables (1) / disables (0) programmatic dependent launch of the substep kernels (default 1):
+ * each kernel may start, and read its setup-time data, while its predecessor finishes.  Results
+ * are identical either way.  No reference counterpart (a launch option of this library). */
+xrt_status xrt_set_dependent_launch(xrt_ctx* ctx, int32_t enabled);
+/* Tile size of the tile-local Gauss-Seidel schedule of stretch and bend constraints, in
+ * consecutive vertices (default 256; halved while a tile's footprint exceeds 4,096 vertices),
+ * or 0 for one launch per color of a greedy coloring.  Before xrt_start; a caller coloring
+ * (xrt_set_coloring) always runs as per-color launches.  No reference counterpart (the
+ * reference launches one kernel per color, BasicSolver.cu:131-134). */
+xrt_status xrt_set_tile_vertices(xrt_ctx* ctx, uint32_t tile_vertices);
 
 /* ---- per-phase GPU timing (replaces Timer / ScopedTimerGPU, utils/Timer.hpp:67-114) -------- */
 #define XRT_NUM_PHASES 12

@@ -140,6 +140,52 @@ def test_plain_colored_launches_match_tiled(xrt):
     assert gp.sizes().launches_per_frame > g.sizes().launches_per_frame
 
 
+@pytest.mark.parametrize("tile", [32, 64, 200])
+def test_tile_sizes_match_oracle(xrt, tile):
+    """Any tile size gives a valid schedule; the oracle, run with the exported coloring, matches
+    bit for bit (tiles of 32 vertices on a 24-wide grid have footprints spanning 3 tiles)."""
+    cloth, obs = small_scene(24, attached=scenes.two_corner_pins(24))
+    p = _params(num_substeps=2, num_iterations=4, num_collision_passes=2)
+    from oracle.oracle import OracleSolver
+    g = ClothSolver(p)
+    g.set_tile_vertices(tile)
+    g.add_cloth(cloth, particle_diameter=0.02)
+    g.add_obstacle(obs)
+    g.start()
+    o = OracleSolver(p)
+    o.add_cloth(cloth, particle_diameter=0.02)
+    o.add_obstacle(obs)
+    o.set_coloring(0, g.coloring(0))
+    o.set_coloring(1, g.coloring(1))
+    o.start()
+    for _ in range(2):
+        g.step()
+        o.step()
+    _close(g, o, exact=True)
+    with pytest.raises(XrtError):
+        g.set_tile_vertices(64)  # after start
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_dependent_launch_is_bit_identical(xrt, graph):
+    """Programmatic dependent launch changes only when kernels start, never what they compute:
+    a garment-like scene (tiles, self collision, obstacle contacts, LRA) gives the same bits with
+    it on and off, in graph replay and eagerly, and both match the oracle."""
+    cloth, obs = small_scene(48, attached=scenes.two_corner_pins(48))
+    p = _params(num_substeps=3, num_iterations=6, num_collision_passes=3)
+    runs = []
+    for pdl in (True, False):
+        g, o = make_pair(p, [cloth], [obs], particle_diameter=0.02)
+        g.set_graph_mode(graph)
+        g.set_dependent_launch(pdl)
+        for _ in range(3):
+            g.step()
+            o.step()
+        _close(g, o, exact=True)
+        runs.append(g.host_positions())
+    np.testing.assert_array_equal(bits(runs[0]), bits(runs[1]))
+
+
 def test_pbd_repulsion_frame(xrt):
     cloth, obs = small_scene(14)
     p = _params(solve_bending=0, pbd_repulsion=1, pbd_thickness=1e-3, repulsion_relaxation=0.25,

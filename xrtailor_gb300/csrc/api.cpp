@@ -241,18 +241,26 @@ void record_frame(Context& c) {
           }
         }
       }
-      if (p.geodesic_lra && c.nl) {
-        Timed t(c, kLra, c.lra_by_target ? 1 : (uint32_t)c.lra_blocks.size(), c.nl);
+      // LRA and VF solve: one per-vertex Jacobi launch (LRA runs on its own first when a slot
+      // vertex is free, since slot positions then change during the phase); then EE solve +
+      // ApplyDeltas + binding.
+      const bool lra = p.geodesic_lra && c.nl;
+      if (lra && !c.lra_by_target) {
+        Timed t(c, kLra, (uint32_t)c.lra_blocks.size(), c.nl);
         xrt::launch_lra(c, k);
       }
-      if (has_obstacle) {
-        Timed t(c, kVfSolve, 1, c.nv);
-        xrt::launch_vf_solve(c);
+      const bool lra_fused = lra && c.lra_by_target;
+      if (lra_fused || has_obstacle) {
+        {
+          Timed t(c, has_obstacle ? kVfSolve : kLra, 1, c.nv);
+          xrt::launch_stage(c, k, lra_fused, has_obstacle);
+        }
+        swap_x();
       }
       if (has_obstacle || bindings) {
         {
           Timed t(c, kEeApply, 1, c.nv);
-          xrt::launch_ee_apply(c, k, has_obstacle, bindings);
+          xrt::launch_ee(c, k, has_obstacle, bindings);
         }
         swap_x();
       }
@@ -418,8 +426,8 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   c.bvh.release();
   for (xrt::TiledSet* t : {&c.s_tiles, &c.b_tiles}) {
     t->foot.release();
-    t->foot_ptr.release();
-    t->lc_ptr.release();
+    t->meta.release();
+    t->lofs.release();
   }
   xrt::ProximityState& P = c.prox;
   P.cbvh.release();
@@ -723,11 +731,12 @@ xrt_status xrt_start(xrt_ctx* h) {
                [&] {
                  uint32_t tv = c.tile_vertices;
                  c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv);
-                 while (c.tmp_schedule.max_footprint > 4096 && tv > 32) {  // <= 64 KB of smem
+                 while (c.tmp_schedule.max_footprint > xrt::kTileMaxFootprint && tv > 32) {
                    tv /= 2;
                    c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv);
                  }
-                 return c.tmp_schedule.num_tile_colors > 0 && c.tmp_schedule.max_footprint <= 4096;
+                 return c.tmp_schedule.num_tile_colors > 0 &&
+                        c.tmp_schedule.max_footprint <= xrt::kTileMaxFootprint;
                }()) {
       // tile-local Gauss-Seidel schedule (a coloring; see setup::TileSchedule)
       xrt::TiledSet& T = kind == 0 ? c.s_tiles : c.b_tiles;
@@ -747,9 +756,17 @@ xrt_status xrt_start(xrt_ctx* h) {
         T.tile_color_cons.push_back(S.lc_ptr[S.tile_color_ptr[k + 1] * S.num_local] -
                                     S.lc_ptr[S.tile_color_ptr[k] * S.num_local]);
       }
+      std::vector<int4> meta;
+      std::vector<uint32_t> lofs;
+      for (size_t tt = 0; tt + 1 < S.foot_ptr.size(); ++tt) {
+        const uint32_t c0 = S.lc_ptr[tt * S.num_local], c1 = S.lc_ptr[(tt + 1) * S.num_local];
+        meta.push_back(make_int4((int)S.foot_ptr[tt], (int)(S.foot_ptr[tt + 1] - S.foot_ptr[tt]),
+                                 (int)c0, (int)(c1 - c0)));
+        for (uint32_t l = 0; l <= S.num_local; ++l) lofs.push_back(S.lc_ptr[tt * S.num_local + l] - c0);
+      }
       XRT_CUDA(&c, upload(T.foot, S.foot, c.stream));
-      XRT_CUDA(&c, upload(T.foot_ptr, S.foot_ptr, c.stream));
-      XRT_CUDA(&c, upload(T.lc_ptr, S.lc_ptr, c.stream));
+      XRT_CUDA(&c, upload(T.meta, meta, c.stream));
+      XRT_CUDA(&c, upload(T.lofs, lofs, c.stream));
       (kind == 0 ? c.s_perm : c.b_perm) = S.order;
       (kind == 0 ? c.s_local : c.b_local) = S.local_slot;
       continue;
@@ -1008,6 +1025,28 @@ xrt_status xrt_set_graph_mode(xrt_ctx* h, int32_t enabled) {
   if (!h) return XRT_ERR_INVALID_ARGUMENT;
   h->c.graph_enabled = enabled != 0;
   h->c.graph_dirty = true;
+  return XRT_OK;
+}
+
+xrt_status xrt_set_dependent_launch(xrt_ctx* h, int32_t enabled) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  h->c.pdl = enabled != 0;
+  h->c.graph_dirty = true;
+  return XRT_OK;
+}
+
+xrt_status xrt_set_tile_vertices(xrt_ctx* h, uint32_t tile_vertices) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (c.started) {
+    c.set_error("xrt_set_tile_vertices must precede xrt_start");
+    return XRT_ERR_STATE;
+  }
+  if (tile_vertices != 0 && (tile_vertices < 32 || tile_vertices > (1u << 20))) {
+    c.set_error("tile_vertices must be 0 or in [32, 1048576]");
+    return XRT_ERR_INVALID_ARGUMENT;
+  }
+  c.tile_vertices = tile_vertices;
   return XRT_OK;
 }
 

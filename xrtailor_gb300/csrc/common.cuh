@@ -10,6 +10,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #define XRT_HD __host__ __device__ __forceinline__
 
 namespace xrt {
@@ -62,6 +64,8 @@ constexpr float kScalarMax = 3.402823466e+38f;  // SCALAR_MAX = FLT_MAX (core/Sc
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr uint32_t kMaxCandidates = 256;  // LBVH_MAX_BUFFER_SIZE (core/Common.cuh:23)
 constexpr int kBlock = 256;
+constexpr int kTileBlock = 512;     // threads of a tile-local Gauss-Seidel block
+constexpr int kFootPerThread = 8;   // footprint vertices per thread: footprints <= 4096
 
 // Bits of the sticky device error word.
 enum : uint32_t {
@@ -74,6 +78,35 @@ __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit) { atomi
 
 inline unsigned grid_for(uint32_t n, int block = kBlock) {
   return (unsigned)((n + (uint32_t)block - 1) / (uint32_t)block);
+}
+
+// Programmatic dependent launch.  A kernel launched with programmatic stream serialization may
+// start while its predecessor on the stream still runs.  pdl_wait() returns once every
+// prerequisite grid has completed and its writes are visible; everything before it may touch
+// only data that no earlier kernel of the frame writes (setup-time records, index lists) and
+// must not write global memory.  pdl_release() lets the successor grid start its own prologue.
+// Both are no-ops for a kernel launched without the attribute.  Every kernel launched through
+// launch_k with pdl set calls pdl_wait() in every block before its first dependent access, so
+// grid completion stays ordered along the stream.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... P, typename... A>
+inline cudaError_t launch_k(bool pdl, void (*kern)(P...), unsigned grid, unsigned block,
+                            size_t smem, cudaStream_t s, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
 }
 
 }  // namespace xrt

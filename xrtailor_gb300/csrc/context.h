@@ -100,6 +100,9 @@ struct ColorRange {
 
 // Tile-local Gauss-Seidel schedule of one constraint kind on the device (setup::TileSchedule):
 // one launch per tile color, one block per tile, local colors in shared memory.
+// Largest tile footprint the tile kernels stage (kTileBlock x kFootPerThread in solver.cu).
+constexpr uint32_t kTileMaxFootprint = 4096;
+
 struct TiledSet {
   bool on = false;
   uint32_t num_local = 0;
@@ -107,7 +110,10 @@ struct TiledSet {
   uint32_t max_cons = 0;                // most constraints in one tile
   std::vector<ColorRange> tile_colors;  // ranges of executed tiles per tile color
   std::vector<uint32_t> tile_color_cons;  // constraints per tile color (profiling units)
-  DBuf<uint32_t> foot, foot_ptr, lc_ptr;
+  DBuf<uint32_t> foot;                  // footprint vertices of every executed tile
+  DBuf<int4> meta;                      // per executed tile {first footprint, footprint size,
+                                        //  first constraint, constraint count}
+  DBuf<uint32_t> lofs;                  // per executed tile: num_local + 1 offsets, tile-relative
 };
 
 // Quality-mode self contact (proximity.cu): unified numbering, cloth first then obstacle.
@@ -143,7 +149,8 @@ struct Context {
   uint32_t frame_index = 0;
   uint32_t launches_per_frame = 0;
   bool targets_pending = false;
-  uint32_t tile_vertices = 512;  // 0: plain per-color launches of a greedy coloring
+  uint32_t tile_vertices = 256;  // 0: plain per-color launches of a greedy coloring
+  bool pdl = true;               // programmatic dependent launch of the substep kernels
 
   // host copies (setup)
   struct HostCloth {
@@ -257,9 +264,11 @@ size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes);
 void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, bool reset_lambda);
 void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles);
 void launch_lra(Context& c, const FrameConst& k);
-void launch_vf_solve(Context& c);
-// EE solve + ApplyDeltas + binding: reads x, writes x_alt; caller swaps.
-void launch_ee_apply(Context& c, const FrameConst& k, bool contacts, bool bindings);
+// Iteration tail, each launch reads x and writes x_alt (caller swaps):
+// LRA with all slots pinned (else launch_lra runs before) + VF solve ...
+void launch_stage(Context& c, const FrameConst& k, bool lra, bool contacts);
+// ... then EE solve + ApplyDeltas + binding.
+void launch_ee(Context& c, const FrameConst& k, bool contacts, bool bindings);
 void launch_obstacle_pass(Context& c, int step, int num_steps);
 void launch_generate_contacts(Context& c);
 void launch_obstacle_commit(Context& c);

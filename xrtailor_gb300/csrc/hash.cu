@@ -99,6 +99,8 @@ __device__ __forceinline__ f3 friction_of(float mu, f3 correction, f3 rel_vel) {
 __global__ void k_collide(const float4* __restrict__ x_in, float4* __restrict__ x_out,
                           const float4* __restrict__ x0, const uint32_t* __restrict__ neighbors,
                           uint32_t nv, uint32_t maxnb, float diameter, float mu, float relaxation) {
+  pdl_release();
+  pdl_wait();
   const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= nv) return;
   const float4 pi = x_in[id];
@@ -107,24 +109,41 @@ __global__ void k_collide(const float4* __restrict__ x_in, float4* __restrict__ 
   const float w_i = pi.w;
   f3 pd = mk3(0, 0, 0);
   int cnt = 0;
-  const uint64_t limit = (uint64_t)nv * maxnb;
-  for (uint64_t k = id; k < limit; k += nv) {
-    const uint32_t j = neighbors[k];
-    if (j >= nv) break;  // reference: j > num_particles; j == nv never occurs
-    const float4 pj = x_in[j];
-    const float denom = w_i + pj.w;
-    if (denom <= 0) continue;
-    const f3 pred_j = mk3(pj);
-    const f3 diff = pred_i - pred_j;
-    const float distance = length(diff);
-    if (distance >= diameter) continue;
-    const f3 gradient = diff / (distance + kEps);
-    const float lambda = (distance - diameter) / denom;
-    const f3 common = lambda * gradient;
-    ++cnt;
-    pd = pd - w_i * common;
-    const f3 rel = vel_i - (pred_j - mk3(x0[j]));
-    pd = pd + w_i * friction_of(mu, common, rel);
+  // Neighbor slots are read a batch at a time (ids, then positions, all loads of a batch in
+  // flight); the list ends at the first id >= nv (reference: j > num_particles; j == nv never
+  // occurs) and the batch is then processed in slot order.
+  constexpr uint32_t kBatch = 8;
+  bool done = false;
+  for (uint32_t base = 0; base < maxnb && !done; base += kBatch) {
+    uint32_t nb[kBatch];
+#pragma unroll
+    for (uint32_t r = 0; r < kBatch; ++r)
+      nb[r] = base + r < maxnb ? neighbors[(uint64_t)(base + r) * nv + id] : nv;
+    float4 pj[kBatch];
+#pragma unroll
+    for (uint32_t r = 0; r < kBatch; ++r) pj[r] = nb[r] < nv ? x_in[nb[r]] : make_float4(0, 0, 0, 0);
+#pragma unroll
+    for (uint32_t r = 0; r < kBatch; ++r) {
+      if (done) break;
+      const uint32_t j = nb[r];
+      if (j >= nv) {
+        done = true;
+        break;
+      }
+      const float denom = w_i + pj[r].w;
+      if (denom <= 0) continue;
+      const f3 pred_j = mk3(pj[r]);
+      const f3 diff = pred_i - pred_j;
+      const float distance = length(diff);
+      if (distance >= diameter) continue;
+      const f3 gradient = diff / (distance + kEps);
+      const float lambda = (distance - diameter) / denom;
+      const f3 common = lambda * gradient;
+      ++cnt;
+      pd = pd - w_i * common;
+      const f3 rel = vel_i - (pred_j - mk3(x0[j]));
+      pd = pd + w_i * friction_of(mu, common, rel);
+    }
   }
   f3 q = pred_i;
   const float count = (float)cnt;
@@ -155,9 +174,9 @@ void launch_hash(Context& c) {
 }
 
 void launch_collide(Context& c, const FrameConst& k) {
-  k_collide<<<grid_for(c.nv), kBlock, 0, c.stream>>>(
-      c.x.p, c.x_alt.p, c.x0.p, c.neighbors.p, c.nv, (uint32_t)c.params.max_neighbor_size,
-      k.particle_diameter, k.friction, k.relaxation);
+  launch_k(c.pdl, k_collide, grid_for(c.nv), kBlock, 0, c.stream, c.x.p, c.x_alt.p, c.x0.p,
+           c.neighbors.p, c.nv, (uint32_t)c.params.max_neighbor_size, k.particle_diameter,
+           k.friction, k.relaxation);
 }
 
 }  // namespace xrt

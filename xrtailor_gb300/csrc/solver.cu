@@ -24,6 +24,8 @@ namespace {
 __global__ void k_predict(float4* __restrict__ x, const float4* __restrict__ x0,
                           float4* __restrict__ v, uint32_t nv, float dt, float gx, float gy,
                           float gz) {
+  pdl_release();
+  pdl_wait();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nv) return;
   const float w = x[i].w;
@@ -40,6 +42,8 @@ __global__ void k_finalize(float4* __restrict__ x, float4* __restrict__ x0, floa
                            uint32_t nv, float dt, float damping, float gx, float gy, float gz,
                            const int4* __restrict__ tri, const uint32_t* __restrict__ vf_ptr,
                            const uint32_t* __restrict__ vf_list, float4* __restrict__ nrm) {
+  pdl_release();
+  pdl_wait();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nv) return;
   const float4 p = x[i];
@@ -91,6 +95,8 @@ __device__ __forceinline__ bool stretch_project(float4& a, float4& b, float rest
 template <bool RESET>
 __global__ void k_stretch(const int4* __restrict__ con, float* __restrict__ lambda,
                           float4* __restrict__ x, uint32_t begin, uint32_t end, float dt) {
+  pdl_release();
+  pdl_wait();
   const uint32_t j = begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= end) return;
   const int4 c = __ldg(&con[j]);
@@ -108,32 +114,72 @@ __global__ void k_stretch(const int4* __restrict__ con, float* __restrict__ lamb
 // Tile-local Gauss-Seidel: block = one tile of the launched tile color.  The tile's footprint is
 // staged in shared memory, its local colors run in order with a block barrier between them, and
 // the footprint is written back.  Tiles of one tile color have disjoint footprints.
-// Shared memory of a tile launch: footprint positions, then the tile's constraint records (and,
-// for stretch, the multipliers).  Everything global is read once, up front, in coalesced sweeps,
-// so the chain of local colors touches only shared memory.
+// Shared memory of a tile launch: footprint positions, the tile's constraint records, the
+// multipliers (stretch) or rest angles (bend), then the num_local + 1 local-color offsets.
+// Prologue before pdl_wait (setup-time data only): the tile's metadata, offsets, records and
+// footprint vertex ids, the ids held in registers (kFootPerThread per thread) so the gather and
+// the write-back each issue all their loads and stores at once.
+struct TileFrame {
+  int4 m;                          // first footprint entry, footprint size, first record, count
+  uint32_t fi[kFootPerThread];     // footprint vertex ids of this thread
+};
+
+__device__ __forceinline__ TileFrame tile_prologue(const uint32_t* __restrict__ foot,
+                                                   const int4* __restrict__ meta,
+                                                   const uint32_t* __restrict__ lofs, uint32_t t,
+                                                   uint32_t num_local, uint32_t* so) {
+  TileFrame f;
+  f.m = __ldg(&meta[t]);
+  if (threadIdx.x <= num_local) so[threadIdx.x] = __ldg(&lofs[(size_t)t * (num_local + 1) + threadIdx.x]);
+#pragma unroll
+  for (int r = 0; r < kFootPerThread; ++r) {
+    const uint32_t k = threadIdx.x + (uint32_t)r * kTileBlock;
+    f.fi[r] = k < (uint32_t)f.m.y ? __ldg(&foot[f.m.x + k]) : 0u;
+  }
+  return f;
+}
+
+__device__ __forceinline__ void tile_gather(const TileFrame& f, const float4* __restrict__ x,
+                                            float4* sx) {
+#pragma unroll
+  for (int r = 0; r < kFootPerThread; ++r) {
+    const uint32_t k = threadIdx.x + (uint32_t)r * kTileBlock;
+    if (k < (uint32_t)f.m.y) sx[k] = x[f.fi[r]];
+  }
+}
+
+__device__ __forceinline__ void tile_scatter(const TileFrame& f, float4* __restrict__ x,
+                                             const float4* sx) {
+#pragma unroll
+  for (int r = 0; r < kFootPerThread; ++r) {
+    const uint32_t k = threadIdx.x + (uint32_t)r * kTileBlock;
+    if (k < (uint32_t)f.m.y) x[f.fi[r]] = sx[k];
+  }
+}
+
 template <bool RESET>
-__global__ void __launch_bounds__(kBlock) k_stretch_tiles(
+__global__ void __launch_bounds__(kTileBlock) k_stretch_tiles(
     const int4* __restrict__ con, float* __restrict__ lambda, float4* __restrict__ x,
-    const uint32_t* __restrict__ foot, const uint32_t* __restrict__ foot_ptr,
-    const uint32_t* __restrict__ lc_ptr, uint32_t tile_begin, uint32_t num_local,
+    const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
+    const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
     uint32_t max_foot, uint32_t max_cons, float dt) {
   extern __shared__ float4 smem[];
   float4* sx = smem;
   int4* sc = reinterpret_cast<int4*>(sx + max_foot);
   float* sl = reinterpret_cast<float*>(sc + max_cons);
-  const uint32_t t = tile_begin + blockIdx.x;
-  const uint32_t fb = foot_ptr[t], fe = foot_ptr[t + 1];
-  const uint32_t* lp = lc_ptr + (size_t)t * num_local;
-  const uint32_t c0 = lp[0], c1 = lp[num_local];
-  for (uint32_t k = fb + threadIdx.x; k < fe; k += blockDim.x) sx[k - fb] = x[foot[k]];
-  for (uint32_t j = c0 + threadIdx.x; j < c1; j += blockDim.x) {
-    sc[j - c0] = __ldg(&con[j]);
-    sl[j - c0] = RESET ? 0.0f : lambda[j];
-  }
+  uint32_t* so = reinterpret_cast<uint32_t*>(sl + max_cons);
+  const TileFrame f = tile_prologue(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
+  const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
+#pragma unroll 4
+  for (uint32_t j = threadIdx.x; j < nc; j += kTileBlock) sc[j] = __ldg(&con[c0 + j]);
+  pdl_wait();
+#pragma unroll 4
+  for (uint32_t j = threadIdx.x; j < nc; j += kTileBlock) sl[j] = RESET ? 0.0f : lambda[c0 + j];
+  tile_gather(f, x, sx);
   __syncthreads();
   for (uint32_t l = 0; l < num_local; ++l) {
-    const uint32_t cb = lp[l] - c0, ce = lp[l + 1] - c0;
-    for (uint32_t j = cb + threadIdx.x; j < ce; j += blockDim.x) {
+    const uint32_t ce = so[l + 1];
+    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += kTileBlock) {
       const int4 c = sc[j];
       float lam = sl[j];
       float4 a = sx[c.x], b = sx[c.y];
@@ -145,16 +191,29 @@ __global__ void __launch_bounds__(kBlock) k_stretch_tiles(
     }
     __syncthreads();
   }
-  for (uint32_t k = fb + threadIdx.x; k < fe; k += blockDim.x) x[foot[k]] = sx[k - fb];
-  for (uint32_t j = c0 + threadIdx.x; j < c1; j += blockDim.x) lambda[j] = sl[j - c0];
+  pdl_release();  // late: the successor's blocks arrive as this one drains (measured faster)
+  tile_scatter(f, x, sx);
+#pragma unroll 4
+  for (uint32_t j = threadIdx.x; j < nc; j += kTileBlock) lambda[c0 + j] = sl[j];
 }
 
 // Dihedral bend projection of SolveBend_Kernel on four vertices.
 __device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3, float4& a4,
                                              float theta, float compliance, float dt);
+// The same projection on a lane pair (lanes 2m, 2m+1 of a warp, `half` = lane & 1), for the
+// shared-memory footprint of a tile: each lane evaluates one of the two independent halves of
+// the expression (normal n1 and gradient q3 / normal n2, gradient q4 and the angle), the halves
+// are exchanged by shuffles, and lane 0 writes vertices 1-2, lane 1 vertices 3-4.  Every value is
+// produced by the same operations as bend_project, so the result is identical.  All 32 lanes
+// call it; `active` is false for lanes past the color's last element (they write nothing).
+__device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float theta,
+                                                  float compliance, float dt, uint32_t half,
+                                                  bool active);
 
 __global__ void k_bend(const int4* __restrict__ idx, const float2* __restrict__ tc,
                        float4* __restrict__ x, uint32_t begin, uint32_t end, float dt) {
+  pdl_release();
+  pdl_wait();
   const uint32_t j = begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= end) return;
   const int4 b = __ldg(&idx[j]);
@@ -167,40 +226,43 @@ __global__ void k_bend(const int4* __restrict__ idx, const float2* __restrict__ 
   x[b.w] = a4;
 }
 
-__global__ void __launch_bounds__(kBlock) k_bend_tiles(
+__global__ void __launch_bounds__(kTileBlock) k_bend_tiles(
     const int4* __restrict__ idx, const float2* __restrict__ tc, float4* __restrict__ x,
-    const uint32_t* __restrict__ foot, const uint32_t* __restrict__ foot_ptr,
-    const uint32_t* __restrict__ lc_ptr, uint32_t tile_begin, uint32_t num_local,
+    const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
+    const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
     uint32_t max_foot, uint32_t max_cons, float dt) {
   extern __shared__ float4 smem[];
   float4* sx = smem;
   int4* sc = reinterpret_cast<int4*>(sx + max_foot);
   float2* st = reinterpret_cast<float2*>(sc + max_cons);
-  const uint32_t t = tile_begin + blockIdx.x;
-  const uint32_t fb = foot_ptr[t], fe = foot_ptr[t + 1];
-  const uint32_t* lp = lc_ptr + (size_t)t * num_local;
-  const uint32_t c0 = lp[0], c1 = lp[num_local];
-  for (uint32_t k = fb + threadIdx.x; k < fe; k += blockDim.x) sx[k - fb] = x[foot[k]];
-  for (uint32_t j = c0 + threadIdx.x; j < c1; j += blockDim.x) {
-    sc[j - c0] = __ldg(&idx[j]);
-    st[j - c0] = __ldg(&tc[j]);
+  uint32_t* so = reinterpret_cast<uint32_t*>(st + max_cons);
+  const TileFrame f = tile_prologue(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
+  const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
+#pragma unroll 4
+  for (uint32_t j = threadIdx.x; j < nc; j += kTileBlock) {
+    sc[j] = __ldg(&idx[c0 + j]);
+    st[j] = __ldg(&tc[c0 + j]);
   }
+  pdl_wait();
+  tile_gather(f, x, sx);
   __syncthreads();
+  // Two lanes per bend element (bend_project_pair); the loop trip count is warp-uniform so the
+  // pair exchanges run with full warps.
+  const uint32_t lane0 = threadIdx.x & ~31u;
   for (uint32_t l = 0; l < num_local; ++l) {
-    const uint32_t cb = lp[l] - c0, ce = lp[l + 1] - c0;
-    for (uint32_t j = cb + threadIdx.x; j < ce; j += blockDim.x) {
+    const uint32_t cb = 2 * so[l], ce = 2 * so[l + 1];
+    for (uint32_t base = cb + lane0; base < ce; base += kTileBlock) {
+      const uint32_t s = base + (threadIdx.x & 31u);
+      const bool active = s < ce;
+      const uint32_t j = active ? s >> 1 : cb >> 1;
       const int4 b = sc[j];
       const float2 th = st[j];
-      float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
-      bend_project(a1, a2, a3, a4, th.x, th.y, dt);
-      sx[b.x] = a1;
-      sx[b.y] = a2;
-      sx[b.z] = a3;
-      sx[b.w] = a4;
+      bend_project_pair(sx, b, th.x, th.y, dt, s & 1u, active);
     }
     __syncthreads();
   }
-  for (uint32_t k = fb + threadIdx.x; k < fe; k += blockDim.x) x[foot[k]] = sx[k - fb];
+  pdl_release();
+  tile_scatter(f, x, sx);
 }
 
 __device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3, float4& a4,
@@ -236,6 +298,56 @@ __device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3,
   a4 = make_float4(a4.x + c4.x, a4.y + c4.y, a4.z + c4.z, w4);
 }
 
+// Lane pair form of bend_project.  With (nA, nB, lA) = (n1, n2, |p2 x p3| + eps) on lane 0 and
+// (n2, n1, |p2 x p4| + eps) on lane 1, and pA = p3 / p4:
+//   q3 (lane 0) and q4 (lane 1) are both (p2 x nB + (nA x p2) d) / lA,
+//   the two terms of q2 are -(pA x nB + (nA x pA) d) / lA on lane 0 and +(...) / lA on lane 1;
+// (-X) / L equals -(X / L) bit for bit, so both lanes run one instruction stream.
+__device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float theta,
+                                                  float compliance, float dt, uint32_t half,
+                                                  bool active) {
+  constexpr unsigned kAll = 0xffffffffu;
+  const float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
+  const f3 p1 = mk3(a1);
+  const f3 p2 = mk3(a2) - p1;
+  const f3 p3 = mk3(a3) - p1;
+  const f3 p4 = mk3(a4) - p1;
+  const f3 pA = half ? p4 : p3;
+  const f3 cA = cross(p2, pA);
+  const f3 nA = normalize(cA);
+  const float lA = length(cA) + kEps;
+  const f3 nB = mk3(__shfl_xor_sync(kAll, nA.x, 1), __shfl_xor_sync(kAll, nA.y, 1),
+                    __shfl_xor_sync(kAll, nA.z, 1));
+  const f3 n1 = half ? nB : nA, n2 = half ? nA : nB;
+  const float d = tclamp(dot(n1, n2), 0.0f, 1.0f);
+  const float angle = acos_as(d);
+  const f3 qA = (cross(p2, nB) + cross(nA, p2) * d) / lA;   // q3 on lane 0, q4 on lane 1
+  const f3 vA = (cross(pA, nB) + cross(nA, pA) * d) / lA;   // |terms| of q2
+  const f3 qB = mk3(__shfl_xor_sync(kAll, qA.x, 1), __shfl_xor_sync(kAll, qA.y, 1),
+                    __shfl_xor_sync(kAll, qA.z, 1));
+  const f3 vB = mk3(__shfl_xor_sync(kAll, vA.x, 1), __shfl_xor_sync(kAll, vA.y, 1),
+                    __shfl_xor_sync(kAll, vA.z, 1));
+  const f3 q3 = half ? qB : qA, q4 = half ? qA : qB;
+  const f3 v23 = half ? vB : vA, v24 = half ? vA : vB;
+  const f3 q2 = -v23 - v24;
+  const f3 q1 = -q2 - q3 - q4;
+  const float w1 = a1.w, w2 = a2.w, w3 = a3.w, w4 = a4.w;
+  const float xpbd_bend = compliance / dt / dt;
+  const float denom =
+      xpbd_bend + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) + w4 * dot(q4, q4));
+  if (!active || angle < kEps || isnan(d) || denom < kEps) return;
+  const float lambda = sqrtf(1.0f - d * d) * (angle - theta) / denom;
+  const float scaling = 1.0f;
+  // lane 0 moves vertices 1 and 2, lane 1 vertices 3 and 4
+  const float wa = half ? w3 : w1, wb = half ? w4 : w2;
+  const f3 qa = half ? q3 : q1, qb = half ? q4 : q2;
+  const float4 aa = half ? a3 : a1, ab = half ? a4 : a2;
+  const f3 ca = scaling * wa * lambda * qa;
+  const f3 cb = scaling * wb * lambda * qb;
+  sx[half ? b.z : b.x] = make_float4(aa.x + ca.x, aa.y + ca.y, aa.z + ca.z, wa);
+  sx[half ? b.w : b.y] = make_float4(ab.x + cb.x, ab.y + cb.y, ab.z + cb.z, wb);
+}
+
 __device__ __forceinline__ f3 lra_project(f3 xt, f3 xs, float w_t, float rest, float stretch) {
   const float target = rest * stretch;
   if (w_t < kEps && target > 0) return xt;
@@ -245,24 +357,12 @@ __device__ __forceinline__ f3 lra_project(f3 xt, f3 xs, float w_t, float rest, f
   return xt;
 }
 
-// All slots pinned: per target vertex, its slots in list order (slot sources never move here).
-__global__ void k_lra_by_target(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ src,
-                                const float* __restrict__ rest, float4* __restrict__ x, uint32_t nv,
-                                float stretch) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nv) return;
-  const uint32_t b = ptr[t], e = ptr[t + 1];
-  if (b == e) return;
-  const float4 p = x[t];
-  f3 xt = mk3(p);
-  for (uint32_t k = b; k < e; ++k) xt = lra_project(xt, mk3(x[src[k]]), p.w, rest[k], stretch);
-  if (xt.x != p.x || xt.y != p.y || xt.z != p.z) x[t] = mk4(xt, p.w);
-}
-
 // Free slot vertices: one launch per slot over that slot's constraint block (list order).
 __global__ void k_lra_block(const uint32_t* __restrict__ tgt, const uint32_t* __restrict__ src,
                             const float* __restrict__ rest, float4* __restrict__ x, uint32_t begin,
                             uint32_t end, float stretch) {
+  pdl_release();
+  pdl_wait();
   const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= end) return;
   const uint32_t t = tgt[k];
@@ -275,75 +375,140 @@ __device__ __forceinline__ f3 prim_normal(const float4* __restrict__ pred, int f
   return face_normal(mk3(pred[3 * f]), mk3(pred[3 * f + 1]), mk3(pred[3 * f + 2]));
 }
 
-// SolveVFCCD_Kernel then SolveVFDCD_Kernel for one vertex.
-__global__ void k_vf_solve(float4* __restrict__ x, const int* __restrict__ rt_idx,
-                           const float4* __restrict__ rt_qc, const int* __restrict__ vf_idx,
-                           const float4* __restrict__ vf_qs, const float4* __restrict__ pred,
-                           uint32_t nv) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nv) return;
-  const int rc = rt_idx[i], vc = vf_idx[i];
-  if (rc == -1 && vc == -1) return;
-  float4 p = x[i];
+// Iteration tail, two Jacobi kernels (each reads x_in, writes x_out):
+//   k_stage: LRA (SolveGeodesicLRA_Kernel, all slots pinned: slot positions are constant in the
+//            phase) then SolveVFCCD_Kernel and SolveVFDCD_Kernel (PBDCollision.cu:279-298,
+//            57-80) -- both update a vertex from its own data only;
+//   k_ee:    SolveEEDCD_Kernel + ApplyDeltas_Kernel (PBDCollision.cu:163-212,
+//            ClothSolverHelper.cu:139-148) and SolveBinding_Kernel (BindingConstraint.cu:56-92).
+struct TailArgs {
+  const float4* x_in;
+  float4* x_out;
+  uint32_t nv;
+  const uint32_t *lra_ptr, *lra_src;  // per target vertex, slot order
+  const float* lra_rest;
+  float lra_stretch;
+  const int *rt_idx, *vf_idx;
+  const float4 *rt_qc, *vf_qs, *pred;
+  const uint32_t *ve_ptr, *ve_list;
+  const uint2* edge;
+  const float4 *ee_a, *ee_b, *ee_c;
+  float relaxation;
+  const uint32_t* bind_ptr;
+  const float4* bind_a;
+  const int4* bind_b;
+  const float4* ox;
+};
+
+// Position of vertex j after the LRA and VF phases.
+template <bool LRA, bool CONTACTS>
+__device__ __forceinline__ f3 tail_stage(const TailArgs& a, uint32_t j, const float4 p) {
   f3 q = mk3(p);
-  if (rc != -1) {
-    const f3 nc = prim_normal(pred, rc);
-    const float lambda = dot(nc, q - mk3(rt_qc[i]));
-    if (lambda < 0) q = q + (-lambda * nc);
+  if (LRA) {
+    const uint32_t b = __ldg(&a.lra_ptr[j]), e = __ldg(&a.lra_ptr[j + 1]);
+    if (b != e) {
+      f3 xt = q;
+      for (uint32_t k = b; k < e; ++k)
+        xt = lra_project(xt, mk3(a.x_in[__ldg(&a.lra_src[k])]), p.w, __ldg(&a.lra_rest[k]),
+                         a.lra_stretch);
+      if (xt.x != p.x || xt.y != p.y || xt.z != p.z) q = xt;  // the phase writes only changes
+    }
   }
-  if (vc != -1) {
-    const f3 ns = prim_normal(pred, vc);
-    const float lambda = dot(ns, q - mk3(vf_qs[i])) - 1e-3f;
-    if (lambda < 0) q = q + (-lambda * ns);
+  if (CONTACTS) {
+    const int rc = a.rt_idx[j], vc = a.vf_idx[j];
+    if (rc != -1) {
+      const f3 nc = prim_normal(a.pred, rc);
+      const float lambda = dot(nc, q - mk3(a.rt_qc[j]));
+      if (lambda < 0) q = q + (-lambda * nc);
+    }
+    if (vc != -1) {
+      const f3 ns = prim_normal(a.pred, vc);
+      const float lambda = dot(ns, q - mk3(a.vf_qs[j])) - 1e-3f;
+      if (lambda < 0) q = q + (-lambda * ns);
+    }
   }
-  x[i] = mk4(q, p.w);
+  return q;
 }
 
-// SolveEEDCD_Kernel + ApplyDeltas_Kernel + SolveBinding_Kernel per vertex (Jacobi: reads x_in,
-// writes x_out).
-template <bool CONTACTS, bool BINDINGS>
-__global__ void k_ee_apply(const float4* __restrict__ x_in, float4* __restrict__ x_out, uint32_t nv,
-                           const uint32_t* __restrict__ ve_ptr, const uint32_t* __restrict__ ve_list,
-                           const uint2* __restrict__ edge, const float4* __restrict__ ee_a,
-                           const float4* __restrict__ ee_b, const float4* __restrict__ ee_c,
-                           float relaxation, const uint32_t* __restrict__ bind_ptr,
-                           const float4* __restrict__ bind_a, const int4* __restrict__ bind_b,
-                           const float4* __restrict__ ox) {
+// LRA + VF: x_out = tail_stage(x_in), per vertex.
+template <bool LRA, bool CONTACTS>
+__global__ void k_stage(const TailArgs a) {
+  pdl_release();
+  pdl_wait();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nv) return;
+  const float4 p = a.x_in[i];
+  a.x_out[i] = mk4(tail_stage<LRA, CONTACTS>(a, i, p), p.w);
+}
+
+// EE + ApplyDeltas + binding on the post-VF positions x_in.
+template <bool CONTACTS, bool BINDINGS>
+__global__ void k_ee(const TailArgs a) {
+  pdl_release();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nv = a.nv;
+  // incident-edge list (setup-time) ahead of the wait
+  constexpr int kBatch = 8;
+  uint32_t kb = 0, ke = 0, code[kBatch];
+  if (CONTACTS && i < nv) {
+    kb = __ldg(&a.ve_ptr[i]);
+    ke = __ldg(&a.ve_ptr[i + 1]);
+#pragma unroll
+    for (int r = 0; r < kBatch; ++r) code[r] = kb + r < ke ? __ldg(&a.ve_list[kb + r]) : 0u;
+  }
+  pdl_wait();
   if (i >= nv) return;
+  const float4* __restrict__ x_in = a.x_in;
+  const float4* __restrict__ ee_a = a.ee_a;
+  const float4* __restrict__ ee_b = a.ee_b;
+  const float4* __restrict__ ee_c = a.ee_c;
+  const uint32_t* __restrict__ ve_list = a.ve_list;
+  const float relaxation = a.relaxation;
   const float4 p = x_in[i];
   f3 q = mk3(p);
   if (CONTACTS) {
     f3 delta = mk3(0, 0, 0);
     int count = 0;
-    for (uint32_t k = ve_ptr[i]; k < ve_ptr[i + 1]; ++k) {
-      const uint32_t code = ve_list[k];
-      const uint32_t e = code >> 1;
-      const float4 ca = ee_a[e];
-      if (ca.x > 1e6f) continue;
-      const float4 cb = ee_b[e], cc = ee_c[e];
-      const uint2 ed = edge[e];
-      const f3 p1 = mk3(x_in[ed.x]), q1 = mk3(x_in[ed.y]);
-      const float s = cb.w, t = cc.w;
-      const f3 fn = mk3(cc);
-      const f3 c1 = (1 - s) * p1 + s * q1;
-      const f3 c2 = (1 - t) * mk3(ca.y, ca.z, ca.w) + t * mk3(cb);
-      const f3 d = c1 - c2;
-      const float len = length(d);
-      if (len < kEps) continue;
-      const float lambda = dot(d, fn) - 1e-3f;
-      if (lambda > 0) continue;
-      const f3 corr = (code & 1u) ? (-(s)*lambda * fn) : (-(1 - s) * lambda * fn);
-      delta = delta + corr;
-      ++count;
+    // The contact-flag loads of a batch of incident edges are issued together; the edges are
+    // then processed one by one in list order.
+    for (uint32_t base = kb; base < ke; base += kBatch) {
+      if (base != kb) {
+#pragma unroll
+        for (int r = 0; r < kBatch; ++r) code[r] = base + r < ke ? ve_list[base + r] : 0u;
+      }
+      float flag[kBatch];
+#pragma unroll
+      for (int r = 0; r < kBatch; ++r) flag[r] = base + r < ke ? ee_a[code[r] >> 1].x : 2e6f;
+#pragma unroll
+      for (int r = 0; r < kBatch; ++r) {
+        if (flag[r] > 1e6f) continue;  // no contact on this edge (or past the list)
+        const uint32_t e = code[r] >> 1;
+        const float4 ca = ee_a[e];
+        const float4 cb = ee_b[e], cc = ee_c[e];
+        const uint2 ed = a.edge[e];
+        const f3 p1 = mk3(x_in[ed.x]), q1 = mk3(x_in[ed.y]);
+        const float s = cb.w, t = cc.w;
+        const f3 fn = mk3(cc);
+        const f3 c1 = (1 - s) * p1 + s * q1;
+        const f3 c2 = (1 - t) * mk3(ca.y, ca.z, ca.w) + t * mk3(cb);
+        const f3 d = c1 - c2;
+        const float len = length(d);
+        if (len < kEps) continue;
+        const float lambda = dot(d, fn) - 1e-3f;
+        if (lambda > 0) continue;
+        const f3 corr = (code[r] & 1u) ? (-(s)*lambda * fn) : (-(1 - s) * lambda * fn);
+        delta = delta + corr;
+        ++count;
+      }
     }
     const float fc = (float)count;
     if (fc > 0.0f) q = q + delta / fc * relaxation;
   }
   if (BINDINGS && p.w >= kEps) {
-    for (uint32_t k = bind_ptr[i]; k < bind_ptr[i + 1]; ++k) {
-      const float4 ba = bind_a[k];
-      const int4 bb = bind_b[k];
+    for (uint32_t k = a.bind_ptr[i]; k < a.bind_ptr[i + 1]; ++k) {
+      const float4 ba = a.bind_a[k];
+      const int4 bb = a.bind_b[k];
+      const float4* __restrict__ ox = a.ox;
       const f3 pob = ba.x * mk3(ox[bb.x]) + ba.y * mk3(ox[bb.y]) + ba.z * mk3(ox[bb.z]);
       const float C = length(q - pob) - ba.w;
       const f3 nn = normalize(q - pob);
@@ -354,47 +519,35 @@ __global__ void k_ee_apply(const float4* __restrict__ x_in, float4* __restrict__
       q = q + (-s * p.w * nn);
     }
   }
-  x_out[i] = mk4(q, p.w);
+  a.x_out[i] = mk4(q, p.w);
 }
 
 }  // namespace
 
 void launch_predict(Context& c, const FrameConst& k) {
-  k_predict<<<grid_for(c.nv), kBlock, 0, c.stream>>>(c.x.p, c.x0.p, c.v.p, c.nv, k.dt, k.gx, k.gy,
-                                                     k.gz);
+  launch_k(c.pdl, k_predict, grid_for(c.nv), kBlock, 0, c.stream, c.x.p, c.x0.p, c.v.p, c.nv, k.dt,
+           k.gx, k.gy, k.gz);
 }
 
 void launch_finalize_predict(Context& c, const FrameConst& k, bool predict_next, bool normals) {
-  const unsigned g = grid_for(c.nv);
-  if (predict_next)
-    k_finalize<true, false><<<g, kBlock, 0, c.stream>>>(c.x.p, c.x0.p, c.v.p, c.nv, k.dt, k.damping,
-                                                        k.gx, k.gy, k.gz, c.tri.p, c.vf_ptr.p,
-                                                        c.vf_list.p, c.n.p);
-  else if (normals)
-    k_finalize<false, true><<<g, kBlock, 0, c.stream>>>(c.x.p, c.x0.p, c.v.p, c.nv, k.dt, k.damping,
-                                                        k.gx, k.gy, k.gz, c.tri.p, c.vf_ptr.p,
-                                                        c.vf_list.p, c.n.p);
-  else
-    k_finalize<false, false><<<g, kBlock, 0, c.stream>>>(c.x.p, c.x0.p, c.v.p, c.nv, k.dt,
-                                                         k.damping, k.gx, k.gy, k.gz, c.tri.p,
-                                                         c.vf_ptr.p, c.vf_list.p, c.n.p);
+  auto kern = predict_next ? k_finalize<true, false>
+                           : (normals ? k_finalize<false, true> : k_finalize<false, false>);
+  launch_k(c.pdl, kern, grid_for(c.nv), kBlock, 0, c.stream, c.x.p, c.x0.p, c.v.p, c.nv, k.dt,
+           k.damping, k.gx, k.gy, k.gz, c.tri.p, c.vf_ptr.p, c.vf_list.p, c.n.p);
 }
 
 void launch_stretch(Context& c, const FrameConst& k, ColorRange r, bool reset_lambda) {
   const uint32_t n = r.end - r.begin;
   if (n == 0) return;
-  if (reset_lambda)
-    k_stretch<true><<<grid_for(n), kBlock, 0, c.stream>>>(c.s_con.p, c.s_lambda.p, c.x.p, r.begin,
-                                                          r.end, k.dt);
-  else
-    k_stretch<false><<<grid_for(n), kBlock, 0, c.stream>>>(c.s_con.p, c.s_lambda.p, c.x.p, r.begin,
-                                                           r.end, k.dt);
+  launch_k(c.pdl, reset_lambda ? k_stretch<true> : k_stretch<false>, grid_for(n), kBlock, 0,
+           c.stream, c.s_con.p, c.s_lambda.p, c.x.p, r.begin, r.end, k.dt);
 }
 
 void launch_bend(Context& c, const FrameConst& k, ColorRange r) {
   const uint32_t n = r.end - r.begin;
   if (n == 0) return;
-  k_bend<<<grid_for(n), kBlock, 0, c.stream>>>(c.b_idx.p, c.b_tc.p, c.x.p, r.begin, r.end, k.dt);
+  launch_k(c.pdl, k_bend, grid_for(n), kBlock, 0, c.stream, c.b_idx.p, c.b_tc.p, c.x.p, r.begin,
+           r.end, k.dt);
 }
 
 cudaError_t configure_tile_kernels(size_t max_smem_bytes) {
@@ -409,8 +562,12 @@ cudaError_t configure_tile_kernels(size_t max_smem_bytes) {
   return e;
 }
 
+static_assert(kTileBlock * kFootPerThread >= (int)kTileMaxFootprint,
+              "tile kernels hold every footprint vertex id in registers");
+
 size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes) {
-  return sizeof(float4) * T.max_foot + record_bytes * T.max_cons;
+  return sizeof(float4) * T.max_foot + record_bytes * T.max_cons +
+         sizeof(uint32_t) * (T.num_local + 1);
 }
 
 void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, bool reset_lambda) {
@@ -418,56 +575,68 @@ void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, boo
   if (nt == 0) return;
   const TiledSet& T = c.s_tiles;
   const size_t smem = tile_smem_bytes(T, sizeof(int4) + sizeof(float));
-  if (reset_lambda)
-    k_stretch_tiles<true><<<nt, kBlock, smem, c.stream>>>(c.s_con.p, c.s_lambda.p, c.x.p, T.foot.p,
-                                                          T.foot_ptr.p, T.lc_ptr.p, tiles.begin,
-                                                          T.num_local, T.max_foot, T.max_cons,
-                                                          k.dt);
-  else
-    k_stretch_tiles<false><<<nt, kBlock, smem, c.stream>>>(
-        c.s_con.p, c.s_lambda.p, c.x.p, T.foot.p, T.foot_ptr.p, T.lc_ptr.p, tiles.begin,
-        T.num_local, T.max_foot, T.max_cons, k.dt);
+  launch_k(c.pdl, reset_lambda ? k_stretch_tiles<true> : k_stretch_tiles<false>, nt, kTileBlock,
+           smem, c.stream, c.s_con.p, c.s_lambda.p, c.x.p, T.foot.p, T.meta.p, T.lofs.p,
+           tiles.begin, T.num_local, T.max_foot, T.max_cons, k.dt);
 }
 
 void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles) {
   const uint32_t nt = tiles.end - tiles.begin;
   if (nt == 0) return;
   const TiledSet& T = c.b_tiles;
-  k_bend_tiles<<<nt, kBlock, tile_smem_bytes(T, sizeof(int4) + sizeof(float2)), c.stream>>>(
-      c.b_idx.p, c.b_tc.p, c.x.p, T.foot.p, T.foot_ptr.p, T.lc_ptr.p, tiles.begin, T.num_local,
-      T.max_foot, T.max_cons, k.dt);
+  launch_k(c.pdl, k_bend_tiles, nt, kTileBlock, tile_smem_bytes(T, sizeof(int4) + sizeof(float2)),
+           c.stream, c.b_idx.p, c.b_tc.p, c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin,
+           T.num_local, T.max_foot, T.max_cons, k.dt);
 }
 
-// LRA phase: one per-target launch when every slot vertex is pinned (slot positions are then
-// constant during the phase), else one launch per slot block in list order.
+// LRA phase with a free slot vertex: one launch per slot block in list order.  (With every slot
+// vertex pinned, slot positions are constant during the phase and it runs per target inside
+// k_tail.)
 void launch_lra(Context& c, const FrameConst& k) {
   if (c.nl == 0) return;
-  if (c.lra_by_target) {
-    k_lra_by_target<<<grid_for(c.nv), kBlock, 0, c.stream>>>(c.lra_ptr.p, c.lra_src.p,
-                                                             c.lra_rest.p, c.x.p, c.nv,
-                                                             k.lra_stretch);
-  } else {
-    for (const ColorRange& r : c.lra_blocks)
-      k_lra_block<<<grid_for(r.end - r.begin), kBlock, 0, c.stream>>>(
-          c.lra_l_tgt.p, c.lra_l_src.p, c.lra_l_rest.p, c.x.p, r.begin, r.end, k.lra_stretch);
-  }
+  for (const ColorRange& r : c.lra_blocks)
+    launch_k(c.pdl, k_lra_block, grid_for(r.end - r.begin), kBlock, 0, c.stream, c.lra_l_tgt.p,
+             c.lra_l_src.p, c.lra_l_rest.p, c.x.p, r.begin, r.end, k.lra_stretch);
 }
 
-void launch_vf_solve(Context& c) {
-  k_vf_solve<<<grid_for(c.nv), kBlock, 0, c.stream>>>(c.x.p, c.rt_idx.p, c.rt_qc.p, c.vf_idx.p,
-                                                      c.vf_qs.p, c.bvh.pred.p, c.nv);
+static TailArgs tail_args(Context& c, const FrameConst& k) {
+  TailArgs a;
+  a.x_in = c.x.p;
+  a.x_out = c.x_alt.p;
+  a.nv = c.nv;
+  a.lra_ptr = c.lra_ptr.p;
+  a.lra_src = c.lra_src.p;
+  a.lra_rest = c.lra_rest.p;
+  a.lra_stretch = k.lra_stretch;
+  a.rt_idx = c.rt_idx.p;
+  a.vf_idx = c.vf_idx.p;
+  a.rt_qc = c.rt_qc.p;
+  a.vf_qs = c.vf_qs.p;
+  a.pred = c.bvh.pred.p;
+  a.ve_ptr = c.ve_ptr.p;
+  a.ve_list = c.ve_list.p;
+  a.edge = c.edge.p;
+  a.ee_a = c.ee_a.p;
+  a.ee_b = c.ee_b.p;
+  a.ee_c = c.ee_c.p;
+  a.relaxation = k.relaxation;
+  a.bind_ptr = c.bind_ptr.p;
+  a.bind_a = c.bind_a.p;
+  a.bind_b = c.bind_b.p;
+  a.ox = c.ox.p;
+  return a;
 }
 
-void launch_ee_apply(Context& c, const FrameConst& k, bool contacts, bool bindings) {
-  const unsigned g = grid_for(c.nv);
-  auto args = [&](auto kern) {
-    kern<<<g, kBlock, 0, c.stream>>>(c.x.p, c.x_alt.p, c.nv, c.ve_ptr.p, c.ve_list.p, c.edge.p,
-                                     c.ee_a.p, c.ee_b.p, c.ee_c.p, k.relaxation, c.bind_ptr.p,
-                                     c.bind_a.p, c.bind_b.p, c.ox.p);
-  };
-  if (contacts && bindings) args(k_ee_apply<true, true>);
-  else if (contacts) args(k_ee_apply<true, false>);
-  else if (bindings) args(k_ee_apply<false, true>);
+void launch_stage(Context& c, const FrameConst& k, bool lra, bool contacts) {
+  if (!lra && !contacts) return;
+  auto kern = lra ? (contacts ? k_stage<true, true> : k_stage<true, false>) : k_stage<false, true>;
+  launch_k(c.pdl, kern, grid_for(c.nv), kBlock, 0, c.stream, tail_args(c, k));
+}
+
+void launch_ee(Context& c, const FrameConst& k, bool contacts, bool bindings) {
+  if (!contacts && !bindings) return;
+  auto kern = contacts ? (bindings ? k_ee<true, true> : k_ee<true, false>) : k_ee<false, true>;
+  launch_k(c.pdl, kern, grid_for(c.nv), kBlock, 0, c.stream, tail_args(c, k));
 }
 
 }  // namespace xrt

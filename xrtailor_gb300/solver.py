@@ -264,6 +264,16 @@ class ClothSolver:
     def set_graph_mode(self, enabled: bool):
         L.check(self._lib.xrt_set_graph_mode(self._h, int(bool(enabled))), self._h, "graph mode")
 
+    def set_tile_vertices(self, n: int):
+        """Tile size of the tile-local Gauss-Seidel schedule (0: per-color launches); before
+        start()."""
+        L.check(self._lib.xrt_set_tile_vertices(self._h, int(n)), self._h, "tile vertices")
+
+    def set_dependent_launch(self, enabled: bool):
+        """Programmatic dependent launch of the substep kernels (default on)."""
+        L.check(self._lib.xrt_set_dependent_launch(self._h, int(bool(enabled))), self._h,
+                "dependent launch")
+
     def set_profiling(self, enabled: bool):
         """Per-launch CUDA-event timing of every phase (eager frames); resets the totals."""
         L.check(self._lib.xrt_set_profiling(self._h, int(bool(enabled))), self._h, "profiling")
