@@ -154,6 +154,8 @@ def run_ours(args, rank, local_rank, world):
     sc = _workload(args.workload)
     p = scenes.scene_params(sc)
     solver = ClothSolver(p, device=local_rank)
+    if args.tile_vertices is not None:
+        solver.set_tile_vertices(args.tile_vertices)
     _setup(solver, sc)
     s = solver.sizes()
     V, S = s.num_vertices, p.num_substeps
@@ -277,6 +279,135 @@ def run_ours(args, rank, local_rank, world):
     return result
 
 
+def run_batched(args, local_rank):
+    """The batched workload: `--instances` garments (default 512), each on its own body, stepped
+    by one context in one launch per phase; then the same garments stepped one context each
+    (the plain step per garment) on the same GPU, frames timed the same way."""
+    import torch
+    from xrtailor_gb300 import ClothSolver, build as xb, scenes
+    xb.build()
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    t_setup = time.perf_counter()
+    gs = scenes.batched_garments(args.instances)
+    p = scenes._params(**scenes.BATCHED_PARAMS)
+    S = p.num_substeps
+    s = ClothSolver(p, device=local_rank)
+    if args.tile_vertices is not None:
+        s.set_tile_vertices(args.tile_vertices)
+    for g in gs:
+        s.add_instance(g.cloth, g.body.mesh)
+    s.set_compliance(0, np.concatenate([np.full(g.num_edges, g.stretch_compliance, np.float32)
+                                        for g in gs]))
+    s.start()
+    setup_s = time.perf_counter() - t_setup
+    sz = s.sizes()
+    V = sz.num_vertices
+    nframes = args.warmup + args.steps + 1
+    ov = [len(g.body.rest) for g in gs]
+    obase = np.concatenate([[0], np.cumsum(ov)])
+    tg = torch.empty((nframes, int(obase[-1]), 3), dtype=torch.float32, device=dev)
+    for f in range(nframes):
+        tg[f] = torch.from_numpy(np.concatenate([g.body.pose((f + 1) / 60.0) for g in gs]))
+    torch.cuda.synchronize()
+    _, _, sp = s.device_state()
+    stream = torch.cuda.ExternalStream(sp, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    lib = s._lib
+    fi = 0
+    for _ in range(args.warmup):
+        lib.xrt_set_obstacle_targets_device(s._h, tg[fi].data_ptr())
+        fi += 1
+        s.step()
+    s.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        with torch.cuda.stream(stream):
+            for a, b in ev:
+                lib.xrt_set_obstacle_targets_device(s._h, tg[fi].data_ptr())
+                fi += 1
+                a.record(stream)
+                s.step()
+                b.record(stream)
+                flush.zero_()
+        torch.cuda.synchronize()
+    s.synchronize()
+    t_batch = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    value = V * S * args.steps / t_batch
+    launches = s.sizes().launches_per_frame
+    # per-phase profile (one eager frame with CUDA events around every launch)
+    s.set_profiling(True)
+    lib.xrt_set_obstacle_targets_device(s._h, tg[fi % nframes].data_ptr())
+    s.step()
+    prof = s.profile()
+    s.set_profiling(False)
+    phases = {k: round(v["ms"] / max(prof["frames"], 1), 3) for k, v in prof.items()
+              if k != "frames" and v["launches"]}
+    s.close()
+    del s
+    torch.cuda.empty_cache()
+    # the plain step per garment: one context per garment, frames timed with events on its stream
+    step_idx = max(1, len(gs) // max(1, args.plain_sample))
+    sample = list(range(0, len(gs), step_idx))[: args.plain_sample] if args.plain_sample > 0 else []
+    plain_t, plain_units = 0.0, 0
+    t_plain_wall = time.perf_counter()
+    for i in sample:
+        g = gs[i]
+        q = ClothSolver(p, device=local_rank)
+        if args.tile_vertices is not None:
+            q.set_tile_vertices(args.tile_vertices)
+        q.add_cloth(g.cloth)
+        q.add_obstacle(g.body.mesh)
+        q.set_compliance(0, np.full(g.num_edges, g.stretch_compliance, np.float32))
+        q.start()
+        _, _, qsp = q.device_state()
+        qs = torch.cuda.ExternalStream(qsp, device=dev)
+        o0, o1 = int(obase[i]), int(obase[i + 1])
+        lib.xrt_set_obstacle_targets_device(q._h, tg[0, o0:o1].data_ptr())
+        q.step()  # warm-up (captures the frame graph)
+        q.synchronize()
+        pe = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.plain_frames)]
+        with torch.cuda.stream(qs):
+            for k, (a, b) in enumerate(pe):
+                lib.xrt_set_obstacle_targets_device(q._h, tg[1 + k, o0:o1].data_ptr())
+                a.record(qs)
+                q.step()
+                b.record(qs)
+        torch.cuda.synchronize()
+        plain_t += sum(a.elapsed_time(b) for a, b in pe) / 1e3 / args.plain_frames
+        plain_units += len(g.cloth.positions) * S
+        q.close()
+    plain_wall = time.perf_counter() - t_plain_wall
+    plain_value = plain_units / plain_t if plain_t > 0 else None
+    return {
+        "metric": METRIC, "value": value, "unit": "vertex-substeps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_batch / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded: xrtailor_gb300/scenes.py batched_garments)",
+        "config": {"workload": f"batched_{len(gs)}", "instances": len(gs), "vertices": V,
+                   "edges": sz.num_edges, "bends": sz.num_bends,
+                   "obstacle_triangles": sz.num_obstacle_triangles, "substeps": S,
+                   "iterations": p.num_iterations, "collision_passes": p.num_collision_passes,
+                   "self_collision": bool(p.enable_self_collision),
+                   "l2": "flushed between frames (512 MiB write, outside the timed events)",
+                   "setup_s": round(setup_s, 1), "parallelism": "single"},
+        "gpu_launches": int(launches) * args.steps,
+        "plain_per_garment": {
+            "value": plain_value, "unit": "vertex-substeps/s",
+            "garments_timed": len(sample), "frames_each": args.plain_frames,
+            "wall_s": round(plain_wall, 1),
+            "method": "each garment alone in its own context (graph replay), CUDA events per "
+                      "frame; throughput = sum of vertex-substeps / sum of frame times"},
+        "batched_over_plain": value / plain_value if plain_value else None,
+        "phase_ms_per_frame": phases,
+        "clocks": clocks.summary(),
+    }
+
+
 def run_cpu(workload, frames, warmup=1, threads=0):
     from oracle.oracle import OracleSolver, lib
     from xrtailor_gb300 import scenes
@@ -308,9 +439,16 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="garment", choices=["garment", "small", "heavy"])
+    ap.add_argument("--workload", default="garment",
+                    choices=["garment", "small", "heavy", "batched"])
     ap.add_argument("--cpu-frames", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--instances", type=int, default=512, help="batched workload: garments")
+    ap.add_argument("--plain-sample", type=int, default=512,
+                    help="batched workload: garments timed alone (evenly spaced)")
+    ap.add_argument("--plain-frames", type=int, default=2)
+    ap.add_argument("--tile-vertices", type=int, default=None,
+                    help="tile size of the Gauss-Seidel schedule (library default if omitted)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -334,6 +472,10 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.workload == "batched":
+        if rank == 0:
+            print(json.dumps(run_batched(args, local_rank)))
+        return
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")

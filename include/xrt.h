@@ -123,8 +123,10 @@ typedef struct xrt_sizes {
   uint32_t num_stretch_colors, num_bend_colors;
   uint32_t launches_per_frame;     /* kernels launched by one xrt_step_frame */
   uint32_t frame_index;
-  float particle_diameter;
-  uint32_t reserved[7];
+  float particle_diameter;         /* of instance 0 (merged mode: the last cloth added) */
+  uint32_t num_instances;          /* 1 in merged mode */
+  uint32_t num_obstacle_bvh_nodes; /* sum over instances of 2 F_i - 1 (F_i > 0) */
+  uint32_t reserved[5];
 } xrt_sizes;
 
 typedef struct xrt_ctx xrt_ctx;
@@ -146,6 +148,18 @@ xrt_status xrt_set_params(xrt_ctx* ctx, const xrt_swift_params* params);
 xrt_status xrt_add_cloth(xrt_ctx* ctx, const xrt_cloth_desc* desc, int32_t* out_vertex_offset);
 /* ClothSolverUniversal::AddObstacle. */
 xrt_status xrt_add_obstacle(xrt_ctx* ctx, const xrt_obstacle_desc* desc, int32_t* out_vertex_offset);
+/* Batched form: adds an independent instance, a cloth with its own obstacle (`obstacle` may be
+ * NULL).  Every instance runs in the same launches as the others, but sees only itself: its own
+ * particle diameter, particle-hash table (2 V_i cells) and obstacle LBVH, no contact with other
+ * instances.  Instance i's frame is bit for bit that of a context holding only cloth i and
+ * obstacle i.  Cloth vertices, obstacle vertices and triangles are numbered over all instances
+ * in the order added (obstacle targets, exports); binding obstacle indices are local to the
+ * instance's obstacle.  Per-instance compliance goes through xrt_set_compliance.  A context is
+ * either batched or merged (xrt_add_cloth / xrt_add_obstacle: the reference's single mesh);
+ * Quality-mode repulsion (pbd_repulsion) is merged-mode only.  No reference counterpart: the
+ * reference steps one solver per scene. */
+xrt_status xrt_add_instance(xrt_ctx* ctx, const xrt_cloth_desc* cloth,
+                            const xrt_obstacle_desc* obstacle, int32_t* out_instance);
 /* Overrides the graph coloring of the stretch (kind 0) or bend (kind 1) constraints, in the
  * constraint order reported by xrt_get_edges / xrt_get_bends.  Replaces
  * GraphColoring::Paint (src/physics/graph_coloring/Base.cu:163-317), whose randomized result
@@ -224,7 +238,10 @@ xrt_status xrt_get_obstacle_rtri(const xrt_ctx* ctx, uint32_t* masks);
 /* Obstacle LBVH as built at the last frame start (BVH::Construct, BVH.cu:618-722) and refit
  * by the last collision pass.  sorted_morton/sorted_objects: num_obstacle_triangles;
  * nodes: 4 int32 per node (parent, left, right, object; 0xFFFFFFFF = none), 2F-1 nodes;
- * aabbs: 6 floats per node (lower xyz, upper xyz); i_esc: F-1, e_esc: F.  Any pointer may be NULL. */
+ * aabbs: 6 floats per node (lower xyz, upper xyz); i_esc: F-1, e_esc: F.  Any pointer may be NULL.
+ * Batched contexts: the instances' trees one after the other (num_obstacle_bvh_nodes nodes,
+ * num_obstacle_bvh_nodes - F internal escapes); links and objects are local to each tree,
+ * sorted_objects are global triangle ids. */
 xrt_status xrt_export_obstacle_bvh(xrt_ctx* ctx, uint32_t* sorted_morton, uint32_t* sorted_objects,
                                    uint32_t* nodes, float* aabbs, int32_t* i_esc, int32_t* e_esc);
 /* Contacts of the last collision pass (VFContact / RTContact / EEContact, pbd_collision/Contact.cuh):

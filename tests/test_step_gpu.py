@@ -166,6 +166,28 @@ def test_tile_sizes_match_oracle(xrt, tile):
         g.set_tile_vertices(64)  # after start
 
 
+def test_later_context_with_smaller_tiles(xrt):
+    """A context started after another, with smaller tile footprints, must not break the first
+    (the tile kernels' shared-memory limit is shared by the process)."""
+    big_cloth, obs = small_scene(40)
+    small_cloth, _ = small_scene(8)
+    p = _params(num_substeps=2, num_iterations=3, num_collision_passes=2)
+    big = ClothSolver(p)
+    big.set_tile_vertices(1024)
+    big.add_cloth(big_cloth, particle_diameter=0.02)
+    big.add_obstacle(obs)
+    big.start()
+    small = ClothSolver(p)
+    small.add_cloth(small_cloth, particle_diameter=0.02)
+    small.start()
+    for _ in range(2):
+        big.step()
+        small.step()
+    big.synchronize()
+    small.synchronize()
+    assert np.isfinite(big.host_positions()).all()
+
+
 @pytest.mark.parametrize("graph", [True, False])
 def test_dependent_launch_is_bit_identical(xrt, graph):
     """Programmatic dependent launch changes only when kernels start, never what they compute:

@@ -94,7 +94,8 @@ class Sizes(C.Structure):
         ("num_obstacle_vertices", C.c_uint32), ("num_obstacle_triangles", C.c_uint32),
         ("num_stretch_colors", C.c_uint32), ("num_bend_colors", C.c_uint32),
         ("launches_per_frame", C.c_uint32), ("frame_index", C.c_uint32),
-        ("particle_diameter", C.c_float), ("reserved", C.c_uint32 * 7),
+        ("particle_diameter", C.c_float), ("num_instances", C.c_uint32),
+        ("num_obstacle_bvh_nodes", C.c_uint32), ("reserved", C.c_uint32 * 5),
     ]
 
 
@@ -120,6 +121,7 @@ SIGNATURES = {
     "xrt_set_params": (C.c_int32, [P, C.POINTER(SwiftParams)]),
     "xrt_add_cloth": (C.c_int32, [P, C.POINTER(ClothDesc), IP]),
     "xrt_add_obstacle": (C.c_int32, [P, C.POINTER(ObstacleDesc), IP]),
+    "xrt_add_instance": (C.c_int32, [P, C.POINTER(ClothDesc), C.POINTER(ObstacleDesc), IP]),
     "xrt_set_coloring": (C.c_int32, [P, C.c_int32, UP, C.c_uint32]),
     "xrt_set_compliance": (C.c_int32, [P, C.c_int32, FP, C.c_uint32]),
     "xrt_set_inv_mass": (C.c_int32, [P, FP, C.c_uint32]),

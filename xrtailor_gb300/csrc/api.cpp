@@ -424,6 +424,8 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   c.edge.release(); c.vf_idx.release(); c.rt_idx.release();
   c.hash_sorter.keys_tmp.release(); c.hash_sorter.vals_tmp.release(); c.hash_sorter.hist.release();
   c.bvh.release();
+  c.inst.release();
+  c.vinst.release();
   for (xrt::TiledSet* t : {&c.s_tiles, &c.b_tiles}) {
     t->foot.release();
     t->meta.release();
@@ -454,13 +456,12 @@ xrt_status xrt_set_params(xrt_ctx* h, const xrt_swift_params* p) {
   return XRT_OK;
 }
 
-xrt_status xrt_add_cloth(xrt_ctx* h, const xrt_cloth_desc* d, int32_t* out_offset) {
-  if (!h || !d || !d->positions || !d->triangles) return XRT_ERR_INVALID_ARGUMENT;
-  Context& c = h->c;
-  if (c.started) {
-    c.set_error("xrt_add_cloth after xrt_start");
-    return XRT_ERR_STATE;
-  }
+}  // extern "C"
+
+// Appends one cloth (validated first; nothing changes on error).  Binding obstacle indices are
+// offset by `bind_base` (the instance's first obstacle vertex in the batched form).
+static xrt_status add_cloth_impl(Context& c, const xrt_cloth_desc* d, uint32_t bind_base,
+                                 uint32_t bind_limit, int32_t* out_offset) {
   if (d->num_vertices == 0 || d->num_triangles == 0) {
     c.set_error("empty cloth mesh");
     return XRT_ERR_INVALID_MESH;
@@ -486,6 +487,8 @@ xrt_status xrt_add_cloth(xrt_ctx* h, const xrt_cloth_desc* d, int32_t* out_offse
   if (why.empty()) why = check_list(d->binded_indices, d->num_binded, "binded");
   if (why.empty() && d->num_binded && (!d->bind_obstacle_tri || !d->bind_barycentric))
     why = "binding needs bind_obstacle_tri and bind_barycentric";
+  for (uint64_t k = 0; why.empty() && k < 3ull * d->num_binded; ++k)
+    if (d->bind_obstacle_tri[k] >= bind_limit) why = "binding refers to a missing obstacle vertex";
   if (!why.empty()) {
     c.set_error(why);
     return XRT_ERR_INVALID_MESH;
@@ -549,9 +552,9 @@ xrt_status xrt_add_cloth(xrt_ctx* h, const xrt_cloth_desc* d, int32_t* out_offse
   for (uint32_t i = 0; i < d->num_binded; ++i) {
     Context::HostBinding b;
     b.cloth = d->binded_indices[i] + cl.offset;
-    b.iu = d->bind_obstacle_tri[3 * i];
-    b.iv = d->bind_obstacle_tri[3 * i + 1];
-    b.iw = d->bind_obstacle_tri[3 * i + 2];
+    b.iu = d->bind_obstacle_tri[3 * i] + bind_base;
+    b.iv = d->bind_obstacle_tri[3 * i + 1] + bind_base;
+    b.iw = d->bind_obstacle_tri[3 * i + 2] + bind_base;
     b.u = d->bind_barycentric[3 * i];
     b.v = d->bind_barycentric[3 * i + 1];
     b.w = d->bind_barycentric[3 * i + 2];
@@ -570,18 +573,16 @@ xrt_status xrt_add_cloth(xrt_ctx* h, const xrt_cloth_desc* d, int32_t* out_offse
   return XRT_OK;
 }
 
-xrt_status xrt_add_obstacle(xrt_ctx* h, const xrt_obstacle_desc* d, int32_t* out_offset) {
-  if (!h || !d || !d->positions || !d->triangles) return XRT_ERR_INVALID_ARGUMENT;
-  Context& c = h->c;
-  if (c.started) {
-    c.set_error("xrt_add_obstacle after xrt_start");
-    return XRT_ERR_STATE;
-  }
+static xrt_status check_obstacle(Context& c, const xrt_obstacle_desc* d) {
   for (uint64_t k = 0; k < 3ull * d->num_triangles; ++k)
     if (d->triangles[k] >= d->num_vertices) {
       c.set_error("obstacle triangle index out of range");
       return XRT_ERR_INVALID_MESH;
     }
+  return XRT_OK;
+}
+
+static void add_obstacle_impl(Context& c, const xrt_obstacle_desc* d, int32_t* out_offset) {
   const uint32_t off = (uint32_t)(c.h_ox0.size() / 3);
   for (uint32_t i = 0; i < d->num_vertices; ++i) {
     xrt::setup::V3 q{d->positions[3 * i], d->positions[3 * i + 1], d->positions[3 * i + 2]};
@@ -595,6 +596,74 @@ xrt_status xrt_add_obstacle(xrt_ctx* h, const xrt_obstacle_desc* d, int32_t* out
   }
   for (uint64_t k = 0; k < 3ull * d->num_triangles; ++k) c.h_otri.push_back(d->triangles[k] + off);
   if (out_offset) *out_offset = (int32_t)off;
+}
+
+extern "C" {
+
+xrt_status xrt_add_cloth(xrt_ctx* h, const xrt_cloth_desc* d, int32_t* out_offset) {
+  if (!h || !d || !d->positions || !d->triangles) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (c.started) {
+    c.set_error("xrt_add_cloth after xrt_start");
+    return XRT_ERR_STATE;
+  }
+  if (c.instanced) {
+    c.set_error("xrt_add_cloth in a batched context (use xrt_add_instance)");
+    return XRT_ERR_STATE;
+  }
+  // bindings may name obstacle vertices added later; xrt_start checks them
+  return add_cloth_impl(c, d, 0, 0xFFFFFFFFu, out_offset);
+}
+
+xrt_status xrt_add_obstacle(xrt_ctx* h, const xrt_obstacle_desc* d, int32_t* out_offset) {
+  if (!h || !d || !d->positions || !d->triangles) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (c.started) {
+    c.set_error("xrt_add_obstacle after xrt_start");
+    return XRT_ERR_STATE;
+  }
+  if (c.instanced) {
+    c.set_error("xrt_add_obstacle in a batched context (use xrt_add_instance)");
+    return XRT_ERR_STATE;
+  }
+  const xrt_status st = check_obstacle(c, d);
+  if (st != XRT_OK) return st;
+  add_obstacle_impl(c, d, out_offset);
+  return XRT_OK;
+}
+
+xrt_status xrt_add_instance(xrt_ctx* h, const xrt_cloth_desc* cloth,
+                            const xrt_obstacle_desc* obstacle, int32_t* out_instance) {
+  if (!h || !cloth || !cloth->positions || !cloth->triangles) return XRT_ERR_INVALID_ARGUMENT;
+  if (obstacle && (!obstacle->positions || !obstacle->triangles)) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (c.started) {
+    c.set_error("xrt_add_instance after xrt_start");
+    return XRT_ERR_STATE;
+  }
+  if (!c.instanced && (!c.cloths.empty() || !c.h_ox0.empty())) {
+    c.set_error("xrt_add_instance in a context that already has xrt_add_cloth / xrt_add_obstacle");
+    return XRT_ERR_STATE;
+  }
+  if (obstacle) {
+    const xrt_status st = check_obstacle(c, obstacle);
+    if (st != XRT_OK) return st;
+  }
+  Context::HostInstance I{};
+  I.vertex_base = (uint32_t)c.h_w.size();
+  I.overtex_base = (uint32_t)(c.h_ox0.size() / 3);
+  I.oface_base = (uint32_t)(c.h_otri.size() / 3);
+  const xrt_status st =
+      add_cloth_impl(c, cloth, I.overtex_base, obstacle ? obstacle->num_vertices : 0u, nullptr);
+  if (st != XRT_OK) return st;
+  if (obstacle) add_obstacle_impl(c, obstacle, nullptr);
+  I.num_vertices = (uint32_t)c.h_w.size() - I.vertex_base;
+  I.num_overtices = (uint32_t)(c.h_ox0.size() / 3) - I.overtex_base;
+  I.num_ofaces = (uint32_t)(c.h_otri.size() / 3) - I.oface_base;
+  I.diameter = c.particle_diameter;  // this cloth's (add_cloth_impl)
+  c.instanced = true;
+  if (out_instance) *out_instance = (int32_t)c.instances.size();
+  c.instances.push_back(I);
   return XRT_OK;
 }
 
@@ -712,6 +781,42 @@ xrt_status xrt_start(xrt_ctx* h) {
       c.set_error("binding refers to a missing obstacle vertex");
       return XRT_ERR_INVALID_MESH;
     }
+  if (c.instanced && c.params.pbd_repulsion) {
+    c.set_error("pbd_repulsion (Quality-mode self contact) is not available in a batched context");
+    return XRT_ERR_INVALID_ARGUMENT;
+  }
+  // instances: merged mode is one instance holding every cloth and obstacle
+  if (!c.instanced)
+    c.instances.assign(1, Context::HostInstance{0, c.nv, 0, c.onv, 0, c.onf, c.particle_diameter});
+  std::vector<uint32_t> segments;  // first cloth vertex of each instance
+  {
+    c.h_inst.clear();
+    uint32_t tb = 0;
+    for (const auto& I : c.instances) {
+      xrt::InstanceRec r{};
+      r.diameter = I.diameter;
+      r.spacing = I.diameter * c.params.hash_cell_size;  // SpatialHashGPU: diameter x cell size
+      r.spacing2 = r.spacing * r.spacing;
+      r.d2 = I.diameter * I.diameter;
+      r.table_base = tb;
+      r.table_size = 2 * I.num_vertices;                  // table of 2V (SpatialHashGPU.cu:166)
+      tb += r.table_size;
+      r.vertex_base = I.vertex_base;
+      r.num_vertices = I.num_vertices;
+      c.h_inst.push_back(r);
+      segments.push_back(I.vertex_base);
+    }
+    if (c.h_inst.size() > 1) {
+      XRT_CUDA(&c, upload(c.inst, c.h_inst, c.stream));
+      std::vector<uint32_t> vi(c.nv);
+      for (uint32_t s = 0; s < (uint32_t)c.instances.size(); ++s)
+        std::fill(vi.begin() + c.instances[s].vertex_base,
+                  vi.begin() + c.instances[s].vertex_base + c.instances[s].num_vertices, s);
+      XRT_CUDA(&c, upload(c.vinst, vi, c.stream));
+    } else {
+      segments.clear();
+    }
+  }
   // coloring
   for (int kind = 0; kind < 2; ++kind) {
     const std::vector<uint32_t>& idx = kind == 0 ? c.h_edges : c.h_bends;
@@ -730,10 +835,10 @@ xrt_status xrt_start(xrt_ctx* h) {
     } else if (c.tile_vertices > 0 && !idx.empty() &&
                [&] {
                  uint32_t tv = c.tile_vertices;
-                 c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv);
+                 c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv, segments);
                  while (c.tmp_schedule.max_footprint > xrt::kTileMaxFootprint && tv > 32) {
                    tv /= 2;
-                   c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv);
+                   c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv, segments);
                  }
                  return c.tmp_schedule.num_tile_colors > 0 &&
                         c.tmp_schedule.max_footprint <= xrt::kTileMaxFootprint;
@@ -747,8 +852,11 @@ xrt_status xrt_start(xrt_ctx* h) {
       T.num_local = S.num_local;
       T.max_foot = S.max_footprint;
       T.max_cons = 0;
+      T.max_step = 0;
       for (size_t tt = 0; tt + 1 < S.foot_ptr.size(); ++tt)
         T.max_cons = std::max(T.max_cons, S.lc_ptr[(tt + 1) * S.num_local] - S.lc_ptr[tt * S.num_local]);
+      for (size_t k = 0; k + 1 < S.lc_ptr.size(); ++k)
+        T.max_step = std::max(T.max_step, S.lc_ptr[k + 1] - S.lc_ptr[k]);
       T.tile_colors.clear();
       T.tile_color_cons.clear();
       for (uint32_t k = 0; k < S.num_tile_colors; ++k) {
@@ -784,6 +892,8 @@ xrt_status xrt_start(xrt_ctx* h) {
       return XRT_ERR_INVALID_MESH;
     }
     XRT_CUDA(&c, xrt::configure_tile_kernels(std::max<size_t>(smem, 16)));
+    if (c.s_tiles.on) XRT_CUDA(&c, xrt::choose_tile_block(c.s_tiles, false));
+    if (c.b_tiles.on) XRT_CUDA(&c, xrt::choose_tile_block(c.b_tiles, true));
   }
   xrt_status st = upload_constraints(c);
   if (st != XRT_OK) return st;
@@ -931,6 +1041,11 @@ xrt_status xrt_start(xrt_ctx* h) {
     XRT_CUDA(&c, cudaMemcpyAsync(c.on1.p, c.on.p, sizeof(float4) * c.onv, cudaMemcpyDeviceToDevice,
                                  c.stream));
     if (c.onf > 0) {
+      if (c.instanced) {  // one tree per instance (a forest over the instances' triangles)
+        std::vector<uint32_t> counts;
+        for (const auto& I : c.instances) counts.push_back(I.num_ofaces);
+        XRT_CUDA(&c, c.bvh.set_segments(counts, c.stream));
+      }
       XRT_CUDA(&c, c.bvh.reserve(c.onf));
       c.bvh.n = c.onf;
       xrt::launch_prims_obstacle(c, 0.0f);  // ClothSolverUniversal::Start: UpdateData(0) + Construct
@@ -1099,7 +1214,9 @@ xrt_status xrt_get_sizes(const xrt_ctx* h, xrt_sizes* out) {
   out->num_bend_colors = c.n_bcolors;
   out->launches_per_frame = c.launches_per_frame;
   out->frame_index = c.frame_index;
-  out->particle_diameter = c.particle_diameter;
+  out->particle_diameter = c.h_inst.empty() ? c.particle_diameter : c.h_inst[0].diameter;
+  out->num_instances = c.h_inst.empty() ? 1u : (uint32_t)c.h_inst.size();
+  out->num_obstacle_bvh_nodes = c.bvh.active ? c.bvh.nodes : 0u;
   return XRT_OK;
 }
 
@@ -1205,7 +1322,7 @@ xrt_status xrt::export_lbvh(xrt::Lbvh& b, cudaStream_t s, std::string& err, uint
     err = "LBVH not built";
     return XRT_ERR_STATE;
   }
-  const uint32_t nn = 2 * n - 1;
+  const uint32_t nn = b.nodes;  // 2n - 1 for a single tree
   auto fail = [&](cudaError_t e) {
     err = cudaGetErrorString(e);
     return XRT_ERR_CUDA;
@@ -1225,7 +1342,9 @@ xrt_status xrt::export_lbvh(xrt::Lbvh& b, cudaStream_t s, std::string& err, uint
       a[3] = hi[k].x; a[4] = hi[k].y; a[5] = hi[k].z;
     }
   }
-  if (iesc && n > 1 && (e = cudaMemcpy(iesc, b.iesc.p, 4 * (n - 1), cudaMemcpyDeviceToHost))) return fail(e);
+  if (iesc && b.internal > 0 &&
+      (e = cudaMemcpy(iesc, b.iesc.p, 4 * (size_t)b.internal, cudaMemcpyDeviceToHost)))
+    return fail(e);
   if (eesc && (e = cudaMemcpy(eesc, b.eesc.p, 4 * n, cudaMemcpyDeviceToHost))) return fail(e);
   if (unique) {
     uint32_t dup = 0;

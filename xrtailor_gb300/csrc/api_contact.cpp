@@ -88,6 +88,10 @@ xrt_status xrt::prox_prepare(Context& c) {
     c.set_error("call xrt_start first");
     return XRT_ERR_STATE;
   }
+  if (c.instanced) {  // the obstacle LBVH of a batched context is a forest, one tree per instance
+    c.set_error("Quality-mode self contact is available in merged contexts only");
+    return XRT_ERR_STATE;
+  }
   std::vector<int4> face, fedge, eadj;
   std::vector<float4> fn0;
   std::vector<uint2> uedge;

@@ -64,8 +64,7 @@ constexpr float kScalarMax = 3.402823466e+38f;  // SCALAR_MAX = FLT_MAX (core/Sc
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr uint32_t kMaxCandidates = 256;  // LBVH_MAX_BUFFER_SIZE (core/Common.cuh:23)
 constexpr int kBlock = 256;
-constexpr int kTileBlock = 512;     // threads of a tile-local Gauss-Seidel block
-constexpr int kFootPerThread = 8;   // footprint vertices per thread: footprints <= 4096
+constexpr int kFootPerThread = 8;   // footprint vertices per tile-block thread (x 512 <= 4096)
 
 // Bits of the sticky device error word.
 enum : uint32_t {

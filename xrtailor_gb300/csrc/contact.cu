@@ -86,8 +86,10 @@ __global__ void k_obstacle_commit(const float4* __restrict__ x, float4* __restri
 }
 
 // VF-DCD (nearest obstacle point of the predicted vertex) and VF-CCD (first hit of the segment
-// x0 -> x), one thread per cloth vertex.
-__global__ void __launch_bounds__(kBlock) k_generate_vf(LbvhView b, const float4* __restrict__ x,
+// x0 -> x), one thread per cloth vertex, against the tree of the vertex's instance; contacts
+// record global triangle ids.
+__global__ void __launch_bounds__(kBlock) k_generate_vf(LbvhForest F, InstView I,
+                                                        const float4* __restrict__ x,
                                                         const float4* __restrict__ x0, uint32_t nv,
                                                         int* __restrict__ vf_idx,
                                                         float4* __restrict__ vf_qs,
@@ -95,6 +97,9 @@ __global__ void __launch_bounds__(kBlock) k_generate_vf(LbvhView b, const float4
                                                         float4* __restrict__ rt_qc, uint32_t* err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nv) return;
+  const uint32_t s = inst_index(I, i);
+  const LbvhView b = forest_view(F, s);
+  const int base = forest_rec(F, s).x;
   const f3 pred = mk3(x[i]);
   {
     float hit = kScalarMax;
@@ -109,7 +114,7 @@ __global__ void __launch_bounds__(kBlock) k_generate_vf(LbvhView b, const float4
           if (dist < hit) {
             hit = dist;
             hit_qs = qs;
-            hit_idx = (int)f;
+            hit_idx = base + (int)f;
           }
         },
         err);
@@ -133,7 +138,7 @@ __global__ void __launch_bounds__(kBlock) k_generate_vf(LbvhView b, const float4
             if (dist < hit) {
               qc = p1 + dist * d;
               hit = dist;
-              hit_idx = (int)f;
+              hit_idx = base + (int)f;
             }
           },
           err);
@@ -144,15 +149,19 @@ __global__ void __launch_bounds__(kBlock) k_generate_vf(LbvhView b, const float4
 }
 
 // EE-DCD: closest R-triangle-owned obstacle edge to each cloth edge.
-__global__ void __launch_bounds__(kBlock) k_generate_ee(LbvhView b, const float4* __restrict__ x,
+__global__ void __launch_bounds__(kBlock) k_generate_ee(LbvhForest F, InstView I,
+                                                        const float4* __restrict__ x,
                                                         const uint2* __restrict__ edge, uint32_t ne,
-                                                        const int4* __restrict__ otri,
+                                                        const int4* __restrict__ otri_all,
                                                         float4* __restrict__ ee_a,
                                                         float4* __restrict__ ee_b,
                                                         float4* __restrict__ ee_c, uint32_t* err) {
   const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   const uint2 ed = edge[e];
+  const uint32_t sg = inst_index(I, ed.x);
+  const LbvhView b = forest_view(F, sg);
+  const int4* __restrict__ otri = otri_all + forest_rec(F, sg).x;
   const f3 pc = mk3(x[ed.x]), qc = mk3(x[ed.y]);
   float s = 0, t = 0;
   f3 p2 = mk3(0, 0, 0), q2 = mk3(0, 0, 0), fn = mk3(0, 0, 0);
@@ -201,12 +210,13 @@ void launch_obstacle_pass(Context& c, int step, int num_steps) {
 
 void launch_generate_contacts(Context& c) {
   if (!c.bvh.active) return;
-  k_generate_vf<<<grid_for(c.nv), kBlock, 0, c.stream>>>(c.bvh.view(), c.x.p, c.x0.p, c.nv,
-                                                         c.vf_idx.p, c.vf_qs.p, c.rt_idx.p,
-                                                         c.rt_qc.p, c.err.p);
-  k_generate_ee<<<grid_for(c.ne), kBlock, 0, c.stream>>>(c.bvh.view(), c.x.p, c.edge.p, c.ne,
-                                                         c.otri.p, c.ee_a.p, c.ee_b.p, c.ee_c.p,
+  const LbvhForest F = c.bvh.forest();
+  const InstView I = c.inst_view();
+  k_generate_vf<<<grid_for(c.nv), kBlock, 0, c.stream>>>(F, I, c.x.p, c.x0.p, c.nv, c.vf_idx.p,
+                                                         c.vf_qs.p, c.rt_idx.p, c.rt_qc.p,
                                                          c.err.p);
+  k_generate_ee<<<grid_for(c.ne), kBlock, 0, c.stream>>>(F, I, c.x.p, c.edge.p, c.ne, c.otri.p,
+                                                         c.ee_a.p, c.ee_b.p, c.ee_c.p, c.err.p);
 }
 
 void launch_obstacle_commit(Context& c) {

@@ -49,6 +49,8 @@ struct RadixSort {
 };
 
 // ---- LBVH (lbvh.cu) ---------------------------------------------------------------------------
+// One tree (a segment of a forest, see LbvhForest): node ids, child / escape links and objects
+// are local to the tree, `pred` points at the tree's first primitive.
 struct LbvhView {
   uint32_t n;          // primitives
   const float4* pred;  // 3 per primitive (pred1..3), original order
@@ -56,29 +58,54 @@ struct LbvhView {
   const float4* hi;    // 2n-1 nodes; xyz = upper, w = escape index (-1 = end)
 };
 
+// A forest of independent trees over consecutive primitive ranges (segments), in shared arrays.
+// Segment s owns primitives [prim_base, prim_base + n), nodes [node_base, node_base + 2n - 1)
+// (internal nodes first, then leaves, as in a single tree) and merge counters
+// [internal_base, internal_base + n - 1).  Every link is local to its segment, so each segment is
+// bit for bit the tree its primitives alone would give.  One segment = the classic single tree.
+struct LbvhForest {
+  LbvhView all;       // n = total primitives; lo / hi over all nodes
+  const int4* seg;    // per segment {prim_base, n, node_base, internal_base}; unused if nseg == 1
+  uint32_t nseg;
+  int4 one;           // the record when nseg == 1
+};
+
 struct Lbvh {
-  uint32_t n = 0;
+  uint32_t n = 0;                  // total primitives
+  uint32_t nodes = 0;              // total nodes (sum of 2 n_s - 1 over non-empty segments)
+  uint32_t internal = 0;           // total internal nodes
   bool active = false;
   DBuf<float4> v, pred;            // 3 per primitive
   DBuf<float4> leaf_lo, leaf_hi;   // per primitive (original order) before sorting
   DBuf<float4> lo, hi;             // per node
-  DBuf<int4> node;                 // parent, left, right, object
+  DBuf<int4> node;                 // parent, left, right, object (segment-local)
   DBuf<uint32_t> morton, index;    // sort inputs
+  DBuf<uint32_t> skey, sval;       // segment pass of the sort (nseg > 1)
   DBuf<unsigned long long> key64;
   DBuf<uint32_t> flags;            // arrival counters of the bottom-up merge (parity)
   DBuf<int32_t> iesc, eesc;
-  DBuf<float> root;                // 6 floats
+  DBuf<float> root;                // 6 floats per segment (ordered-int encoded)
   DBuf<uint32_t> dup;              // number of equal adjacent Morton codes
   uint32_t* sorted_morton = nullptr;
   uint32_t* sorted_index = nullptr;
   RadixSort sorter;
+  std::vector<int4> h_seg;         // segment records (host); empty = one segment of n
+  DBuf<int4> seg;
 
+  // Segments of the forest: primitive counts in primitive order (empty = one segment).
+  // Uploads the table; call before reserve.
+  cudaError_t set_segments(const std::vector<uint32_t>& counts, cudaStream_t s);
   cudaError_t reserve(uint32_t n_prims);
-  // BVH::Construct(scr) on v / pred already in device memory (BVH.cu:618-722).
+  // BVH::Construct(scr) on v / pred already in device memory (BVH.cu:618-722), every segment.
   void construct(float scr, cudaStream_t s, uint32_t* d_err);
   // Leaves grow by pred (already updated), internal boxes recomputed bottom-up.
   void refit_from_pred(cudaStream_t s, uint32_t* d_err);
-  LbvhView view() const { return LbvhView{n, pred.p, lo.p, hi.p}; }
+  uint32_t nseg() const { return h_seg.empty() ? 1u : (uint32_t)h_seg.size(); }
+  int4 seg_one() const { return make_int4(0, (int)n, 0, 0); }
+  LbvhView view() const { return LbvhView{n, pred.p, lo.p, hi.p}; }  // single-segment trees
+  LbvhForest forest() const {
+    return LbvhForest{view(), seg.p, nseg(), h_seg.empty() ? seg_one() : h_seg[0]};
+  }
   void release();
 };
 
@@ -93,6 +120,22 @@ void launch_lbvh_query(const Lbvh& b, int kind, const float* d_q, uint32_t nq, u
                        uint32_t* d_cands, cudaStream_t s, uint32_t* d_err);
 void launch_float9_to_float4(const float* d_in, float4* d_out, uint32_t n_prims, cudaStream_t s);
 
+// ---- instances (batched form) -------------------------------------------------------------------
+// Per-instance constants.  In merged mode (the reference's one mesh of every cloth) there is one
+// instance; in the batched form instance i is cloth i with its own obstacle (segment i of the
+// obstacle LBVH forest), its own particle diameter and its own slice of the particle hash table.
+struct InstanceRec {
+  float spacing, spacing2, d2, diameter;  // hash cell size, its square, diameter^2, diameter
+  uint32_t table_base, table_size;        // hash keys of the instance: [base, base + size)
+  uint32_t vertex_base, num_vertices;     // cloth vertices
+};
+struct InstView {
+  uint32_t count;
+  const InstanceRec* rec;      // count records (unused when count == 1)
+  const uint32_t* of_vertex;   // cloth vertex -> instance (unused when count == 1)
+  InstanceRec one;             // the record when count == 1
+};
+
 // ---- cloth state --------------------------------------------------------------------------------
 struct ColorRange {
   uint32_t begin, end;
@@ -100,7 +143,7 @@ struct ColorRange {
 
 // Tile-local Gauss-Seidel schedule of one constraint kind on the device (setup::TileSchedule):
 // one launch per tile color, one block per tile, local colors in shared memory.
-// Largest tile footprint the tile kernels stage (kTileBlock x kFootPerThread in solver.cu).
+// Largest tile footprint the tile kernels stage (512 threads x kFootPerThread in solver.cu).
 constexpr uint32_t kTileMaxFootprint = 4096;
 
 struct TiledSet {
@@ -108,6 +151,9 @@ struct TiledSet {
   uint32_t num_local = 0;
   uint32_t max_foot = 0;
   uint32_t max_cons = 0;                // most constraints in one tile
+  uint32_t max_step = 0;                // most constraints in one local color of one tile
+  uint32_t block = 512;                 // threads per tile block (256 or 512)
+  uint32_t resident = 0;                // tile blocks the GPU holds at once (pair-mode bound)
   std::vector<ColorRange> tile_colors;  // ranges of executed tiles per tile color
   std::vector<uint32_t> tile_color_cons;  // constraints per tile color (profiling units)
   DBuf<uint32_t> foot;                  // footprint vertices of every executed tile
@@ -151,6 +197,22 @@ struct Context {
   bool targets_pending = false;
   uint32_t tile_vertices = 256;  // 0: plain per-color launches of a greedy coloring
   bool pdl = true;               // programmatic dependent launch of the substep kernels
+  // batched form: instance i = cloth i + obstacle i (xrt_add_instance)
+  bool instanced = false;
+  struct HostInstance {
+    uint32_t vertex_base, num_vertices;      // cloth
+    uint32_t overtex_base, num_overtices;    // obstacle
+    uint32_t oface_base, num_ofaces;
+    float diameter;
+  };
+  std::vector<HostInstance> instances;
+  std::vector<InstanceRec> h_inst;
+  DBuf<InstanceRec> inst;
+  DBuf<uint32_t> vinst;          // cloth vertex -> instance (batched form only)
+  InstView inst_view() const {
+    return InstView{(uint32_t)h_inst.size(), inst.p, vinst.p,
+                    h_inst.empty() ? InstanceRec{} : h_inst[0]};
+  }
 
   // host copies (setup)
   struct HostCloth {
@@ -260,6 +322,8 @@ void launch_stretch(Context& c, const FrameConst& k, ColorRange r, bool reset_la
 void launch_bend(Context& c, const FrameConst& k, ColorRange r);
 cudaError_t configure_tile_kernels(size_t max_smem_bytes);
 size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes);
+// Sets T.block (256 / 512 threads) and T.resident; after configure_tile_kernels.
+cudaError_t choose_tile_block(TiledSet& T, bool bend);
 // tile-local Gauss-Seidel: all tiles of one tile color (range of executed tiles)
 void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, bool reset_lambda);
 void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles);

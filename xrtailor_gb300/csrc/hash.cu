@@ -12,6 +12,7 @@
 // caller swaps them), which is the reference's deltas + ApplyDeltas pair in one launch.
 #include "common.cuh"
 #include "context.h"
+#include "lbvh_dev.cuh"
 
 namespace xrt {
 namespace {
@@ -25,13 +26,16 @@ __device__ __forceinline__ int hash_coords(int x, int y, int z, int table) {
   return abs(h % table);
 }
 
-__global__ void k_hash(const float4* __restrict__ x, uint32_t nv, float spacing, int table,
+// Keys of instance s lie in [table_base, table_base + table_size): each instance hashes into its
+// own table of 2 V_s cells (the reference's 2V for that cloth alone), laid end to end.
+__global__ void k_hash(const float4* __restrict__ x, uint32_t nv, InstView I,
                        uint32_t* __restrict__ key, uint32_t* __restrict__ val) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nv) return;
+  const InstanceRec r = inst_rec(I, inst_index(I, i));
   const float4 p = x[i];
-  key[i] = (uint32_t)hash_coords(int_coord(p.x, spacing), int_coord(p.y, spacing),
-                                 int_coord(p.z, spacing), table);
+  key[i] = r.table_base + (uint32_t)hash_coords(int_coord(p.x, r.spacing), int_coord(p.y, r.spacing),
+                                                int_coord(p.z, r.spacing), (int)r.table_size);
   val[i] = i;
 }
 
@@ -51,11 +55,14 @@ __global__ void k_cache_neighbors(const uint32_t* __restrict__ sidx,
                                   const uint32_t* __restrict__ cell_start,
                                   const uint32_t* __restrict__ cell_end,
                                   const float4* __restrict__ x, const float4* __restrict__ x_init,
-                                  uint32_t nv, float spacing, float spacing2, float d2, int table,
-                                  uint32_t maxnb, uint32_t* __restrict__ neighbors) {
+                                  uint32_t nv, InstView I, uint32_t maxnb,
+                                  uint32_t* __restrict__ neighbors) {
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= nv) return;
   const uint32_t id = sidx[tid];
+  const InstanceRec r = inst_rec(I, inst_index(I, id));
+  const float spacing = r.spacing, spacing2 = r.spacing2, d2 = r.d2;
+  const int table = (int)r.table_size;
   const f3 pos = mk3(x[id]);
   const f3 orig = mk3(x_init[id]);
   const int ix = int_coord(pos.x, spacing), iy = int_coord(pos.y, spacing),
@@ -65,7 +72,7 @@ __global__ void k_cache_neighbors(const uint32_t* __restrict__ sidx,
   for (int xx = ix - 1; xx <= ix + 1; ++xx)
     for (int yy = iy - 1; yy <= iy + 1; ++yy)
       for (int zz = iz - 1; zz <= iz + 1; ++zz) {
-        const int h = hash_coords(xx, yy, zz, table);
+        const uint32_t h = r.table_base + (uint32_t)hash_coords(xx, yy, zz, table);
         const uint32_t start = cell_start[h];
         if (start == kNone) continue;
         const uint32_t end = min(cell_end[h], start + maxnb);
@@ -98,11 +105,12 @@ __device__ __forceinline__ f3 friction_of(float mu, f3 correction, f3 rel_vel) {
 
 __global__ void k_collide(const float4* __restrict__ x_in, float4* __restrict__ x_out,
                           const float4* __restrict__ x0, const uint32_t* __restrict__ neighbors,
-                          uint32_t nv, uint32_t maxnb, float diameter, float mu, float relaxation) {
+                          uint32_t nv, uint32_t maxnb, InstView I, float mu, float relaxation) {
   pdl_release();
   pdl_wait();
   const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= nv) return;
+  const float diameter = inst_rec(I, inst_index(I, id)).diameter;
   const float4 pi = x_in[id];
   const f3 pred_i = mk3(pi);
   const f3 vel_i = pred_i - mk3(x0[id]);
@@ -156,27 +164,24 @@ __global__ void k_collide(const float4* __restrict__ x_in, float4* __restrict__ 
 void launch_hash(Context& c) {
   const uint32_t nv = c.nv;
   if (nv == 0) return;
-  const float spacing = c.particle_diameter * c.params.hash_cell_size;
-  const float spacing2 = spacing * spacing;
-  const float d2 = c.particle_diameter * c.particle_diameter;
-  const int table = (int)(2 * nv);
+  const uint32_t table = 2 * nv;  // the instances' tables end to end
   int bits = 0;
-  while ((1u << bits) < (uint32_t)table) ++bits;
-  k_hash<<<grid_for(nv), kBlock, 0, c.stream>>>(c.x.p, nv, spacing, table, c.hash_key.p,
-                                                c.hash_val.p);
+  while ((1u << bits) < table) ++bits;
+  const InstView I = c.inst_view();
+  k_hash<<<grid_for(nv), kBlock, 0, c.stream>>>(c.x.p, nv, I, c.hash_key.p, c.hash_val.p);
   uint32_t *skey = nullptr, *sidx = nullptr;
   c.hash_sorter.sort(c.hash_key.p, c.hash_val.p, nv, bits, c.stream, &skey, &sidx);
   cudaMemsetAsync(c.cell_start.p, 0xFF, sizeof(uint32_t) * table, c.stream);
   k_cell_bounds<<<grid_for(nv), kBlock, 0, c.stream>>>(skey, nv, c.cell_start.p, c.cell_end.p);
   k_cache_neighbors<<<grid_for(nv), kBlock, 0, c.stream>>>(
-      sidx, c.cell_start.p, c.cell_end.p, c.x.p, c.x_init.p, nv, spacing, spacing2, d2, table,
+      sidx, c.cell_start.p, c.cell_end.p, c.x.p, c.x_init.p, nv, I,
       (uint32_t)c.params.max_neighbor_size, c.neighbors.p);
 }
 
 void launch_collide(Context& c, const FrameConst& k) {
   launch_k(c.pdl, k_collide, grid_for(c.nv), kBlock, 0, c.stream, c.x.p, c.x_alt.p, c.x0.p,
-           c.neighbors.p, c.nv, (uint32_t)c.params.max_neighbor_size, k.particle_diameter,
-           k.friction, k.relaxation);
+           c.neighbors.p, c.nv, (uint32_t)c.params.max_neighbor_size, c.inst_view(), k.friction,
+           k.relaxation);
 }
 
 }  // namespace xrt

@@ -45,18 +45,24 @@ __device__ __forceinline__ float o2f(uint32_t u) {
   return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
 }
 
-__global__ void k_root_init(uint32_t* root, uint32_t* dup) {
-  if (threadIdx.x < 3) root[threadIdx.x] = f2o(__int_as_float(0x7f800000));          // +inf
-  else if (threadIdx.x < 6) root[threadIdx.x] = f2o(__int_as_float((int)0xff800000));  // -inf
-  if (threadIdx.x == 0) *dup = 0;
+// Root boxes of every segment: 6 ordered-int extrema each.
+__global__ void k_root_init(uint32_t* root, uint32_t nseg, uint32_t* dup) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 6 * nseg) {
+    const uint32_t k = t % 6;
+    root[t] = k < 3 ? f2o(__int_as_float(0x7f800000)) : f2o(__int_as_float((int)0xff800000));
+  }
+  if (t == 0) *dup = 0;
 }
 
-// InitAABBs_Kernel + the root reduction (thrust::reduce of Bounds::Merge).
+// InitAABBs_Kernel + the root reduction (thrust::reduce of Bounds::Merge), per segment.  Min /
+// max are exact, so the reduction order does not matter: warps whose lanes share one segment
+// reduce by shuffles, a warp that straddles a segment boundary commits lane by lane.
 __global__ void __launch_bounds__(kBlock) k_leaf_boxes(const float4* __restrict__ v,
                                                        const float4* __restrict__ pred, uint32_t n,
                                                        float scr, float4* __restrict__ leaf_lo,
                                                        float4* __restrict__ leaf_hi,
-                                                       uint32_t* __restrict__ root) {
+                                                       uint32_t* __restrict__ root, LbvhForest F) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   float lo[3] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000)};
   float hi[3] = {-lo[0], -lo[1], -lo[2]};
@@ -79,37 +85,39 @@ __global__ void __launch_bounds__(kBlock) k_leaf_boxes(const float4* __restrict_
     lo[0] = bl.x; lo[1] = bl.y; lo[2] = bl.z;
     hi[0] = bu.x; hi[1] = bu.y; hi[2] = bu.z;
   }
-  // block reduction of the six extrema (min / max are exact, so order does not matter)
-  __shared__ float s[6][kBlock / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t seg = i < n ? forest_find(F, i, 0) : 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  if (__match_any_sync(0xFFFFFFFFu, seg) == 0xFFFFFFFFu) {
+    if (seg == 0xFFFFFFFFu) return;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float a = lo[k], b = hi[k];
+      for (int off = 16; off > 0; off >>= 1) {
+        a = fminf(a, __shfl_xor_sync(0xFFFFFFFFu, a, off));
+        b = fmaxf(b, __shfl_xor_sync(0xFFFFFFFFu, b, off));
+      }
+      lo[k] = a;
+      hi[k] = b;
+    }
+    if (lane != 0) return;
+  } else if (seg == 0xFFFFFFFFu) {
+    return;
+  }
+  uint32_t* r = root + 6 * (size_t)seg;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    float a = lo[k], b = hi[k];
-    for (int off = 16; off > 0; off >>= 1) {
-      a = fminf(a, __shfl_xor_sync(0xFFFFFFFFu, a, off));
-      b = fmaxf(b, __shfl_xor_sync(0xFFFFFFFFu, b, off));
-    }
-    if (lane == 0) {
-      s[k][warp] = a;
-      s[3 + k][warp] = b;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < 6) {
-    const int k = threadIdx.x;
-    float r = s[k][0];
-    for (int w = 1; w < kBlock / 32; ++w) r = k < 3 ? fminf(r, s[k][w]) : fmaxf(r, s[k][w]);
-    if (k < 3) atomicMin(&root[k], f2o(r));
-    else atomicMax(&root[k], f2o(r));
+    atomicMin(&r[k], f2o(lo[k]));
+    atomicMax(&r[3 + k], f2o(hi[k]));
   }
 }
 
-// ComputeMortons_Kernel: centre of the leaf box normalised by the root box.
+// ComputeMortons_Kernel: centre of the leaf box normalised by its segment's root box.
 __global__ void k_morton(const float4* __restrict__ leaf_lo, const float4* __restrict__ leaf_hi,
-                         const uint32_t* __restrict__ root, uint32_t n, uint32_t* __restrict__ morton,
-                         uint32_t* __restrict__ index) {
+                         const uint32_t* __restrict__ root_all, uint32_t n,
+                         uint32_t* __restrict__ morton, uint32_t* __restrict__ index, LbvhForest F) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const uint32_t* root = root_all + 6 * (size_t)forest_find(F, i, 0);
   const f3 wl = mk3(o2f(root[0]), o2f(root[1]), o2f(root[2]));
   const f3 wu = mk3(o2f(root[3]), o2f(root[4]), o2f(root[5]));
   f3 p = 0.5f * (mk3(leaf_lo[i]) + mk3(leaf_hi[i]));
@@ -123,34 +131,64 @@ __global__ void k_morton(const float4* __restrict__ leaf_lo, const float4* __res
   index[i] = i;
 }
 
+// Segment pass of the sort: after the Morton pass, a stable sort by segment groups each
+// segment's primitives in (code, index) order, the order the segment alone would have.
+__global__ void k_seg_keys(const uint32_t* __restrict__ sindex, uint32_t n, uint32_t* __restrict__ key,
+                           uint32_t* __restrict__ val, LbvhForest F) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  key[i] = forest_find(F, sindex[i], 0);
+  val[i] = i;
+}
+__global__ void k_seg_gather(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ m_in,
+                             const uint32_t* __restrict__ i_in, uint32_t n,
+                             uint32_t* __restrict__ m_out, uint32_t* __restrict__ i_out) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t q = perm[p];
+  m_out[p] = m_in[q];
+  i_out[p] = i_in[q];
+}
+
 // ConstructLeafNodes_Kernel + leaf boxes in sorted order + 64-bit keys + uniqueness count.
+// Objects and keys use segment-local primitive ids.
 __global__ void k_leaves(const uint32_t* __restrict__ smorton, const uint32_t* __restrict__ sindex,
                          const float4* __restrict__ leaf_lo, const float4* __restrict__ leaf_hi,
                          uint32_t n, float4* __restrict__ lo, float4* __restrict__ hi,
                          int4* __restrict__ node, unsigned long long* __restrict__ key64,
-                         uint32_t* __restrict__ dup) {
+                         uint32_t* __restrict__ dup, LbvhForest F) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const uint32_t obj = sindex[i];
-  const uint32_t k = n - 1 + i;
-  const float4 a = leaf_lo[obj], b = leaf_hi[obj];
+  const int4 r = forest_rec(F, forest_find(F, i, 0));
+  const uint32_t li = i - (uint32_t)r.x;
+  const uint32_t gobj = sindex[i];
+  const uint32_t obj = gobj - (uint32_t)r.x;
+  const uint32_t k = (uint32_t)r.z + (uint32_t)r.y - 1 + li;
+  const float4 a = leaf_lo[gobj], b = leaf_hi[gobj];
   lo[k] = make_float4(a.x, a.y, a.z, __int_as_float((int)obj));
   hi[k] = make_float4(b.x, b.y, b.z, __int_as_float(-1));
   node[k] = make_int4(-1, -1, -1, (int)obj);
   const uint32_t m = smorton[i];
   key64[i] = ((unsigned long long)m << 32) | obj;
-  if (i > 0 && smorton[i - 1] == m) atomicAdd(dup, 1u);
+  if (li > 0 && smorton[i - 1] == m) atomicAdd(dup, 1u);
 }
 
 __device__ __forceinline__ int cub64(unsigned long long a, unsigned long long b) {
   return __clzll((long long)(a ^ b));
 }
 
-// ConstructInternalNodes64Bits_Kernel with determine_range / find_split.
-__global__ void k_internal(const unsigned long long* __restrict__ code, uint32_t n,
-                           float4* __restrict__ lo, int4* __restrict__ node) {
-  const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx + 1 >= n) return;
+// ConstructInternalNodes64Bits_Kernel with determine_range / find_split, one thread per internal
+// node of the forest, on its segment's keys with local ids.
+__global__ void k_internal(const unsigned long long* __restrict__ code_all, uint32_t n_internal,
+                           float4* __restrict__ lo_all, int4* __restrict__ node_all, LbvhForest F) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_internal) return;
+  const int4 r = forest_rec(F, forest_find(F, g, 3));
+  const uint32_t idx = g - (uint32_t)r.w;
+  const uint32_t n = (uint32_t)r.y;
+  const unsigned long long* __restrict__ code = code_all + r.x;
+  float4* __restrict__ lo = lo_all + r.z;
+  int4* __restrict__ node = node_all + r.z;
   uint32_t first, last;
   if (idx == 0) {
     first = 0;
@@ -211,24 +249,35 @@ __global__ void k_internal(const unsigned long long* __restrict__ code, uint32_t
   lo[idx].w = __int_as_float((int)left);
 }
 
-__device__ __forceinline__ void merge_upwards(uint32_t leaf_node, uint32_t n, float4* lo, float4* hi,
-                                              const int4* node, uint32_t* flags, uint32_t* err) {
-  lbvh_merge_upwards(leaf_node, n, lo, hi, node, flags, err);
+// Bottom-up merge from the leaf at sorted position i (forest-wide), within its segment.
+__device__ __forceinline__ void merge_from_leaf(const LbvhForest& F, uint32_t i, float4* lo,
+                                                float4* hi, const int4* node, uint32_t* flags,
+                                                uint32_t* err) {
+  const int4 r = forest_rec(F, forest_find(F, i, 0));
+  const uint32_t n = (uint32_t)r.y;
+  if (n < 2) return;
+  lbvh_merge_upwards(n - 1 + (i - (uint32_t)r.x), n, lo + r.z, hi + r.z, node + r.z, flags + r.w,
+                     err);
 }
 
 __global__ void k_build_internal_boxes(uint32_t n, float4* lo, float4* hi, const int4* node,
-                                       uint32_t* flags, uint32_t* err) {
+                                       uint32_t* flags, uint32_t* err, LbvhForest F) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  merge_upwards(n - 1 + i, n, lo, hi, node, flags, err);
+  merge_from_leaf(F, i, lo, hi, node, flags, err);
 }
 
-// BuildInternal/ExternalEscapeIndexTable_Kernel, stored in hi.w and in the export tables.
-__global__ void k_escape(uint32_t n, const int4* __restrict__ node, float4* __restrict__ hi,
-                         int32_t* __restrict__ iesc, int32_t* __restrict__ eesc, uint32_t* err) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t nn = 2 * n - 1;
-  if (k >= nn) return;
+// BuildInternal/ExternalEscapeIndexTable_Kernel, stored in hi.w and in the export tables (internal
+// nodes at internal_base, leaves at prim_base of their segment), one thread per forest node.
+__global__ void k_escape(uint32_t n_nodes, const int4* __restrict__ node_all,
+                         float4* __restrict__ hi_all, int32_t* __restrict__ iesc,
+                         int32_t* __restrict__ eesc, uint32_t* err, LbvhForest F) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_nodes) return;
+  const int4 r = forest_rec(F, forest_find(F, g, 2));
+  const uint32_t n = (uint32_t)r.y;
+  const uint32_t k = g - (uint32_t)r.z;
+  const int4* __restrict__ node = node_all + r.z;
   const int parent = node[k].x;
   int esc = -1;
   if (parent >= 0) {
@@ -256,9 +305,9 @@ __global__ void k_escape(uint32_t n, const int4* __restrict__ node, float4* __re
       }
     }
   }
-  hi[k].w = __int_as_float(esc);
-  if (k + 1 < n) iesc[k] = esc;
-  else eesc[k - (n - 1)] = esc;
+  hi_all[g].w = __int_as_float(esc);
+  if (k + 1 < n) iesc[r.w + k] = esc;
+  else eesc[r.x + k - (n - 1)] = esc;
 }
 
 __global__ void k_prims_mesh(const float4* __restrict__ x, const float4* __restrict__ nrm,
@@ -276,16 +325,25 @@ __global__ void k_prims_mesh(const float4* __restrict__ x, const float4* __restr
   }
 }
 
+// Forest node of the leaf at sorted position i, and its global primitive (from the leaf's
+// local object).
+__device__ __forceinline__ uint32_t leaf_node_of(const LbvhForest& F, uint32_t i, uint32_t& base) {
+  const int4 r = forest_rec(F, forest_find(F, i, 0));
+  base = (uint32_t)r.x;
+  return (uint32_t)r.z + (uint32_t)r.y - 1 + (i - (uint32_t)r.x);
+}
+
 // RefitExternalNodeMidstep_Kernel + AssignAABBCAS_Kernel, fused.
 __global__ void k_refit_midstep(uint32_t n, const float4* __restrict__ x1,
                                 const float4* __restrict__ n1, const int4* __restrict__ tri,
                                 float tol, float4* pred, float4* lo, float4* hi, const int4* node,
-                                uint32_t* flags, uint32_t* err) {
+                                uint32_t* flags, uint32_t* err, LbvhForest F) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const uint32_t k = n - 1 + i;
+  uint32_t base;
+  const uint32_t k = leaf_node_of(F, i, base);
   float4 l = lo[k], h = hi[k];
-  const uint32_t obj = (uint32_t)__float_as_int(l.w);
+  const uint32_t obj = base + (uint32_t)__float_as_int(l.w);
   const int4 t = tri[obj];
   const int id[3] = {t.x, t.y, t.z};
 #pragma unroll
@@ -297,17 +355,18 @@ __global__ void k_refit_midstep(uint32_t n, const float4* __restrict__ x1,
   }
   __stcg(&lo[k], l);
   __stcg(&hi[k], h);
-  merge_upwards(k, n, lo, hi, node, flags, err);
+  merge_from_leaf(F, i, lo, hi, node, flags, err);
 }
 
 // RefitExternalNode_Kernel(predicted) with per-primitive pred already in place.
 __global__ void k_refit_pred(uint32_t n, const float4* __restrict__ pred, float4* lo, float4* hi,
-                             const int4* node, uint32_t* flags, uint32_t* err) {
+                             const int4* node, uint32_t* flags, uint32_t* err, LbvhForest F) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const uint32_t k = n - 1 + i;
+  uint32_t base;
+  const uint32_t k = leaf_node_of(F, i, base);
   float4 l = lo[k], h = hi[k];
-  const uint32_t obj = (uint32_t)__float_as_int(l.w);
+  const uint32_t obj = base + (uint32_t)__float_as_int(l.w);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const f3 q = mk3(pred[3 * obj + c]);
@@ -316,7 +375,7 @@ __global__ void k_refit_pred(uint32_t n, const float4* __restrict__ pred, float4
   }
   __stcg(&lo[k], l);
   __stcg(&hi[k], h);
-  merge_upwards(k, n, lo, hi, node, flags, err);
+  merge_from_leaf(F, i, lo, hi, node, flags, err);
 }
 
 }  // namespace
@@ -357,9 +416,29 @@ __global__ void k_float9_to_float4(const float* __restrict__ in, float4* __restr
 
 }  // namespace
 
+cudaError_t Lbvh::set_segments(const std::vector<uint32_t>& counts, cudaStream_t s) {
+  h_seg.clear();
+  if (counts.size() <= 1) return cudaSuccess;
+  uint32_t pb = 0, nb = 0, ib = 0;
+  for (uint32_t c : counts) {
+    h_seg.push_back(make_int4((int)pb, (int)c, (int)nb, (int)ib));
+    pb += c;
+    nb += c ? 2 * c - 1 : 0;
+    ib += c ? c - 1 : 0;
+  }
+  cudaError_t e = seg.reserve(h_seg.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(seg.p, h_seg.data(), sizeof(int4) * h_seg.size(), cudaMemcpyHostToDevice, s);
+  return e;
+}
+
 cudaError_t Lbvh::reserve(uint32_t np) {
   const size_t nn = np ? 2 * (size_t)np - 1 : 1;
   cudaError_t e = cudaSuccess;
+  if (nseg() > 1) {
+    if (e == cudaSuccess) e = skey.reserve(np);
+    if (e == cudaSuccess) e = sval.reserve(np);
+  }
   if (e == cudaSuccess) e = v.reserve(3 * (size_t)np);
   if (e == cudaSuccess) e = pred.reserve(3 * (size_t)np);
   if (e == cudaSuccess) e = leaf_lo.reserve(np);
@@ -373,7 +452,7 @@ cudaError_t Lbvh::reserve(uint32_t np) {
   if (e == cudaSuccess) e = flags.reserve(np);
   if (e == cudaSuccess) e = iesc.reserve(np);
   if (e == cudaSuccess) e = eesc.reserve(np);
-  if (e == cudaSuccess) e = root.reserve(6);
+  if (e == cudaSuccess) e = root.reserve(6 * (size_t)nseg());
   if (e == cudaSuccess) e = dup.reserve(1);
   if (e == cudaSuccess) e = sorter.reserve(np);
   return e;
@@ -382,32 +461,60 @@ cudaError_t Lbvh::reserve(uint32_t np) {
 void Lbvh::construct(float scr, cudaStream_t s, uint32_t* d_err) {
   active = n > 0;
   if (n == 0) return;
-  k_root_init<<<1, 32, 0, s>>>(reinterpret_cast<uint32_t*>(root.p), dup.p);
-  k_leaf_boxes<<<grid_for(n), kBlock, 0, s>>>(v.p, pred.p, n, scr, leaf_lo.p, leaf_hi.p,
-                                              reinterpret_cast<uint32_t*>(root.p));
-  k_morton<<<grid_for(n), kBlock, 0, s>>>(leaf_lo.p, leaf_hi.p,
-                                          reinterpret_cast<const uint32_t*>(root.p), n, morton.p,
-                                          index.p);
-  sorter.sort(morton.p, index.p, n, 30, s, &sorted_morton, &sorted_index);
-  k_leaves<<<grid_for(n), kBlock, 0, s>>>(sorted_morton, sorted_index, leaf_lo.p, leaf_hi.p, n, lo.p,
-                                          hi.p, node.p, key64.p, dup.p);
-  if (n > 1) {
-    k_internal<<<grid_for(n - 1), kBlock, 0, s>>>(key64.p, n, lo.p, node.p);
-    cudaMemsetAsync(flags.p, 0, sizeof(uint32_t) * (n - 1), s);
-    k_build_internal_boxes<<<grid_for(n), kBlock, 0, s>>>(n, lo.p, hi.p, node.p, flags.p, d_err);
+  const LbvhForest F = forest();
+  const uint32_t S = nseg();
+  nodes = 0;
+  internal = 0;
+  if (S == 1) {
+    nodes = 2 * n - 1;
+    internal = n - 1;
+  } else {
+    for (const int4& r : h_seg) {
+      nodes += r.y ? 2 * (uint32_t)r.y - 1 : 0;
+      internal += r.y ? (uint32_t)r.y - 1 : 0;
+    }
   }
-  k_escape<<<grid_for(2 * n - 1), kBlock, 0, s>>>(n, node.p, hi.p, iesc.p, eesc.p, d_err);
+  uint32_t* rootu = reinterpret_cast<uint32_t*>(root.p);
+  k_root_init<<<grid_for(6 * S), kBlock, 0, s>>>(rootu, S, dup.p);
+  k_leaf_boxes<<<grid_for(n), kBlock, 0, s>>>(v.p, pred.p, n, scr, leaf_lo.p, leaf_hi.p, rootu, F);
+  k_morton<<<grid_for(n), kBlock, 0, s>>>(leaf_lo.p, leaf_hi.p, rootu, n, morton.p, index.p, F);
+  // Morton codes have 30 bits: four 8-bit passes leave the result in (morton, index)
+  sorter.sort(morton.p, index.p, n, 30, s, &sorted_morton, &sorted_index);
+  if (S > 1) {
+    int bits = 0;
+    while ((1u << bits) < S) ++bits;
+    k_seg_keys<<<grid_for(n), kBlock, 0, s>>>(sorted_index, n, skey.p, sval.p, F);
+    uint32_t *k2 = nullptr, *perm = nullptr;
+    sorter.sort(skey.p, sval.p, n, bits, s, &k2, &perm);
+    // gather into whichever key / value pair the segment pass's result does not occupy
+    const bool in_own = perm == sval.p;
+    uint32_t* m_out = in_own ? sorter.keys_tmp.p : skey.p;
+    uint32_t* i_out = in_own ? sorter.vals_tmp.p : sval.p;
+    k_seg_gather<<<grid_for(n), kBlock, 0, s>>>(perm, sorted_morton, sorted_index, n, m_out, i_out);
+    sorted_morton = m_out;
+    sorted_index = i_out;
+  }
+  k_leaves<<<grid_for(n), kBlock, 0, s>>>(sorted_morton, sorted_index, leaf_lo.p, leaf_hi.p, n, lo.p,
+                                          hi.p, node.p, key64.p, dup.p, F);
+  if (internal > 0) {
+    k_internal<<<grid_for(internal), kBlock, 0, s>>>(key64.p, internal, lo.p, node.p, F);
+    cudaMemsetAsync(flags.p, 0, sizeof(uint32_t) * internal, s);
+    k_build_internal_boxes<<<grid_for(n), kBlock, 0, s>>>(n, lo.p, hi.p, node.p, flags.p, d_err, F);
+  }
+  k_escape<<<grid_for(nodes), kBlock, 0, s>>>(nodes, node.p, hi.p, iesc.p, eesc.p, d_err, F);
 }
 
 void Lbvh::refit_from_pred(cudaStream_t s, uint32_t* d_err) {
   if (!active) return;
-  k_refit_pred<<<grid_for(n), kBlock, 0, s>>>(n, pred.p, lo.p, hi.p, node.p, flags.p, d_err);
+  k_refit_pred<<<grid_for(n), kBlock, 0, s>>>(n, pred.p, lo.p, hi.p, node.p, flags.p, d_err,
+                                              forest());
 }
 
 void Lbvh::release() {
   v.release(); pred.release(); leaf_lo.release(); leaf_hi.release(); lo.release(); hi.release();
   node.release(); morton.release(); index.release(); key64.release(); flags.release();
-  iesc.release(); eesc.release(); root.release(); dup.release();
+  iesc.release(); eesc.release(); root.release(); dup.release(); skey.release(); sval.release();
+  seg.release();
   sorter.keys_tmp.release(); sorter.vals_tmp.release(); sorter.hist.release();
 }
 
@@ -421,7 +528,7 @@ void launch_refit_midstep(Lbvh& b, const float4* x1, const float4* n1, const int
                           cudaStream_t s, uint32_t* d_err) {
   if (!b.active) return;
   k_refit_midstep<<<grid_for(b.n), kBlock, 0, s>>>(b.n, x1, n1, tri, tol, b.pred.p, b.lo.p, b.hi.p,
-                                                   b.node.p, b.flags.p, d_err);
+                                                   b.node.p, b.flags.p, d_err, b.forest());
 }
 
 void launch_lbvh_query(const Lbvh& b, int kind, const float* d_q, uint32_t nq, uint32_t* d_counts,

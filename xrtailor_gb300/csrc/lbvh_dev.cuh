@@ -80,10 +80,46 @@ __device__ __forceinline__ void lbvh_merge_upwards(uint32_t leaf_node, uint32_t 
   }
 }
 
+// ---- instances (InstView) ----------------------------------------------------------------------
+__device__ __forceinline__ uint32_t inst_index(const InstView& I, uint32_t v) {
+  return I.count == 1 ? 0u : __ldg(&I.of_vertex[v]);
+}
+__device__ __forceinline__ InstanceRec inst_rec(const InstView& I, uint32_t s) {
+  return I.count == 1 ? I.one : I.rec[s];
+}
+
+// ---- forests (LbvhForest) ----------------------------------------------------------------------
+__device__ __forceinline__ int4 forest_rec(const LbvhForest& F, uint32_t s) {
+  return F.nseg == 1 ? F.one : F.seg[s];
+}
+
+// Segment owning element i of a forest-wide range: field 0 = primitive / sorted leaf position,
+// 2 = node, 3 = internal node.  The last segment whose base is <= i: empty segments share their
+// base with the next one, so the segment found always owns i.
+__device__ __forceinline__ uint32_t forest_find(const LbvhForest& F, uint32_t i, int field) {
+  if (F.nseg == 1) return 0;
+  uint32_t lo = 0, hi = F.nseg;  // base(lo) <= i < base(hi)
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const int4 r = F.seg[mid];
+    const uint32_t b = (uint32_t)(field == 0 ? r.x : (field == 2 ? r.z : r.w));
+    if (b <= i) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// The tree of segment s with local links; objects are local, global = rec.x + object.
+__device__ __forceinline__ LbvhView forest_view(const LbvhForest& F, uint32_t s) {
+  const int4 r = forest_rec(F, s);
+  return LbvhView{(uint32_t)r.y, F.all.pred + 3 * (size_t)r.x, F.all.lo + r.z, F.all.hi + r.z};
+}
+
 // Stackless traversal; `ov(lo, hi)` tests a node box, `visit(object)` receives each hit.
 template <class Overlap, class Visit>
 __device__ __forceinline__ uint32_t lbvh_traverse(const LbvhView& b, Overlap ov, Visit visit,
                                                   uint32_t* err) {
+  if (b.n == 0) return 0;
   const uint32_t ni = b.n - 1;
   int nodei = 0;
   uint32_t found = 0, guard = 0;

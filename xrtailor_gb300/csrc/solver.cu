@@ -15,6 +15,10 @@
 // color and lets the other colors exit) and, because a color is an independent set, writes its
 // vertices without atomics.  Contact deltas are gathered per vertex over its incident edges in
 // ascending edge order, replacing float atomics with a fixed summation order.
+#include <algorithm>
+#include <map>
+#include <mutex>
+
 #include "common.cuh"
 #include "context.h"
 
@@ -118,47 +122,57 @@ __global__ void k_stretch(const int4* __restrict__ con, float* __restrict__ lamb
 // multipliers (stretch) or rest angles (bend), then the num_local + 1 local-color offsets.
 // Prologue before pdl_wait (setup-time data only): the tile's metadata, offsets, records and
 // footprint vertex ids, the ids held in registers (kFootPerThread per thread) so the gather and
-// the write-back each issue all their loads and stores at once.
+// the write-back each issue all their loads and stores at once.  NT threads per block: 512 for
+// footprints up to 4,096 vertices, 256 (twice the resident blocks per SM) up to 2,048.
 struct TileFrame {
   int4 m;                          // first footprint entry, footprint size, first record, count
   uint32_t fi[kFootPerThread];     // footprint vertex ids of this thread
 };
 
+template <int NT>
 __device__ __forceinline__ TileFrame tile_prologue(const uint32_t* __restrict__ foot,
                                                    const int4* __restrict__ meta,
                                                    const uint32_t* __restrict__ lofs, uint32_t t,
                                                    uint32_t num_local, uint32_t* so) {
   TileFrame f;
   f.m = __ldg(&meta[t]);
-  if (threadIdx.x <= num_local) so[threadIdx.x] = __ldg(&lofs[(size_t)t * (num_local + 1) + threadIdx.x]);
+  for (uint32_t k = threadIdx.x; k <= num_local; k += NT)
+    so[k] = __ldg(&lofs[(size_t)t * (num_local + 1) + k]);
 #pragma unroll
   for (int r = 0; r < kFootPerThread; ++r) {
-    const uint32_t k = threadIdx.x + (uint32_t)r * kTileBlock;
+    const uint32_t k = threadIdx.x + (uint32_t)r * NT;
     f.fi[r] = k < (uint32_t)f.m.y ? __ldg(&foot[f.m.x + k]) : 0u;
   }
   return f;
 }
 
+// The gather also parks the ids in shared memory (slot k is written and later read by the same
+// thread), so they need no registers through the local-color loop.
+template <int NT>
 __device__ __forceinline__ void tile_gather(const TileFrame& f, const float4* __restrict__ x,
-                                            float4* sx) {
+                                            float4* sx, uint32_t* sf) {
 #pragma unroll
   for (int r = 0; r < kFootPerThread; ++r) {
-    const uint32_t k = threadIdx.x + (uint32_t)r * kTileBlock;
-    if (k < (uint32_t)f.m.y) sx[k] = x[f.fi[r]];
+    const uint32_t k = threadIdx.x + (uint32_t)r * NT;
+    if (k < (uint32_t)f.m.y) {
+      sx[k] = x[f.fi[r]];
+      sf[k] = f.fi[r];
+    }
   }
 }
 
-__device__ __forceinline__ void tile_scatter(const TileFrame& f, float4* __restrict__ x,
-                                             const float4* sx) {
+template <int NT>
+__device__ __forceinline__ void tile_scatter(uint32_t nfoot, float4* __restrict__ x,
+                                             const float4* sx, const uint32_t* sf) {
 #pragma unroll
   for (int r = 0; r < kFootPerThread; ++r) {
-    const uint32_t k = threadIdx.x + (uint32_t)r * kTileBlock;
-    if (k < (uint32_t)f.m.y) x[f.fi[r]] = sx[k];
+    const uint32_t k = threadIdx.x + (uint32_t)r * NT;
+    if (k < nfoot) x[sf[k]] = sx[k];
   }
 }
 
-template <bool RESET>
-__global__ void __launch_bounds__(kTileBlock) k_stretch_tiles(
+template <bool RESET, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_stretch_tiles(
     const int4* __restrict__ con, float* __restrict__ lambda, float4* __restrict__ x,
     const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
     const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
@@ -168,18 +182,19 @@ __global__ void __launch_bounds__(kTileBlock) k_stretch_tiles(
   int4* sc = reinterpret_cast<int4*>(sx + max_foot);
   float* sl = reinterpret_cast<float*>(sc + max_cons);
   uint32_t* so = reinterpret_cast<uint32_t*>(sl + max_cons);
-  const TileFrame f = tile_prologue(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
+  uint32_t* sf = so + num_local + 1;
+  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
   const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
 #pragma unroll 4
-  for (uint32_t j = threadIdx.x; j < nc; j += kTileBlock) sc[j] = __ldg(&con[c0 + j]);
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) sc[j] = __ldg(&con[c0 + j]);
   pdl_wait();
 #pragma unroll 4
-  for (uint32_t j = threadIdx.x; j < nc; j += kTileBlock) sl[j] = RESET ? 0.0f : lambda[c0 + j];
-  tile_gather(f, x, sx);
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) sl[j] = RESET ? 0.0f : lambda[c0 + j];
+  tile_gather<NT>(f, x, sx, sf);
   __syncthreads();
   for (uint32_t l = 0; l < num_local; ++l) {
     const uint32_t ce = so[l + 1];
-    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += kTileBlock) {
+    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
       const int4 c = sc[j];
       float lam = sl[j];
       float4 a = sx[c.x], b = sx[c.y];
@@ -192,9 +207,9 @@ __global__ void __launch_bounds__(kTileBlock) k_stretch_tiles(
     __syncthreads();
   }
   pdl_release();  // late: the successor's blocks arrive as this one drains (measured faster)
-  tile_scatter(f, x, sx);
+  tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
 #pragma unroll 4
-  for (uint32_t j = threadIdx.x; j < nc; j += kTileBlock) lambda[c0 + j] = sl[j];
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) lambda[c0 + j] = sl[j];
 }
 
 // Dihedral bend projection of SolveBend_Kernel on four vertices.
@@ -226,7 +241,11 @@ __global__ void k_bend(const int4* __restrict__ idx, const float2* __restrict__ 
   x[b.w] = a4;
 }
 
-__global__ void __launch_bounds__(kTileBlock) k_bend_tiles(
+// PAIR: two lanes per bend element (bend_project_pair), half the dependency chain per step, for
+// launches whose tiles are all resident at once (latency-bound); otherwise one lane per element
+// (fewer instructions in total, for launches with many waves of tiles).
+template <int NT, bool PAIR>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
     const int4* __restrict__ idx, const float2* __restrict__ tc, float4* __restrict__ x,
     const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
     const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
@@ -236,33 +255,50 @@ __global__ void __launch_bounds__(kTileBlock) k_bend_tiles(
   int4* sc = reinterpret_cast<int4*>(sx + max_foot);
   float2* st = reinterpret_cast<float2*>(sc + max_cons);
   uint32_t* so = reinterpret_cast<uint32_t*>(st + max_cons);
-  const TileFrame f = tile_prologue(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
+  uint32_t* sf = so + num_local + 1;
+  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
   const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
 #pragma unroll 4
-  for (uint32_t j = threadIdx.x; j < nc; j += kTileBlock) {
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) {
     sc[j] = __ldg(&idx[c0 + j]);
     st[j] = __ldg(&tc[c0 + j]);
   }
   pdl_wait();
-  tile_gather(f, x, sx);
+  tile_gather<NT>(f, x, sx, sf);
   __syncthreads();
-  // Two lanes per bend element (bend_project_pair); the loop trip count is warp-uniform so the
-  // pair exchanges run with full warps.
-  const uint32_t lane0 = threadIdx.x & ~31u;
-  for (uint32_t l = 0; l < num_local; ++l) {
-    const uint32_t cb = 2 * so[l], ce = 2 * so[l + 1];
-    for (uint32_t base = cb + lane0; base < ce; base += kTileBlock) {
-      const uint32_t s = base + (threadIdx.x & 31u);
-      const bool active = s < ce;
-      const uint32_t j = active ? s >> 1 : cb >> 1;
-      const int4 b = sc[j];
-      const float2 th = st[j];
-      bend_project_pair(sx, b, th.x, th.y, dt, s & 1u, active);
+  if (PAIR) {
+    // the loop trip count is warp-uniform so the pair exchanges run with full warps
+    const uint32_t lane0 = threadIdx.x & ~31u;
+    for (uint32_t l = 0; l < num_local; ++l) {
+      const uint32_t cb = 2 * so[l], ce = 2 * so[l + 1];
+      for (uint32_t base = cb + lane0; base < ce; base += NT) {
+        const uint32_t s = base + (threadIdx.x & 31u);
+        const bool active = s < ce;
+        const uint32_t j = active ? s >> 1 : cb >> 1;
+        const int4 b = sc[j];
+        const float2 th = st[j];
+        bend_project_pair(sx, b, th.x, th.y, dt, s & 1u, active);
+      }
+      __syncthreads();
     }
-    __syncthreads();
+  } else {
+    for (uint32_t l = 0; l < num_local; ++l) {
+      const uint32_t ce = so[l + 1];
+      for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
+        const int4 b = sc[j];
+        const float2 th = st[j];
+        float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
+        bend_project(a1, a2, a3, a4, th.x, th.y, dt);
+        sx[b.x] = a1;
+        sx[b.y] = a2;
+        sx[b.z] = a3;
+        sx[b.w] = a4;
+      }
+      __syncthreads();
+    }
   }
   pdl_release();
-  tile_scatter(f, x, sx);
+  tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
 }
 
 __device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3, float4& a4,
@@ -550,24 +586,60 @@ void launch_bend(Context& c, const FrameConst& k, ColorRange r) {
            r.end, k.dt);
 }
 
+// The limit is a property of the kernel function on the current device, shared by every
+// context of the process, so it only ever grows: a context started later with smaller tiles
+// must not lower it under one that is already running.
 cudaError_t configure_tile_kernels(size_t max_smem_bytes) {
-  const int bytes = (int)max_smem_bytes;
-  cudaError_t e = cudaFuncSetAttribute(k_stretch_tiles<true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_stretch_tiles<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             bytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_bend_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  return e;
+  static std::mutex mu;
+  static std::map<int, int> configured;  // device -> bytes
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  int& cur = configured[dev];
+  const int bytes = std::max(cur, (int)max_smem_bytes);
+  if (bytes == cur) return cudaSuccess;
+  const void* kernels[] = {
+      (const void*)k_stretch_tiles<true, 256>, (const void*)k_stretch_tiles<false, 256>,
+      (const void*)k_stretch_tiles<true, 512>, (const void*)k_stretch_tiles<false, 512>,
+      (const void*)k_bend_tiles<256, true>,    (const void*)k_bend_tiles<256, false>,
+      (const void*)k_bend_tiles<512, true>,    (const void*)k_bend_tiles<512, false>};
+  for (const void* kern : kernels) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+  }
+  cur = bytes;
+  return cudaSuccess;
 }
 
-static_assert(kTileBlock * kFootPerThread >= (int)kTileMaxFootprint,
+static_assert(512 * kFootPerThread >= (int)kTileMaxFootprint,
               "tile kernels hold every footprint vertex id in registers");
 
 size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes) {
   return sizeof(float4) * T.max_foot + record_bytes * T.max_cons +
-         sizeof(uint32_t) * (T.num_local + 1);
+         sizeof(uint32_t) * (T.num_local + 1) + sizeof(uint32_t) * T.max_foot;
+}
+
+// Block size of a tile set: 256 threads when the footprint fits 256 x kFootPerThread and a local
+// color's elements (two lanes each for bend) fill at most one pass, else 512; and how many of its
+// bend blocks the GPU holds at once.
+cudaError_t choose_tile_block(TiledSet& T, bool bend) {
+  const uint32_t lanes = bend ? 2 * T.max_step : T.max_step;
+  T.block = (T.max_foot <= 256u * kFootPerThread && lanes <= 256) ? 256 : 512;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const size_t smem = tile_smem_bytes(T, bend ? sizeof(int4) + sizeof(float2)
+                                              : sizeof(int4) + sizeof(float));
+  const void* kern = bend ? (T.block == 256 ? (const void*)k_bend_tiles<256, true>
+                                            : (const void*)k_bend_tiles<512, true>)
+                          : (T.block == 256 ? (const void*)k_stretch_tiles<false, 256>
+                                            : (const void*)k_stretch_tiles<false, 512>);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)T.block, smem);
+  if (e != cudaSuccess) return e;
+  T.resident = (uint32_t)std::max(per_sm, 1) * (uint32_t)sms;
+  return cudaSuccess;
 }
 
 void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, bool reset_lambda) {
@@ -575,18 +647,22 @@ void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, boo
   if (nt == 0) return;
   const TiledSet& T = c.s_tiles;
   const size_t smem = tile_smem_bytes(T, sizeof(int4) + sizeof(float));
-  launch_k(c.pdl, reset_lambda ? k_stretch_tiles<true> : k_stretch_tiles<false>, nt, kTileBlock,
-           smem, c.stream, c.s_con.p, c.s_lambda.p, c.x.p, T.foot.p, T.meta.p, T.lofs.p,
-           tiles.begin, T.num_local, T.max_foot, T.max_cons, k.dt);
+  auto kern = T.block == 256 ? (reset_lambda ? k_stretch_tiles<true, 256> : k_stretch_tiles<false, 256>)
+                             : (reset_lambda ? k_stretch_tiles<true, 512> : k_stretch_tiles<false, 512>);
+  launch_k(c.pdl, kern, nt, T.block, smem, c.stream, c.s_con.p, c.s_lambda.p, c.x.p, T.foot.p,
+           T.meta.p, T.lofs.p, tiles.begin, T.num_local, T.max_foot, T.max_cons, k.dt);
 }
 
 void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles) {
   const uint32_t nt = tiles.end - tiles.begin;
   if (nt == 0) return;
   const TiledSet& T = c.b_tiles;
-  launch_k(c.pdl, k_bend_tiles, nt, kTileBlock, tile_smem_bytes(T, sizeof(int4) + sizeof(float2)),
-           c.stream, c.b_idx.p, c.b_tc.p, c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin,
-           T.num_local, T.max_foot, T.max_cons, k.dt);
+  const bool pair = nt <= T.resident;  // one wave: latency-bound, halve the chain
+  auto kern = T.block == 256 ? (pair ? k_bend_tiles<256, true> : k_bend_tiles<256, false>)
+                             : (pair ? k_bend_tiles<512, true> : k_bend_tiles<512, false>);
+  launch_k(c.pdl, kern, nt, T.block, tile_smem_bytes(T, sizeof(int4) + sizeof(float2)), c.stream,
+           c.b_idx.p, c.b_tc.p, c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin, T.num_local,
+           T.max_foot, T.max_cons, k.dt);
 }
 
 // LRA phase with a free slot vertex: one launch per slot block in list order.  (With every slot

@@ -18,24 +18,32 @@ import numpy as np
 from .solver import Mesh
 
 
-def grid_cloth(n: int, size: float = 1.0, origin=(0.0, 0.0, 0.0), jitter: float = 1e-3,
-               seed: int = 1) -> Mesh:
-    """n x n grid in the xz plane at height origin[1]; normal +y; vertex (i, j) = i * n + j."""
+def rect_cloth(nx: int, ny: int, width: float = 1.0, depth: float = 1.0,
+               origin=(0.0, 0.0, 0.0), jitter: float = 1e-3, seed: int = 1) -> Mesh:
+    """nx x ny grid (nx vertices along x over `width`, ny rows along z over `depth`) in the xz
+    plane at height origin[1]; normal +y; vertex (i, j) = i * nx + j."""
     rng = np.random.default_rng(seed)
-    h = size / (n - 1)
-    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
-    pos = np.stack([origin[0] + j * h, np.full_like(i, origin[1], dtype=np.float64),
-                    origin[2] + i * h], axis=-1).reshape(-1, 3)
+    hx = width / (nx - 1)
+    hz = depth / (ny - 1)
+    i, j = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    pos = np.stack([origin[0] + j * hx, np.full_like(i, origin[1], dtype=np.float64),
+                    origin[2] + i * hz], axis=-1).reshape(-1, 3)
     if jitter > 0:
         pos = pos + rng.uniform(-jitter, jitter, size=pos.shape)
-    a = (i[:-1, :-1] * n + j[:-1, :-1]).reshape(-1)
+    a = (i[:-1, :-1] * nx + j[:-1, :-1]).reshape(-1)
     b = a + 1
-    c = a + n
+    c = a + nx
     d = c + 1
     tri = np.empty((a.size * 2, 3), np.uint32)
     tri[0::2] = np.stack([a, c, b], -1)
     tri[1::2] = np.stack([b, c, d], -1)
     return Mesh(positions=pos.astype(np.float32), triangles=tri)
+
+
+def grid_cloth(n: int, size: float = 1.0, origin=(0.0, 0.0, 0.0), jitter: float = 1e-3,
+               seed: int = 1) -> Mesh:
+    """n x n grid in the xz plane at height origin[1]; normal +y; vertex (i, j) = i * n + j."""
+    return rect_cloth(n, n, size, size, origin, jitter, seed)
 
 
 def icosphere(subdiv: int = 3, radius: float = 0.3, center=(0.0, 0.0, 0.0)) -> Mesh:
@@ -220,6 +228,48 @@ def plain_heavy(n: int = 1024, frames: int = 180, seed: int = 3) -> Scene:
     return Scene("plain_heavy", cloth, ground,
                  dict(num_substeps=10, num_iterations=10, stretch_compliance=1e-8,
                       bend_compliance=1e-6), particle_diameter=1e-3, frames=frames)
+
+
+@dataclass
+class Garment:
+    """One instance of the batched workload."""
+    cloth: Mesh
+    body: TubeBody
+    nx: int
+    ny: int
+    stretch_compliance: float
+
+    @property
+    def num_edges(self) -> int:
+        nx, ny = self.nx, self.ny
+        return nx * (ny - 1) + ny * (nx - 1) + (nx - 1) * (ny - 1)
+
+
+# 10 substeps x 10 iterations, bend compliance 1e-6, stretch per instance.
+BATCHED_PARAMS = dict(num_substeps=10, num_iterations=10, bend_compliance=1e-6)
+
+
+def batched_garments(count: int = 512, seed: int = 4) -> list:
+    """`count` independent garments: vertex counts log-uniform in [2,000, 100,000], aspect
+    (x : z) uniform in [0.5, 2], square cells, 1 m wide, draped 5 cm above their own tube body
+    (joint motion seeded with seed + i), two corners pinned and LRA-attached; stretch compliance
+    log-uniform in [1e-9, 1e-5] per instance."""
+    rng = np.random.default_rng(seed)
+    V = np.exp(rng.uniform(np.log(2000.0), np.log(100000.0), count))
+    aspect = rng.uniform(0.5, 2.0, count)
+    comp = np.exp(rng.uniform(np.log(1e-9), np.log(1e-5), count))
+    out = []
+    for i in range(count):
+        ny = max(2, int(round(np.sqrt(V[i] / aspect[i]))))
+        nx = max(2, int(round(V[i] / ny)))
+        body = TubeBody(seed=seed + i)
+        depth = (ny - 1) / (nx - 1)
+        cloth = rect_cloth(nx, ny, 1.0, depth, origin=(-0.5, body.height + 0.05, -0.5 * depth),
+                           jitter=1e-3, seed=seed + i)
+        cloth.fixed_indices = np.array([0, nx - 1], np.uint32)
+        cloth.attached_indices = np.array([0, nx - 1], np.uint32)
+        out.append(Garment(cloth, body, nx, ny, float(comp[i])))
+    return out
 
 
 def scene_params(scene: Scene, **overrides):

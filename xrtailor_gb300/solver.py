@@ -232,6 +232,19 @@ class ClothSolver:
         del keep
         return off.value
 
+    def add_instance(self, cloth: Mesh, obstacle: Mesh = None, cloth_matrix=None,
+                     obstacle_matrix=None, particle_diameter: float = 0.0) -> int:
+        """Batched form: an independent cloth + its own obstacle; returns the instance index."""
+        d, keep = cloth_desc(cloth, cloth_matrix, particle_diameter)
+        od, okeep = (None, None)
+        if obstacle is not None:
+            od, okeep = obstacle_desc(obstacle, obstacle_matrix)
+        idx = C.c_int32()
+        L.check(self._lib.xrt_add_instance(self._h, C.byref(d), C.byref(od) if od is not None
+                                           else None, C.byref(idx)), self._h, "add_instance")
+        del keep, okeep
+        return idx.value
+
     def set_coloring(self, kind: int, colors):
         c = _u32(colors)
         L.check(self._lib.xrt_set_coloring(self._h, kind, L.uptr(c), c.size), self._h, "set_coloring")
@@ -355,15 +368,19 @@ class ClothSolver:
         return m
 
     def export_obstacle_bvh(self):
-        n = self.sizes().num_obstacle_triangles
-        nn = 2 * n - 1
+        """Obstacle LBVH; in a batched context the instances' trees one after the other (links
+        and objects local to each tree, `objects` global)."""
+        s = self.sizes()
+        n = s.num_obstacle_triangles
+        nn = s.num_obstacle_bvh_nodes or (2 * n - 1)
+        ni = nn - n
         out = dict(morton=np.empty(n, np.uint32), objects=np.empty(n, np.uint32),
                    nodes=np.empty((nn, 4), np.uint32), aabbs=np.empty((nn, 6), np.float32),
-                   iesc=np.empty(max(n - 1, 1), np.int32), eesc=np.empty(n, np.int32))
+                   iesc=np.empty(max(ni, 1), np.int32), eesc=np.empty(n, np.int32))
         L.check(self._lib.xrt_export_obstacle_bvh(
             self._h, L.uptr(out["morton"]), L.uptr(out["objects"]), L.uptr(out["nodes"]),
             L.fptr(out["aabbs"]), L.iptr(out["iesc"]), L.iptr(out["eesc"])), self._h, "bvh")
-        out["iesc"] = out["iesc"][: max(n - 1, 0)]
+        out["iesc"] = out["iesc"][: max(ni, 0)]
         return out
 
     def export_contacts(self):
