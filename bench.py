@@ -288,21 +288,10 @@ def run_batched(args, local_rank):
     xb.build()
     torch.cuda.set_device(local_rank)
     dev = f"cuda:{local_rank}"
-    t_setup = time.perf_counter()
+    from xrtailor_gb300 import autotune
     gs = scenes.batched_garments(args.instances)
     p = scenes._params(**scenes.BATCHED_PARAMS)
     S = p.num_substeps
-    s = ClothSolver(p, device=local_rank)
-    if args.tile_vertices is not None:
-        s.set_tile_vertices(args.tile_vertices)
-    for g in gs:
-        s.add_instance(g.cloth, g.body.mesh)
-    s.set_compliance(0, np.concatenate([np.full(g.num_edges, g.stretch_compliance, np.float32)
-                                        for g in gs]))
-    s.start()
-    setup_s = time.perf_counter() - t_setup
-    sz = s.sizes()
-    V = sz.num_vertices
     nframes = args.warmup + args.steps + 1
     ov = [len(g.body.rest) for g in gs]
     obase = np.concatenate([[0], np.cumsum(ov)])
@@ -310,6 +299,39 @@ def run_batched(args, local_rank):
     for f in range(nframes):
         tg[f] = torch.from_numpy(np.concatenate([g.body.pose((f + 1) / 60.0) for g in gs]))
     torch.cuda.synchronize()
+
+    def comps(idx):
+        return np.concatenate([np.full(gs[i].num_edges, gs[i].stretch_compliance, np.float32)
+                               for i in idx])
+
+    def make(tile, idx):
+        q = ClothSolver(p, device=local_rank)
+        if tile is not None:
+            q.set_tile_vertices(tile)
+        for i in idx:
+            q.add_instance(gs[i].cloth, gs[i].body.mesh)
+        q.set_compliance(0, comps(idx))
+        q.start()
+        return q
+
+    # launch configuration: autotuned on an evenly spaced subset of the garments
+    tuned, trials, tune_s = None, [], 0.0
+    if args.tile_vertices is None and args.tune_instances > 0:
+        t0 = time.perf_counter()
+        sub = autotune.subset(len(gs), args.tune_instances)
+        tg_sub = torch.cat([tg[:, int(obase[i]):int(obase[i + 1])] for i in sub], dim=1)
+        tuned, trials = autotune.tune(lambda t: make(t, sub), frames=2, warmup=1,
+                                      targets=lambda k: tg_sub[k % nframes].data_ptr())
+        del tg_sub
+        tune_s = time.perf_counter() - t0
+    t_setup = time.perf_counter()
+    tile = args.tile_vertices if tuned is None else tuned["tile_vertices"]
+    s = make(tile, range(len(gs)))
+    if tuned is not None:
+        s.set_dependent_launch(tuned["dependent_launch"])
+    setup_s = time.perf_counter() - t_setup
+    sz = s.sizes()
+    V = sz.num_vertices
     _, _, sp = s.device_state()
     stream = torch.cuda.ExternalStream(sp, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -394,7 +416,11 @@ def run_batched(args, local_rank):
                    "iterations": p.num_iterations, "collision_passes": p.num_collision_passes,
                    "self_collision": bool(p.enable_self_collision),
                    "l2": "flushed between frames (512 MiB write, outside the timed events)",
-                   "setup_s": round(setup_s, 1), "parallelism": "single"},
+                   "setup_s": round(setup_s, 1), "parallelism": "single",
+                   "launch": tuned or {"tile_vertices": tile},
+                   "autotune": {"instances": args.tune_instances, "seconds": round(tune_s, 1),
+                                "trials_ms_per_frame": [[t, d, round(ms, 2)]
+                                                        for t, d, ms in trials]}},
         "gpu_launches": int(launches) * args.steps,
         "plain_per_garment": {
             "value": plain_value, "unit": "vertex-substeps/s",
@@ -447,6 +473,9 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=512,
                     help="batched workload: garments timed alone (evenly spaced)")
     ap.add_argument("--plain-frames", type=int, default=2)
+    ap.add_argument("--tune-instances", type=int, default=32,
+                    help="batched workload: garments the launch autotuner times (0: library "
+                         "defaults)")
     ap.add_argument("--tile-vertices", type=int, default=None,
                     help="tile size of the Gauss-Seidel schedule (library default if omitted)")
     args = ap.parse_args()

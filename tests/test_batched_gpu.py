@@ -164,6 +164,24 @@ def test_tiles_off_matches_too(xrt):
         off += n
 
 
+def test_autotune_picks_a_timed_candidate(xrt):
+    from xrtailor_gb300 import autotune
+    inst = _instances()[:2]
+
+    def make(t):
+        s = ClothSolver(_params())
+        s.set_tile_vertices(t)
+        for c, o, _ in inst:
+            s.add_instance(c, o)
+        s.start()
+        return s
+
+    best, trials = autotune.tune(make, tiles=(64, 128), frames=1, warmup=1)
+    assert len(trials) == 4 and all(ms > 0 for _, _, ms in trials)
+    assert (best["tile_vertices"], best["dependent_launch"]) == min(trials, key=lambda r: r[2])[:2]
+    assert autotune.subset(10, 4) == [0, 3, 6, 9] and autotune.subset(3, 8) == [0, 1, 2]
+
+
 def test_batched_errors(xrt):
     c, o, _ = _instances()[0]
     s = ClothSolver(_params())

@@ -394,7 +394,9 @@ xrt_status xrt_create(xrt_ctx** out, int32_t device) {
   xrt_default_params(&c.params);
   if (cudaSetDevice(device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess ||
-      c.err.reserve(1) != cudaSuccess || cudaMemset(c.err.p, 0, sizeof(uint32_t)) != cudaSuccess) {
+      c.err.reserve(1) != cudaSuccess || cudaMemset(c.err.p, 0, sizeof(uint32_t)) != cudaSuccess ||
+      c.gen_counter.reserve(4) != cudaSuccess ||
+      cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
     delete h;
     return XRT_ERR_CUDA;
   }
@@ -423,9 +425,11 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   c.s_lambda.release(); c.lra_rest.release(); c.lra_l_rest.release(); c.b_tc.release();
   c.edge.release(); c.vf_idx.release(); c.rt_idx.release();
   c.hash_sorter.keys_tmp.release(); c.hash_sorter.vals_tmp.release(); c.hash_sorter.hist.release();
+  c.hash_sorter.sums.release();
   c.bvh.release();
   c.inst.release();
   c.vinst.release();
+  c.gen_counter.release();
   for (xrt::TiledSet* t : {&c.s_tiles, &c.b_tiles}) {
     t->foot.release();
     t->meta.release();

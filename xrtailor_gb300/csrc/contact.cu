@@ -10,6 +10,8 @@
 // Vertex normals are gathered per vertex over its faces in ascending face order (the reference
 // scatters them with float atomics); the interpolated midstep position x1 of a neighbor is
 // recomputed from x0 and x inside the gather, so interpolation and normals are one kernel.
+#include <algorithm>
+
 #include "common.cuh"
 #include "context.h"
 #include "lbvh_dev.cuh"
@@ -85,67 +87,99 @@ __global__ void k_obstacle_commit(const float4* __restrict__ x, float4* __restri
   nrm[i] = mk4(normalize(acc), 0.0f);
 }
 
-// VF-DCD (nearest obstacle point of the predicted vertex) and VF-CCD (first hit of the segment
-// x0 -> x), one thread per cloth vertex, against the tree of the vertex's instance; contacts
-// record global triangle ids.
-__global__ void __launch_bounds__(kBlock) k_generate_vf(LbvhForest F, InstView I,
-                                                        const float4* __restrict__ x,
-                                                        const float4* __restrict__ x0, uint32_t nv,
-                                                        int* __restrict__ vf_idx,
-                                                        float4* __restrict__ vf_qs,
-                                                        int* __restrict__ rt_idx,
-                                                        float4* __restrict__ rt_qc, uint32_t* err) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nv) return;
-  const uint32_t s = inst_index(I, i);
-  const LbvhView b = forest_view(F, s);
-  const int base = forest_rec(F, s).x;
-  const f3 pred = mk3(x[i]);
-  {
-    float hit = kScalarMax;
-    int hit_idx = -1;
-    f3 hit_qs = mk3(0, 0, 0);
-    lbvh_traverse(
-        b, [&](float4 l, float4 h) { return overlap_point(l, h, pred); },
-        [&](uint32_t f) {
-          f3 qs;
-          const float dist = nearest_point(pred, mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]),
-                                           mk3(b.pred[3 * f + 2]), qs);
-          if (dist < hit) {
-            hit = dist;
-            hit_qs = qs;
-            hit_idx = base + (int)f;
-          }
-        },
-        err);
-    vf_idx[i] = hit_idx;
-    vf_qs[i] = mk4(hit_qs, 0.0f);
-  }
-  {
-    const f3 p1 = mk3(x0[i]), p2 = pred;
-    f3 d = p2 - p1;
-    const float len = length(d);
-    int hit_idx = -1;
-    f3 qc = mk3(0, 0, 0);
-    if (!(len < kEps)) {
-      d = d / len;
-      float hit = kScalarMax;
-      lbvh_traverse(
-          b, [&](float4 l, float4 h) { return overlap_segment(l, h, p1, p2); },
-          [&](uint32_t f) {
-            const float dist = ray_intersect(p1, d, len, mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]),
-                                             mk3(b.pred[3 * f + 2]));
-            if (dist < hit) {
-              qc = p1 + dist * d;
-              hit = dist;
-              hit_idx = base + (int)f;
-            }
-          },
-          err);
+// Contact generation, one query per cloth vertex (VF) or edge (EE) against the tree of its
+// instance, run as persistent work queues (work_queue, lbvh_dev.cuh): traversal lengths differ by
+// orders of magnitude between cloth near the obstacle and cloth away from it, and a plain
+// one-thread-per-query launch left ~2 of 32 lanes of a warp busy.  Contacts record global
+// triangle ids.
+
+// VF-DCD: nearest obstacle point of the predicted vertex.
+__global__ void __launch_bounds__(kBlock) k_generate_vf_dcd(LbvhForest F, InstView I,
+                                                            const float4* __restrict__ x,
+                                                            uint32_t nv, int* __restrict__ vf_idx,
+                                                            float4* __restrict__ vf_qs,
+                                                            uint32_t* err, uint32_t* counter) {
+  LbvhView b{};
+  TraverseState st{};
+  f3 pred{}, hit_qs{};
+  float hit = kScalarMax;
+  int hit_idx = -1, base = 0;
+  auto overlap = [&](float4 l, float4 h) { return overlap_point(l, h, pred); };
+  auto visit = [&](uint32_t f) {
+    f3 qs;
+    const float dist = nearest_point(pred, mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]),
+                                     mk3(b.pred[3 * f + 2]), qs);
+    if (dist < hit) {
+      hit = dist;
+      hit_qs = qs;
+      hit_idx = base + (int)f;
     }
-    rt_idx[i] = hit_idx;
-    rt_qc[i] = mk4(qc, 0.0f);
-  }
+  };
+  work_queue(
+      counter, nv,
+      [&](uint32_t i) {
+        const uint32_t sg = inst_index(I, i);
+        b = forest_view(F, sg);
+        base = forest_rec(F, sg).x;
+        pred = mk3(x[i]);
+        hit = kScalarMax;
+        hit_idx = -1;
+        hit_qs = mk3(0, 0, 0);
+        st = lbvh_begin(b);
+        return st.node != -1;
+      },
+      [&]() { return lbvh_step(b, st, overlap, visit, err); },
+      [&](uint32_t i) {
+        vf_idx[i] = hit_idx;
+        vf_qs[i] = mk4(hit_qs, 0.0f);
+      });
+}
+
+// VF-CCD: first obstacle hit of the segment x0 -> x.
+__global__ void __launch_bounds__(kBlock) k_generate_vf_ccd(LbvhForest F, InstView I,
+                                                            const float4* __restrict__ x,
+                                                            const float4* __restrict__ x0,
+                                                            uint32_t nv, int* __restrict__ rt_idx,
+                                                            float4* __restrict__ rt_qc,
+                                                            uint32_t* err, uint32_t* counter) {
+  LbvhView b{};
+  TraverseState st{};
+  f3 p1{}, p2{}, d{}, qc{};
+  float len = 0, hit = kScalarMax;
+  int hit_idx = -1, base = 0;
+  auto overlap = [&](float4 l, float4 h) { return overlap_segment(l, h, p1, p2); };
+  auto visit = [&](uint32_t f) {
+    const float dist =
+        ray_intersect(p1, d, len, mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]), mk3(b.pred[3 * f + 2]));
+    if (dist < hit) {
+      qc = p1 + dist * d;
+      hit = dist;
+      hit_idx = base + (int)f;
+    }
+  };
+  work_queue(
+      counter, nv,
+      [&](uint32_t i) {
+        const uint32_t sg = inst_index(I, i);
+        b = forest_view(F, sg);
+        base = forest_rec(F, sg).x;
+        p1 = mk3(x0[i]);
+        p2 = mk3(x[i]);
+        d = p2 - p1;
+        len = length(d);
+        hit_idx = -1;
+        qc = mk3(0, 0, 0);
+        if (len < kEps) return false;
+        d = d / len;
+        hit = kScalarMax;
+        st = lbvh_begin(b);
+        return st.node != -1;
+      },
+      [&]() { return lbvh_step(b, st, overlap, visit, err); },
+      [&](uint32_t i) {
+        rt_idx[i] = hit_idx;
+        rt_qc[i] = mk4(qc, 0.0f);
+      });
 }
 
 // EE-DCD: closest R-triangle-owned obstacle edge to each cloth edge.
@@ -155,46 +189,61 @@ __global__ void __launch_bounds__(kBlock) k_generate_ee(LbvhForest F, InstView I
                                                         const int4* __restrict__ otri_all,
                                                         float4* __restrict__ ee_a,
                                                         float4* __restrict__ ee_b,
-                                                        float4* __restrict__ ee_c, uint32_t* err) {
-  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= ne) return;
-  const uint2 ed = edge[e];
-  const uint32_t sg = inst_index(I, ed.x);
-  const LbvhView b = forest_view(F, sg);
-  const int4* __restrict__ otri = otri_all + forest_rec(F, sg).x;
-  const f3 pc = mk3(x[ed.x]), qc = mk3(x[ed.y]);
-  float s = 0, t = 0;
-  f3 p2 = mk3(0, 0, 0), q2 = mk3(0, 0, 0), fn = mk3(0, 0, 0);
-  float min_dist = kScalarMax;
-  lbvh_traverse(
-      b, [&](float4 l, float4 h) { return overlap_segment(l, h, pc, qc); },
-      [&](uint32_t f) {
-        const uint32_t info = (uint32_t)otri[f].w;
-        const f3 ov[3] = {mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]), mk3(b.pred[3 * f + 2])};
+                                                        float4* __restrict__ ee_c, uint32_t* err,
+                                                        uint32_t* counter) {
+  LbvhView b{};
+  TraverseState st{};
+  const int4* otri = nullptr;
+  f3 pc{}, qc{}, p2{}, q2{}, fn{};
+  float s = 0, t = 0, min_dist = kScalarMax;
+  auto overlap = [&](float4 l, float4 h) { return overlap_segment(l, h, pc, qc); };
+  auto visit = [&](uint32_t f) {
+    const uint32_t info = (uint32_t)otri[f].w;
+    const f3 ov[3] = {mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]), mk3(b.pred[3 * f + 2])};
 #pragma unroll
-        for (uint32_t a = 0; a < 3; ++a) {
-          if ((info >> (a + 3u)) & 1u) {
-            float _s, _t;
-            f3 c1, c2;
-            const uint32_t bb = (a + 1u) % 3u;
-            if (closest_seg_seg(pc, qc, ov[a], ov[bb], _s, _t, c1, c2) != 0.0f) {
-              const float dist = length(c1 - c2);
-              if (dist < min_dist) {
-                min_dist = dist;
-                p2 = ov[a];
-                q2 = ov[bb];
-                s = _s;
-                t = _t;
-                fn = face_normal(ov[0], ov[1], ov[2]);
-              }
-            }
+    for (uint32_t a = 0; a < 3; ++a) {
+      if ((info >> (a + 3u)) & 1u) {
+        float _s, _t;
+        f3 c1, c2;
+        const uint32_t bb = (a + 1u) % 3u;
+        if (closest_seg_seg(pc, qc, ov[a], ov[bb], _s, _t, c1, c2) != 0.0f) {
+          const float dist = length(c1 - c2);
+          if (dist < min_dist) {
+            min_dist = dist;
+            p2 = ov[a];
+            q2 = ov[bb];
+            s = _s;
+            t = _t;
+            fn = face_normal(ov[0], ov[1], ov[2]);
           }
         }
+      }
+    }
+  };
+  work_queue(
+      counter, ne,
+      [&](uint32_t e) {
+        const uint2 ed = edge[e];
+        const uint32_t sg = inst_index(I, ed.x);
+        b = forest_view(F, sg);
+        otri = otri_all + forest_rec(F, sg).x;
+        pc = mk3(x[ed.x]);
+        qc = mk3(x[ed.y]);
+        s = 0;
+        t = 0;
+        p2 = mk3(0, 0, 0);
+        q2 = mk3(0, 0, 0);
+        fn = mk3(0, 0, 0);
+        min_dist = kScalarMax;
+        st = lbvh_begin(b);
+        return st.node != -1;
       },
-      err);
-  ee_a[e] = make_float4(min_dist, p2.x, p2.y, p2.z);
-  ee_b[e] = make_float4(q2.x, q2.y, q2.z, s);
-  ee_c[e] = make_float4(fn.x, fn.y, fn.z, t);
+      [&]() { return lbvh_step(b, st, overlap, visit, err); },
+      [&](uint32_t e) {
+        ee_a[e] = make_float4(min_dist, p2.x, p2.y, p2.z);
+        ee_b[e] = make_float4(q2.x, q2.y, q2.z, s);
+        ee_c[e] = make_float4(fn.x, fn.y, fn.z, t);
+      });
 }
 
 }  // namespace
@@ -212,11 +261,17 @@ void launch_generate_contacts(Context& c) {
   if (!c.bvh.active) return;
   const LbvhForest F = c.bvh.forest();
   const InstView I = c.inst_view();
-  k_generate_vf<<<grid_for(c.nv), kBlock, 0, c.stream>>>(F, I, c.x.p, c.x0.p, c.nv, c.vf_idx.p,
-                                                         c.vf_qs.p, c.rt_idx.p, c.rt_qc.p,
-                                                         c.err.p);
-  k_generate_ee<<<grid_for(c.ne), kBlock, 0, c.stream>>>(F, I, c.x.p, c.edge.p, c.ne, c.otri.p,
-                                                         c.ee_a.p, c.ee_b.p, c.ee_c.p, c.err.p);
+  // persistent work queues: a few resident waves of blocks fetch queries until the counters
+  // pass the end
+  const unsigned cap = (unsigned)c.num_sms * 8u;
+  cudaMemsetAsync(c.gen_counter.p, 0, sizeof(uint32_t) * 3, c.stream);
+  k_generate_vf_dcd<<<std::min(grid_for(c.nv), cap), kBlock, 0, c.stream>>>(
+      F, I, c.x.p, c.nv, c.vf_idx.p, c.vf_qs.p, c.err.p, c.gen_counter.p);
+  k_generate_vf_ccd<<<std::min(grid_for(c.nv), cap), kBlock, 0, c.stream>>>(
+      F, I, c.x.p, c.x0.p, c.nv, c.rt_idx.p, c.rt_qc.p, c.err.p, c.gen_counter.p + 1);
+  k_generate_ee<<<std::min(grid_for(c.ne), cap), kBlock, 0, c.stream>>>(
+      F, I, c.x.p, c.edge.p, c.ne, c.otri.p, c.ee_a.p, c.ee_b.p, c.ee_c.p, c.err.p,
+      c.gen_counter.p + 2);
 }
 
 void launch_obstacle_commit(Context& c) {

@@ -39,7 +39,7 @@ struct DBuf {
 
 // ---- radix sort (radix.cu) --------------------------------------------------------------------
 struct RadixSort {
-  DBuf<uint32_t> keys_tmp, vals_tmp, hist;
+  DBuf<uint32_t> keys_tmp, vals_tmp, hist, sums;
   cudaError_t reserve(uint32_t n);
   // Stable LSD sort of (keys, vals) by the low `bits` bits of keys.  The result is left in
   // (keys, vals) if the number of 8-bit passes is even, else in the tmp buffers; returns the
@@ -197,6 +197,8 @@ struct Context {
   bool targets_pending = false;
   uint32_t tile_vertices = 256;  // 0: plain per-color launches of a greedy coloring
   bool pdl = true;               // programmatic dependent launch of the substep kernels
+  int num_sms = 1;               // multiprocessors of the device (persistent launches)
+  DBuf<uint32_t> gen_counter;    // work-queue counters of the contact-generation kernels
   // batched form: instance i = cloth i + obstacle i (xrt_add_instance)
   bool instanced = false;
   struct HostInstance {

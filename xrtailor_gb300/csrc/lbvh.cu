@@ -515,7 +515,7 @@ void Lbvh::release() {
   node.release(); morton.release(); index.release(); key64.release(); flags.release();
   iesc.release(); eesc.release(); root.release(); dup.release(); skey.release(); sval.release();
   seg.release();
-  sorter.keys_tmp.release(); sorter.vals_tmp.release(); sorter.hist.release();
+  sorter.keys_tmp.release(); sorter.vals_tmp.release(); sorter.hist.release(); sorter.sums.release();
 }
 
 void launch_prims_from_mesh(Lbvh& b, const float4* x, const float4* nrm, const int4* tri,

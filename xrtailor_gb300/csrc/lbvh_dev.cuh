@@ -115,35 +115,93 @@ __device__ __forceinline__ LbvhView forest_view(const LbvhForest& F, uint32_t s)
   return LbvhView{(uint32_t)r.y, F.all.pred + 3 * (size_t)r.x, F.all.lo + r.z, F.all.hi + r.z};
 }
 
+// Stackless traversal state; one node visit per lbvh_step.
+struct TraverseState {
+  int node;        // next node, -1 = done
+  uint32_t found;  // leaves visited (capped at kMaxCandidates)
+  uint32_t guard;  // node visits (bounded by 2n + 2)
+};
+
+__device__ __forceinline__ TraverseState lbvh_begin(const LbvhView& b) {
+  return TraverseState{b.n == 0 ? -1 : 0, 0u, 0u};
+}
+
+// One node visit; returns false once the traversal has ended (no visit made).
+template <class Overlap, class Visit>
+__device__ __forceinline__ bool lbvh_step(const LbvhView& b, TraverseState& st, Overlap ov,
+                                          Visit visit, uint32_t* err) {
+  if (st.node == -1 || st.found >= kMaxCandidates) return false;
+  if (++st.guard > 2 * b.n + 2) {
+    raise_error(err, kErrTraversal);
+    st.node = -1;
+    return false;
+  }
+  const float4 l = b.lo[st.node], h = b.hi[st.node];
+  if (ov(l, h)) {
+    if ((uint32_t)st.node >= b.n - 1) {
+      visit((uint32_t)__float_as_int(l.w));
+      ++st.found;
+      st.node = __float_as_int(h.w);
+    } else {
+      st.node = __float_as_int(l.w);
+    }
+  } else {
+    st.node = __float_as_int(h.w);
+  }
+  return true;
+}
+
 // Stackless traversal; `ov(lo, hi)` tests a node box, `visit(object)` receives each hit.
 template <class Overlap, class Visit>
 __device__ __forceinline__ uint32_t lbvh_traverse(const LbvhView& b, Overlap ov, Visit visit,
                                                   uint32_t* err) {
-  if (b.n == 0) return 0;
-  const uint32_t ni = b.n - 1;
-  int nodei = 0;
-  uint32_t found = 0, guard = 0;
-  const uint32_t limit = 2 * b.n + 2;
-  while (nodei != -1) {
-    if (found >= kMaxCandidates) break;
-    if (++guard > limit) {
-      raise_error(err, kErrTraversal);
-      break;
-    }
-    const float4 l = b.lo[nodei], h = b.hi[nodei];
-    if (ov(l, h)) {
-      if ((uint32_t)nodei >= ni) {
-        visit((uint32_t)__float_as_int(l.w));
-        ++found;
-        nodei = __float_as_int(h.w);
-      } else {
-        nodei = __float_as_int(l.w);
+  TraverseState st = lbvh_begin(b);
+  while (lbvh_step(b, st, ov, visit, err)) {
+  }
+  return st.found;
+}
+
+// Persistent query loop with dynamic work fetch: every lane works on one query at a time and
+// takes a new one from `counter` when its query is done, so a warp's lanes stay busy while the
+// traversal lengths of neighbouring queries differ by orders of magnitude.  Lanes refill together
+// (one atomic per warp) once at least `kRefill` of them are idle.  A query is still processed by
+// exactly one lane, in the same order, so its result is that of a plain per-thread traversal.
+//   start(q)  -> bool:  set up query q, false = nothing to traverse (finish(q) still runs)
+//   step()    -> bool:  one traversal step of the lane's query, false = done
+//   finish(q):          write the result of query q
+template <class Start, class Step, class Finish>
+__device__ __forceinline__ void work_queue(uint32_t* counter, uint32_t nq, Start start, Step step,
+                                           Finish finish) {
+  constexpr unsigned kAll = 0xFFFFFFFFu;
+  constexpr int kRefill = 8;
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t q = kNone;
+  bool drained = false;  // the counter has passed nq
+  for (;;) {
+    const unsigned idle = __ballot_sync(kAll, q == kNone);
+    if (!drained && (idle == kAll || __popc(idle) >= kRefill)) {
+      const int leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(idle));
+      base = __shfl_sync(kAll, base, leader);
+      if (base + (uint32_t)__popc(idle) >= nq) drained = true;
+      if (q == kNone) {
+        const uint32_t cand = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+        if (cand < nq) {
+          q = cand;
+          if (!start(q)) {
+            finish(q);
+            q = kNone;
+          }
+        }
       }
-    } else {
-      nodei = __float_as_int(h.w);
+    }
+    if (__all_sync(kAll, q == kNone) && drained) break;
+    if (q != kNone && !step()) {
+      finish(q);
+      q = kNone;
     }
   }
-  return found;
 }
 
 }  // namespace xrt

@@ -7,8 +7,9 @@
 // what makes the sorted primitive order and the neighbor lists bit-identical to the reference's.
 //
 // Per 8-bit pass: (1) one block per 2048-key tile counts its digits (digit-major histogram);
-// (2) one block scans the histogram into global offsets; (3) each tile ranks its keys stably
-// (warp match + per-warp digit counts in shared memory, items in tile order) and scatters.
+// (2) the histogram is scanned into global offsets (one block, or three phases when large);
+// (3) each tile ranks its keys stably (warp match + per-warp digit counts in shared memory, items
+// in tile order) and scatters.
 #include "common.cuh"
 #include "context.h"
 
@@ -37,7 +38,81 @@ __global__ void __launch_bounds__(kThreads) k_histogram(const uint32_t* __restri
   hist[threadIdx.x * num_tiles + blockIdx.x] = s_count[threadIdx.x];
 }
 
-// Exclusive scan of `count` entries by one block of 1024 threads.
+// Exclusive scan of the digit-major histogram in three phases: each block of 1024 threads scans
+// kScanChunk consecutive entries (4 per thread, coalesced) and records its total; one block scans
+// the totals; each block adds its offset.  Integer sums, so the result does not depend on the
+// split.
+constexpr int kScanChunk = 4096;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan_1024(uint32_t v, uint32_t* s_warp,
+                                                             uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = s_warp[lane];
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, off);
+      if (lane >= off) w += y;
+    }
+    s_warp[lane] = w;  // inclusive warp totals
+  }
+  __syncthreads();
+  const uint32_t before = warp > 0 ? s_warp[warp - 1] : 0u;
+  if (total) *total = s_warp[31];
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_chunks(uint32_t* __restrict__ data, uint32_t count,
+                                                      uint32_t* __restrict__ sums) {
+  __shared__ uint32_t s_warp[32];
+  const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * 4;
+  uint32_t v[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) v[r] = base + r < count ? data[base + r] : 0u;
+  const uint32_t mine = v[0] + v[1] + v[2] + v[3];
+  uint32_t total = 0;
+  uint32_t run = block_exclusive_scan_1024(mine, s_warp, &total);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    if (base + r < count) data[base + r] = run;
+    run += v[r];
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// Exclusive scan of the chunk totals (one block; `n` small) in place.
+__global__ void __launch_bounds__(1024) k_scan_sums(uint32_t* __restrict__ sums, uint32_t n) {
+  __shared__ uint32_t s_warp[32];
+  uint32_t carry = 0;
+  for (uint32_t b = 0; b < n; b += 1024) {
+    const uint32_t i = b + threadIdx.x;
+    const uint32_t v = i < n ? sums[i] : 0u;
+    uint32_t total = 0;
+    const uint32_t ex = block_exclusive_scan_1024(v, s_warp, &total);
+    if (i < n) sums[i] = carry + ex;
+    carry += total;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_add(uint32_t* __restrict__ data, uint32_t count,
+                                                   const uint32_t* __restrict__ sums) {
+  const uint32_t off = sums[blockIdx.x];
+  const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * 4;
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+    if (base + r < count) data[base + r] += off;
+}
+
+// Exclusive scan of `count` entries by one block of 1024 threads (small histograms).
 __global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ data, uint32_t count) {
   __shared__ uint32_t s_part[1024];
   const uint32_t per = (count + 1023) / 1024;
@@ -119,7 +194,9 @@ cudaError_t RadixSort::reserve(uint32_t n) {
   cudaError_t e = keys_tmp.reserve(n);
   if (e == cudaSuccess) e = vals_tmp.reserve(n);
   const uint32_t tiles = (n + kTile - 1) / kTile;
-  if (e == cudaSuccess) e = hist.reserve((size_t)kRadix * (tiles ? tiles : 1));
+  const size_t entries = (size_t)kRadix * (tiles ? tiles : 1);
+  if (e == cudaSuccess) e = hist.reserve(entries);
+  if (e == cudaSuccess) e = sums.reserve((entries + kScanChunk - 1) / kScanChunk);
   return e;
 }
 
@@ -133,7 +210,15 @@ void RadixSort::sort(uint32_t* keys, uint32_t* vals, uint32_t n, int bits, cudaS
     const uint32_t tiles = (n + kTile - 1) / kTile;
     for (int shift = 0; shift < bits; shift += 8) {
       k_histogram<<<tiles, kThreads, 0, s>>>(k_in, n, shift, tiles, hist.p);
-      k_scan<<<1, 1024, 0, s>>>(hist.p, kRadix * tiles);
+      const uint32_t entries = kRadix * tiles;
+      if (entries <= 4 * kScanChunk) {
+        k_scan<<<1, 1024, 0, s>>>(hist.p, entries);
+      } else {
+        const uint32_t chunks = (entries + kScanChunk - 1) / kScanChunk;
+        k_scan_chunks<<<chunks, 1024, 0, s>>>(hist.p, entries, sums.p);
+        k_scan_sums<<<1, 1024, 0, s>>>(sums.p, chunks);
+        k_scan_add<<<chunks, 1024, 0, s>>>(hist.p, entries, sums.p);
+      }
       k_scatter<<<tiles, kThreads, 0, s>>>(k_in, v_in, k_out, v_out, n, shift, tiles, hist.p);
       uint32_t* t = k_in;
       k_in = k_out;

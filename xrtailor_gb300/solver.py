@@ -204,6 +204,7 @@ class ClothSolver:
     def __init__(self, params=None, device: int = 0):
         self._lib = L.load()
         self._h = C.c_void_p()
+        self.device = int(device)
         L.check(self._lib.xrt_create(C.byref(self._h), int(device)), None, "xrt_create")
         if params is None:
             params = L.SwiftParams()
