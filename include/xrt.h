@@ -167,7 +167,8 @@ xrt_status xrt_add_instance(xrt_ctx* ctx, const xrt_cloth_desc* cloth,
 xrt_status xrt_set_coloring(xrt_ctx* ctx, int32_t kind, const uint32_t* colors, uint32_t n);
 /* Per-edge stretch / per-bend compliance (FABRIC.*_COMPLIANCE per element).  Before or after start. */
 xrt_status xrt_set_compliance(xrt_ctx* ctx, int32_t kind, const float* compliance, uint32_t n);
-/* Per-vertex inverse mass override (Node::inv_mass, PhysicsMeshHelper.cu:139 gives 1 / 0 pinned). */
+/* Per-vertex inverse mass override (Node::inv_mass, PhysicsMeshHelper.cu:139 gives 1 / 0 pinned).
+ * Before start any values; after start new masses for the free vertices (pinned stay 0). */
 xrt_status xrt_set_inv_mass(xrt_ctx* ctx, const float* inv_mass, uint32_t n);
 /* ClothSolverUniversal::Start (ClothSolver.cpp:46-93): normals, obstacle LBVH, R-triangles,
  * spatial hash, coloring, LRA, device upload. */
@@ -235,6 +236,8 @@ xrt_status xrt_get_bends(const xrt_ctx* ctx, uint32_t* out4, float* rest_angles)
 xrt_status xrt_get_coloring(const xrt_ctx* ctx, int32_t kind, uint32_t* colors);
 xrt_status xrt_get_lra(const xrt_ctx* ctx, uint32_t* src, uint32_t* tgt, float* rest);
 xrt_status xrt_get_obstacle_rtri(const xrt_ctx* ctx, uint32_t* masks);
+/* Per-vertex inverse mass as set (0 = pinned): num_vertices floats. */
+xrt_status xrt_get_inv_mass(const xrt_ctx* ctx, float* out);
 /* Obstacle LBVH as built at the last frame start (BVH::Construct, BVH.cu:618-722) and refit
  * by the last collision pass.  sorted_morton/sorted_objects: num_obstacle_triangles;
  * nodes: 4 int32 per node (parent, left, right, object; 0xFFFFFFFF = none), 2F-1 nodes;

@@ -326,7 +326,7 @@ class OracleLbvh:
         qa = _f(q).reshape(-1)
         nq = qa.size // (3 if kind == 0 else 6)
         counts = np.empty(nq, np.uint32)
-        cands = np.empty((nq, 256), np.uint32)
+        cands = np.zeros((nq, 256), np.uint32)  # slots past a query's count stay 0
         self._l.orc_lbvh_query(self._h, kind, qa.ctypes.data_as(FP), nq, counts.ctypes.data_as(UP),
                                cands.ctypes.data_as(UP))
         return counts, cands

@@ -99,6 +99,14 @@ class Sizes(C.Structure):
     ]
 
 
+class Grads(C.Structure):
+    """xrt_grads (include/xrt_diff.h): output pointers, any may be NULL."""
+    _fields_ = [("stretch_compliance", C.POINTER(C.c_float)),
+                ("bend_compliance", C.POINTER(C.c_float)),
+                ("mass", C.POINTER(C.c_float)), ("velocity", C.POINTER(C.c_float)),
+                ("position", C.POINTER(C.c_float))]
+
+
 class Profile(C.Structure):
     _fields_ = [("ms", C.c_double * 16), ("launches", C.c_uint64 * 16), ("units", C.c_uint64 * 16),
                 ("frames", C.c_uint32), ("reserved", C.c_uint32 * 7)]
@@ -150,6 +158,7 @@ SIGNATURES = {
     "xrt_get_coloring": (C.c_int32, [P, C.c_int32, UP]),
     "xrt_get_lra": (C.c_int32, [P, UP, UP, FP]),
     "xrt_get_obstacle_rtri": (C.c_int32, [P, UP]),
+    "xrt_get_inv_mass": (C.c_int32, [P, FP]),
     "xrt_export_obstacle_bvh": (C.c_int32, [P, UP, UP, UP, FP, IP, IP]),
     "xrt_export_contacts": (C.c_int32, [P, IP, FP, IP, FP, FP]),
     "xrt_export_neighbors": (C.c_int32, [P, UP]),
@@ -174,6 +183,10 @@ SIGNATURES = {
     "xrt_export_cloth_bvh": (C.c_int32, [P, UP, UP, UP, FP, IP, IP]),
     "xrt_get_predicted": (C.c_int32, [P, FP]),
     "xrt_set_predicted": (C.c_int32, [P, FP]),
+    # include/xrt_diff.h
+    "xrt_diff_begin": (C.c_int32, [P]),
+    "xrt_backward": (C.c_int32, [P, FP, FP, C.POINTER(Grads)]),
+    "xrt_diff_end": (C.c_int32, [P]),
 }
 
 _lib = None

@@ -33,15 +33,6 @@ struct xrt_lbvh {
 
 namespace {
 
-#define XRT_CUDA(ctxp, expr)                                                          \
-  do {                                                                                \
-    cudaError_t e_ = (expr);                                                          \
-    if (e_ != cudaSuccess) {                                                          \
-      (ctxp)->set_error(std::string(#expr) + ": " + cudaGetErrorString(e_));          \
-      return XRT_ERR_CUDA;                                                            \
-    }                                                                                 \
-  } while (0)
-
 xrt_status check_device(int device, std::string& why) {
   int count = 0;
   cudaError_t e = cudaGetDeviceCount(&count);
@@ -97,21 +88,6 @@ xrt_status validate_params(const xrt_swift_params& p, std::string& why) {
   return XRT_ERR_INVALID_CONFIG;
 }
 
-xrt::FrameConst frame_const(const Context& c) {
-  const xrt_swift_params& p = c.params;
-  xrt::FrameConst k;
-  k.dt = p.frame_time / (float)p.num_substeps;
-  k.gx = p.gravity[0];
-  k.gy = p.gravity[1];
-  k.gz = p.gravity[2];
-  k.damping = p.damping;
-  k.relaxation = p.relaxation_factor;
-  k.lra_stretch = p.long_range_stretchiness;
-  k.friction = p.friction;
-  k.particle_diameter = c.particle_diameter;
-  return k;
-}
-
 enum Phase {
   kPredict = 0, kHash, kCollide, kBvhBuild, kObstaclePass, kGenerate, kStretch, kBend, kLra,
   kVfSolve, kEeApply, kObstacleCommit
@@ -162,7 +138,7 @@ void collect_profile(Context& c) {
 // The launch sequence of one frame (ClothSolverBase::SimulateSwift, ClothSolverBase.cpp:171-261).
 void record_frame(Context& c) {
   const xrt_swift_params& p = c.params;
-  const xrt::FrameConst k = frame_const(c);
+  const xrt::FrameConst k = xrt::frame_const(c);
   float4* const x_start = c.x.p;
   int swaps = 0;
   auto swap_x = [&]() {
@@ -410,6 +386,7 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   cudaSetDevice(c.device);
   if (c.stream) cudaStreamSynchronize(c.stream);
   if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+  xrt::diff_release(c);
   for (auto& e : c.prof_events) {
     cudaEventDestroy(e.a);
     cudaEventDestroy(e.b);
@@ -706,9 +683,24 @@ xrt_status xrt_set_inv_mass(xrt_ctx* h, const float* w, uint32_t n) {
     c.set_error("inverse-mass count does not match the vertex count");
     return XRT_ERR_INVALID_ARGUMENT;
   }
-  if (c.started) {
-    c.set_error("xrt_set_inv_mass after xrt_start");
-    return XRT_ERR_STATE;
+  if (!c.started) {
+    c.h_w.assign(w, w + n);
+    return XRT_OK;
+  }
+  // after start: new masses for the free vertices; the set of pinned vertices (inverse mass 0)
+  // fixes the LRA mode and stays as it was
+  for (uint32_t i = 0; i < n; ++i)
+    if ((w[i] > 0.0f) != (c.h_w[i] > 0.0f) || !(w[i] >= 0.0f)) {
+      c.set_error("xrt_set_inv_mass after xrt_start must keep the pinned vertices (inverse mass 0)");
+      return XRT_ERR_INVALID_ARGUMENT;
+    }
+  cudaSetDevice(c.device);
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  std::vector<float4> x(c.nv);
+  for (DBuf<float4>* b : {&c.x, &c.x_alt}) {
+    XRT_CUDA(&c, cudaMemcpy(x.data(), b->p, sizeof(float4) * c.nv, cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < c.nv; ++i) x[i].w = w[i];
+    XRT_CUDA(&c, cudaMemcpy(b->p, x.data(), sizeof(float4) * c.nv, cudaMemcpyHostToDevice));
   }
   c.h_w.assign(w, w + n);
   return XRT_OK;
@@ -879,6 +871,8 @@ xrt_status xrt_start(xrt_ctx* h) {
       XRT_CUDA(&c, upload(T.foot, S.foot, c.stream));
       XRT_CUDA(&c, upload(T.meta, meta, c.stream));
       XRT_CUDA(&c, upload(T.lofs, lofs, c.stream));
+      c.h_tile_meta[kind] = meta;
+      c.h_tile_lofs[kind] = lofs;
       (kind == 0 ? c.s_perm : c.b_perm) = S.order;
       (kind == 0 ? c.s_local : c.b_local) = S.local_slot;
       continue;
@@ -1099,6 +1093,7 @@ xrt_status xrt_step_frame(xrt_ctx* h) {
     xrt_status st = xrt::prox_prepare(c);
     if (st != XRT_OK) return st;
   }
+  if (c.diff.active) xrt::diff_checkpoint(c);  // state at the frame start, for xrt_backward
   if (c.profiling) {
     record_frame(c);
     XRT_CUDA(&c, cudaGetLastError());
@@ -1313,6 +1308,11 @@ xrt_status xrt_get_lra(const xrt_ctx* h, uint32_t* src, uint32_t* tgt, float* re
 xrt_status xrt_get_obstacle_rtri(const xrt_ctx* h, uint32_t* masks) {
   if (!h || !masks) return XRT_ERR_INVALID_ARGUMENT;
   std::copy(h->c.h_ortri.begin(), h->c.h_ortri.end(), masks);
+  return XRT_OK;
+}
+xrt_status xrt_get_inv_mass(const xrt_ctx* h, float* out) {
+  if (!h || !out) return XRT_ERR_INVALID_ARGUMENT;
+  std::copy(h->c.h_w.begin(), h->c.h_w.end(), out);
   return XRT_OK;
 }
 

@@ -22,15 +22,6 @@ using xrt::Context;
 
 namespace {
 
-#define XC_CUDA(ctxp, expr)                                                  \
-  do {                                                                       \
-    cudaError_t e_ = (expr);                                                 \
-    if (e_ != cudaSuccess) {                                                 \
-      (ctxp)->set_error(std::string(#expr) + ": " + cudaGetErrorString(e_)); \
-      return XRT_ERR_CUDA;                                                   \
-    }                                                                        \
-  } while (0)
-
 template <typename T>
 cudaError_t put(xrt::DBuf<T>& d, const std::vector<T>& h, cudaStream_t s) {
   cudaError_t e = d.reserve(h.empty() ? 1 : h.size());
@@ -108,21 +99,21 @@ xrt_status xrt::prox_prepare(Context& c) {
                   uedge, eadj);
   }
   cudaStream_t s = c.stream;
-  XC_CUDA(&c, put(c.prox.face, face, s));
-  XC_CUDA(&c, put(c.prox.fedge, fedge, s));
-  XC_CUDA(&c, put(c.prox.fn0, fn0, s));
-  XC_CUDA(&c, put(c.prox.edge, uedge, s));
-  XC_CUDA(&c, put(c.prox.eadj, eadj, s));
-  XC_CUDA(&c, put(c.prox.cfree, c.h_cfree, s));
-  XC_CUDA(&c, c.prox.counts.reserve(std::max(c.nf, 1u)));
-  XC_CUDA(&c, c.prox.incl.reserve(2 * (size_t)std::max(c.nf, 1u)));
-  XC_CUDA(&c, c.prox.total.reserve(2));
-  XC_CUDA(&c, c.prox.deltas.reserve(3 * (size_t)c.nv));
-  XC_CUDA(&c, c.prox.rcounts.reserve(c.nv));
-  XC_CUDA(&c, cudaMemsetAsync(c.prox.deltas.p, 0, sizeof(float) * 3 * c.nv, s));
-  XC_CUDA(&c, cudaMemsetAsync(c.prox.rcounts.p, 0, sizeof(int) * c.nv, s));
-  XC_CUDA(&c, c.prox.cbvh.reserve(c.nf));
-  XC_CUDA(&c, cudaStreamSynchronize(s));
+  XRT_CUDA(&c, put(c.prox.face, face, s));
+  XRT_CUDA(&c, put(c.prox.fedge, fedge, s));
+  XRT_CUDA(&c, put(c.prox.fn0, fn0, s));
+  XRT_CUDA(&c, put(c.prox.edge, uedge, s));
+  XRT_CUDA(&c, put(c.prox.eadj, eadj, s));
+  XRT_CUDA(&c, put(c.prox.cfree, c.h_cfree, s));
+  XRT_CUDA(&c, c.prox.counts.reserve(std::max(c.nf, 1u)));
+  XRT_CUDA(&c, c.prox.incl.reserve(2 * (size_t)std::max(c.nf, 1u)));
+  XRT_CUDA(&c, c.prox.total.reserve(2));
+  XRT_CUDA(&c, c.prox.deltas.reserve(3 * (size_t)c.nv));
+  XRT_CUDA(&c, c.prox.rcounts.reserve(c.nv));
+  XRT_CUDA(&c, cudaMemsetAsync(c.prox.deltas.p, 0, sizeof(float) * 3 * c.nv, s));
+  XRT_CUDA(&c, cudaMemsetAsync(c.prox.rcounts.p, 0, sizeof(int) * c.nv, s));
+  XRT_CUDA(&c, c.prox.cbvh.reserve(c.nf));
+  XRT_CUDA(&c, cudaStreamSynchronize(s));
   c.prox.ready = true;
   return XRT_OK;
 }
@@ -138,7 +129,7 @@ xrt_status xrt_cloth_bvh_build(xrt_ctx* h) {
   xrt_status st = prox_prepare(c);
   if (st != XRT_OK) return st;
   xrt::launch_cloth_bvh_build(c);
-  XC_CUDA(&c, cudaGetLastError());
+  XRT_CUDA(&c, cudaGetLastError());
   return XRT_OK;
 }
 
@@ -149,7 +140,7 @@ xrt_status xrt_obstacle_bvh_update_ccd(xrt_ctx* h) {
   xrt_status st = prox_prepare(c);
   if (st != XRT_OK) return st;
   xrt::launch_update_ccd(c.bvh, c.ox.p, c.ox0.p, c.otri.p, c.stream, c.err.p);
-  XC_CUDA(&c, cudaGetLastError());
+  XRT_CUDA(&c, cudaGetLastError());
   return XRT_OK;
 }
 
@@ -163,7 +154,7 @@ xrt_status xrt_proximity_update_pairs(xrt_ctx* h, float thickness, uint32_t* out
     c.set_error("build the cloth LBVH first (xrt_cloth_bvh_build)");
     return XRT_ERR_STATE;
   }
-  XC_CUDA(&c, xrt::prox_update_pairs(c, thickness));
+  XRT_CUDA(&c, xrt::prox_update_pairs(c, thickness));
   if (out_n) *out_n = c.prox.npairs;
   return XRT_OK;
 }
@@ -175,7 +166,7 @@ xrt_status xrt_proximity_solve(xrt_ctx* h, float thickness, float relaxation) {
   xrt_status st = prox_prepare(c);
   if (st != XRT_OK) return st;
   xrt::prox_solve(c, thickness, relaxation);
-  XC_CUDA(&c, cudaGetLastError());
+  XRT_CUDA(&c, cudaGetLastError());
   return XRT_OK;
 }
 
@@ -185,7 +176,7 @@ xrt_status xrt_impacts_check(xrt_ctx* h, float thickness, uint32_t* out_n) {
   cudaSetDevice(c.device);
   xrt_status st = prox_prepare(c);
   if (st != XRT_OK) return st;
-  XC_CUDA(&c, xrt::prox_check_impacts(c, thickness));
+  XRT_CUDA(&c, xrt::prox_check_impacts(c, thickness));
   if (out_n) *out_n = c.prox.nimpacts;
   return XRT_OK;
 }
@@ -194,9 +185,9 @@ xrt_status xrt_export_pairs(xrt_ctx* h, uint32_t* pairs) {
   if (!h || !pairs) return XRT_ERR_INVALID_ARGUMENT;
   Context& c = h->c;
   cudaSetDevice(c.device);
-  XC_CUDA(&c, cudaStreamSynchronize(c.stream));
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
   if (c.prox.npairs)
-    XC_CUDA(&c, cudaMemcpy(pairs, c.prox.pairs.p, 8 * (size_t)c.prox.npairs, cudaMemcpyDeviceToHost));
+    XRT_CUDA(&c, cudaMemcpy(pairs, c.prox.pairs.p, 8 * (size_t)c.prox.npairs, cudaMemcpyDeviceToHost));
   return XRT_OK;
 }
 
@@ -205,15 +196,15 @@ xrt_status xrt_export_impacts(xrt_ctx* h, float* t, float* w, float* n, uint32_t
   if (!h) return XRT_ERR_INVALID_ARGUMENT;
   Context& c = h->c;
   cudaSetDevice(c.device);
-  XC_CUDA(&c, cudaStreamSynchronize(c.stream));
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
   const size_t ni = c.prox.nimpacts;
   if (ni == 0) return XRT_OK;
-  if (t) XC_CUDA(&c, cudaMemcpy(t, c.prox.imp_t.p, 4 * ni, cudaMemcpyDeviceToHost));
-  if (w) XC_CUDA(&c, cudaMemcpy(w, c.prox.imp_w.p, 16 * ni, cudaMemcpyDeviceToHost));
-  if (nodes) XC_CUDA(&c, cudaMemcpy(nodes, c.prox.imp_nodes.p, 16 * ni, cudaMemcpyDeviceToHost));
+  if (t) XRT_CUDA(&c, cudaMemcpy(t, c.prox.imp_t.p, 4 * ni, cudaMemcpyDeviceToHost));
+  if (w) XRT_CUDA(&c, cudaMemcpy(w, c.prox.imp_w.p, 16 * ni, cudaMemcpyDeviceToHost));
+  if (nodes) XRT_CUDA(&c, cudaMemcpy(nodes, c.prox.imp_nodes.p, 16 * ni, cudaMemcpyDeviceToHost));
   if (n || is_vf) {
     std::vector<float4> hn(ni);
-    XC_CUDA(&c, cudaMemcpy(hn.data(), c.prox.imp_n.p, 16 * ni, cudaMemcpyDeviceToHost));
+    XRT_CUDA(&c, cudaMemcpy(hn.data(), c.prox.imp_n.p, 16 * ni, cudaMemcpyDeviceToHost));
     for (size_t k = 0; k < ni; ++k) {
       if (n) {
         n[3 * k] = hn[k].x;
@@ -244,8 +235,8 @@ xrt_status xrt_get_predicted(xrt_ctx* h, float* out) {
   if (!c.started) return XRT_ERR_STATE;
   cudaSetDevice(c.device);
   std::vector<float4> x(c.nv);
-  XC_CUDA(&c, cudaMemcpyAsync(x.data(), c.x.p, 16 * (size_t)c.nv, cudaMemcpyDeviceToHost, c.stream));
-  XC_CUDA(&c, cudaStreamSynchronize(c.stream));
+  XRT_CUDA(&c, cudaMemcpyAsync(x.data(), c.x.p, 16 * (size_t)c.nv, cudaMemcpyDeviceToHost, c.stream));
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
   for (uint32_t i = 0; i < c.nv; ++i) {
     out[3 * i] = x[i].x;
     out[3 * i + 1] = x[i].y;
@@ -262,8 +253,8 @@ xrt_status xrt_set_predicted(xrt_ctx* h, const float* pos) {
   std::vector<float4> x(c.nv);
   for (uint32_t i = 0; i < c.nv; ++i)
     x[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], c.h_w[i]);
-  XC_CUDA(&c, cudaMemcpyAsync(c.x.p, x.data(), 16 * (size_t)c.nv, cudaMemcpyHostToDevice, c.stream));
-  XC_CUDA(&c, cudaStreamSynchronize(c.stream));
+  XRT_CUDA(&c, cudaMemcpyAsync(c.x.p, x.data(), 16 * (size_t)c.nv, cudaMemcpyHostToDevice, c.stream));
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
   return XRT_OK;
 }
 

@@ -1,0 +1,43 @@
+// api_diff.cpp — C ABI of the adjoint (include/xrt_diff.h); the work is in diff.cu.
+#include <cuda_runtime.h>
+
+#include "../../include/xrt_diff.h"
+#include "context.h"
+
+using xrt::Context;
+
+extern "C" {
+
+xrt_status xrt_diff_begin(xrt_ctx* h) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (!c.started) {
+    c.set_error("call xrt_start first");
+    return XRT_ERR_STATE;
+  }
+  cudaSetDevice(c.device);
+  if (c.diff.active) xrt::diff_release(c);
+  return xrt::diff_prepare(c);
+}
+
+xrt_status xrt_backward(xrt_ctx* h, const float* dL_dx, const float* dL_dv,
+                        const xrt_grads* out) {
+  if (!h || !dL_dx) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  cudaSetDevice(c.device);
+  const xrt_grads none{};
+  const xrt_grads& o = out ? *out : none;
+  return xrt::diff_backward(c, dL_dx, dL_dv, o.stretch_compliance, o.bend_compliance, o.mass,
+                            o.velocity, o.position);
+}
+
+xrt_status xrt_diff_end(xrt_ctx* h) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  cudaSetDevice(c.device);
+  cudaStreamSynchronize(c.stream);
+  xrt::diff_release(c);
+  return XRT_OK;
+}
+
+}  // extern "C"

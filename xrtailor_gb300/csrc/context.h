@@ -10,6 +10,16 @@
 #include "../../include/xrt.h"
 #include "setup.h"
 
+// Returns XRT_ERR_CUDA from the enclosing function, with the failing call in the context's error.
+#define XRT_CUDA(ctxp, expr)                                                 \
+  do {                                                                       \
+    cudaError_t e_ = (expr);                                                 \
+    if (e_ != cudaSuccess) {                                                 \
+      (ctxp)->set_error(std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+      return XRT_ERR_CUDA;                                                   \
+    }                                                                        \
+  } while (0)
+
 namespace xrt {
 
 constexpr uint32_t kMaxCandidatesHost = 256;         // LBVH_MAX_BUFFER_SIZE
@@ -139,6 +149,39 @@ struct InstView {
 // ---- cloth state --------------------------------------------------------------------------------
 struct ColorRange {
   uint32_t begin, end;
+};
+
+// ---- hand-written adjoint (diff.cu) --------------------------------------------------------------
+// Between xrt_diff_begin and xrt_backward every frame start is checkpointed; the reverse pass
+// replays each frame from its checkpoint (same colors, same order: the same bits) while taping
+// the inputs of every projection, then walks the tape backwards.
+struct DiffState {
+  bool active = false;
+  uint32_t frames = 0;  // frames checkpointed since xrt_diff_begin
+  struct Checkpoint {
+    DBuf<float4> x, x0, v, ox0, ox, on;
+    uint32_t frame_index = 0;
+  };
+  std::vector<Checkpoint> ck;
+  // execution slots grouped by color, colors in forward order
+  std::vector<ColorRange> s_colors, b_colors;
+  DBuf<uint32_t> s_order, b_order;
+  DBuf<int2> s_gidx;  // per stretch execution slot: global vertex ids
+  DBuf<int4> b_gidx;  // per bend execution slot
+  // one frame of tape
+  uint32_t S = 0, I = 0, P = 0;
+  std::vector<int> it_pass;             // (substep, iteration) -> collision pass of the frame
+  DBuf<float4> t_sx;                    // S x I x E x 2: stretch inputs (x with inverse mass)
+  DBuf<float> t_sl;                     // S x I x E: stretch multipliers in
+  DBuf<float4> t_bx;                    // S x I x B x 4: bend inputs
+  DBuf<float4> t_stage, t_ee;           // S x I x V: inputs of the LRA+VF and EE launches
+  DBuf<int> t_vf_idx, t_rt_idx;         // P x V
+  DBuf<float4> t_vf_qs, t_rt_qc;        // P x V
+  DBuf<float4> t_ee_a, t_ee_b, t_ee_c;  // P x E
+  DBuf<float4> t_pred;                  // P x 3F (obstacle primitives of the pass)
+  // adjoint
+  DBuf<float4> G, G2, Gv, H, Gs;        // x-bar (+ inverse-mass bar in w), v-bar, temporaries
+  DBuf<float> cnt, lam_bar, comp_bar, bcomp_bar;
 };
 
 // Tile-local Gauss-Seidel schedule of one constraint kind on the device (setup::TileSchedule):
@@ -287,6 +330,10 @@ struct Context {
   DBuf<uint32_t> ovf_ptr, ovf_list;
   Lbvh bvh;
   ProximityState prox;
+  DiffState diff;
+  // host copies of the tile schedules (the adjoint regroups their slots by color)
+  std::vector<int4> h_tile_meta[2];
+  std::vector<uint32_t> h_tile_lofs[2];
   // error word
   DBuf<uint32_t> err;
   // per-phase profiling (eager frames only)
@@ -317,6 +364,22 @@ struct FrameConst {
   float friction;
   float particle_diameter;
 };
+
+// Per-frame constants from the parameters (dt = frame time / substeps).
+inline FrameConst frame_const(const Context& c) {
+  const xrt_swift_params& p = c.params;
+  FrameConst k;
+  k.dt = p.frame_time / (float)p.num_substeps;
+  k.gx = p.gravity[0];
+  k.gy = p.gravity[1];
+  k.gz = p.gravity[2];
+  k.damping = p.damping;
+  k.relaxation = p.relaxation_factor;
+  k.lra_stretch = p.long_range_stretchiness;
+  k.friction = p.friction;
+  k.particle_diameter = c.particle_diameter;
+  return k;
+}
 
 void launch_predict(Context& c, const FrameConst& k);
 void launch_finalize_predict(Context& c, const FrameConst& k, bool predict_next, bool normals);
@@ -349,6 +412,15 @@ xrt_status export_lbvh(Lbvh& b, cudaStream_t s, std::string& err, uint32_t* mort
                        uint32_t* nodes, float* aabbs, int32_t* iesc, int32_t* eesc, int32_t* unique);
 
 // ---- Quality-mode self contact (proximity.cu) ----------------------------------------------------
+// ---- adjoint (diff.cu) ---------------------------------------------------------------------------
+xrt_status diff_prepare(Context& c);     // schedule, tape and adjoint buffers
+void diff_checkpoint(Context& c);        // state at the start of the next frame
+// Reverse pass over the checkpointed frames; host outputs may be null (sizes: E, B, V, 3V, 3V).
+xrt_status diff_backward(Context& c, const float* dLdx, const float* dLdv, float* d_compliance,
+                         float* d_bend_compliance, float* d_mass, float* d_velocity,
+                         float* d_position);
+void diff_release(Context& c);
+
 xrt_status prox_prepare(Context& c);  // uploads the unified topology once (api_contact.cpp)
 void launch_cloth_bvh_build(Context& c);
 void launch_update_ccd(Lbvh& b, const float4* x, const float4* x0, const int4* tri, cudaStream_t s,

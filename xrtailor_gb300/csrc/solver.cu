@@ -21,6 +21,7 @@
 
 #include "common.cuh"
 #include "context.h"
+#include "project_dev.cuh"
 
 namespace xrt {
 namespace {
@@ -74,26 +75,6 @@ __global__ void k_finalize(float4* __restrict__ x, float4* __restrict__ x0, floa
     }
     nrm[i] = mk4(normalize(acc), 0.0f);
   }
-}
-
-// XPBD distance constraint on two vertices; returns true when it moved them (lam updated).
-__device__ __forceinline__ bool stretch_project(float4& a, float4& b, float rest, float compliance,
-                                                float dt, float& lam) {
-  const f3 diff = mk3(a) - mk3(b);
-  const float distance = length(diff);
-  const float w1 = a.w, w2 = b.w;
-  if (!(distance != rest && w1 + w2 > 0.0f)) return false;
-  const f3 gradient = diff / (distance + kEps);
-  const float alpha_tilde = compliance / (dt * dt);
-  const float constraint = distance - rest;
-  const float dl = (-constraint - alpha_tilde * lam) / (w1 + w2 + alpha_tilde);
-  const f3 corr = dl * gradient;
-  lam = lam + dl;
-  const f3 c1 = corr * w1;
-  const f3 c2 = -corr * w2;
-  a = make_float4(a.x + c1.x, a.y + c1.y, a.z + c1.z, a.w);
-  b = make_float4(b.x + c2.x, b.y + c2.y, b.z + c2.z, b.w);
-  return true;
 }
 
 template <bool RESET>
@@ -212,9 +193,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_stretch_tiles(
   for (uint32_t j = threadIdx.x; j < nc; j += NT) lambda[c0 + j] = sl[j];
 }
 
-// Dihedral bend projection of SolveBend_Kernel on four vertices.
-__device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3, float4& a4,
-                                             float theta, float compliance, float dt);
 // The same projection on a lane pair (lanes 2m, 2m+1 of a warp, `half` = lane & 1), for the
 // shared-memory footprint of a tile: each lane evaluates one of the two independent halves of
 // the expression (normal n1 and gradient q3 / normal n2, gradient q4 and the angle), the halves
@@ -301,39 +279,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
   tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
 }
 
-__device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3, float4& a4,
-                                             float theta, float compliance, float dt) {
-  const float w1 = a1.w, w2 = a2.w, w3 = a3.w, w4 = a4.w;
-  const f3 p1 = mk3(a1);
-  const f3 p2 = mk3(a2) - p1;
-  const f3 p3 = mk3(a3) - p1;
-  const f3 p4 = mk3(a4) - p1;
-  const f3 n1 = normalize(cross(p2, p3));
-  const f3 n2 = normalize(cross(p2, p4));
-  const float d = tclamp(dot(n1, n2), 0.0f, 1.0f);
-  const float angle = acos_as(d);  // d in [0, 1] (or NaN, rejected below)
-  if (angle < kEps || isnan(d)) return;
-  const f3 q3 = (cross(p2, n2) + cross(n1, p2) * d) / (length(cross(p2, p3)) + kEps);
-  const f3 q4 = (cross(p2, n1) + cross(n2, p2) * d) / (length(cross(p2, p4)) + kEps);
-  const f3 q2 = -(cross(p3, n2) + cross(n1, p3) * d) / (length(cross(p2, p3)) + kEps) -
-                (cross(p4, n1) + cross(n2, p4) * d) / (length(cross(p2, p4)) + kEps);
-  const f3 q1 = -q2 - q3 - q4;
-  const float xpbd_bend = compliance / dt / dt;
-  const float denom =
-      xpbd_bend + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) + w4 * dot(q4, q4));
-  if (denom < kEps) return;
-  const float lambda = sqrtf(1.0f - d * d) * (angle - theta) / denom;
-  const float scaling = 1.0f;
-  const f3 c1 = scaling * w1 * lambda * q1;
-  const f3 c2 = scaling * w2 * lambda * q2;
-  const f3 c3 = scaling * w3 * lambda * q3;
-  const f3 c4 = scaling * w4 * lambda * q4;
-  a1 = make_float4(a1.x + c1.x, a1.y + c1.y, a1.z + c1.z, w1);
-  a2 = make_float4(a2.x + c2.x, a2.y + c2.y, a2.z + c2.z, w2);
-  a3 = make_float4(a3.x + c3.x, a3.y + c3.y, a3.z + c3.z, w3);
-  a4 = make_float4(a4.x + c4.x, a4.y + c4.y, a4.z + c4.z, w4);
-}
-
 // Lane pair form of bend_project.  With (nA, nB, lA) = (n1, n2, |p2 x p3| + eps) on lane 0 and
 // (n2, n1, |p2 x p4| + eps) on lane 1, and pA = p3 / p4:
 //   q3 (lane 0) and q4 (lane 1) are both (p2 x nB + (nA x p2) d) / lA,
@@ -384,14 +329,6 @@ __device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float thet
   sx[half ? b.w : b.y] = make_float4(ab.x + cb.x, ab.y + cb.y, ab.z + cb.z, wb);
 }
 
-__device__ __forceinline__ f3 lra_project(f3 xt, f3 xs, float w_t, float rest, float stretch) {
-  const float target = rest * stretch;
-  if (w_t < kEps && target > 0) return xt;
-  const f3 diff = xt - xs;
-  const float dist = length(diff);
-  if (dist > target) xt = xt + (-diff + diff / dist * target);
-  return xt;
-}
 
 // Free slot vertices: one launch per slot over that slot's constraint block (list order).
 __global__ void k_lra_block(const uint32_t* __restrict__ tgt, const uint32_t* __restrict__ src,
@@ -407,9 +344,6 @@ __global__ void k_lra_block(const uint32_t* __restrict__ tgt, const uint32_t* __
   if (xt.x != p.x || xt.y != p.y || xt.z != p.z) x[t] = mk4(xt, p.w);
 }
 
-__device__ __forceinline__ f3 prim_normal(const float4* __restrict__ pred, int f) {
-  return face_normal(mk3(pred[3 * f]), mk3(pred[3 * f + 1]), mk3(pred[3 * f + 2]));
-}
 
 // Iteration tail, two Jacobi kernels (each reads x_in, writes x_out):
 //   k_stage: LRA (SolveGeodesicLRA_Kernel, all slots pinned: slot positions are constant in the

@@ -363,6 +363,11 @@ class ClothSolver:
         L.check(self._lib.xrt_get_lra(self._h, L.uptr(src), L.uptr(tgt), L.fptr(rest)), self._h, "lra")
         return src, tgt, rest
 
+    def inv_mass(self):
+        w = np.empty(self.sizes().num_vertices, np.float32)
+        L.check(self._lib.xrt_get_inv_mass(self._h, L.fptr(w)), self._h, "inv_mass")
+        return w
+
     def obstacle_rtri(self):
         m = np.empty(self.sizes().num_obstacle_triangles, np.uint32)
         L.check(self._lib.xrt_get_obstacle_rtri(self._h, L.uptr(m)), self._h, "rtri")
@@ -460,6 +465,34 @@ class ClothSolver:
         a = _f32(x).reshape(-1)
         L.check(self._lib.xrt_set_predicted(self._h, L.fptr(a)), self._h, "set predicted")
 
+    # -- adjoint (include/xrt_diff.h) ----------------------------------------------------------
+    def diff_begin(self):
+        """Checkpoint the following frames for backward()."""
+        L.check(self._lib.xrt_diff_begin(self._h), self._h, "diff_begin")
+
+    def backward(self, dL_dx, dL_dv=None) -> dict:
+        """Gradients of a loss on the final positions (and velocities) with respect to per-edge
+        stretch compliance, per-bend compliance, per-vertex mass, initial velocity and initial
+        position, over the frames stepped since diff_begin()."""
+        s = self.sizes()
+        gx = _f32(dL_dx).reshape(-1)
+        gv = None if dL_dv is None else _f32(dL_dv).reshape(-1)
+        out = dict(stretch_compliance=np.zeros(max(s.num_edges, 1), np.float32),
+                   bend_compliance=np.zeros(max(s.num_bends, 1), np.float32),
+                   mass=np.zeros(s.num_vertices, np.float32),
+                   velocity=np.zeros((s.num_vertices, 3), np.float32),
+                   position=np.zeros((s.num_vertices, 3), np.float32))
+        g = L.Grads(L.fptr(out["stretch_compliance"]), L.fptr(out["bend_compliance"]),
+                    L.fptr(out["mass"]), L.fptr(out["velocity"]), L.fptr(out["position"]))
+        L.check(self._lib.xrt_backward(self._h, L.fptr(gx), L.fptr(gv), C.byref(g)), self._h,
+                "backward")
+        out["stretch_compliance"] = out["stretch_compliance"][: s.num_edges]
+        out["bend_compliance"] = out["bend_compliance"][: s.num_bends]
+        return out
+
+    def diff_end(self):
+        L.check(self._lib.xrt_diff_end(self._h), self._h, "diff_end")
+
     def close(self):
         if self._h:
             self._lib.xrt_destroy(self._h)
@@ -511,7 +544,7 @@ class Lbvh:
         per = 3 if kind == 0 else 6
         nq = qa.size // per
         counts = np.empty(nq, np.uint32)
-        cands = np.empty((nq, 256), np.uint32)
+        cands = np.zeros((nq, 256), np.uint32)  # slots past a query's count stay 0
         L.check(self._lib.xrt_lbvh_query(self._h, int(kind), L.fptr(qa), nq, L.uptr(counts),
                                          L.uptr(cands)), None, "query")
         return counts, cands
