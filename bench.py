@@ -434,6 +434,117 @@ def run_batched(args, local_rank):
     }
 
 
+def run_diff(args, local_rank):
+    """The differentiation workload: `--diff-instances` sheets of `--diff-n`^2 vertices in one
+    batched context, each pinned along its top edge and falling onto its own sphere, rolled out
+    `--diff-frames` frames of 10 substeps.  The target rollout uses the seeded ground truth
+    (per-edge stretch and per-bend compliance, masses); each timed step is one gradient
+    evaluation from a uniform guess: the forward rollout with per-frame checkpoints, the L2 loss
+    against the target on the host, and the reverse pass (xrt_backward: replay + adjoint)."""
+    import torch
+    from xrtailor_gb300 import ClothSolver, build as xb, scenes
+    from xrtailor_gb300.diff import rollout as torch_rollout
+    xb.build()
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    insts = scenes.diff_batch(args.diff_instances, args.diff_n)
+    p = scenes._params(**scenes.DIFF_PARAMS)
+    S, F = p.num_substeps, args.diff_frames
+    s = ClothSolver(p, device=local_rank)
+    for d in insts:
+        s.add_instance(d.cloth, d.sphere)
+    s.start()
+    sz = s.sizes()
+    V, E, B = sz.num_vertices, sz.num_edges, sz.num_bends
+    cat = lambda f: np.concatenate([f(d) for d in insts])  # noqa: E731
+    x0, v0 = cat(lambda d: d.cloth.positions), cat(lambda d: d.velocity)
+    comp_true, bcomp_true = cat(lambda d: d.stretch_compliance), cat(lambda d: d.bend_compliance)
+    mass = cat(lambda d: d.mass)
+    assert (len(comp_true), len(bcomp_true)) == (E, B)
+    pinned = s.inv_mass() == 0.0
+    w = np.where(pinned, 0.0, 1.0 / mass).astype(np.float32)
+    comp_guess = np.full(E, 1e-6, np.float32)
+    bcomp_guess = np.full(B, 100.0, np.float32)
+    _, _, sp = s.device_state()
+    stream = torch.cuda.ExternalStream(sp, device=dev)
+
+    def forward(comp, bcomp, record):
+        s.set_compliance(0, comp)
+        s.set_compliance(1, bcomp)
+        s.set_inv_mass(w)
+        s.set_state(x0, v0)
+        if record:
+            s.diff_begin()
+        s.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            s.step(F)
+            b.record(stream)
+        torch.cuda.synchronize()
+        return s.host_positions(), a.elapsed_time(b) / 1e3
+
+    x_target, _ = forward(comp_true, bcomp_true, False)
+
+    def evaluate():
+        xf, t_fwd = forward(comp_guess, bcomp_guess, True)
+        dL = 2.0 * (xf - x_target)
+        loss = float((dL * dL).sum() / 4.0)
+        t0 = time.perf_counter()
+        g = s.backward(dL)
+        t_bwd = time.perf_counter() - t0
+        return loss, g, t_fwd, t_bwd
+
+    for _ in range(args.warmup):
+        evaluate()
+    _, t_plain = forward(comp_guess, bcomp_guess, False)
+    rec = []
+    with ClockSampler(local_rank) as clocks:
+        for _ in range(args.steps):
+            loss, g, t_fwd, t_bwd = evaluate()
+            rec.append((t_fwd, t_bwd))
+    s.diff_end()
+    t_fwd = float(np.mean([r[0] for r in rec]))
+    t_bwd = float(np.mean([r[1] for r in rec]))
+    units = V * S * F
+    value = units / (t_fwd + t_bwd)
+    # end to end: the torch.autograd binding with host tensors (uploads, reverse pass, readback)
+    tt = {k: torch.tensor(a, requires_grad=True) for k, a in
+          (("x0", x0), ("v0", v0), ("mass", mass), ("comp", comp_guess), ("bcomp", bcomp_guess))}
+    xt = torch.from_numpy(x_target)
+    t0 = time.perf_counter()
+    xf, _ = torch_rollout(s, F, tt["x0"], tt["v0"], tt["mass"], tt["comp"], tt["bcomp"])
+    ((xf - xt) ** 2).sum().backward()
+    t_e2e = time.perf_counter() - t0
+    s.diff_end()
+    grads = {"stretch_compliance": g["stretch_compliance"], "bend_compliance": g["bend_compliance"],
+             "mass": g["mass"][~pinned], "velocity": g["velocity"]}
+    s.close()
+    return {
+        "metric": "vertex-substeps/s (forward + reverse)", "value": value,
+        "unit": "vertex-substeps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * (t_fwd + t_bwd), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded: xrtailor_gb300/scenes.py diff_batch)",
+        "config": {"workload": f"diff_{len(insts)}x{args.diff_n}", "instances": len(insts),
+                   "vertices": V, "edges": E, "bends": B, "frames": F, "substeps": S,
+                   "iterations": p.num_iterations, "collision_passes": p.num_collision_passes,
+                   "checkpoint": "every frame (10 substeps)",
+                   "l2": "working set (tape) far larger than L2", "parallelism": "single"},
+        "forward_s": t_fwd, "forward_plain_s": t_plain, "backward_s": t_bwd,
+        "backward_over_forward": t_bwd / t_plain,
+        "backward_over_recorded_forward": t_bwd / t_fwd,
+        "loss": loss,
+        "grad_norms": {k: float(np.linalg.norm(v)) for k, v in grads.items()},
+        "grads_finite": bool(all(np.isfinite(v).all() for v in grads.values())),
+        "e2e": {"value": units / t_e2e, "unit": "vertex-substeps/s",
+                "h2d_bytes_per_step": int(4 * (2 * 3 * V + V + E + B) + 4 * 3 * V),
+                "d2h_bytes_per_step": int(4 * (3 * V + 3 * V + V + E + B + 3 * V)),
+                "path": "xrtailor_gb300.diff.rollout + torch backward, host tensors"},
+        "clocks": clocks.summary(),
+    }
+
+
 def run_cpu(workload, frames, warmup=1, threads=0):
     from oracle.oracle import OracleSolver, lib
     from xrtailor_gb300 import scenes
@@ -466,7 +577,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="garment",
-                    choices=["garment", "small", "heavy", "batched"])
+                    choices=["garment", "small", "heavy", "batched", "diff"])
     ap.add_argument("--cpu-frames", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--instances", type=int, default=512, help="batched workload: garments")
@@ -476,6 +587,9 @@ def main():
     ap.add_argument("--tune-instances", type=int, default=32,
                     help="batched workload: garments the launch autotuner times (0: library "
                          "defaults)")
+    ap.add_argument("--diff-instances", type=int, default=16)
+    ap.add_argument("--diff-n", type=int, default=128)
+    ap.add_argument("--diff-frames", type=int, default=60)
     ap.add_argument("--tile-vertices", type=int, default=None,
                     help="tile size of the Gauss-Seidel schedule (library default if omitted)")
     args = ap.parse_args()
@@ -504,6 +618,10 @@ def main():
     if args.workload == "batched":
         if rank == 0:
             print(json.dumps(run_batched(args, local_rank)))
+        return
+    if args.workload == "diff":
+        if rank == 0:
+            print(json.dumps(run_diff(args, local_rank)))
         return
     if world > 1:
         import torch

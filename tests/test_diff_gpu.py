@@ -25,7 +25,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _setup(n=16, obstacle=False, seed=0, substeps=3, iterations=4, passes=1, bending=True,
-           bend_compliance=1e-5):
+           bend_compliance=1e-5, tile=None):
     # with the obstacle the sheet starts 5 mm into the sphere's cap: VF, RT and EE records
     cloth = scenes.grid_cloth(n, 0.4, origin=(0.3, 0.295 if obstacle else 0.6, 0.3),
                               jitter=1e-3, seed=seed + 1)
@@ -37,6 +37,8 @@ def _setup(n=16, obstacle=False, seed=0, substeps=3, iterations=4, passes=1, ben
                        enable_self_collision=0, solve_bending=int(bending),
                        num_collision_passes=passes, update_obstacle_animation=0)
     s = ClothSolver(p)
+    if tile is not None:
+        s.set_tile_vertices(tile)
     s.add_cloth(cloth, particle_diameter=0.02)
     obs = None
     if obstacle:
@@ -101,9 +103,15 @@ def _check(s, p, pinned, a, c, contacts, cv=None, factor=4.0, floor=2e-4, forwar
     return errs
 
 
-def test_adjoint_matches_fp64_reference_without_bending(xrt):
+# schedules: the default tiles, small tiles (many tile colors: the tiled replay and reverse
+# launch per tile color), none (one launch per color)
+TILES = [None, 32, 0]
+
+
+@pytest.mark.parametrize("tile", TILES)
+def test_adjoint_matches_fp64_reference_without_bending(xrt, tile):
     """Two frames of 3 substeps x 4 iterations: stretch, LRA, predict, finalize."""
-    s, p, obs, pinned, a = _setup(n=16, bending=False)
+    s, p, obs, pinned, a = _setup(n=16, bending=False, tile=tile)
     s.diff_begin()
     s.step()
     s.step()
@@ -111,20 +119,26 @@ def test_adjoint_matches_fp64_reference_without_bending(xrt):
     _check(s, p, pinned, a, c, [[None], [None]])
 
 
-def test_adjoint_matches_fp64_reference_with_stiff_bending_one_substep(xrt):
-    s, p, obs, pinned, a = _setup(n=16, substeps=1, iterations=1, bend_compliance=1e-5)
+@pytest.mark.parametrize("tile", TILES)
+def test_adjoint_matches_fp64_reference_with_stiff_bending_one_substep(xrt, tile):
+    s, p, obs, pinned, a = _setup(n=16, substeps=1, iterations=1, bend_compliance=1e-5,
+                                  tile=tile)
     s.diff_begin()
     s.step()
     c = np.random.default_rng(6).normal(size=(len(a["x0"]), 3)).astype(np.float32)
     _check(s, p, pinned, a, c, [[None]])
 
 
-def test_adjoint_matches_fp64_reference_with_soft_bending(xrt):
-    s, p, obs, pinned, a = _setup(n=16, substeps=2, iterations=2, bend_compliance=1e-2)
+@pytest.mark.parametrize("tile", TILES)
+def test_adjoint_matches_fp64_reference_with_soft_bending(xrt, tile):
+    s, p, obs, pinned, a = _setup(n=16, substeps=2, iterations=2, bend_compliance=1e-2,
+                                  tile=tile)
     s.diff_begin()
     s.step()
     c = np.random.default_rng(7).normal(size=(len(a["x0"]), 3)).astype(np.float32)
-    _check(s, p, pinned, a, c, [[None]])
+    # four bend sweeps on a folding sheet: the float32 trajectories (library, torch) part
+    # further than in the other cases, hence the wider multiple of the float32 floor
+    _check(s, p, pinned, a, c, [[None]], factor=6.0)
 
 
 def test_adjoint_matches_fp64_reference_with_obstacle_contacts(xrt):
@@ -231,10 +245,11 @@ def test_batched_adjoint_matches_single_contexts(xrt):
         bb += sz.num_bends
 
 
-def test_backward_leaves_the_rollout_unchanged(xrt):
+@pytest.mark.parametrize("tile", TILES)
+def test_backward_leaves_the_rollout_unchanged(xrt, tile):
     """Stepping on after a reverse pass gives the same bits as a context that never ran one."""
-    s, p, obs, pinned, a = _setup(n=10, obstacle=True, passes=3)
-    t, _, _, _, _ = _setup(n=10, obstacle=True, passes=3)
+    s, p, obs, pinned, a = _setup(n=16, obstacle=True, passes=3, tile=tile)
+    t, _, _, _, _ = _setup(n=16, obstacle=True, passes=3, tile=tile)
     s.diff_begin()
     for solver in (s, t):
         solver.step()

@@ -847,6 +847,7 @@ xrt_status xrt_start(xrt_ctx* h) {
       T.on = true;
       T.num_local = S.num_local;
       T.max_foot = S.max_footprint;
+      T.foot_len = S.foot.size();
       T.max_cons = 0;
       T.max_step = 0;
       for (size_t tt = 0; tt + 1 < S.foot_ptr.size(); ++tt)

@@ -171,9 +171,15 @@ struct DiffState {
   // one frame of tape
   uint32_t S = 0, I = 0, P = 0;
   std::vector<int> it_pass;             // (substep, iteration) -> collision pass of the frame
+  // per-color schedule: every projection's inputs; tiled schedule (s_tiled / b_tiled): the same
+  // arrays sized for one iteration are the reverse's per-slot scratch, and the tape holds each
+  // tile's entry footprint (t_fs, t_fb: S x I x footprint entries) and multipliers (t_lam)
+  bool s_tiled = false, b_tiled = false;
   DBuf<float4> t_sx;                    // S x I x E x 2: stretch inputs (x with inverse mass)
   DBuf<float> t_sl;                     // S x I x E: stretch multipliers in
   DBuf<float4> t_bx;                    // S x I x B x 4: bend inputs
+  DBuf<float4> t_fs, t_fb;              // S x I x stretch / bend footprint entries
+  DBuf<float> t_lam;                    // S x I x E: stretch multipliers at iteration start
   DBuf<float4> t_stage, t_ee;           // S x I x V: inputs of the LRA+VF and EE launches
   DBuf<int> t_vf_idx, t_rt_idx;         // P x V
   DBuf<float4> t_vf_qs, t_rt_qc;        // P x V
@@ -203,6 +209,7 @@ struct TiledSet {
   DBuf<int4> meta;                      // per executed tile {first footprint, footprint size,
                                         //  first constraint, constraint count}
   DBuf<uint32_t> lofs;                  // per executed tile: num_local + 1 offsets, tile-relative
+  size_t foot_len = 0;                  // entries of `foot` (footprints of all tiles)
 };
 
 // Quality-mode self contact (proximity.cu): unified numbering, cloth first then obstacle.

@@ -23,6 +23,9 @@
 // independent, so each backward launch updates the adjoints of its vertices without atomics; the
 // inverse-mass adjoint rides in the w lane of the position adjoint.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "common.cuh"
 #include "context.h"
@@ -87,31 +90,17 @@ __device__ __forceinline__ void cross_bwd(f3 a, f3 b, f3 cb, f3& ab, f3& bb) {
   bb = bb + cross(cb, a);
 }
 
-// XPBD distance: inputs (a, b, lambda), outputs (a', b', lambda').  G holds x-bar (xyz) and the
-// accumulated inverse-mass bar (w); lam_bar holds lambda'-bar on entry, lambda-bar on exit.
-template <bool RESET>
-__global__ void k_stretch_bwd(const uint32_t* __restrict__ order, uint32_t begin, uint32_t end,
-                              const int2* __restrict__ gidx, const int4* __restrict__ con,
-                              const float4* __restrict__ tx, const float* __restrict__ tl,
-                              float4* __restrict__ G, float* __restrict__ lam_bar,
-                              float* __restrict__ comp_bar, float dt) {
-  const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= end) return;
-  const uint32_t j = order[k];
-  const int2 g = gidx[j];
-  const int4 c = con[j];
-  const float rest = __int_as_float(c.z), comp = __int_as_float(c.w);
-  const float4 A = tx[2 * (size_t)j], B = tx[2 * (size_t)j + 1];
-  const float lam = tl[j];
-  const float lbo = lam_bar[j];
+// XPBD distance (stretch_project): inputs (a, b, lambda), outputs (a', b', lambda').  ga, gb hold
+// the outputs' adjoints on entry (xyz; w accumulates the inverse-mass adjoint) and the inputs'
+// on exit; lbo is lambda'-bar.  Returns false for an inactive projection (the identity: nothing
+// changes, lambda-bar = lbo); else sets lam_in_bar and adds the compliance adjoint to cbar.
+__device__ __forceinline__ bool stretch_vjp(float4 A, float4 B, float lam, float rest, float comp,
+                                            float dt, float lbo, float4& ga, float4& gb,
+                                            float& lam_in_bar, float& cbar) {
   const f3 d = mk3(A) - mk3(B);
   const float dist = length(d);
   const float wa = A.w, wb = B.w;
-  if (!(dist != rest && wa + wb > 0.0f)) {  // not projected: identity (lambda' = lambda or 0)
-    lam_bar[j] = RESET ? 0.0f : lbo;
-    return;
-  }
-  const float4 ga = G[g.x], gb = G[g.y];
+  if (!(dist != rest && wa + wb > 0.0f)) return false;
   const float e = dist + kEps;
   const f3 n = d / e;
   const float at = comp / (dt * dt);
@@ -129,15 +118,40 @@ __global__ void k_stretch_bwd(const uint32_t* __restrict__ order, uint32_t begin
   const float D_bar = -dl_bar * dl / D;
   const float C_bar = -N_bar;            // N = -C - at lambda
   const float at_bar = -N_bar * lam + D_bar;
-  const float lam_in_bar = lbo - N_bar * at;
+  lam_in_bar = lbo - N_bar * at;
   wa_bar += D_bar;
   wb_bar += D_bar;
   const float dist_bar = C_bar - dot(n_bar, n) / e;  // n = d / (dist + eps)
   const f3 d_bar = n_bar / e + (dist > 0.0f ? (dist_bar / dist) * d : mk3(0, 0, 0));
-  G[g.x] = mk4(mk3(ga) + d_bar, ga.w + wa_bar);
-  G[g.y] = mk4(mk3(gb) - d_bar, gb.w + wb_bar);
-  lam_bar[j] = RESET ? 0.0f : lam_in_bar;
-  comp_bar[j] += at_bar / (dt * dt);
+  ga = mk4(mk3(ga) + d_bar, ga.w + wa_bar);
+  gb = mk4(mk3(gb) - d_bar, gb.w + wb_bar);
+  cbar += at_bar / (dt * dt);
+  return true;
+}
+
+// Per color: G holds x-bar and the inverse-mass bar; lam_bar holds lambda'-bar on entry,
+// lambda-bar on exit (0 when RESET: the iteration started from lambda = 0).
+template <bool RESET>
+__global__ void k_stretch_bwd(const uint32_t* __restrict__ order, uint32_t begin, uint32_t end,
+                              const int2* __restrict__ gidx, const int4* __restrict__ con,
+                              const float4* __restrict__ tx, const float* __restrict__ tl,
+                              float4* __restrict__ G, float* __restrict__ lam_bar,
+                              float* __restrict__ comp_bar, float dt) {
+  const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= end) return;
+  const uint32_t j = order[k];
+  const int2 g = gidx[j];
+  const int4 c = con[j];
+  const float lbo = lam_bar[j];
+  float4 ga = G[g.x], gb = G[g.y];
+  float lin = lbo, cb = 0.0f;
+  if (stretch_vjp(tx[2 * (size_t)j], tx[2 * (size_t)j + 1], tl[j], __int_as_float(c.z),
+                  __int_as_float(c.w), dt, lbo, ga, gb, lin, cb)) {
+    G[g.x] = ga;
+    G[g.y] = gb;
+    comp_bar[j] += cb;
+  }
+  lam_bar[j] = RESET ? 0.0f : lin;
 }
 
 // d/dx of acos_as (the polynomial of common.cuh): sqrt(1-x) P'(x) - P(x) / (2 sqrt(1-x)).
@@ -155,17 +169,11 @@ __device__ __forceinline__ float acos_as_deriv(float x) {
 }
 
 // Dihedral bend: inputs x1..x4 (w in .w), outputs x_i' = x_i + w_i lambda q_i.
-__global__ void k_bend_bwd(const uint32_t* __restrict__ order, uint32_t begin, uint32_t end,
-                           const int4* __restrict__ gidx, const float2* __restrict__ tc,
-                           const float4* __restrict__ tx, float4* __restrict__ G,
-                           float* __restrict__ bcomp_bar, float dt) {
-  const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= end) return;
-  const uint32_t j = order[k];
-  const int4 b = gidx[j];
-  const float theta = tc[j].x, comp = tc[j].y;
-  const float4* t = tx + 4 * (size_t)j;
-  const float4 A1 = t[0], A2 = t[1], A3 = t[2], A4 = t[3];
+// G1..G4 hold the outputs' adjoints on entry and the inputs' on exit; returns false for an
+// inactive projection (the identity), else adds the compliance adjoint to cbar.
+__device__ __forceinline__ bool bend_vjp(float4 A1, float4 A2, float4 A3, float4 A4, float theta,
+                                         float comp, float dt, float4& G1, float4& G2, float4& G3,
+                                         float4& G4, float& cbar) {
   const float w1 = A1.w, w2 = A2.w, w3 = A3.w, w4 = A4.w;
   const f3 p1 = mk3(A1);
   const f3 p2 = mk3(A2) - p1, p3 = mk3(A3) - p1, p4 = mk3(A4) - p1;
@@ -174,7 +182,7 @@ __global__ void k_bend_bwd(const uint32_t* __restrict__ order, uint32_t begin, u
   const float draw = dot(n1, n2);
   const float d = tclamp(draw, 0.0f, 1.0f);
   const float angle = acos_as(d);
-  if (angle < kEps || isnan(d)) return;  // not projected: identity
+  if (angle < kEps || isnan(d)) return false;  // not projected: identity
   const float L23 = length(c23), L24 = length(c24);
   const float e23 = L23 + kEps, e24 = L24 + kEps;
   const f3 B3 = cross(n1, p2), B4 = cross(n2, p2), B23 = cross(n1, p3), B24 = cross(n2, p4);
@@ -188,10 +196,9 @@ __global__ void k_bend_bwd(const uint32_t* __restrict__ order, uint32_t begin, u
   const float at = comp / dt / dt;
   const float denom = at + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) +
                             w4 * dot(q4, q4));
-  if (denom < kEps) return;
+  if (denom < kEps) return false;
   const float s = sqrtf(1.0f - d * d);
   const float lam = s * (angle - theta) / denom;
-  const float4 G1 = G[b.x], G2 = G[b.y], G3 = G[b.z], G4 = G[b.w];
   const f3 g1 = mk3(G1), g2 = mk3(G2), g3 = mk3(G3), g4 = mk3(G4);
   // c_i = w_i lam q_i
   const float lam_bar = w1 * dot(g1, q1) + w2 * dot(g2, q2) + w3 * dot(g3, q3) + w4 * dot(g4, q4);
@@ -211,7 +218,7 @@ __global__ void k_bend_bwd(const uint32_t* __restrict__ order, uint32_t begin, u
   w2b += denom_bar * dot(q2, q2);
   w3b += denom_bar * dot(q3, q3);
   w4b += denom_bar * dot(q4, q4);
-  bcomp_bar[j] += denom_bar / dt / dt;
+  cbar += denom_bar / dt / dt;
   // q1 = -q2 - q3 - q4
   q2b = q2b - q1b;
   q3b = q3b - q1b;
@@ -252,10 +259,274 @@ __global__ void k_bend_bwd(const uint32_t* __restrict__ order, uint32_t begin, u
   cross_bwd(p2, p3, c23b, p2b, p3b);
   cross_bwd(p2, p4, c24b, p2b, p4b);
   const f3 p1b = -(p2b + p3b + p4b);
-  G[b.x] = mk4(g1 + p1b, G1.w + w1b);
-  G[b.y] = mk4(g2 + p2b, G2.w + w2b);
-  G[b.z] = mk4(g3 + p3b, G3.w + w3b);
-  G[b.w] = mk4(g4 + p4b, G4.w + w4b);
+  G1 = mk4(g1 + p1b, G1.w + w1b);
+  G2 = mk4(g2 + p2b, G2.w + w2b);
+  G3 = mk4(g3 + p3b, G3.w + w3b);
+  G4 = mk4(g4 + p4b, G4.w + w4b);
+  return true;
+}
+
+__global__ void k_bend_bwd(const uint32_t* __restrict__ order, uint32_t begin, uint32_t end,
+                           const int4* __restrict__ gidx, const float2* __restrict__ tc,
+                           const float4* __restrict__ tx, float4* __restrict__ G,
+                           float* __restrict__ bcomp_bar, float dt) {
+  const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= end) return;
+  const uint32_t j = order[k];
+  const int4 b = gidx[j];
+  const float2 th = tc[j];
+  const float4* t = tx + 4 * (size_t)j;
+  float4 G1 = G[b.x], G2 = G[b.y], G3 = G[b.z], G4 = G[b.w];
+  float cb = 0.0f;
+  if (bend_vjp(t[0], t[1], t[2], t[3], th.x, th.y, dt, G1, G2, G3, G4, cb)) {
+    G[b.x] = G1;
+    G[b.y] = G2;
+    G[b.z] = G3;
+    G[b.w] = G4;
+    bcomp_bar[j] += cb;
+  }
+}
+
+// ---- tiled replay and reverse ---------------------------------------------------------------
+// With the tile-local schedule the replay runs the forward's tile kernels (one launch per tile
+// color, footprint in shared memory) and tapes each tile's footprint as it enters the launch
+// (plus the multipliers, stretch) instead of every projection's inputs.  The reverse of a tile
+// color launch is one block per tile, tile colors last to first: the block reloads the tile's
+// entry footprint, re-runs its local colors in shared memory (the forward's code in the
+// forward's order, hence its bits) while it parks each projection's inputs in a per-slot
+// scratch array, then walks the local colors backwards with the footprint's adjoint staged in
+// shared memory.  Tiles of one tile color have disjoint footprints, so the write-back of the
+// adjoint needs no atomics.  Shared memory: footprint positions and adjoints (2 x 16 B), ids
+// (4 B) per footprint vertex; record (16 B) + multiplier and its adjoint (stretch, 8 B) or
+// rest angle and compliance (bend, 8 B) per constraint; num_local + 1 offsets.
+
+template <bool RESET, int NT>
+__global__ void __launch_bounds__(NT) k_stretch_tiles_tape(
+    const int4* __restrict__ con, float* __restrict__ lambda, float4* __restrict__ x,
+    const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
+    const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
+    uint32_t max_foot, uint32_t max_cons, float dt, float4* __restrict__ tfx,
+    float* __restrict__ tlam) {
+  extern __shared__ float4 smem[];
+  float4* sx = smem;
+  int4* sc = reinterpret_cast<int4*>(sx + max_foot);
+  float* sl = reinterpret_cast<float*>(sc + max_cons);
+  uint32_t* so = reinterpret_cast<uint32_t*>(sl + max_cons);
+  uint32_t* sf = so + num_local + 1;
+  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
+  const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) {
+    sc[j] = __ldg(&con[c0 + j]);
+    sl[j] = RESET ? 0.0f : lambda[c0 + j];
+    if (!RESET) tlam[c0 + j] = sl[j];
+  }
+  tile_gather<NT>(f, x, sx, sf);
+  for (uint32_t k = threadIdx.x; k < (uint32_t)f.m.y; k += NT) tfx[f.m.x + k] = sx[k];
+  __syncthreads();
+  for (uint32_t l = 0; l < num_local; ++l) {
+    const uint32_t ce = so[l + 1];
+    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
+      const int4 c = sc[j];
+      float lam = sl[j];
+      float4 a = sx[c.x], b = sx[c.y];
+      if (stretch_project(a, b, __int_as_float(c.z), __int_as_float(c.w), dt, lam)) {
+        sx[c.x] = a;
+        sx[c.y] = b;
+        sl[j] = lam;
+      }
+    }
+    __syncthreads();
+  }
+  tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) lambda[c0 + j] = sl[j];
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_bend_tiles_tape(
+    const int4* __restrict__ idx, const float2* __restrict__ tc, float4* __restrict__ x,
+    const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
+    const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
+    uint32_t max_foot, uint32_t max_cons, float dt, float4* __restrict__ tfx) {
+  extern __shared__ float4 smem[];
+  float4* sx = smem;
+  int4* sc = reinterpret_cast<int4*>(sx + max_foot);
+  float2* st = reinterpret_cast<float2*>(sc + max_cons);
+  uint32_t* so = reinterpret_cast<uint32_t*>(st + max_cons);
+  uint32_t* sf = so + num_local + 1;
+  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
+  const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) {
+    sc[j] = __ldg(&idx[c0 + j]);
+    st[j] = __ldg(&tc[c0 + j]);
+  }
+  tile_gather<NT>(f, x, sx, sf);
+  for (uint32_t k = threadIdx.x; k < (uint32_t)f.m.y; k += NT) tfx[f.m.x + k] = sx[k];
+  __syncthreads();
+  for (uint32_t l = 0; l < num_local; ++l) {
+    const uint32_t ce = so[l + 1];
+    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
+      const int4 b = sc[j];
+      const float2 th = st[j];
+      float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
+      bend_project(a1, a2, a3, a4, th.x, th.y, dt);
+      sx[b.x] = a1;
+      sx[b.y] = a2;
+      sx[b.z] = a3;
+      sx[b.w] = a4;
+    }
+    __syncthreads();
+  }
+  tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
+}
+
+// Stages a tile for its reverse: records, entry footprint (from the tape) and the footprint's
+// adjoint (from G); returns the frame.
+template <int NT>
+__device__ __forceinline__ TileFrame tile_bwd_gather(const uint32_t* __restrict__ foot,
+                                                     const int4* __restrict__ meta,
+                                                     const uint32_t* __restrict__ lofs,
+                                                     uint32_t t, uint32_t num_local,
+                                                     const float4* __restrict__ tfx,
+                                                     const float4* __restrict__ G, float4* sx,
+                                                     float4* sg, uint32_t* so, uint32_t* sf) {
+  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, t, num_local, so);
+#pragma unroll
+  for (int r = 0; r < kFootPerThread; ++r) {
+    const uint32_t k = threadIdx.x + (uint32_t)r * NT;
+    if (k < (uint32_t)f.m.y) {
+      sx[k] = tfx[f.m.x + k];
+      sg[k] = G[f.fi[r]];
+      sf[k] = f.fi[r];
+    }
+  }
+  return f;
+}
+
+template <bool RESET, int NT>
+__global__ void __launch_bounds__(NT) k_stretch_tiles_bwd(
+    const int4* __restrict__ con, const uint32_t* __restrict__ foot,
+    const int4* __restrict__ meta, const uint32_t* __restrict__ lofs, uint32_t tile_begin,
+    uint32_t num_local, uint32_t max_foot, uint32_t max_cons, float dt,
+    const float4* __restrict__ tfx, const float* __restrict__ tlam, float4* __restrict__ G,
+    float* __restrict__ lam_bar, float* __restrict__ comp_bar, float4* __restrict__ scr_x,
+    float* __restrict__ scr_l) {
+  extern __shared__ float4 smem[];
+  float4* sx = smem;
+  float4* sg = sx + max_foot;
+  int4* sc = reinterpret_cast<int4*>(sg + max_foot);
+  float* sl = reinterpret_cast<float*>(sc + max_cons);
+  float* slb = sl + max_cons;
+  uint32_t* so = reinterpret_cast<uint32_t*>(slb + max_cons);
+  uint32_t* sf = so + num_local + 1;
+  const TileFrame f = tile_bwd_gather<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local,
+                                          tfx, G, sx, sg, so, sf);
+  const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) {
+    sc[j] = __ldg(&con[c0 + j]);
+    sl[j] = RESET ? 0.0f : tlam[c0 + j];
+    slb[j] = lam_bar[c0 + j];
+  }
+  __syncthreads();
+  // forward again, parking each projection's inputs (slot j is handled by the same thread in
+  // both sweeps, so the scratch is read back by the thread that wrote it)
+  for (uint32_t l = 0; l < num_local; ++l) {
+    const uint32_t ce = so[l + 1];
+    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
+      const int4 c = sc[j];
+      float lam = sl[j];
+      float4 a = sx[c.x], b = sx[c.y];
+      scr_x[2 * (size_t)(c0 + j)] = a;
+      scr_x[2 * (size_t)(c0 + j) + 1] = b;
+      scr_l[c0 + j] = lam;
+      if (stretch_project(a, b, __int_as_float(c.z), __int_as_float(c.w), dt, lam)) {
+        sx[c.x] = a;
+        sx[c.y] = b;
+        sl[j] = lam;
+      }
+    }
+    __syncthreads();
+  }
+  for (int l = (int)num_local - 1; l >= 0; --l) {
+    const uint32_t ce = so[l + 1];
+    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
+      const int4 c = sc[j];
+      float4 ga = sg[c.x], gb = sg[c.y];
+      float lin = slb[j], cb = 0.0f;
+      if (stretch_vjp(scr_x[2 * (size_t)(c0 + j)], scr_x[2 * (size_t)(c0 + j) + 1],
+                      scr_l[c0 + j], __int_as_float(c.z), __int_as_float(c.w), dt, slb[j], ga,
+                      gb, lin, cb)) {
+        sg[c.x] = ga;
+        sg[c.y] = gb;
+        comp_bar[c0 + j] += cb;
+      }
+      slb[j] = RESET ? 0.0f : lin;
+    }
+    __syncthreads();
+  }
+  tile_scatter<NT>((uint32_t)f.m.y, G, sg, sf);
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) lam_bar[c0 + j] = slb[j];
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_bend_tiles_bwd(
+    const int4* __restrict__ idx, const float2* __restrict__ tc,
+    const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
+    const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
+    uint32_t max_foot, uint32_t max_cons, float dt, const float4* __restrict__ tfx,
+    float4* __restrict__ G, float* __restrict__ bcomp_bar, float4* __restrict__ scr_x) {
+  extern __shared__ float4 smem[];
+  float4* sx = smem;
+  float4* sg = sx + max_foot;
+  int4* sc = reinterpret_cast<int4*>(sg + max_foot);
+  float2* st = reinterpret_cast<float2*>(sc + max_cons);
+  uint32_t* so = reinterpret_cast<uint32_t*>(st + max_cons);
+  uint32_t* sf = so + num_local + 1;
+  const TileFrame f = tile_bwd_gather<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local,
+                                          tfx, G, sx, sg, so, sf);
+  const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) {
+    sc[j] = __ldg(&idx[c0 + j]);
+    st[j] = __ldg(&tc[c0 + j]);
+  }
+  __syncthreads();
+  for (uint32_t l = 0; l < num_local; ++l) {
+    const uint32_t ce = so[l + 1];
+    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
+      const int4 b = sc[j];
+      const float2 th = st[j];
+      float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
+      float4* s = scr_x + 4 * (size_t)(c0 + j);
+      s[0] = a1;
+      s[1] = a2;
+      s[2] = a3;
+      s[3] = a4;
+      bend_project(a1, a2, a3, a4, th.x, th.y, dt);
+      sx[b.x] = a1;
+      sx[b.y] = a2;
+      sx[b.z] = a3;
+      sx[b.w] = a4;
+    }
+    __syncthreads();
+  }
+  for (int l = (int)num_local - 1; l >= 0; --l) {
+    const uint32_t ce = so[l + 1];
+    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
+      const int4 b = sc[j];
+      const float2 th = st[j];
+      const float4* s = scr_x + 4 * (size_t)(c0 + j);
+      float4 G1 = sg[b.x], G2 = sg[b.y], G3 = sg[b.z], G4 = sg[b.w];
+      float cb = 0.0f;
+      if (bend_vjp(s[0], s[1], s[2], s[3], th.x, th.y, dt, G1, G2, G3, G4, cb)) {
+        sg[b.x] = G1;
+        sg[b.y] = G2;
+        sg[b.z] = G3;
+        sg[b.w] = G4;
+        bcomp_bar[c0 + j] += cb;
+      }
+    }
+    __syncthreads();
+  }
+  tile_scatter<NT>((uint32_t)f.m.y, G, sg, sf);
 }
 
 // LRA (all slots pinned) + VF-CCD + VF-DCD, per vertex, Jacobi (Gin -> Gout).  The slot sources'
@@ -484,6 +755,133 @@ void color_groups(const Context& c, int kind, std::vector<uint32_t>& order,
   }
 }
 
+// Shared memory per constraint of the tiled reverse: record + multiplier + its adjoint
+// (stretch), record + rest angle and compliance (bend).
+constexpr size_t kStretchBwdRecord = sizeof(int4) + 2 * sizeof(float);
+constexpr size_t kBendBwdRecord = sizeof(int4) + sizeof(float2);
+
+size_t tiles_bwd_smem(const TiledSet& T, size_t record) {
+  return (2 * sizeof(float4) + sizeof(uint32_t)) * T.max_foot + record * T.max_cons +
+         sizeof(uint32_t) * (T.num_local + 1);
+}
+
+// The dynamic shared-memory limit of a kernel is process-wide: only ever raised, so a context
+// with smaller tiles does not lower it under another's launches.
+cudaError_t raise_smem(const void* kern, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> set;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = set[{dev, kern}];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
+cudaError_t configure_tiled_adjoint(const Context& c) {
+  const DiffState& D = c.diff;
+  cudaError_t e = cudaSuccess;
+  auto set = [&](const void* k, size_t b) {
+    if (e == cudaSuccess) e = raise_smem(k, b);
+  };
+  if (D.s_tiled) {
+    const TiledSet& T = c.s_tiles;
+    const size_t ft = tile_smem_bytes(T, sizeof(int4) + sizeof(float));
+    const size_t bw = tiles_bwd_smem(T, kStretchBwdRecord);
+    if (T.block == 256) {
+      set((const void*)k_stretch_tiles_tape<true, 256>, ft);
+      set((const void*)k_stretch_tiles_tape<false, 256>, ft);
+      set((const void*)k_stretch_tiles_bwd<true, 256>, bw);
+      set((const void*)k_stretch_tiles_bwd<false, 256>, bw);
+    } else {
+      set((const void*)k_stretch_tiles_tape<true, 512>, ft);
+      set((const void*)k_stretch_tiles_tape<false, 512>, ft);
+      set((const void*)k_stretch_tiles_bwd<true, 512>, bw);
+      set((const void*)k_stretch_tiles_bwd<false, 512>, bw);
+    }
+  }
+  if (D.b_tiled) {
+    const TiledSet& T = c.b_tiles;
+    const size_t ft = tile_smem_bytes(T, sizeof(int4) + sizeof(float2));
+    const size_t bw = tiles_bwd_smem(T, kBendBwdRecord);
+    if (T.block == 256) {
+      set((const void*)k_bend_tiles_tape<256>, ft);
+      set((const void*)k_bend_tiles_bwd<256>, bw);
+    } else {
+      set((const void*)k_bend_tiles_tape<512>, ft);
+      set((const void*)k_bend_tiles_bwd<512>, bw);
+    }
+  }
+  return e;
+}
+
+// Tiled replay of one stretch / bend phase (all tile colors, in order) and its reverse.
+void stretch_tiles_tape(Context& c, float dt, bool reset, size_t ti) {
+  DiffState& D = c.diff;
+  const TiledSet& T = c.s_tiles;
+  const size_t smem = tile_smem_bytes(T, sizeof(int4) + sizeof(float));
+  auto kern = T.block == 256
+                  ? (reset ? k_stretch_tiles_tape<true, 256> : k_stretch_tiles_tape<false, 256>)
+                  : (reset ? k_stretch_tiles_tape<true, 512> : k_stretch_tiles_tape<false, 512>);
+  float4* tfx = D.t_fs.p + ti * T.foot_len;
+  float* tl = D.t_lam.p + ti * c.ne;
+  for (const ColorRange& r : T.tile_colors)
+    if (r.end > r.begin)
+      kern<<<r.end - r.begin, T.block, smem, c.stream>>>(c.s_con.p, c.s_lambda.p, c.x.p,
+                                                         T.foot.p, T.meta.p, T.lofs.p, r.begin,
+                                                         T.num_local, T.max_foot, T.max_cons, dt,
+                                                         tfx, tl);
+}
+
+void bend_tiles_tape(Context& c, float dt, size_t ti) {
+  DiffState& D = c.diff;
+  const TiledSet& T = c.b_tiles;
+  const size_t smem = tile_smem_bytes(T, sizeof(int4) + sizeof(float2));
+  auto kern = T.block == 256 ? k_bend_tiles_tape<256> : k_bend_tiles_tape<512>;
+  float4* tfx = D.t_fb.p + ti * T.foot_len;
+  for (const ColorRange& r : T.tile_colors)
+    if (r.end > r.begin)
+      kern<<<r.end - r.begin, T.block, smem, c.stream>>>(c.b_idx.p, c.b_tc.p, c.x.p, T.foot.p,
+                                                         T.meta.p, T.lofs.p, r.begin, T.num_local,
+                                                         T.max_foot, T.max_cons, dt, tfx);
+}
+
+void stretch_tiles_bwd(Context& c, float dt, bool reset, size_t ti) {
+  DiffState& D = c.diff;
+  const TiledSet& T = c.s_tiles;
+  const size_t smem = tiles_bwd_smem(T, kStretchBwdRecord);
+  auto kern = T.block == 256
+                  ? (reset ? k_stretch_tiles_bwd<true, 256> : k_stretch_tiles_bwd<false, 256>)
+                  : (reset ? k_stretch_tiles_bwd<true, 512> : k_stretch_tiles_bwd<false, 512>);
+  const float4* tfx = D.t_fs.p + ti * T.foot_len;
+  const float* tl = D.t_lam.p + ti * c.ne;
+  for (int k = (int)T.tile_colors.size() - 1; k >= 0; --k) {
+    const ColorRange r = T.tile_colors[k];
+    if (r.end > r.begin)
+      kern<<<r.end - r.begin, T.block, smem, c.stream>>>(
+          c.s_con.p, T.foot.p, T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot, T.max_cons,
+          dt, tfx, tl, D.G.p, D.lam_bar.p, D.comp_bar.p, D.t_sx.p, D.t_sl.p);
+  }
+}
+
+void bend_tiles_bwd(Context& c, float dt, size_t ti) {
+  DiffState& D = c.diff;
+  const TiledSet& T = c.b_tiles;
+  const size_t smem = tiles_bwd_smem(T, kBendBwdRecord);
+  auto kern = T.block == 256 ? k_bend_tiles_bwd<256> : k_bend_tiles_bwd<512>;
+  const float4* tfx = D.t_fb.p + ti * T.foot_len;
+  for (int k = (int)T.tile_colors.size() - 1; k >= 0; --k) {
+    const ColorRange r = T.tile_colors[k];
+    if (r.end > r.begin)
+      kern<<<r.end - r.begin, T.block, smem, c.stream>>>(
+          c.b_idx.p, c.b_tc.p, T.foot.p, T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot,
+          T.max_cons, dt, tfx, D.G.p, D.bcomp_bar.p, D.t_bx.p);
+  }
+}
+
 cudaError_t copy_d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
   return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s) : cudaSuccess;
 }
@@ -535,7 +933,8 @@ void record_frame_diff(Context& c) {
       }
       D.it_pass[cur] = cnt - 1;
       const size_t ti = (size_t)cur;
-      for (const ColorRange& r : D.s_colors) {
+      if (D.s_tiled) stretch_tiles_tape(c, k.dt, it == 0, ti);
+      else for (const ColorRange& r : D.s_colors) {
         const unsigned g = grid_for(r.end - r.begin);
         if (it == 0)
           k_stretch_tape<true><<<g, blk, 0, c.stream>>>(D.s_order.p, r.begin, r.end, D.s_gidx.p,
@@ -548,7 +947,8 @@ void record_frame_diff(Context& c) {
                                                           D.t_sx.p + 2 * ti * E,
                                                           D.t_sl.p + ti * E, k.dt);
       }
-      if (p.solve_bending)
+      if (p.solve_bending && D.b_tiled) bend_tiles_tape(c, k.dt, ti);
+      else if (p.solve_bending)
         for (const ColorRange& r : D.b_colors)
           k_bend_tape<<<grid_for(r.end - r.begin), blk, 0, c.stream>>>(
               D.b_order.p, r.begin, r.end, D.b_gidx.p, c.b_tc.p, c.x.p, D.t_bx.p + 4 * ti * B,
@@ -610,14 +1010,16 @@ void backward_frame(Context& c) {
         if (lra_fused) k_add_sources<<<gv, blk, 0, c.stream>>>(D.G2.p, D.Gs.p, V);
         std::swap(D.G.p, D.G2.p);
       }
-      if (p.solve_bending)
+      if (p.solve_bending && D.b_tiled) bend_tiles_bwd(c, k.dt, ti);
+      else if (p.solve_bending)
         for (int ci = (int)D.b_colors.size() - 1; ci >= 0; --ci) {
           const ColorRange r = D.b_colors[ci];
           k_bend_bwd<<<grid_for(r.end - r.begin), blk, 0, c.stream>>>(
               D.b_order.p, r.begin, r.end, D.b_gidx.p, c.b_tc.p, D.t_bx.p + 4 * ti * B, D.G.p,
               D.bcomp_bar.p, k.dt);
         }
-      for (int ci = (int)D.s_colors.size() - 1; ci >= 0; --ci) {
+      if (D.s_tiled) stretch_tiles_bwd(c, k.dt, it == 0, ti);
+      else for (int ci = (int)D.s_colors.size() - 1; ci >= 0; --ci) {
         const ColorRange r = D.s_colors[ci];
         const unsigned g = grid_for(r.end - r.begin);
         if (it == 0)
@@ -707,9 +1109,24 @@ xrt_status diff_prepare(Context& c) {
   D.P = (uint32_t)p.num_collision_passes;
   const size_t V = c.nv, E = std::max(c.ne, 1u), Bn = std::max(c.nb, 1u), SI = (size_t)D.S * D.I;
   const size_t P = c.onf ? D.P : 1, F = std::max(c.onf, 1u);
-  XRT_CUDA(&c, D.t_sx.reserve(2 * SI * E));
-  XRT_CUDA(&c, D.t_sl.reserve(SI * E));
-  XRT_CUDA(&c, D.t_bx.reserve(4 * SI * Bn));
+  // tiled replay / reverse where the schedule is tiled and the reverse's shared memory fits
+  int dev = 0, smem_max = 0;
+  XRT_CUDA(&c, cudaGetDevice(&dev));
+  XRT_CUDA(&c, cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  D.s_tiled = c.s_tiles.on && c.ne > 0 &&
+              tiles_bwd_smem(c.s_tiles, kStretchBwdRecord) <= (size_t)smem_max;
+  D.b_tiled = c.b_tiles.on && c.nb > 0 && p.solve_bending &&
+              tiles_bwd_smem(c.b_tiles, kBendBwdRecord) <= (size_t)smem_max;
+  if (D.s_tiled || D.b_tiled) XRT_CUDA(&c, configure_tiled_adjoint(c));
+  const size_t s_it = D.s_tiled ? 1 : SI, b_it = D.b_tiled ? 1 : SI;
+  XRT_CUDA(&c, D.t_sx.reserve(2 * s_it * E));
+  XRT_CUDA(&c, D.t_sl.reserve(s_it * E));
+  XRT_CUDA(&c, D.t_bx.reserve(4 * b_it * Bn));
+  if (D.s_tiled) {
+    XRT_CUDA(&c, D.t_fs.reserve(SI * c.s_tiles.foot_len));
+    XRT_CUDA(&c, D.t_lam.reserve(SI * E));
+  }
+  if (D.b_tiled) XRT_CUDA(&c, D.t_fb.reserve(SI * c.b_tiles.foot_len));
   XRT_CUDA(&c, D.t_stage.reserve(SI * V));
   XRT_CUDA(&c, D.t_ee.reserve(c.onf ? SI * V : 1));
   XRT_CUDA(&c, D.t_vf_idx.reserve(P * V));
@@ -814,9 +1231,9 @@ void diff_release(Context& c) {
   D.s_order.release(); D.b_order.release(); D.s_gidx.release(); D.b_gidx.release();
   for (DBuf<float4>* b : {&D.t_sx, &D.t_bx, &D.t_stage, &D.t_ee, &D.t_vf_qs, &D.t_rt_qc,
                           &D.t_ee_a, &D.t_ee_b, &D.t_ee_c, &D.t_pred, &D.G, &D.G2, &D.Gv, &D.H,
-                          &D.Gs})
+                          &D.Gs, &D.t_fs, &D.t_fb})
     b->release();
-  D.t_sl.release(); D.t_vf_idx.release(); D.t_rt_idx.release();
+  D.t_sl.release(); D.t_lam.release(); D.t_vf_idx.release(); D.t_rt_idx.release();
   D.cnt.release(); D.lam_bar.release(); D.comp_bar.release(); D.bcomp_bar.release();
   D.active = false;
   D.frames = 0;

@@ -10,6 +10,55 @@
 
 namespace xrt {
 
+// One tile of a tile-local Gauss-Seidel launch (block = tile): its metadata and the footprint
+// vertex ids of this thread (kFootPerThread per thread, NT threads).
+struct TileFrame {
+  int4 m;                          // first footprint entry, footprint size, first record, count
+  uint32_t fi[kFootPerThread];     // footprint vertex ids of this thread
+};
+
+template <int NT>
+__device__ __forceinline__ TileFrame tile_prologue(const uint32_t* __restrict__ foot,
+                                                   const int4* __restrict__ meta,
+                                                   const uint32_t* __restrict__ lofs, uint32_t t,
+                                                   uint32_t num_local, uint32_t* so) {
+  TileFrame f;
+  f.m = __ldg(&meta[t]);
+  for (uint32_t k = threadIdx.x; k <= num_local; k += NT)
+    so[k] = __ldg(&lofs[(size_t)t * (num_local + 1) + k]);
+#pragma unroll
+  for (int r = 0; r < kFootPerThread; ++r) {
+    const uint32_t k = threadIdx.x + (uint32_t)r * NT;
+    f.fi[r] = k < (uint32_t)f.m.y ? __ldg(&foot[f.m.x + k]) : 0u;
+  }
+  return f;
+}
+
+// The gather also parks the ids in shared memory (slot k is written and later read by the same
+// thread), so they need no registers through the local-color loop.
+template <int NT>
+__device__ __forceinline__ void tile_gather(const TileFrame& f, const float4* __restrict__ x,
+                                            float4* sx, uint32_t* sf) {
+#pragma unroll
+  for (int r = 0; r < kFootPerThread; ++r) {
+    const uint32_t k = threadIdx.x + (uint32_t)r * NT;
+    if (k < (uint32_t)f.m.y) {
+      sx[k] = x[f.fi[r]];
+      sf[k] = f.fi[r];
+    }
+  }
+}
+
+template <int NT>
+__device__ __forceinline__ void tile_scatter(uint32_t nfoot, float4* __restrict__ x,
+                                             const float4* sx, const uint32_t* sf) {
+#pragma unroll
+  for (int r = 0; r < kFootPerThread; ++r) {
+    const uint32_t k = threadIdx.x + (uint32_t)r * NT;
+    if (k < nfoot) x[sf[k]] = sx[k];
+  }
+}
+
 // XPBD distance constraint on two vertices; returns true when it moved them (lam updated).
 __device__ __forceinline__ bool stretch_project(float4& a, float4& b, float rest, float compliance,
                                                 float dt, float& lam) {

@@ -96,62 +96,16 @@ __global__ void k_stretch(const int4* __restrict__ con, float* __restrict__ lamb
   }
 }
 
-// Tile-local Gauss-Seidel: block = one tile of the launched tile color.  The tile's footprint is
-// staged in shared memory, its local colors run in order with a block barrier between them, and
-// the footprint is written back.  Tiles of one tile color have disjoint footprints.
+// Tile-local Gauss-Seidel: block = one tile of the launched tile color (TileFrame and the
+// prologue / gather / scatter helpers in project_dev.cuh).  The tile's footprint is staged in
+// shared memory, its local colors run in order with a block barrier between them, and the
+// footprint is written back.  Tiles of one tile color have disjoint footprints.
 // Shared memory of a tile launch: footprint positions, the tile's constraint records, the
 // multipliers (stretch) or rest angles (bend), then the num_local + 1 local-color offsets.
 // Prologue before pdl_wait (setup-time data only): the tile's metadata, offsets, records and
 // footprint vertex ids, the ids held in registers (kFootPerThread per thread) so the gather and
 // the write-back each issue all their loads and stores at once.  NT threads per block: 512 for
 // footprints up to 4,096 vertices, 256 (twice the resident blocks per SM) up to 2,048.
-struct TileFrame {
-  int4 m;                          // first footprint entry, footprint size, first record, count
-  uint32_t fi[kFootPerThread];     // footprint vertex ids of this thread
-};
-
-template <int NT>
-__device__ __forceinline__ TileFrame tile_prologue(const uint32_t* __restrict__ foot,
-                                                   const int4* __restrict__ meta,
-                                                   const uint32_t* __restrict__ lofs, uint32_t t,
-                                                   uint32_t num_local, uint32_t* so) {
-  TileFrame f;
-  f.m = __ldg(&meta[t]);
-  for (uint32_t k = threadIdx.x; k <= num_local; k += NT)
-    so[k] = __ldg(&lofs[(size_t)t * (num_local + 1) + k]);
-#pragma unroll
-  for (int r = 0; r < kFootPerThread; ++r) {
-    const uint32_t k = threadIdx.x + (uint32_t)r * NT;
-    f.fi[r] = k < (uint32_t)f.m.y ? __ldg(&foot[f.m.x + k]) : 0u;
-  }
-  return f;
-}
-
-// The gather also parks the ids in shared memory (slot k is written and later read by the same
-// thread), so they need no registers through the local-color loop.
-template <int NT>
-__device__ __forceinline__ void tile_gather(const TileFrame& f, const float4* __restrict__ x,
-                                            float4* sx, uint32_t* sf) {
-#pragma unroll
-  for (int r = 0; r < kFootPerThread; ++r) {
-    const uint32_t k = threadIdx.x + (uint32_t)r * NT;
-    if (k < (uint32_t)f.m.y) {
-      sx[k] = x[f.fi[r]];
-      sf[k] = f.fi[r];
-    }
-  }
-}
-
-template <int NT>
-__device__ __forceinline__ void tile_scatter(uint32_t nfoot, float4* __restrict__ x,
-                                             const float4* sx, const uint32_t* sf) {
-#pragma unroll
-  for (int r = 0; r < kFootPerThread; ++r) {
-    const uint32_t k = threadIdx.x + (uint32_t)r * NT;
-    if (k < nfoot) x[sf[k]] = sx[k];
-  }
-}
-
 template <bool RESET, int NT>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_stretch_tiles(
     const int4* __restrict__ con, float* __restrict__ lambda, float4* __restrict__ x,

@@ -272,6 +272,51 @@ def batched_garments(count: int = 512, seed: int = 4) -> list:
     return out
 
 
+# 10 substeps x 10 iterations, one collision pass per substep, no particle self-collision.
+DIFF_PARAMS = dict(num_substeps=10, num_iterations=10, num_collision_passes=10,
+                   enable_self_collision=0, update_obstacle_animation=0)
+
+
+@dataclass
+class DiffInstance:
+    """One instance of the differentiation workload, with its seeded ground truth."""
+    cloth: Mesh
+    sphere: Mesh
+    stretch_compliance: np.ndarray  # per edge, the ground truth of the target rollout
+    bend_compliance: np.ndarray     # per bend
+    mass: np.ndarray                # per vertex
+    velocity: np.ndarray            # (V, 3) initial velocity
+
+
+def diff_batch(count: int = 16, n: int = 128, seed: int = 7) -> list:
+    """`count` n x n sheets (1 m, jitter 1e-3), each pinned along its top edge (row 0, the two
+    corners LRA-attached) and 5 cm above its own sphere of radius 0.3 m (icosphere, 3
+    subdivisions, centre offset seeded within 5 cm).  Ground truth per instance: stretch
+    compliance log-uniform in [1e-8, 1e-5] per edge, bend compliance log-uniform in [10, 1000]
+    per bend (about the reference's default of 100: stiffer bends fold a flat sheet, because the
+    solve's normals are oriented against the rest angle's), vertex mass uniform in [0.5, 2] (the reference's unit inverse mass scale), initial
+    velocity N(0, 0.05 m/s).
+    Edge and bend counts are those the solver builds for an n x n grid:
+    3 n^2 - 4 n + 1 edges, one bend per interior edge."""
+    rng = np.random.default_rng(seed)
+    out = []
+    E = 3 * n * n - 4 * n + 1
+    B = E - 4 * (n - 1)
+    for i in range(count):
+        off = rng.uniform(-0.05, 0.05, 2)
+        sphere = icosphere(3, 0.3, center=(off[0], 0.0, off[1]))
+        cloth = grid_cloth(n, 1.0, origin=(-0.5, 0.35, -0.5), jitter=1e-3, seed=seed + i)
+        cloth.fixed_indices = np.arange(n, dtype=np.uint32)
+        cloth.attached_indices = np.array([0, n - 1], np.uint32)
+        out.append(DiffInstance(
+            cloth, sphere,
+            np.exp(rng.uniform(np.log(1e-8), np.log(1e-5), E)).astype(np.float32),
+            np.exp(rng.uniform(np.log(10.0), np.log(1000.0), B)).astype(np.float32),
+            rng.uniform(0.5, 2.0, n * n).astype(np.float32),
+            rng.normal(0.0, 0.05, (n * n, 3)).astype(np.float32)))
+    return out
+
+
 def scene_params(scene: Scene, **overrides):
     kw = dict(scene.params)
     kw.update(overrides)
