@@ -503,6 +503,13 @@ def run_diff(args, local_rank):
         for _ in range(args.steps):
             loss, g, t_fwd, t_bwd = evaluate()
             rec.append((t_fwd, t_bwd))
+    # per-phase profile of one more evaluation (eager frames, CUDA events around each phase)
+    s.set_profiling(True)
+    evaluate()
+    prof = s.profile()
+    s.set_profiling(False)
+    phases = {k: round(v["ms"] / F, 3) for k, v in prof.items()
+              if k != "frames" and v["launches"]}
     s.diff_end()
     t_fwd = float(np.mean([r[0] for r in rec]))
     t_bwd = float(np.mean([r[1] for r in rec]))
@@ -535,6 +542,7 @@ def run_diff(args, local_rank):
         "backward_over_forward": t_bwd / t_plain,
         "backward_over_recorded_forward": t_bwd / t_fwd,
         "loss": loss,
+        "phase_ms_per_frame": phases,
         "grad_norms": {k: float(np.linalg.norm(v)) for k, v in grads.items()},
         "grads_finite": bool(all(np.isfinite(v).all() for v in grads.values())),
         "e2e": {"value": units / t_e2e, "unit": "vertex-substeps/s",

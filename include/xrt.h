@@ -200,7 +200,7 @@ xrt_status xrt_set_dependent_launch(xrt_ctx* ctx, int32_t enabled);
 xrt_status xrt_set_tile_vertices(xrt_ctx* ctx, uint32_t tile_vertices);
 
 /* ---- per-phase GPU timing (replaces Timer / ScopedTimerGPU, utils/Timer.hpp:67-114) -------- */
-#define XRT_NUM_PHASES 12
+#define XRT_NUM_PHASES 16
 typedef struct xrt_profile {
   double ms[16];        /* summed CUDA-event time of the phase's launches */
   uint64_t launches[16];/* kernel launches of the phase */
@@ -213,7 +213,9 @@ typedef struct xrt_profile {
 xrt_status xrt_set_profiling(xrt_ctx* ctx, int32_t enabled);
 xrt_status xrt_get_profile(xrt_ctx* ctx, xrt_profile* out);
 /* Phase names: 0 predict_finalize, 1 hash, 2 collide, 3 bvh_build, 4 obstacle_pass, 5 generate,
- * 6 stretch, 7 bend, 8 lra, 9 vf_solve, 10 ee_apply, 11 obstacle_commit. */
+ * 6 stretch, 7 bend, 8 lra, 9 vf_solve, 10 ee_apply, 11 obstacle_commit; the reverse pass
+ * (xrt_backward, include/xrt_diff.h) while profiling: 12 adjoint_replay (taping re-run of each
+ * frame), 13 adjoint_stretch, 14 adjoint_bend, 15 adjoint_vertex (LRA, contacts, integration). */
 const char* xrt_phase_name(int32_t phase);
 
 /* ---- state ---------------------------------------------------------------------------- */

@@ -113,7 +113,8 @@ class Profile(C.Structure):
 
 
 PHASES = ["predict_finalize", "hash", "collide", "bvh_build", "obstacle_pass", "generate",
-          "stretch", "bend", "lra", "vf_solve", "ee_apply", "obstacle_commit"]
+          "stretch", "bend", "lra", "vf_solve", "ee_apply", "obstacle_commit",
+          "adjoint_replay", "adjoint_stretch", "adjoint_bend", "adjoint_vertex"]
 
 # name -> (restype, argtypes); every symbol declared in include/xrt.h
 P = C.c_void_p

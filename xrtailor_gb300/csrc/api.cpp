@@ -17,9 +17,11 @@
 #include "context.h"
 #include "setup.h"
 
+using xrt::collect_profile;
 using xrt::ColorRange;
 using xrt::Context;
 using xrt::DBuf;
+using xrt::Timed;
 
 
 struct xrt_lbvh {
@@ -94,46 +96,10 @@ enum Phase {
 };
 const char* const kPhaseNames[XRT_NUM_PHASES] = {
     "predict_finalize", "hash", "collide", "bvh_build", "obstacle_pass", "generate",
-    "stretch", "bend", "lra", "vf_solve", "ee_apply", "obstacle_commit"};
-
-// CUDA-event pair around one launch group when profiling (eager frames only).
-struct Timed {
-  Context& c;
-  size_t idx = (size_t)-1;
-  Timed(Context& ctx, int phase, uint32_t kernels, uint64_t units) : c(ctx) {
-    if (!c.profiling) return;
-    if (c.prof_used == c.prof_events.size()) {
-      Context::ProfEvent e{};
-      cudaEventCreate(&e.a);
-      cudaEventCreate(&e.b);
-      c.prof_events.push_back(e);
-    }
-    idx = c.prof_used++;
-    Context::ProfEvent& e = c.prof_events[idx];
-    e.phase = phase;
-    e.kernels = kernels;
-    e.units = units;
-    cudaEventRecord(e.a, c.stream);
-  }
-  ~Timed() {
-    if (idx != (size_t)-1) cudaEventRecord(c.prof_events[idx].b, c.stream);
-  }
-};
-
-void collect_profile(Context& c) {
-  if (!c.profiling) return;
-  cudaStreamSynchronize(c.stream);
-  for (size_t i = 0; i < c.prof_used; ++i) {
-    const Context::ProfEvent& e = c.prof_events[i];
-    float ms = 0.0f;
-    cudaEventElapsedTime(&ms, e.a, e.b);
-    c.prof_ms[e.phase] += ms;
-    c.prof_launches[e.phase] += e.kernels;
-    c.prof_units[e.phase] += e.units;
-  }
-  c.prof_used = 0;
-  c.prof_frames++;
-}
+    "stretch", "bend", "lra", "vf_solve", "ee_apply", "obstacle_commit",
+    "adjoint_replay", "adjoint_stretch", "adjoint_bend", "adjoint_vertex"};
+static_assert(xrt::kAdjReplay == 12 && xrt::kAdjVertex == XRT_NUM_PHASES - 1,
+              "adjoint phases follow the frame's");
 
 // The launch sequence of one frame (ClothSolverBase::SimulateSwift, ClothSolverBase.cpp:171-261).
 void record_frame(Context& c) {
@@ -847,7 +813,6 @@ xrt_status xrt_start(xrt_ctx* h) {
       T.on = true;
       T.num_local = S.num_local;
       T.max_foot = S.max_footprint;
-      T.foot_len = S.foot.size();
       T.max_cons = 0;
       T.max_step = 0;
       for (size_t tt = 0; tt + 1 < S.foot_ptr.size(); ++tt)

@@ -171,15 +171,13 @@ struct DiffState {
   // one frame of tape
   uint32_t S = 0, I = 0, P = 0;
   std::vector<int> it_pass;             // (substep, iteration) -> collision pass of the frame
-  // per-color schedule: every projection's inputs; tiled schedule (s_tiled / b_tiled): the same
-  // arrays sized for one iteration are the reverse's per-slot scratch, and the tape holds each
-  // tile's entry footprint (t_fs, t_fb: S x I x footprint entries) and multipliers (t_lam)
+  // every projection's inputs by execution slot; replayed and reversed per tile color where the
+  // schedule is tiled (s_tiled / b_tiled), per color otherwise
   bool s_tiled = false, b_tiled = false;
+  bool s_stage = false, b_stage = false;  // tiled reverse stages each tile's tape in shared memory
   DBuf<float4> t_sx;                    // S x I x E x 2: stretch inputs (x with inverse mass)
   DBuf<float> t_sl;                     // S x I x E: stretch multipliers in
   DBuf<float4> t_bx;                    // S x I x B x 4: bend inputs
-  DBuf<float4> t_fs, t_fb;              // S x I x stretch / bend footprint entries
-  DBuf<float> t_lam;                    // S x I x E: stretch multipliers at iteration start
   DBuf<float4> t_stage, t_ee;           // S x I x V: inputs of the LRA+VF and EE launches
   DBuf<int> t_vf_idx, t_rt_idx;         // P x V
   DBuf<float4> t_vf_qs, t_rt_qc;        // P x V
@@ -188,6 +186,13 @@ struct DiffState {
   // adjoint
   DBuf<float4> G, G2, Gv, H, Gs;        // x-bar (+ inverse-mass bar in w), v-bar, temporaries
   DBuf<float> cnt, lam_bar, comp_bar, bcomp_bar;
+  // one frame's replay + reverse as a CUDA graph (built per xrt_backward call), per starting
+  // assignment of the G / G2 double buffer, with the assignment the frame leaves
+  struct FrameGraph {
+    cudaGraphExec_t exec = nullptr;
+    float4 *g_in = nullptr, *g_out = nullptr, *g2_out = nullptr;
+  };
+  FrameGraph graph[2];
 };
 
 // Tile-local Gauss-Seidel schedule of one constraint kind on the device (setup::TileSchedule):
@@ -209,7 +214,6 @@ struct TiledSet {
   DBuf<int4> meta;                      // per executed tile {first footprint, footprint size,
                                         //  first constraint, constraint count}
   DBuf<uint32_t> lofs;                  // per executed tile: num_local + 1 offsets, tile-relative
-  size_t foot_len = 0;                  // entries of `foot` (footprints of all tiles)
 };
 
 // Quality-mode self contact (proximity.cu): unified numbering, cloth first then obstacle.
@@ -360,6 +364,49 @@ struct Context {
 
   void set_error(const std::string& m) { last_error = m; }
 };
+
+// Profile phases of the reverse pass (after the frame's, which api.cpp names).
+enum AdjointPhase { kAdjReplay = 12, kAdjStretch, kAdjBend, kAdjVertex };
+
+// CUDA-event pair around one launch group when profiling (eager frames only).
+struct Timed {
+  Context& c;
+  size_t idx = (size_t)-1;
+  Timed(Context& ctx, int phase, uint32_t kernels, uint64_t units) : c(ctx) {
+    if (!c.profiling) return;
+    if (c.prof_used == c.prof_events.size()) {
+      Context::ProfEvent e{};
+      cudaEventCreate(&e.a);
+      cudaEventCreate(&e.b);
+      c.prof_events.push_back(e);
+    }
+    idx = c.prof_used++;
+    Context::ProfEvent& e = c.prof_events[idx];
+    e.phase = phase;
+    e.kernels = kernels;
+    e.units = units;
+    cudaEventRecord(e.a, c.stream);
+  }
+  ~Timed() {
+    if (idx != (size_t)-1) cudaEventRecord(c.prof_events[idx].b, c.stream);
+  }
+};
+
+// Adds the recorded event pairs to the per-phase sums (one more frame).
+inline void collect_profile(Context& c) {
+  if (!c.profiling) return;
+  cudaStreamSynchronize(c.stream);
+  for (size_t i = 0; i < c.prof_used; ++i) {
+    const Context::ProfEvent& e = c.prof_events[i];
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e.a, e.b);
+    c.prof_ms[e.phase] += ms;
+    c.prof_launches[e.phase] += e.kernels;
+    c.prof_units[e.phase] += e.units;
+  }
+  c.prof_used = 0;
+  c.prof_frames++;
+}
 
 // ---- kernels (solver.cu / contact.cu / hash.cu) ---------------------------------------------------
 struct FrameConst {

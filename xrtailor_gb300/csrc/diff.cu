@@ -90,6 +90,13 @@ __device__ __forceinline__ void cross_bwd(f3 a, f3 b, f3 cb, f3& ab, f3& bb) {
   bb = bb + cross(cb, a);
 }
 
+// The reverse's own arithmetic is not replayed, so it need not match the forward's IEEE-rounded
+// divisions and square roots bit for bit: reciprocals come from the hardware approximation
+// (__fdividef, rsqrtf; a few ulp), which shortens each VJP's dependency chain.  Every value that
+// decides whether a projection ran (distance, normals, clamped cosine, angle) is recomputed
+// exactly as the forward computes it.
+__device__ __forceinline__ float frcp(float x) { return __fdividef(1.0f, x); }
+
 // XPBD distance (stretch_project): inputs (a, b, lambda), outputs (a', b', lambda').  ga, gb hold
 // the outputs' adjoints on entry (xyz; w accumulates the inverse-mass adjoint) and the inputs'
 // on exit; lbo is lambda'-bar.  Returns false for an inactive projection (the identity: nothing
@@ -98,15 +105,16 @@ __device__ __forceinline__ bool stretch_vjp(float4 A, float4 B, float lam, float
                                             float dt, float lbo, float4& ga, float4& gb,
                                             float& lam_in_bar, float& cbar) {
   const f3 d = mk3(A) - mk3(B);
-  const float dist = length(d);
+  const float dist = length(d);  // as the forward: it decides whether the projection ran
   const float wa = A.w, wb = B.w;
   if (!(dist != rest && wa + wb > 0.0f)) return false;
-  const float e = dist + kEps;
-  const f3 n = d / e;
-  const float at = comp / (dt * dt);
+  const float re = frcp(dist + kEps);
+  const f3 n = d * re;
+  const float idt2 = frcp(dt * dt);
+  const float at = comp * idt2;
   const float C = dist - rest;
-  const float D = wa + wb + at;
-  const float dl = (-C - at * lam) / D;
+  const float rD = frcp(wa + wb + at);
+  const float dl = (-C - at * lam) * rD;
   const f3 corr = dl * n;
   // x_a' = x_a + w_a corr, x_b' = x_b - w_b corr, lambda' = lambda + dl
   const f3 corr_bar = wa * mk3(ga) - wb * mk3(gb);
@@ -114,18 +122,18 @@ __device__ __forceinline__ bool stretch_vjp(float4 A, float4 B, float lam, float
   float wb_bar = -dot(corr, mk3(gb));
   const float dl_bar = dot(corr_bar, n) + lbo;
   const f3 n_bar = dl * corr_bar;
-  const float N_bar = dl_bar / D;        // dl = N / D
-  const float D_bar = -dl_bar * dl / D;
+  const float N_bar = dl_bar * rD;       // dl = N / D
+  const float D_bar = -dl_bar * dl * rD;
   const float C_bar = -N_bar;            // N = -C - at lambda
   const float at_bar = -N_bar * lam + D_bar;
   lam_in_bar = lbo - N_bar * at;
   wa_bar += D_bar;
   wb_bar += D_bar;
-  const float dist_bar = C_bar - dot(n_bar, n) / e;  // n = d / (dist + eps)
-  const f3 d_bar = n_bar / e + (dist > 0.0f ? (dist_bar / dist) * d : mk3(0, 0, 0));
+  const float dist_bar = C_bar - dot(n_bar, n) * re;  // n = d / (dist + eps)
+  const f3 d_bar = n_bar * re + (dist > 0.0f ? (dist_bar * frcp(dist)) * d : mk3(0, 0, 0));
   ga = mk4(mk3(ga) + d_bar, ga.w + wa_bar);
   gb = mk4(mk3(gb) - d_bar, gb.w + wb_bar);
-  cbar += at_bar / (dt * dt);
+  cbar += at_bar * idt2;
   return true;
 }
 
@@ -164,8 +172,8 @@ __device__ __forceinline__ float acos_as_deriv(float x) {
     dp = dp * x + p;
     p = p * x + c[i];
   }
-  const float s = sqrtf(1.0f - x);
-  return s * dp - p / (2.0f * s);
+  const float rs = rsqrtf(1.0f - x);  // x < 1 wherever the projection ran
+  return (1.0f - x) * rs * dp - 0.5f * p * rs;
 }
 
 // Dihedral bend: inputs x1..x4 (w in .w), outputs x_i' = x_i + w_i lambda q_i.
@@ -178,27 +186,33 @@ __device__ __forceinline__ bool bend_vjp(float4 A1, float4 A2, float4 A3, float4
   const f3 p1 = mk3(A1);
   const f3 p2 = mk3(A2) - p1, p3 = mk3(A3) - p1, p4 = mk3(A4) - p1;
   const f3 c23 = cross(p2, p3), c24 = cross(p2, p4);
-  const f3 n1 = normalize(c23), n2 = normalize(c24);
+  const float d23 = dot(c23, c23), d24 = dot(c24, c24);
+  const float i23 = 1.0f / sqrtf(d23), i24 = 1.0f / sqrtf(d24);  // normalize's, exactly
+  const f3 n1 = c23 * i23, n2 = c24 * i24;
   const float draw = dot(n1, n2);
   const float d = tclamp(draw, 0.0f, 1.0f);
   const float angle = acos_as(d);
   if (angle < kEps || isnan(d)) return false;  // not projected: identity
-  const float L23 = length(c23), L24 = length(c24);
-  const float e23 = L23 + kEps, e24 = L24 + kEps;
+  const float L23 = d23 * i23, L24 = d24 * i24;  // |c23|, |c24|
+  const float r23 = frcp(L23 + kEps), r24 = frcp(L24 + kEps);
   const f3 B3 = cross(n1, p2), B4 = cross(n2, p2), B23 = cross(n1, p3), B24 = cross(n2, p4);
   const f3 A3v = cross(p2, n2) + B3 * d;
   const f3 A4v = cross(p2, n1) + B4 * d;
   const f3 A23 = cross(p3, n2) + B23 * d;
   const f3 A24 = cross(p4, n1) + B24 * d;
-  const f3 q3 = A3v / e23, q4 = A4v / e24;
-  const f3 q2 = -A23 / e23 - A24 / e24;
+  const f3 q3 = A3v * r23, q4 = A4v * r24;
+  const f3 q2 = -(A23 * r23) - A24 * r24;
   const f3 q1 = -q2 - q3 - q4;
-  const float at = comp / dt / dt;
+  const float idt2 = frcp(dt * dt);
+  const float at = comp * idt2;
   const float denom = at + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) +
                             w4 * dot(q4, q4));
   if (denom < kEps) return false;
-  const float s = sqrtf(1.0f - d * d);
-  const float lam = s * (angle - theta) / denom;
+  const float om = 1.0f - d * d;  // > 0: d < 1 wherever the angle passed
+  const float rs = rsqrtf(om);
+  const float s = om * rs;
+  const float rden = frcp(denom);
+  const float lam = s * (angle - theta) * rden;
   const f3 g1 = mk3(G1), g2 = mk3(G2), g3 = mk3(G3), g4 = mk3(G4);
   // c_i = w_i lam q_i
   const float lam_bar = w1 * dot(g1, q1) + w2 * dot(g2, q2) + w3 * dot(g3, q3) + w4 * dot(g4, q4);
@@ -206,9 +220,9 @@ __device__ __forceinline__ bool bend_vjp(float4 A1, float4 A2, float4 A3, float4
   float w1b = lam * dot(g1, q1), w2b = lam * dot(g2, q2), w3b = lam * dot(g3, q3),
         w4b = lam * dot(g4, q4);
   // lam = s (angle - theta) / denom
-  const float s_bar = lam_bar * (angle - theta) / denom;
-  const float angle_bar = lam_bar * s / denom;
-  const float denom_bar = -lam_bar * lam / denom;
+  const float s_bar = lam_bar * (angle - theta) * rden;
+  const float angle_bar = lam_bar * s * rden;
+  const float denom_bar = -lam_bar * lam * rden;
   // denom = at + sum w_i |q_i|^2
   q1b = q1b + (2.0f * denom_bar * w1) * q1;
   q2b = q2b + (2.0f * denom_bar * w2) * q2;
@@ -218,15 +232,15 @@ __device__ __forceinline__ bool bend_vjp(float4 A1, float4 A2, float4 A3, float4
   w2b += denom_bar * dot(q2, q2);
   w3b += denom_bar * dot(q3, q3);
   w4b += denom_bar * dot(q4, q4);
-  cbar += denom_bar / dt / dt;
+  cbar += denom_bar * idt2;
   // q1 = -q2 - q3 - q4
   q2b = q2b - q1b;
   q3b = q3b - q1b;
   q4b = q4b - q1b;
-  // q3 = A3v / e23, q4 = A4v / e24, q2 = -A23 / e23 - A24 / e24
-  const f3 A3b = q3b / e23, A4b = q4b / e24, A23b = -q2b / e23, A24b = -q2b / e24;
-  const float e23b = -dot(q3b, q3) / e23 + dot(q2b, A23) / (e23 * e23);
-  const float e24b = -dot(q4b, q4) / e24 + dot(q2b, A24) / (e24 * e24);
+  // q3 = A3v / e23, q4 = A4v / e24, q2 = -A23 / e23 - A24 / e24  (e = |c| + eps)
+  const f3 A3b = q3b * r23, A4b = q4b * r24, A23b = -(q2b * r23), A24b = -(q2b * r24);
+  const float e23b = (-dot(q3b, q3) + dot(q2b, A23) * r23) * r23;
+  const float e24b = (-dot(q4b, q4) + dot(q2b, A24) * r24) * r24;
   f3 p2b = mk3(0, 0, 0), p3b = mk3(0, 0, 0), p4b = mk3(0, 0, 0);
   f3 n1b = mk3(0, 0, 0), n2b = mk3(0, 0, 0);
   float db = 0.0f;
@@ -247,15 +261,15 @@ __device__ __forceinline__ bool bend_vjp(float4 A1, float4 A2, float4 A3, float4
   cross_bwd(n2, p4, A24b * d, n2b, p4b);
   db += dot(A24b, B24);
   // s = sqrt(1 - d^2); angle = acos_as(d)
-  db += s_bar * (-d / s) + angle_bar * acos_as_deriv(d);
+  db += s_bar * (-d * rs) + angle_bar * acos_as_deriv(d);
   // d = clamp(n1 . n2, 0, 1)
   if (draw > 0.0f && draw < 1.0f) {
     n1b = n1b + db * n2;
     n2b = n2b + db * n1;
   }
   // n = c / |c|, e = |c| + eps
-  const f3 c23b = (n1b - dot(n1, n1b) * n1) / L23 + e23b * n1;
-  const f3 c24b = (n2b - dot(n2, n2b) * n2) / L24 + e24b * n2;
+  const f3 c23b = (n1b - dot(n1, n1b) * n1) * i23 + e23b * n1;
+  const f3 c24b = (n2b - dot(n2, n2b) * n2) * i24 + e24b * n2;
   cross_bwd(p2, p3, c23b, p2b, p3b);
   cross_bwd(p2, p4, c24b, p2b, p4b);
   const f3 p1b = -(p2b + p3b + p4b);
@@ -289,24 +303,23 @@ __global__ void k_bend_bwd(const uint32_t* __restrict__ order, uint32_t begin, u
 
 // ---- tiled replay and reverse ---------------------------------------------------------------
 // With the tile-local schedule the replay runs the forward's tile kernels (one launch per tile
-// color, footprint in shared memory) and tapes each tile's footprint as it enters the launch
-// (plus the multipliers, stretch) instead of every projection's inputs.  The reverse of a tile
-// color launch is one block per tile, tile colors last to first: the block reloads the tile's
-// entry footprint, re-runs its local colors in shared memory (the forward's code in the
-// forward's order, hence its bits) while it parks each projection's inputs in a per-slot
-// scratch array, then walks the local colors backwards with the footprint's adjoint staged in
-// shared memory.  Tiles of one tile color have disjoint footprints, so the write-back of the
-// adjoint needs no atomics.  Shared memory: footprint positions and adjoints (2 x 16 B), ids
-// (4 B) per footprint vertex; record (16 B) + multiplier and its adjoint (stretch, 8 B) or
-// rest angle and compliance (bend, 8 B) per constraint; num_local + 1 offsets.
+// color, footprint in shared memory, the forward's code in the forward's order, hence its bits)
+// and tapes each projection's inputs by execution slot (a local color's slots are contiguous, so
+// the tape writes coalesce).  The reverse of a tile color launch is one block per tile, tile
+// colors last to first: the block stages the footprint's adjoint in shared memory and walks the
+// tile's local colors backwards, reading the taped inputs.  Tiles of one tile color have
+// disjoint footprints, so the write-back of the adjoint needs no atomics.  Shared memory of the
+// reverse: adjoint (16 B) and id (4 B) per footprint vertex; record (16 B) + multiplier adjoint
+// (stretch, 4 B) or rest angle and compliance (bend, 8 B) per constraint; num_local + 1
+// offsets.
 
 template <bool RESET, int NT>
 __global__ void __launch_bounds__(NT) k_stretch_tiles_tape(
     const int4* __restrict__ con, float* __restrict__ lambda, float4* __restrict__ x,
     const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
     const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
-    uint32_t max_foot, uint32_t max_cons, float dt, float4* __restrict__ tfx,
-    float* __restrict__ tlam) {
+    uint32_t max_foot, uint32_t max_cons, float dt, float4* __restrict__ tx,
+    float* __restrict__ tl) {
   extern __shared__ float4 smem[];
   float4* sx = smem;
   int4* sc = reinterpret_cast<int4*>(sx + max_foot);
@@ -318,10 +331,8 @@ __global__ void __launch_bounds__(NT) k_stretch_tiles_tape(
   for (uint32_t j = threadIdx.x; j < nc; j += NT) {
     sc[j] = __ldg(&con[c0 + j]);
     sl[j] = RESET ? 0.0f : lambda[c0 + j];
-    if (!RESET) tlam[c0 + j] = sl[j];
   }
   tile_gather<NT>(f, x, sx, sf);
-  for (uint32_t k = threadIdx.x; k < (uint32_t)f.m.y; k += NT) tfx[f.m.x + k] = sx[k];
   __syncthreads();
   for (uint32_t l = 0; l < num_local; ++l) {
     const uint32_t ce = so[l + 1];
@@ -329,6 +340,9 @@ __global__ void __launch_bounds__(NT) k_stretch_tiles_tape(
       const int4 c = sc[j];
       float lam = sl[j];
       float4 a = sx[c.x], b = sx[c.y];
+      tx[2 * (size_t)(c0 + j)] = a;
+      tx[2 * (size_t)(c0 + j) + 1] = b;
+      tl[c0 + j] = lam;
       if (stretch_project(a, b, __int_as_float(c.z), __int_as_float(c.w), dt, lam)) {
         sx[c.x] = a;
         sx[c.y] = b;
@@ -346,7 +360,7 @@ __global__ void __launch_bounds__(NT) k_bend_tiles_tape(
     const int4* __restrict__ idx, const float2* __restrict__ tc, float4* __restrict__ x,
     const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
     const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
-    uint32_t max_foot, uint32_t max_cons, float dt, float4* __restrict__ tfx) {
+    uint32_t max_foot, uint32_t max_cons, float dt, float4* __restrict__ tx) {
   extern __shared__ float4 smem[];
   float4* sx = smem;
   int4* sc = reinterpret_cast<int4*>(sx + max_foot);
@@ -360,7 +374,6 @@ __global__ void __launch_bounds__(NT) k_bend_tiles_tape(
     st[j] = __ldg(&tc[c0 + j]);
   }
   tile_gather<NT>(f, x, sx, sf);
-  for (uint32_t k = threadIdx.x; k < (uint32_t)f.m.y; k += NT) tfx[f.m.x + k] = sx[k];
   __syncthreads();
   for (uint32_t l = 0; l < num_local; ++l) {
     const uint32_t ce = so[l + 1];
@@ -368,6 +381,11 @@ __global__ void __launch_bounds__(NT) k_bend_tiles_tape(
       const int4 b = sc[j];
       const float2 th = st[j];
       float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
+      float4* t = tx + 4 * (size_t)(c0 + j);
+      t[0] = a1;
+      t[1] = a2;
+      t[2] = a3;
+      t[3] = a4;
       bend_project(a1, a2, a3, a4, th.x, th.y, dt);
       sx[b.x] = a1;
       sx[b.y] = a2;
@@ -379,82 +397,47 @@ __global__ void __launch_bounds__(NT) k_bend_tiles_tape(
   tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
 }
 
-// Stages a tile for its reverse: records, entry footprint (from the tape) and the footprint's
-// adjoint (from G); returns the frame.
-template <int NT>
-__device__ __forceinline__ TileFrame tile_bwd_gather(const uint32_t* __restrict__ foot,
-                                                     const int4* __restrict__ meta,
-                                                     const uint32_t* __restrict__ lofs,
-                                                     uint32_t t, uint32_t num_local,
-                                                     const float4* __restrict__ tfx,
-                                                     const float4* __restrict__ G, float4* sx,
-                                                     float4* sg, uint32_t* so, uint32_t* sf) {
-  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, t, num_local, so);
-#pragma unroll
-  for (int r = 0; r < kFootPerThread; ++r) {
-    const uint32_t k = threadIdx.x + (uint32_t)r * NT;
-    if (k < (uint32_t)f.m.y) {
-      sx[k] = tfx[f.m.x + k];
-      sg[k] = G[f.fi[r]];
-      sf[k] = f.fi[r];
-    }
-  }
-  return f;
-}
-
-template <bool RESET, int NT>
+// STAGE: the tile's slice of the tape (contiguous slots c0 .. c0 + nc) is loaded into shared
+// memory up front, all loads in flight at once, instead of one dependent global load per local
+// color step; for tiles whose slice does not fit, the reverse reads the tape in place.
+template <bool RESET, int NT, bool STAGE>
 __global__ void __launch_bounds__(NT) k_stretch_tiles_bwd(
     const int4* __restrict__ con, const uint32_t* __restrict__ foot,
     const int4* __restrict__ meta, const uint32_t* __restrict__ lofs, uint32_t tile_begin,
     uint32_t num_local, uint32_t max_foot, uint32_t max_cons, float dt,
-    const float4* __restrict__ tfx, const float* __restrict__ tlam, float4* __restrict__ G,
-    float* __restrict__ lam_bar, float* __restrict__ comp_bar, float4* __restrict__ scr_x,
-    float* __restrict__ scr_l) {
+    const float4* __restrict__ tx, const float* __restrict__ tl, float4* __restrict__ G,
+    float* __restrict__ lam_bar, float* __restrict__ comp_bar) {
   extern __shared__ float4 smem[];
-  float4* sx = smem;
-  float4* sg = sx + max_foot;
-  int4* sc = reinterpret_cast<int4*>(sg + max_foot);
-  float* sl = reinterpret_cast<float*>(sc + max_cons);
-  float* slb = sl + max_cons;
-  uint32_t* so = reinterpret_cast<uint32_t*>(slb + max_cons);
+  float4* sg = smem;
+  float4* stx = sg + max_foot;                               // STAGE: 2 x max_cons
+  int4* sc = reinterpret_cast<int4*>(stx + (STAGE ? 2 * max_cons : 0));
+  float* slb = reinterpret_cast<float*>(sc + max_cons);
+  float* stl = slb + max_cons;                               // STAGE: max_cons
+  uint32_t* so = reinterpret_cast<uint32_t*>(stl + (STAGE ? max_cons : 0));
   uint32_t* sf = so + num_local + 1;
-  const TileFrame f = tile_bwd_gather<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local,
-                                          tfx, G, sx, sg, so, sf);
+  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
   const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
+  if (STAGE) {
+    const float4* src = tx + 2 * (size_t)c0;
+    for (uint32_t k = threadIdx.x; k < 2 * nc; k += NT) stx[k] = __ldg(&src[k]);
+  }
   for (uint32_t j = threadIdx.x; j < nc; j += NT) {
     sc[j] = __ldg(&con[c0 + j]);
-    sl[j] = RESET ? 0.0f : tlam[c0 + j];
     slb[j] = lam_bar[c0 + j];
+    if (STAGE) stl[j] = __ldg(&tl[c0 + j]);
   }
+  tile_gather<NT>(f, G, sg, sf);
   __syncthreads();
-  // forward again, parking each projection's inputs (slot j is handled by the same thread in
-  // both sweeps, so the scratch is read back by the thread that wrote it)
-  for (uint32_t l = 0; l < num_local; ++l) {
-    const uint32_t ce = so[l + 1];
-    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
-      const int4 c = sc[j];
-      float lam = sl[j];
-      float4 a = sx[c.x], b = sx[c.y];
-      scr_x[2 * (size_t)(c0 + j)] = a;
-      scr_x[2 * (size_t)(c0 + j) + 1] = b;
-      scr_l[c0 + j] = lam;
-      if (stretch_project(a, b, __int_as_float(c.z), __int_as_float(c.w), dt, lam)) {
-        sx[c.x] = a;
-        sx[c.y] = b;
-        sl[j] = lam;
-      }
-    }
-    __syncthreads();
-  }
+  const float4* ax = STAGE ? stx : tx + 2 * (size_t)c0;
+  const float* al = STAGE ? stl : tl + c0;
   for (int l = (int)num_local - 1; l >= 0; --l) {
     const uint32_t ce = so[l + 1];
     for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
       const int4 c = sc[j];
       float4 ga = sg[c.x], gb = sg[c.y];
       float lin = slb[j], cb = 0.0f;
-      if (stretch_vjp(scr_x[2 * (size_t)(c0 + j)], scr_x[2 * (size_t)(c0 + j) + 1],
-                      scr_l[c0 + j], __int_as_float(c.z), __int_as_float(c.w), dt, slb[j], ga,
-                      gb, lin, cb)) {
+      if (stretch_vjp(ax[2 * j], ax[2 * j + 1], al[j], __int_as_float(c.z), __int_as_float(c.w),
+                      dt, slb[j], ga, gb, lin, cb)) {
         sg[c.x] = ga;
         sg[c.y] = gb;
         comp_bar[c0 + j] += cb;
@@ -467,53 +450,39 @@ __global__ void __launch_bounds__(NT) k_stretch_tiles_bwd(
   for (uint32_t j = threadIdx.x; j < nc; j += NT) lam_bar[c0 + j] = slb[j];
 }
 
-template <int NT>
+template <int NT, bool STAGE>
 __global__ void __launch_bounds__(NT) k_bend_tiles_bwd(
     const int4* __restrict__ idx, const float2* __restrict__ tc,
     const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
     const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
-    uint32_t max_foot, uint32_t max_cons, float dt, const float4* __restrict__ tfx,
-    float4* __restrict__ G, float* __restrict__ bcomp_bar, float4* __restrict__ scr_x) {
+    uint32_t max_foot, uint32_t max_cons, float dt, const float4* __restrict__ tx,
+    float4* __restrict__ G, float* __restrict__ bcomp_bar) {
   extern __shared__ float4 smem[];
-  float4* sx = smem;
-  float4* sg = sx + max_foot;
-  int4* sc = reinterpret_cast<int4*>(sg + max_foot);
+  float4* sg = smem;
+  float4* stx = sg + max_foot;                               // STAGE: 4 x max_cons
+  int4* sc = reinterpret_cast<int4*>(stx + (STAGE ? 4 * max_cons : 0));
   float2* st = reinterpret_cast<float2*>(sc + max_cons);
   uint32_t* so = reinterpret_cast<uint32_t*>(st + max_cons);
   uint32_t* sf = so + num_local + 1;
-  const TileFrame f = tile_bwd_gather<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local,
-                                          tfx, G, sx, sg, so, sf);
+  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
   const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
+  if (STAGE) {
+    const float4* src = tx + 4 * (size_t)c0;
+    for (uint32_t k = threadIdx.x; k < 4 * nc; k += NT) stx[k] = __ldg(&src[k]);
+  }
   for (uint32_t j = threadIdx.x; j < nc; j += NT) {
     sc[j] = __ldg(&idx[c0 + j]);
     st[j] = __ldg(&tc[c0 + j]);
   }
+  tile_gather<NT>(f, G, sg, sf);
   __syncthreads();
-  for (uint32_t l = 0; l < num_local; ++l) {
-    const uint32_t ce = so[l + 1];
-    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
-      const int4 b = sc[j];
-      const float2 th = st[j];
-      float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
-      float4* s = scr_x + 4 * (size_t)(c0 + j);
-      s[0] = a1;
-      s[1] = a2;
-      s[2] = a3;
-      s[3] = a4;
-      bend_project(a1, a2, a3, a4, th.x, th.y, dt);
-      sx[b.x] = a1;
-      sx[b.y] = a2;
-      sx[b.z] = a3;
-      sx[b.w] = a4;
-    }
-    __syncthreads();
-  }
+  const float4* ax = STAGE ? stx : tx + 4 * (size_t)c0;
   for (int l = (int)num_local - 1; l >= 0; --l) {
     const uint32_t ce = so[l + 1];
     for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
       const int4 b = sc[j];
       const float2 th = st[j];
-      const float4* s = scr_x + 4 * (size_t)(c0 + j);
+      const float4* s = ax + 4 * (size_t)j;
       float4 G1 = sg[b.x], G2 = sg[b.y], G3 = sg[b.z], G4 = sg[b.w];
       float cb = 0.0f;
       if (bend_vjp(s[0], s[1], s[2], s[3], th.x, th.y, dt, G1, G2, G3, G4, cb)) {
@@ -755,14 +724,46 @@ void color_groups(const Context& c, int kind, std::vector<uint32_t>& order,
   }
 }
 
-// Shared memory per constraint of the tiled reverse: record + multiplier + its adjoint
-// (stretch), record + rest angle and compliance (bend).
-constexpr size_t kStretchBwdRecord = sizeof(int4) + 2 * sizeof(float);
+// Shared memory per constraint of the tiled reverse: record + multiplier adjoint (stretch),
+// record + rest angle and compliance (bend); plus, when the tape slice is staged, the taped
+// inputs (two vertices + multiplier, four vertices).
+constexpr size_t kStretchBwdRecord = sizeof(int4) + sizeof(float);
 constexpr size_t kBendBwdRecord = sizeof(int4) + sizeof(float2);
+constexpr size_t kStretchStaged = 2 * sizeof(float4) + sizeof(float);
+constexpr size_t kBendStaged = 4 * sizeof(float4);
 
 size_t tiles_bwd_smem(const TiledSet& T, size_t record) {
-  return (2 * sizeof(float4) + sizeof(uint32_t)) * T.max_foot + record * T.max_cons +
+  return (sizeof(float4) + sizeof(uint32_t)) * T.max_foot + record * T.max_cons +
          sizeof(uint32_t) * (T.num_local + 1);
+}
+size_t stretch_bwd_smem(const Context& c) {
+  return tiles_bwd_smem(c.s_tiles, kStretchBwdRecord + (c.diff.s_stage ? kStretchStaged : 0));
+}
+size_t bend_bwd_smem(const Context& c) {
+  return tiles_bwd_smem(c.b_tiles, kBendBwdRecord + (c.diff.b_stage ? kBendStaged : 0));
+}
+
+using StretchBwdKernel = void (*)(const int4*, const uint32_t*, const int4*, const uint32_t*,
+                                  uint32_t, uint32_t, uint32_t, uint32_t, float, const float4*,
+                                  const float*, float4*, float*, float*);
+using BendBwdKernel = void (*)(const int4*, const float2*, const uint32_t*, const int4*,
+                               const uint32_t*, uint32_t, uint32_t, uint32_t, uint32_t, float,
+                               const float4*, float4*, float*);
+
+template <int NT>
+StretchBwdKernel stretch_bwd_nt(bool reset, bool stage) {
+  return reset ? (stage ? k_stretch_tiles_bwd<true, NT, true> : k_stretch_tiles_bwd<true, NT, false>)
+               : (stage ? k_stretch_tiles_bwd<false, NT, true>
+                        : k_stretch_tiles_bwd<false, NT, false>);
+}
+StretchBwdKernel stretch_bwd_kernel(const Context& c, bool reset) {
+  return c.s_tiles.block == 256 ? stretch_bwd_nt<256>(reset, c.diff.s_stage)
+                                : stretch_bwd_nt<512>(reset, c.diff.s_stage);
+}
+BendBwdKernel bend_bwd_kernel(const Context& c) {
+  const bool st = c.diff.b_stage;
+  return c.b_tiles.block == 256 ? (st ? k_bend_tiles_bwd<256, true> : k_bend_tiles_bwd<256, false>)
+                                : (st ? k_bend_tiles_bwd<512, true> : k_bend_tiles_bwd<512, false>);
 }
 
 // The dynamic shared-memory limit of a kernel is process-wide: only ever raised, so a context
@@ -790,30 +791,21 @@ cudaError_t configure_tiled_adjoint(const Context& c) {
   if (D.s_tiled) {
     const TiledSet& T = c.s_tiles;
     const size_t ft = tile_smem_bytes(T, sizeof(int4) + sizeof(float));
-    const size_t bw = tiles_bwd_smem(T, kStretchBwdRecord);
     if (T.block == 256) {
       set((const void*)k_stretch_tiles_tape<true, 256>, ft);
       set((const void*)k_stretch_tiles_tape<false, 256>, ft);
-      set((const void*)k_stretch_tiles_bwd<true, 256>, bw);
-      set((const void*)k_stretch_tiles_bwd<false, 256>, bw);
     } else {
       set((const void*)k_stretch_tiles_tape<true, 512>, ft);
       set((const void*)k_stretch_tiles_tape<false, 512>, ft);
-      set((const void*)k_stretch_tiles_bwd<true, 512>, bw);
-      set((const void*)k_stretch_tiles_bwd<false, 512>, bw);
     }
+    set((const void*)stretch_bwd_kernel(c, true), stretch_bwd_smem(c));
+    set((const void*)stretch_bwd_kernel(c, false), stretch_bwd_smem(c));
   }
   if (D.b_tiled) {
     const TiledSet& T = c.b_tiles;
-    const size_t ft = tile_smem_bytes(T, sizeof(int4) + sizeof(float2));
-    const size_t bw = tiles_bwd_smem(T, kBendBwdRecord);
-    if (T.block == 256) {
-      set((const void*)k_bend_tiles_tape<256>, ft);
-      set((const void*)k_bend_tiles_bwd<256>, bw);
-    } else {
-      set((const void*)k_bend_tiles_tape<512>, ft);
-      set((const void*)k_bend_tiles_bwd<512>, bw);
-    }
+    set(T.block == 256 ? (const void*)k_bend_tiles_tape<256> : (const void*)k_bend_tiles_tape<512>,
+        tile_smem_bytes(T, sizeof(int4) + sizeof(float2)));
+    set((const void*)bend_bwd_kernel(c), bend_bwd_smem(c));
   }
   return e;
 }
@@ -826,14 +818,14 @@ void stretch_tiles_tape(Context& c, float dt, bool reset, size_t ti) {
   auto kern = T.block == 256
                   ? (reset ? k_stretch_tiles_tape<true, 256> : k_stretch_tiles_tape<false, 256>)
                   : (reset ? k_stretch_tiles_tape<true, 512> : k_stretch_tiles_tape<false, 512>);
-  float4* tfx = D.t_fs.p + ti * T.foot_len;
-  float* tl = D.t_lam.p + ti * c.ne;
+  float4* tx = D.t_sx.p + 2 * ti * c.ne;
+  float* tl = D.t_sl.p + ti * c.ne;
   for (const ColorRange& r : T.tile_colors)
     if (r.end > r.begin)
       kern<<<r.end - r.begin, T.block, smem, c.stream>>>(c.s_con.p, c.s_lambda.p, c.x.p,
                                                          T.foot.p, T.meta.p, T.lofs.p, r.begin,
                                                          T.num_local, T.max_foot, T.max_cons, dt,
-                                                         tfx, tl);
+                                                         tx, tl);
 }
 
 void bend_tiles_tape(Context& c, float dt, size_t ti) {
@@ -841,44 +833,42 @@ void bend_tiles_tape(Context& c, float dt, size_t ti) {
   const TiledSet& T = c.b_tiles;
   const size_t smem = tile_smem_bytes(T, sizeof(int4) + sizeof(float2));
   auto kern = T.block == 256 ? k_bend_tiles_tape<256> : k_bend_tiles_tape<512>;
-  float4* tfx = D.t_fb.p + ti * T.foot_len;
+  float4* tx = D.t_bx.p + 4 * ti * c.nb;
   for (const ColorRange& r : T.tile_colors)
     if (r.end > r.begin)
       kern<<<r.end - r.begin, T.block, smem, c.stream>>>(c.b_idx.p, c.b_tc.p, c.x.p, T.foot.p,
                                                          T.meta.p, T.lofs.p, r.begin, T.num_local,
-                                                         T.max_foot, T.max_cons, dt, tfx);
+                                                         T.max_foot, T.max_cons, dt, tx);
 }
 
 void stretch_tiles_bwd(Context& c, float dt, bool reset, size_t ti) {
   DiffState& D = c.diff;
   const TiledSet& T = c.s_tiles;
-  const size_t smem = tiles_bwd_smem(T, kStretchBwdRecord);
-  auto kern = T.block == 256
-                  ? (reset ? k_stretch_tiles_bwd<true, 256> : k_stretch_tiles_bwd<false, 256>)
-                  : (reset ? k_stretch_tiles_bwd<true, 512> : k_stretch_tiles_bwd<false, 512>);
-  const float4* tfx = D.t_fs.p + ti * T.foot_len;
-  const float* tl = D.t_lam.p + ti * c.ne;
+  const size_t smem = stretch_bwd_smem(c);
+  const StretchBwdKernel kern = stretch_bwd_kernel(c, reset);
+  const float4* tx = D.t_sx.p + 2 * ti * c.ne;
+  const float* tl = D.t_sl.p + ti * c.ne;
   for (int k = (int)T.tile_colors.size() - 1; k >= 0; --k) {
     const ColorRange r = T.tile_colors[k];
     if (r.end > r.begin)
       kern<<<r.end - r.begin, T.block, smem, c.stream>>>(
           c.s_con.p, T.foot.p, T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot, T.max_cons,
-          dt, tfx, tl, D.G.p, D.lam_bar.p, D.comp_bar.p, D.t_sx.p, D.t_sl.p);
+          dt, tx, tl, D.G.p, D.lam_bar.p, D.comp_bar.p);
   }
 }
 
 void bend_tiles_bwd(Context& c, float dt, size_t ti) {
   DiffState& D = c.diff;
   const TiledSet& T = c.b_tiles;
-  const size_t smem = tiles_bwd_smem(T, kBendBwdRecord);
-  auto kern = T.block == 256 ? k_bend_tiles_bwd<256> : k_bend_tiles_bwd<512>;
-  const float4* tfx = D.t_fb.p + ti * T.foot_len;
+  const size_t smem = bend_bwd_smem(c);
+  const BendBwdKernel kern = bend_bwd_kernel(c);
+  const float4* tx = D.t_bx.p + 4 * ti * c.nb;
   for (int k = (int)T.tile_colors.size() - 1; k >= 0; --k) {
     const ColorRange r = T.tile_colors[k];
     if (r.end > r.begin)
       kern<<<r.end - r.begin, T.block, smem, c.stream>>>(
           c.b_idx.p, c.b_tc.p, T.foot.p, T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot,
-          T.max_cons, dt, tfx, D.G.p, D.bcomp_bar.p, D.t_bx.p);
+          T.max_cons, dt, tx, D.G.p, D.bcomp_bar.p);
   }
 }
 
@@ -893,6 +883,7 @@ void record_frame_diff(Context& c) {
   const xrt_swift_params& p = c.params;
   const FrameConst k = frame_const(c);
   const uint32_t V = c.nv, E = c.ne, B = c.nb;
+  Timed timed(c, kAdjReplay, 1, V);  // the frame's launches as one group
   float4* const x_start = c.x.p;
   int swaps = 0;
   auto swap_x = [&]() {
@@ -985,39 +976,56 @@ void backward_frame(Context& c) {
   const bool lra_fused = p.geodesic_lra && c.nl && c.lra_by_target;
   const float kd = 1 - k.damping * k.dt;
   const unsigned gv = grid_for(V), blk = kBlock;
+  const uint32_t n_vertex_launches = (has_obstacle ? 2 : 0) + (lra_fused || has_obstacle ? 1 : 0) +
+                                     (lra_fused ? 1 : 0);
+  const uint32_t n_bend_launches =
+      D.b_tiled ? (uint32_t)c.b_tiles.tile_colors.size() : (uint32_t)D.b_colors.size();
+  const uint32_t n_stretch_launches =
+      D.s_tiled ? (uint32_t)c.s_tiles.tile_colors.size() : (uint32_t)D.s_colors.size();
   for (int s = (int)D.S - 1; s >= 0; --s) {
-    k_finalize_bwd<<<gv, blk, 0, c.stream>>>(D.G.p, D.Gv.p, D.H.p, V, k.dt, kd);
-    cudaMemsetAsync(D.lam_bar.p, 0, sizeof(float) * std::max(E, 1u), c.stream);
+    {
+      Timed t(c, kAdjVertex, 1, V);
+      k_finalize_bwd<<<gv, blk, 0, c.stream>>>(D.G.p, D.Gv.p, D.H.p, V, k.dt, kd);
+      cudaMemsetAsync(D.lam_bar.p, 0, sizeof(float) * std::max(E, 1u), c.stream);
+    }
     for (int it = (int)D.I - 1; it >= 0; --it) {
       const size_t ti = (size_t)s * D.I + it;
       const int pass = D.it_pass[ti];
       const size_t pv = (size_t)pass * V, pe = (size_t)pass * E;
-      if (has_obstacle) {
-        const float4* X = D.t_ee.p + ti * V;
-        k_ee_count<<<gv, blk, 0, c.stream>>>(X, V, c.ve_ptr.p, c.ve_list.p, c.edge.p,
-                                            D.t_ee_a.p + pe, D.t_ee_b.p + pe, D.t_ee_c.p + pe,
-                                            D.cnt.p);
-        k_ee_bwd<<<gv, blk, 0, c.stream>>>(X, D.G.p, D.G2.p, V, c.ve_ptr.p, c.ve_list.p, c.edge.p,
-                                          D.t_ee_a.p + pe, D.t_ee_b.p + pe, D.t_ee_c.p + pe,
-                                          D.cnt.p, k.relaxation);
-        std::swap(D.G.p, D.G2.p);
-      }
-      if (lra_fused || has_obstacle) {
-        k_stage_bwd<<<gv, blk, 0, c.stream>>>(
-            D.t_stage.p + ti * V, D.G.p, D.G2.p, D.Gs.p, V, lra_fused, c.lra_ptr.p, c.lra_src.p,
-            c.lra_rest.p, k.lra_stretch, has_obstacle, D.t_rt_idx.p + pv, D.t_rt_qc.p + pv,
-            D.t_vf_idx.p + pv, D.t_vf_qs.p + pv, D.t_pred.p + (size_t)pass * 3 * c.onf, c.err.p);
-        if (lra_fused) k_add_sources<<<gv, blk, 0, c.stream>>>(D.G2.p, D.Gs.p, V);
-        std::swap(D.G.p, D.G2.p);
-      }
-      if (p.solve_bending && D.b_tiled) bend_tiles_bwd(c, k.dt, ti);
-      else if (p.solve_bending)
-        for (int ci = (int)D.b_colors.size() - 1; ci >= 0; --ci) {
-          const ColorRange r = D.b_colors[ci];
-          k_bend_bwd<<<grid_for(r.end - r.begin), blk, 0, c.stream>>>(
-              D.b_order.p, r.begin, r.end, D.b_gidx.p, c.b_tc.p, D.t_bx.p + 4 * ti * B, D.G.p,
-              D.bcomp_bar.p, k.dt);
+      {
+        Timed tv(c, kAdjVertex, n_vertex_launches, V);
+        if (has_obstacle) {
+          const float4* X = D.t_ee.p + ti * V;
+          k_ee_count<<<gv, blk, 0, c.stream>>>(X, V, c.ve_ptr.p, c.ve_list.p, c.edge.p,
+                                              D.t_ee_a.p + pe, D.t_ee_b.p + pe, D.t_ee_c.p + pe,
+                                              D.cnt.p);
+          k_ee_bwd<<<gv, blk, 0, c.stream>>>(X, D.G.p, D.G2.p, V, c.ve_ptr.p, c.ve_list.p,
+                                            c.edge.p, D.t_ee_a.p + pe, D.t_ee_b.p + pe,
+                                            D.t_ee_c.p + pe, D.cnt.p, k.relaxation);
+          std::swap(D.G.p, D.G2.p);
         }
+        if (lra_fused || has_obstacle) {
+          k_stage_bwd<<<gv, blk, 0, c.stream>>>(
+              D.t_stage.p + ti * V, D.G.p, D.G2.p, D.Gs.p, V, lra_fused, c.lra_ptr.p,
+              c.lra_src.p, c.lra_rest.p, k.lra_stretch, has_obstacle, D.t_rt_idx.p + pv,
+              D.t_rt_qc.p + pv, D.t_vf_idx.p + pv, D.t_vf_qs.p + pv,
+              D.t_pred.p + (size_t)pass * 3 * c.onf, c.err.p);
+          if (lra_fused) k_add_sources<<<gv, blk, 0, c.stream>>>(D.G2.p, D.Gs.p, V);
+          std::swap(D.G.p, D.G2.p);
+        }
+      }
+      if (p.solve_bending) {
+        Timed tb(c, kAdjBend, n_bend_launches, B);
+        if (D.b_tiled) bend_tiles_bwd(c, k.dt, ti);
+        else
+          for (int ci = (int)D.b_colors.size() - 1; ci >= 0; --ci) {
+            const ColorRange r = D.b_colors[ci];
+            k_bend_bwd<<<grid_for(r.end - r.begin), blk, 0, c.stream>>>(
+                D.b_order.p, r.begin, r.end, D.b_gidx.p, c.b_tc.p, D.t_bx.p + 4 * ti * B, D.G.p,
+                D.bcomp_bar.p, k.dt);
+          }
+      }
+      Timed ts(c, kAdjStretch, n_stretch_launches, E);
       if (D.s_tiled) stretch_tiles_bwd(c, k.dt, it == 0, ti);
       else for (int ci = (int)D.s_colors.size() - 1; ci >= 0; --ci) {
         const ColorRange r = D.s_colors[ci];
@@ -1034,8 +1042,55 @@ void backward_frame(Context& c) {
                                                          D.comp_bar.p, k.dt);
       }
     }
+    Timed t(c, kAdjVertex, 1, V);
     k_predict_bwd<<<gv, blk, 0, c.stream>>>(D.G.p, D.Gv.p, D.H.p, V, k.dt);
   }
+}
+
+void destroy_frame_graphs(DiffState& D) {
+  for (DiffState::FrameGraph& g : D.graph) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = DiffState::FrameGraph{};
+  }
+}
+
+// Replay + reverse of the frame whose checkpoint is loaded, as a graph: captured on first use
+// for the current G / G2 assignment (capture only records, so the host-side buffer swaps are
+// undone and re-applied after each launch).
+cudaError_t run_frame_graph(Context& c) {
+  DiffState& D = c.diff;
+  DiffState::FrameGraph* g = nullptr;
+  for (DiffState::FrameGraph& fg : D.graph)
+    if (fg.exec && fg.g_in == D.G.p) g = &fg;
+  if (!g) {
+    g = D.graph[0].exec ? &D.graph[1] : &D.graph[0];
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    *g = DiffState::FrameGraph{};
+    float4* const g_in = D.G.p;
+    float4* const g2_in = D.G2.p;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    record_frame_diff(c);
+    backward_frame(c);
+    e = cudaStreamEndCapture(c.stream, &graph);
+    if (e != cudaSuccess) return e;
+    e = cudaGraphInstantiate(&g->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      g->exec = nullptr;
+      return e;
+    }
+    g->g_in = g_in;
+    g->g_out = D.G.p;
+    g->g2_out = D.G2.p;
+    D.G.p = g_in;
+    D.G2.p = g2_in;
+  }
+  cudaError_t e = cudaGraphLaunch(g->exec, c.stream);
+  D.G.p = g->g_out;
+  D.G2.p = g->g2_out;
+  return e;
 }
 
 void save_state(Context& c, DiffState::Checkpoint& ck) {
@@ -1117,16 +1172,14 @@ xrt_status diff_prepare(Context& c) {
               tiles_bwd_smem(c.s_tiles, kStretchBwdRecord) <= (size_t)smem_max;
   D.b_tiled = c.b_tiles.on && c.nb > 0 && p.solve_bending &&
               tiles_bwd_smem(c.b_tiles, kBendBwdRecord) <= (size_t)smem_max;
+  D.s_stage = D.s_tiled && tiles_bwd_smem(c.s_tiles, kStretchBwdRecord + kStretchStaged) <=
+                               (size_t)smem_max;
+  D.b_stage = D.b_tiled &&
+              tiles_bwd_smem(c.b_tiles, kBendBwdRecord + kBendStaged) <= (size_t)smem_max;
   if (D.s_tiled || D.b_tiled) XRT_CUDA(&c, configure_tiled_adjoint(c));
-  const size_t s_it = D.s_tiled ? 1 : SI, b_it = D.b_tiled ? 1 : SI;
-  XRT_CUDA(&c, D.t_sx.reserve(2 * s_it * E));
-  XRT_CUDA(&c, D.t_sl.reserve(s_it * E));
-  XRT_CUDA(&c, D.t_bx.reserve(4 * b_it * Bn));
-  if (D.s_tiled) {
-    XRT_CUDA(&c, D.t_fs.reserve(SI * c.s_tiles.foot_len));
-    XRT_CUDA(&c, D.t_lam.reserve(SI * E));
-  }
-  if (D.b_tiled) XRT_CUDA(&c, D.t_fb.reserve(SI * c.b_tiles.foot_len));
+  XRT_CUDA(&c, D.t_sx.reserve(2 * SI * E));
+  XRT_CUDA(&c, D.t_sl.reserve(SI * E));
+  XRT_CUDA(&c, D.t_bx.reserve(4 * SI * Bn));
   XRT_CUDA(&c, D.t_stage.reserve(SI * V));
   XRT_CUDA(&c, D.t_ee.reserve(c.onf ? SI * V : 1));
   XRT_CUDA(&c, D.t_vf_idx.reserve(P * V));
@@ -1180,9 +1233,21 @@ xrt_status diff_backward(Context& c, const float* dLdx, const float* dLdv, float
   XRT_CUDA(&c, cudaMemsetAsync(D.bcomp_bar.p, 0, sizeof(float) * std::max(c.nb, 1u), s));
   for (int f = (int)D.frames - 1; f >= 0; --f) {
     load_state(c, D.ck[f]);
-    record_frame_diff(c);
-    backward_frame(c);
+    if (c.graph_enabled && !c.profiling) {
+      const cudaError_t e = run_frame_graph(c);
+      if (e != cudaSuccess) {
+        destroy_frame_graphs(D);
+        load_state(c, now);
+        c.set_error(std::string("reverse frame graph: ") + cudaGetErrorString(e));
+        return XRT_ERR_CUDA;
+      }
+    } else {
+      record_frame_diff(c);
+      backward_frame(c);
+      collect_profile(c);  // when profiling: the frame's replay and reverse phases
+    }
   }
+  destroy_frame_graphs(D);
   load_state(c, now);
   XRT_CUDA(&c, cudaGetLastError());
   // outputs
@@ -1225,15 +1290,16 @@ xrt_status diff_backward(Context& c, const float* dLdx, const float* dLdv, float
 
 void diff_release(Context& c) {
   DiffState& D = c.diff;
+  destroy_frame_graphs(D);
   for (auto& ck : D.ck)
     for (DBuf<float4>* b : {&ck.x, &ck.x0, &ck.v, &ck.ox0, &ck.ox, &ck.on}) b->release();
   D.ck.clear();
   D.s_order.release(); D.b_order.release(); D.s_gidx.release(); D.b_gidx.release();
   for (DBuf<float4>* b : {&D.t_sx, &D.t_bx, &D.t_stage, &D.t_ee, &D.t_vf_qs, &D.t_rt_qc,
                           &D.t_ee_a, &D.t_ee_b, &D.t_ee_c, &D.t_pred, &D.G, &D.G2, &D.Gv, &D.H,
-                          &D.Gs, &D.t_fs, &D.t_fb})
+                          &D.Gs})
     b->release();
-  D.t_sl.release(); D.t_lam.release(); D.t_vf_idx.release(); D.t_rt_idx.release();
+  D.t_sl.release(); D.t_vf_idx.release(); D.t_rt_idx.release();
   D.cnt.release(); D.lam_bar.release(); D.comp_bar.release(); D.bcomp_bar.release();
   D.active = false;
   D.frames = 0;
