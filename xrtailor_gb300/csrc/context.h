@@ -175,6 +175,7 @@ struct DiffState {
   // schedule is tiled (s_tiled / b_tiled), per color otherwise
   bool s_tiled = false, b_tiled = false;
   bool s_stage = false, b_stage = false;  // tiled reverse stages each tile's tape in shared memory
+  uint32_t s_block = 256, b_block = 256;  // threads per tile block of the tiled reverse
   DBuf<float4> t_sx;                    // S x I x E x 2: stretch inputs (x with inverse mass)
   DBuf<float> t_sl;                     // S x I x E: stretch multipliers in
   DBuf<float4> t_bx;                    // S x I x B x 4: bend inputs

@@ -375,22 +375,24 @@ __global__ void __launch_bounds__(NT) k_bend_tiles_tape(
   }
   tile_gather<NT>(f, x, sx, sf);
   __syncthreads();
+  // the forward's lane-pair projection (bend_project_pair, the same bits as bend_project); each
+  // lane tapes the two input vertices it owns.  The loop trip count is warp-uniform.
+  const uint32_t lane0 = threadIdx.x & ~31u;
   for (uint32_t l = 0; l < num_local; ++l) {
-    const uint32_t ce = so[l + 1];
-    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
+    const uint32_t cb = 2 * so[l], ce = 2 * so[l + 1];
+    for (uint32_t base = cb + lane0; base < ce; base += NT) {
+      const uint32_t s = base + (threadIdx.x & 31u);
+      const bool active = s < ce;
+      const uint32_t j = active ? s >> 1 : cb >> 1;
+      const uint32_t half = s & 1u;
       const int4 b = sc[j];
       const float2 th = st[j];
-      float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
-      float4* t = tx + 4 * (size_t)(c0 + j);
-      t[0] = a1;
-      t[1] = a2;
-      t[2] = a3;
-      t[3] = a4;
-      bend_project(a1, a2, a3, a4, th.x, th.y, dt);
-      sx[b.x] = a1;
-      sx[b.y] = a2;
-      sx[b.z] = a3;
-      sx[b.w] = a4;
+      if (active) {
+        float4* t = tx + 4 * (size_t)(c0 + j) + 2 * half;
+        t[0] = sx[half ? b.z : b.x];
+        t[1] = sx[half ? b.w : b.y];
+      }
+      bend_project_pair(sx, b, th.x, th.y, dt, half, active);
     }
     __syncthreads();
   }
@@ -736,12 +738,14 @@ size_t tiles_bwd_smem(const TiledSet& T, size_t record) {
   return (sizeof(float4) + sizeof(uint32_t)) * T.max_foot + record * T.max_cons +
          sizeof(uint32_t) * (T.num_local + 1);
 }
-size_t stretch_bwd_smem(const Context& c) {
-  return tiles_bwd_smem(c.s_tiles, kStretchBwdRecord + (c.diff.s_stage ? kStretchStaged : 0));
+size_t stretch_bwd_smem(const TiledSet& T, bool stage) {
+  return tiles_bwd_smem(T, kStretchBwdRecord + (stage ? kStretchStaged : 0));
 }
-size_t bend_bwd_smem(const Context& c) {
-  return tiles_bwd_smem(c.b_tiles, kBendBwdRecord + (c.diff.b_stage ? kBendStaged : 0));
+size_t bend_bwd_smem(const TiledSet& T, bool stage) {
+  return tiles_bwd_smem(T, kBendBwdRecord + (stage ? kBendStaged : 0));
 }
+size_t stretch_bwd_smem(const Context& c) { return stretch_bwd_smem(c.s_tiles, c.diff.s_stage); }
+size_t bend_bwd_smem(const Context& c) { return bend_bwd_smem(c.b_tiles, c.diff.b_stage); }
 
 using StretchBwdKernel = void (*)(const int4*, const uint32_t*, const int4*, const uint32_t*,
                                   uint32_t, uint32_t, uint32_t, uint32_t, float, const float4*,
@@ -756,14 +760,25 @@ StretchBwdKernel stretch_bwd_nt(bool reset, bool stage) {
                : (stage ? k_stretch_tiles_bwd<false, NT, true>
                         : k_stretch_tiles_bwd<false, NT, false>);
 }
+StretchBwdKernel stretch_bwd_kernel(uint32_t block, bool reset, bool stage) {
+  return block == 128 ? stretch_bwd_nt<128>(reset, stage)
+         : block == 256 ? stretch_bwd_nt<256>(reset, stage)
+                        : stretch_bwd_nt<512>(reset, stage);
+}
 StretchBwdKernel stretch_bwd_kernel(const Context& c, bool reset) {
-  return c.s_tiles.block == 256 ? stretch_bwd_nt<256>(reset, c.diff.s_stage)
-                                : stretch_bwd_nt<512>(reset, c.diff.s_stage);
+  return stretch_bwd_kernel(c.diff.s_block, reset, c.diff.s_stage);
+}
+template <int NT>
+BendBwdKernel bend_bwd_nt(bool stage) {
+  return stage ? k_bend_tiles_bwd<NT, true> : k_bend_tiles_bwd<NT, false>;
+}
+BendBwdKernel bend_bwd_kernel(uint32_t block, bool stage) {
+  return block == 128 ? bend_bwd_nt<128>(stage)
+         : block == 256 ? bend_bwd_nt<256>(stage)
+                        : bend_bwd_nt<512>(stage);
 }
 BendBwdKernel bend_bwd_kernel(const Context& c) {
-  const bool st = c.diff.b_stage;
-  return c.b_tiles.block == 256 ? (st ? k_bend_tiles_bwd<256, true> : k_bend_tiles_bwd<256, false>)
-                                : (st ? k_bend_tiles_bwd<512, true> : k_bend_tiles_bwd<512, false>);
+  return bend_bwd_kernel(c.diff.b_block, c.diff.b_stage);
 }
 
 // The dynamic shared-memory limit of a kernel is process-wide: only ever raised, so a context
@@ -782,8 +797,38 @@ cudaError_t raise_smem(const void* kern, size_t bytes) {
   return e;
 }
 
-cudaError_t configure_tiled_adjoint(const Context& c) {
-  const DiffState& D = c.diff;
+// Launch shape of a tiled reverse: 128-thread blocks where the footprints fit (a local color of
+// a tile rarely has more elements, and four blocks per SM hold more tiles at once), else the
+// forward's; the tape slice is staged when the staged blocks still hold the largest tile color
+// in one wave (or lose no resident blocks), read in place otherwise.
+template <typename K>
+cudaError_t choose_reverse_shape(const Context& c, const TiledSet& T, K (*kernel)(uint32_t, bool),
+                                 size_t smem_plain, size_t smem_staged, int smem_max,
+                                 uint32_t& block, bool& stage) {
+  block = T.max_foot <= kFootPerThread * 128u ? 128u : T.block;
+  uint32_t widest = 0;
+  for (const ColorRange& r : T.tile_colors) widest = std::max(widest, r.end - r.begin);
+  int occ_plain = 0, occ_staged = 0;
+  cudaError_t e = raise_smem((const void*)kernel(block, false), smem_plain);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_plain, kernel(block, false),
+                                                      (int)block, smem_plain);
+  if (e != cudaSuccess) return e;
+  stage = false;
+  if (smem_staged <= (size_t)smem_max) {
+    e = raise_smem((const void*)kernel(block, true), smem_staged);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_staged, kernel(block, true),
+                                                        (int)block, smem_staged);
+    if (e != cudaSuccess) return e;
+    stage = occ_staged > 0 && ((uint64_t)occ_staged * (uint64_t)c.num_sms >= widest ||
+                               occ_staged >= occ_plain);
+  }
+  return cudaSuccess;
+}
+
+cudaError_t configure_tiled_adjoint(Context& c, int smem_max) {
+  DiffState& D = c.diff;
   cudaError_t e = cudaSuccess;
   auto set = [&](const void* k, size_t b) {
     if (e == cudaSuccess) e = raise_smem(k, b);
@@ -798,14 +843,20 @@ cudaError_t configure_tiled_adjoint(const Context& c) {
       set((const void*)k_stretch_tiles_tape<true, 512>, ft);
       set((const void*)k_stretch_tiles_tape<false, 512>, ft);
     }
+    if (e == cudaSuccess)
+      e = choose_reverse_shape(
+          c, T, +[](uint32_t b, bool s) { return stretch_bwd_kernel(b, false, s); },
+          stretch_bwd_smem(T, false), stretch_bwd_smem(T, true), smem_max, D.s_block, D.s_stage);
     set((const void*)stretch_bwd_kernel(c, true), stretch_bwd_smem(c));
-    set((const void*)stretch_bwd_kernel(c, false), stretch_bwd_smem(c));
   }
   if (D.b_tiled) {
     const TiledSet& T = c.b_tiles;
     set(T.block == 256 ? (const void*)k_bend_tiles_tape<256> : (const void*)k_bend_tiles_tape<512>,
         tile_smem_bytes(T, sizeof(int4) + sizeof(float2)));
-    set((const void*)bend_bwd_kernel(c), bend_bwd_smem(c));
+    if (e == cudaSuccess)
+      e = choose_reverse_shape(
+          c, T, +[](uint32_t b, bool s) { return bend_bwd_kernel(b, s); },
+          bend_bwd_smem(T, false), bend_bwd_smem(T, true), smem_max, D.b_block, D.b_stage);
   }
   return e;
 }
@@ -851,7 +902,7 @@ void stretch_tiles_bwd(Context& c, float dt, bool reset, size_t ti) {
   for (int k = (int)T.tile_colors.size() - 1; k >= 0; --k) {
     const ColorRange r = T.tile_colors[k];
     if (r.end > r.begin)
-      kern<<<r.end - r.begin, T.block, smem, c.stream>>>(
+      kern<<<r.end - r.begin, D.s_block, smem, c.stream>>>(
           c.s_con.p, T.foot.p, T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot, T.max_cons,
           dt, tx, tl, D.G.p, D.lam_bar.p, D.comp_bar.p);
   }
@@ -866,7 +917,7 @@ void bend_tiles_bwd(Context& c, float dt, size_t ti) {
   for (int k = (int)T.tile_colors.size() - 1; k >= 0; --k) {
     const ColorRange r = T.tile_colors[k];
     if (r.end > r.begin)
-      kern<<<r.end - r.begin, T.block, smem, c.stream>>>(
+      kern<<<r.end - r.begin, D.b_block, smem, c.stream>>>(
           c.b_idx.p, c.b_tc.p, T.foot.p, T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot,
           T.max_cons, dt, tx, D.G.p, D.bcomp_bar.p);
   }
@@ -1172,11 +1223,7 @@ xrt_status diff_prepare(Context& c) {
               tiles_bwd_smem(c.s_tiles, kStretchBwdRecord) <= (size_t)smem_max;
   D.b_tiled = c.b_tiles.on && c.nb > 0 && p.solve_bending &&
               tiles_bwd_smem(c.b_tiles, kBendBwdRecord) <= (size_t)smem_max;
-  D.s_stage = D.s_tiled && tiles_bwd_smem(c.s_tiles, kStretchBwdRecord + kStretchStaged) <=
-                               (size_t)smem_max;
-  D.b_stage = D.b_tiled &&
-              tiles_bwd_smem(c.b_tiles, kBendBwdRecord + kBendStaged) <= (size_t)smem_max;
-  if (D.s_tiled || D.b_tiled) XRT_CUDA(&c, configure_tiled_adjoint(c));
+  if (D.s_tiled || D.b_tiled) XRT_CUDA(&c, configure_tiled_adjoint(c, smem_max));
   XRT_CUDA(&c, D.t_sx.reserve(2 * SI * E));
   XRT_CUDA(&c, D.t_sl.reserve(SI * E));
   XRT_CUDA(&c, D.t_bx.reserve(4 * SI * Bn));

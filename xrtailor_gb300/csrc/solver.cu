@@ -147,16 +147,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_stretch_tiles(
   for (uint32_t j = threadIdx.x; j < nc; j += NT) lambda[c0 + j] = sl[j];
 }
 
-// The same projection on a lane pair (lanes 2m, 2m+1 of a warp, `half` = lane & 1), for the
-// shared-memory footprint of a tile: each lane evaluates one of the two independent halves of
-// the expression (normal n1 and gradient q3 / normal n2, gradient q4 and the angle), the halves
-// are exchanged by shuffles, and lane 0 writes vertices 1-2, lane 1 vertices 3-4.  Every value is
-// produced by the same operations as bend_project, so the result is identical.  All 32 lanes
-// call it; `active` is false for lanes past the color's last element (they write nothing).
-__device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float theta,
-                                                  float compliance, float dt, uint32_t half,
-                                                  bool active);
-
 __global__ void k_bend(const int4* __restrict__ idx, const float2* __restrict__ tc,
                        float4* __restrict__ x, uint32_t begin, uint32_t end, float dt) {
   pdl_release();
@@ -231,56 +221,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
   }
   pdl_release();
   tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
-}
-
-// Lane pair form of bend_project.  With (nA, nB, lA) = (n1, n2, |p2 x p3| + eps) on lane 0 and
-// (n2, n1, |p2 x p4| + eps) on lane 1, and pA = p3 / p4:
-//   q3 (lane 0) and q4 (lane 1) are both (p2 x nB + (nA x p2) d) / lA,
-//   the two terms of q2 are -(pA x nB + (nA x pA) d) / lA on lane 0 and +(...) / lA on lane 1;
-// (-X) / L equals -(X / L) bit for bit, so both lanes run one instruction stream.
-__device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float theta,
-                                                  float compliance, float dt, uint32_t half,
-                                                  bool active) {
-  constexpr unsigned kAll = 0xffffffffu;
-  const float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
-  const f3 p1 = mk3(a1);
-  const f3 p2 = mk3(a2) - p1;
-  const f3 p3 = mk3(a3) - p1;
-  const f3 p4 = mk3(a4) - p1;
-  const f3 pA = half ? p4 : p3;
-  const f3 cA = cross(p2, pA);
-  const f3 nA = normalize(cA);
-  const float lA = length(cA) + kEps;
-  const f3 nB = mk3(__shfl_xor_sync(kAll, nA.x, 1), __shfl_xor_sync(kAll, nA.y, 1),
-                    __shfl_xor_sync(kAll, nA.z, 1));
-  const f3 n1 = half ? nB : nA, n2 = half ? nA : nB;
-  const float d = tclamp(dot(n1, n2), 0.0f, 1.0f);
-  const float angle = acos_as(d);
-  const f3 qA = (cross(p2, nB) + cross(nA, p2) * d) / lA;   // q3 on lane 0, q4 on lane 1
-  const f3 vA = (cross(pA, nB) + cross(nA, pA) * d) / lA;   // |terms| of q2
-  const f3 qB = mk3(__shfl_xor_sync(kAll, qA.x, 1), __shfl_xor_sync(kAll, qA.y, 1),
-                    __shfl_xor_sync(kAll, qA.z, 1));
-  const f3 vB = mk3(__shfl_xor_sync(kAll, vA.x, 1), __shfl_xor_sync(kAll, vA.y, 1),
-                    __shfl_xor_sync(kAll, vA.z, 1));
-  const f3 q3 = half ? qB : qA, q4 = half ? qA : qB;
-  const f3 v23 = half ? vB : vA, v24 = half ? vA : vB;
-  const f3 q2 = -v23 - v24;
-  const f3 q1 = -q2 - q3 - q4;
-  const float w1 = a1.w, w2 = a2.w, w3 = a3.w, w4 = a4.w;
-  const float xpbd_bend = compliance / dt / dt;
-  const float denom =
-      xpbd_bend + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) + w4 * dot(q4, q4));
-  if (!active || angle < kEps || isnan(d) || denom < kEps) return;
-  const float lambda = sqrtf(1.0f - d * d) * (angle - theta) / denom;
-  const float scaling = 1.0f;
-  // lane 0 moves vertices 1 and 2, lane 1 vertices 3 and 4
-  const float wa = half ? w3 : w1, wb = half ? w4 : w2;
-  const f3 qa = half ? q3 : q1, qb = half ? q4 : q2;
-  const float4 aa = half ? a3 : a1, ab = half ? a4 : a2;
-  const f3 ca = scaling * wa * lambda * qa;
-  const f3 cb = scaling * wb * lambda * qb;
-  sx[half ? b.z : b.x] = make_float4(aa.x + ca.x, aa.y + ca.y, aa.z + ca.z, wa);
-  sx[half ? b.w : b.y] = make_float4(ab.x + cb.x, ab.y + cb.y, ab.z + cb.z, wb);
 }
 
 
