@@ -7,7 +7,10 @@ finalize.
 Tolerances.  The library computes in float32, so its gradients carry the float32 error floor of
 the reference's own formulas.  Each test evaluates the same reference program under
 `diff_ref.precision(torch.float32)` and bounds the library's relative error by a small multiple
-of that program's error (plus a floor).  The reference's bend constraint is the stiff, badly
+of that program's error (plus a floor).  Where the frame is well conditioned in float32 (no
+bending), the library's gradients must also match the float32 autodiff of the same program to
+1e-4: that isolates the hand-written adjoint from the forward's rounding (measured: 1e-7 to
+6e-6).  The reference's bend constraint is the stiff, badly
 conditioned part in single precision: its rest angle takes the second normal with the opposite
 orientation to the solve (BasicSolverHelper.cu:8-72 against the rest-angle setup), so a flat
 sheet starts a quarter turn from its target and folds; rollouts that keep the bend stiff are
@@ -72,9 +75,12 @@ def _rel(a, b):
 KEYS = ("position", "velocity", "mass", "stretch_compliance", "bend_compliance")
 
 
-def _check(s, p, pinned, a, c, contacts, cv=None, factor=4.0, floor=2e-4, forward=1e-4, g=None):
+def _check(s, p, pinned, a, c, contacts, cv=None, factor=4.0, floor=2e-4, forward=1e-4, g=None,
+           same_program=None):
     """Run the library's reverse pass (or take its gradients `g`) and compare with the
-    reference in float64 (and float32 for the error floor).  Returns the relative errors."""
+    reference in float64 (and float32 for the error floor).  `same_program`: bound on the
+    relative error against the float32 autodiff of the same program (whose trajectory follows
+    the library's where the frame is well conditioned).  Returns the relative errors."""
     xf = s.host_positions()
     if g is None:
         g = s.backward(c, cv)
@@ -96,8 +102,10 @@ def _check(s, p, pinned, a, c, contacts, cv=None, factor=4.0, floor=2e-4, forwar
         sel = free if k == "mass" else slice(None)
         e = _rel(g[k][sel], g64[k][sel])
         e32 = _rel(g32[k][sel], g64[k][sel])
-        errs[k] = (e, e32)
+        errs[k] = (e, e32, _rel(g[k][sel], g32[k][sel]))
         assert e <= max(factor * e32, floor), (k, e, e32)
+        if same_program is not None:
+            assert errs[k][2] <= same_program, (k, errs[k])
     # the state after the reverse pass is the state before it
     np.testing.assert_array_equal(bits(s.host_positions()), bits(xf))
     return errs
@@ -116,7 +124,7 @@ def test_adjoint_matches_fp64_reference_without_bending(xrt, tile):
     s.step()
     s.step()
     c = np.random.default_rng(5).normal(size=(len(a["x0"]), 3)).astype(np.float32)
-    _check(s, p, pinned, a, c, [[None], [None]])
+    _check(s, p, pinned, a, c, [[None], [None]], same_program=1e-4)
 
 
 @pytest.mark.parametrize("tile", TILES)
@@ -151,7 +159,7 @@ def test_adjoint_matches_fp64_reference_with_obstacle_contacts(xrt):
     assert (ct.vf_idx >= 0).sum() + (ct.rt_idx >= 0).sum() > 0, "the scene has no contact"
     assert (ct.ee_a[:, 0] <= 1e6).sum() > 0, "the scene has no edge contact"
     c = np.random.default_rng(8).normal(size=(len(a["x0"]), 3)).astype(np.float32)
-    _check(s, p, pinned, a, c, [[ct]])
+    _check(s, p, pinned, a, c, [[ct]], same_program=1e-4)
 
 
 def test_torch_rollout_gradients(xrt):
@@ -172,7 +180,7 @@ def test_torch_rollout_gradients(xrt):
              mass=t["mass"].grad.numpy(), stretch_compliance=t["comp"].grad.numpy(),
              bend_compliance=np.zeros(0))
     np.testing.assert_array_equal(bits(x.detach().numpy()), bits(s.host_positions()))
-    _check(s, p, pinned, a, c, [[ct]], cv=cv, g=g)
+    _check(s, p, pinned, a, c, [[ct]], cv=cv, g=g, same_program=1e-4)
 
 
 def test_batched_adjoint_matches_single_contexts(xrt):
