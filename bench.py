@@ -553,6 +553,82 @@ def run_diff(args, local_rank):
     }
 
 
+# Algorithmic bytes per object of the LBVH (fp32, index 4 B): build = primitive read 36 + leaf
+# box 24 + Morton code 4 + radix sort (key + value, read + write, 4 passes of 8 bits) 128 +
+# node 16 + internal box 24; refit = predicted primitive read 36 + leaf box 24 + internal box 24.
+LBVH_BUILD_BYTES = 36 + 24 + 4 + 2 * (4 + 4) * 4 * 2 + 16 + 24
+LBVH_REFIT_BYTES = 36 + 24 + 24
+
+
+def run_lbvh(args, local_rank):
+    """The LBVH of the 1024 x 1024 sheet (2,093,058 triangles): BVH::UpdateData + Construct and
+    the per-pass refit (BVH::RefitMidstep) from device buffers.  One step = one build + one
+    refit, each timed with CUDA events on its own stream; L2 flushed (512 MiB write) before each
+    launch group, outside the events."""
+    import torch
+    from xrtailor_gb300 import Lbvh, build as xb, scenes
+    xb.build()
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    sc = scenes.plain_heavy(1024)
+    pos = sc.cloth.positions.astype(np.float32)
+    tri = sc.cloth.triangles.astype(np.int64)
+    prims = torch.from_numpy(pos[tri].reshape(-1, 9).copy()).to(dev)
+    n = prims.shape[0]
+    rng = np.random.default_rng(3)
+    shift = torch.from_numpy(rng.uniform(-1e-3, 1e-3, size=(len(pos), 3)).astype(np.float32))
+    pred = torch.from_numpy((pos + shift.numpy())[tri].reshape(-1, 9).copy()).to(dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    b = Lbvh(local_rank)
+    for _ in range(max(args.warmup, 1)):
+        b.build_device(prims.data_ptr(), n, pred.data_ptr(), 0.0, sp)
+        b.refit_device(pred.data_ptr(), sp)
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    with ClockSampler(local_rank) as clocks:
+        for e in ev:
+            flush.zero_()
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                e[0].record(stream)
+                b.build_device(prims.data_ptr(), n, pred.data_ptr(), 0.0, sp)
+                e[1].record(stream)
+            torch.cuda.synchronize()
+            flush.zero_()
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                e[2].record(stream)
+                b.refit_device(pred.data_ptr(), sp)
+                e[3].record(stream)
+            torch.cuda.synchronize()
+    t_build = statistics.median(e[0].elapsed_time(e[1]) for e in ev) / 1e3
+    t_refit = statistics.median(e[2].elapsed_time(e[3]) for e in ev) / 1e3
+    peak, peak_kind = _peaks()
+    gb_build = n * LBVH_BUILD_BYTES / t_build / 1e9
+    gb_refit = n * LBVH_REFIT_BYTES / t_refit / 1e9
+    b.close()
+    return {
+        "metric": "LBVH build GB/s (algorithmic bytes)", "value": gb_build, "unit": "GB/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * (t_build + t_refit), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 boxes, u32 codes",
+        "data": "synthetic (seeded: xrtailor_gb300/scenes.py plain_heavy, 1024 x 1024 sheet)",
+        "config": {"workload": "lbvh_1024x1024", "objects": n,
+                   "l2": "flushed before each build and each refit (512 MiB write)",
+                   "parallelism": "single"},
+        "build": {"ms": 1e3 * t_build, "objects_per_s": n / t_build, "GB/s": gb_build,
+                  "bytes_per_object": LBVH_BUILD_BYTES},
+        "refit": {"ms": 1e3 * t_refit, "objects_per_s": n / t_refit, "GB/s": gb_refit,
+                  "bytes_per_object": LBVH_REFIT_BYTES},
+        "roofline": {"bound": "hbm", "achieved": gb_build, "peak": peak, "unit": "GB/s",
+                     "frac": gb_build / peak, "peak_kind": peak_kind,
+                     "refit_frac": gb_refit / peak},
+        "clocks": clocks.summary(),
+    }
+
+
 def run_cpu(workload, frames, warmup=1, threads=0):
     from oracle.oracle import OracleSolver, lib
     from xrtailor_gb300 import scenes
@@ -585,7 +661,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="garment",
-                    choices=["garment", "small", "heavy", "batched", "diff"])
+                    choices=["garment", "small", "heavy", "batched", "diff", "lbvh"])
     ap.add_argument("--cpu-frames", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--instances", type=int, default=512, help="batched workload: garments")
@@ -630,6 +706,10 @@ def main():
     if args.workload == "diff":
         if rank == 0:
             print(json.dumps(run_diff(args, local_rank)))
+        return
+    if args.workload == "lbvh":
+        if rank == 0:
+            print(json.dumps(run_lbvh(args, local_rank)))
         return
     if world > 1:
         import torch

@@ -179,6 +179,22 @@ xrt_status xrt_start(xrt_ctx* ctx);
  * ClothSolverHelper.cu:71-97): world space, 3 * num_obstacle_vertices floats. */
 xrt_status xrt_set_obstacle_targets(xrt_ctx* ctx, const float* positions);
 xrt_status xrt_set_obstacle_targets_device(xrt_ctx* ctx, const float* d_positions);
+/* Obstacle skinning on the device: each xrt_step_frame first computes the obstacle's targets by
+ * linear blend skinning, as SMPL's lbs kernel (src/runtime/rag_doll/smpl/cuda/body.cu:39-60), on
+ * the context stream, so a moving body costs one upload of its joint transforms per frame
+ * instead of its vertex positions.  After xrt_start.  rest: 3 floats per obstacle vertex (the
+ * shaped rest pose, obstacle numbering); influences in CSR over the obstacle vertices: outer
+ * (num_obstacle_vertices + 1 offsets, outer[0] = 0), then per influence a joint index
+ * (< num_joints; joints numbered across all instances of a batched context) and a weight.
+ * rest = NULL turns skinning off.  While it is on, xrt_set_obstacle_targets* return
+ * XRT_ERR_STATE.  Transforms start as identities. */
+xrt_status xrt_set_obstacle_skinning(xrt_ctx* ctx, const float* rest, const uint32_t* outer,
+                                     const uint32_t* joints, const float* weights,
+                                     uint32_t num_joints);
+/* Joint global transforms for the following frames: 12 floats per joint, the top three rows of
+ * the 4x4 homogeneous transform, row-major (SMPL's d_joint_global_transform layout). */
+xrt_status xrt_set_joint_transforms(xrt_ctx* ctx, const float* transforms);
+xrt_status xrt_set_joint_transforms_device(xrt_ctx* ctx, const float* d_transforms);
 /* One frame = ClothSolverBase::SimulateSwift (ClothSolverBase.cpp:171-261). Asynchronous on the
  * context stream; the first call (and the first after set_params) records the frame as a
  * CUDA graph which later calls replay. */

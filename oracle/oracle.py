@@ -344,6 +344,34 @@ class OracleLbvh:
 
 
 # ---- primitive KATs ---------------------------------------------------------------------------
+def lbs(rest, outer, joints, weights, transforms):
+    """Linear blend skinning, SMPL's lbs kernel (src/runtime/rag_doll/smpl/cuda/body.cu:39-60),
+    in float32 with the kernel's products and sums in its order: per vertex and row i, over the
+    vertex's influences in CSR order, out_i += (w T[i][j]) v_j for j = 0, 1, 2, then
+    out_i += w T[i][3].  Every numpy float32 operation rounds once, as the library's kernel
+    (built without contraction) does.  Returns (V, 3) float32."""
+    rest = np.asarray(rest, np.float32).reshape(-1, 3)
+    outer = np.asarray(outer, np.int64)
+    joints = np.asarray(joints, np.int64)
+    w = np.asarray(weights, np.float32)
+    T = np.asarray(transforms, np.float32).reshape(-1, 12)
+    n = len(rest)
+    deg = np.diff(outer)
+    out = np.zeros((n, 3), np.float32)
+    for s in range(int(deg.max()) if n else 0):
+        v = np.nonzero(deg > s)[0]
+        k = outer[v] + s
+        wk, t, p = w[k], T[joints[k]], rest[v]
+        for i in range(3):
+            acc = out[v, i]
+            acc = acc + (wk * t[:, 4 * i]) * p[:, 0]
+            acc = acc + (wk * t[:, 4 * i + 1]) * p[:, 1]
+            acc = acc + (wk * t[:, 4 * i + 2]) * p[:, 2]
+            acc = acc + wk * t[:, 4 * i + 3]
+            out[v, i] = acc
+    return out
+
+
 def expand_bits(v):
     return int(lib().orc_expand_bits(int(v)))
 

@@ -137,6 +137,9 @@ SIGNATURES = {
     "xrt_start": (C.c_int32, [P]),
     "xrt_set_obstacle_targets": (C.c_int32, [P, FP]),
     "xrt_set_obstacle_targets_device": (C.c_int32, [P, P]),
+    "xrt_set_obstacle_skinning": (C.c_int32, [P, FP, UP, UP, FP, C.c_uint32]),
+    "xrt_set_joint_transforms": (C.c_int32, [P, FP]),
+    "xrt_set_joint_transforms_device": (C.c_int32, [P, P]),
     "xrt_step_frame": (C.c_int32, [P]),
     "xrt_step_frames": (C.c_int32, [P, C.c_int32]),
     "xrt_synchronize": (C.c_int32, [P]),

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -373,6 +374,8 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   c.inst.release();
   c.vinst.release();
   c.gen_counter.release();
+  c.skin.rest.release(); c.skin.outer.release(); c.skin.joint.release();
+  c.skin.weight.release(); c.skin.transforms.release();
   for (xrt::TiledSet* t : {&c.s_tiles, &c.b_tiles}) {
     t->foot.release();
     t->meta.release();
@@ -1031,6 +1034,10 @@ xrt_status xrt_set_obstacle_targets(xrt_ctx* h, const float* pos) {
     c.set_error("no obstacle");
     return XRT_ERR_STATE;
   }
+  if (c.skin.on) {
+    c.set_error("obstacle skinning is on: its targets come from the joint transforms");
+    return XRT_ERR_STATE;
+  }
   cudaSetDevice(c.device);
   std::vector<float4> t(c.onv);
   for (uint32_t i = 0; i < c.onv; ++i) t[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0);
@@ -1039,10 +1046,93 @@ xrt_status xrt_set_obstacle_targets(xrt_ctx* h, const float* pos) {
   return XRT_OK;
 }
 
+xrt_status xrt_set_obstacle_skinning(xrt_ctx* h, const float* rest, const uint32_t* outer,
+                                     const uint32_t* joints, const float* weights,
+                                     uint32_t num_joints) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (require_started(c) != XRT_OK) return XRT_ERR_STATE;
+  cudaSetDevice(c.device);
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  if (!rest) {  // off: targets come from xrt_set_obstacle_targets again
+    c.skin.on = false;
+    return XRT_OK;
+  }
+  if (!outer || !joints || !weights || num_joints == 0) return XRT_ERR_INVALID_ARGUMENT;
+  if (c.onv == 0) {
+    c.set_error("no obstacle");
+    return XRT_ERR_STATE;
+  }
+  const uint32_t n = c.onv;
+  if (outer[0] != 0) {
+    c.set_error("skinning weights: outer[0] must be 0");
+    return XRT_ERR_INVALID_ARGUMENT;
+  }
+  for (uint32_t i = 0; i < n; ++i)
+    if (outer[i + 1] < outer[i]) {
+      c.set_error("skinning weights: outer offsets must not decrease");
+      return XRT_ERR_INVALID_ARGUMENT;
+    }
+  const uint32_t nnz = outer[n];
+  for (uint32_t k = 0; k < nnz; ++k)
+    if (joints[k] >= num_joints || !std::isfinite(weights[k])) {
+      c.set_error("skinning weights: joint index out of range or weight not finite");
+      return XRT_ERR_INVALID_ARGUMENT;
+    }
+  std::vector<float4> r(n);
+  for (uint32_t i = 0; i < n; ++i)
+    r[i] = make_float4(rest[3 * i], rest[3 * i + 1], rest[3 * i + 2], 0.0f);
+  XRT_CUDA(&c, upload(c.skin.rest, r, c.stream));
+  XRT_CUDA(&c, upload(c.skin.outer, std::vector<uint32_t>(outer, outer + n + 1), c.stream));
+  XRT_CUDA(&c, upload(c.skin.joint, std::vector<uint32_t>(joints, joints + nnz), c.stream));
+  XRT_CUDA(&c, upload(c.skin.weight, std::vector<float>(weights, weights + nnz), c.stream));
+  // identity transforms until the first xrt_set_joint_transforms
+  std::vector<float> eye((size_t)12 * num_joints, 0.0f);
+  for (uint32_t j = 0; j < num_joints; ++j) eye[12 * j] = eye[12 * j + 5] = eye[12 * j + 10] = 1.0f;
+  XRT_CUDA(&c, upload(c.skin.transforms, eye, c.stream));
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  c.skin.num_joints = num_joints;
+  c.skin.on = true;
+  return XRT_OK;
+}
+
+xrt_status xrt_set_joint_transforms(xrt_ctx* h, const float* transforms) {
+  if (!h || !transforms) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (!c.skin.on) {
+    c.set_error("call xrt_set_obstacle_skinning first");
+    return XRT_ERR_STATE;
+  }
+  cudaSetDevice(c.device);
+  XRT_CUDA(&c, cudaMemcpyAsync(c.skin.transforms.p, transforms,
+                               sizeof(float) * 12 * c.skin.num_joints, cudaMemcpyHostToDevice,
+                               c.stream));
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  return XRT_OK;
+}
+
+xrt_status xrt_set_joint_transforms_device(xrt_ctx* h, const float* d_transforms) {
+  if (!h || !d_transforms) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (!c.skin.on) {
+    c.set_error("call xrt_set_obstacle_skinning first");
+    return XRT_ERR_STATE;
+  }
+  cudaSetDevice(c.device);
+  XRT_CUDA(&c, cudaMemcpyAsync(c.skin.transforms.p, d_transforms,
+                               sizeof(float) * 12 * c.skin.num_joints, cudaMemcpyDeviceToDevice,
+                               c.stream));
+  return XRT_OK;
+}
+
 xrt_status xrt_set_obstacle_targets_device(xrt_ctx* h, const float* d_pos) {
   if (!h || !d_pos) return XRT_ERR_INVALID_ARGUMENT;
   Context& c = h->c;
   if (require_started(c) != XRT_OK) return XRT_ERR_STATE;
+  if (c.skin.on) {
+    c.set_error("obstacle skinning is on: its targets come from the joint transforms");
+    return XRT_ERR_STATE;
+  }
   cudaSetDevice(c.device);
   // 3 floats -> float4 with a strided 2D copy (pitch 12 B in, 16 B out)
   XRT_CUDA(&c, cudaMemcpy2DAsync(c.ox.p, sizeof(float4), d_pos, 3 * sizeof(float), 3 * sizeof(float),
@@ -1059,6 +1149,7 @@ xrt_status xrt_step_frame(xrt_ctx* h) {
     xrt_status st = xrt::prox_prepare(c);
     if (st != XRT_OK) return st;
   }
+  xrt::launch_skin(c);  // obstacle targets from the joint transforms, when skinning is on
   if (c.diff.active) xrt::diff_checkpoint(c);  // state at the frame start, for xrt_backward
   if (c.profiling) {
     record_frame(c);

@@ -217,6 +217,17 @@ struct TiledSet {
   DBuf<uint32_t> lofs;                  // per executed tile: num_local + 1 offsets, tile-relative
 };
 
+// Obstacle skinning on the device (skin.cu): rest pose, CSR influences, joint transforms.
+struct SkinState {
+  bool on = false;
+  uint32_t num_joints = 0;
+  DBuf<float4> rest;        // per obstacle vertex
+  DBuf<uint32_t> outer;     // num_obstacle_vertices + 1
+  DBuf<uint32_t> joint;     // per influence
+  DBuf<float> weight;       // per influence
+  DBuf<float> transforms;   // 12 per joint (3 x 4, row-major)
+};
+
 // Quality-mode self contact (proximity.cu): unified numbering, cloth first then obstacle.
 struct ProximityState {
   bool ready = false;
@@ -342,6 +353,7 @@ struct Context {
   DBuf<uint32_t> ovf_ptr, ovf_list;
   Lbvh bvh;
   ProximityState prox;
+  SkinState skin;
   DiffState diff;
   // host copies of the tile schedules (the adjoint regroups their slots by color)
   std::vector<int4> h_tile_meta[2];
@@ -456,6 +468,8 @@ void launch_ee(Context& c, const FrameConst& k, bool contacts, bool bindings);
 void launch_obstacle_pass(Context& c, int step, int num_steps);
 void launch_generate_contacts(Context& c);
 void launch_obstacle_commit(Context& c);
+// Obstacle targets from the joint transforms (skin.cu), when skinning is on.
+void launch_skin(Context& c);
 void launch_vertex_normals(const float4* x, const int4* tri, const uint32_t* ptr,
                            const uint32_t* list, float4* out, uint32_t nv, cudaStream_t s);
 void launch_hash(Context& c);

@@ -158,6 +158,34 @@ class TubeBody:
         out = np.einsum("vij,vj->vi", Rs[self.bone_of], local) + bases[self.bone_of]
         return out.astype(np.float32)
 
+    def skin(self):
+        """Skinning data of the rigid binding: (rest (V, 3) float32, CSR outer (V + 1),
+        joints (V), weights (V)); one influence of weight 1 per vertex, its bone."""
+        V = len(self.rest)
+        return (self.rest.astype(np.float32), np.arange(V + 1, dtype=np.uint32),
+                self.bone_of.astype(np.uint32), np.ones(V, np.float32))
+
+    def joint_transforms(self, t: float) -> np.ndarray:
+        """(bones, 12) float32: bone b's global transform at time t, top three rows of the 4x4,
+        row-major, so that pose(t) = R_b rest + t_b for the vertices of bone b."""
+        L = self.height / self.bones
+        ang = self.joint_angles(t) / 6.0
+        Rcur = np.eye(3)
+        base0 = np.asarray(self.base, np.float64)
+        base = base0.copy()
+        out = np.zeros((self.bones, 12))
+        for b in range(self.bones):
+            ax = self.axis[b]
+            c, s = np.cos(ang[b]), np.sin(ang[b])
+            K = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+            Rrel = np.eye(3) + s * K + (1 - c) * K @ K
+            if b > 0:
+                base = base + Rcur @ np.array([0.0, L, 0.0])
+            Rcur = Rcur @ Rrel
+            tr = base - Rcur @ (base0 + np.array([0.0, b * L, 0.0]))
+            out[b] = np.concatenate([Rcur, tr[:, None]], axis=1).reshape(-1)
+        return out.astype(np.float32)
+
 
 def two_corner_pins(n: int) -> np.ndarray:
     """Pins the two corners of the edge i = 0 (vertices 0 and n-1)."""

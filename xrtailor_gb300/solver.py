@@ -266,6 +266,28 @@ class ClothSolver:
         p = _f32(positions).reshape(-1)
         L.check(self._lib.xrt_set_obstacle_targets(self._h, L.fptr(p)), self._h, "targets")
 
+    def set_obstacle_skinning(self, rest=None, outer=None, joints=None, weights=None,
+                              num_joints: int = 0):
+        """Obstacle targets by linear blend skinning on the device (xrt_set_obstacle_skinning);
+        `rest=None` turns it off."""
+        if rest is None:
+            L.check(self._lib.xrt_set_obstacle_skinning(self._h, None, None, None, None, 0),
+                    self._h, "skinning")
+            return
+        r, o, j, w = _f32(rest).reshape(-1), _u32(outer), _u32(joints), _f32(weights)
+        L.check(self._lib.xrt_set_obstacle_skinning(self._h, L.fptr(r), L.uptr(o), L.uptr(j),
+                                                    L.fptr(w), int(num_joints)),
+                self._h, "skinning")
+
+    def set_joint_transforms(self, transforms):
+        """12 floats per joint (3 x 4 row-major), host array."""
+        t = _f32(transforms).reshape(-1)
+        L.check(self._lib.xrt_set_joint_transforms(self._h, L.fptr(t)), self._h, "joints")
+
+    def set_joint_transforms_device(self, d_transforms: int):
+        L.check(self._lib.xrt_set_joint_transforms_device(self._h, C.c_void_p(d_transforms)),
+                self._h, "joints")
+
     def fixed_update(self, frames: int = 1):
         """ClothSolverBase::FixedUpdate -> SimulateSwift, `frames` times (asynchronous)."""
         L.check(self._lib.xrt_step_frames(self._h, int(frames)), self._h, "step")
@@ -523,6 +545,18 @@ class Lbvh:
     def refit(self, pred):
         b = _f32(pred).reshape(-1)
         L.check(self._lib.xrt_lbvh_refit(self._h, L.fptr(b), self.n), None, "refit")
+
+    def build_device(self, d_prims: int, n: int, d_pred: int = 0, scr: float = 0.0,
+                     stream: int = 0):
+        """Build from device pointers (9 floats per primitive) on `stream`; no host sync."""
+        self.n = int(n)
+        L.check(self._lib.xrt_lbvh_build_device(self._h, C.c_void_p(d_prims),
+                                                C.c_void_p(d_pred or None), self.n, float(scr),
+                                                C.c_void_p(stream or None)), None, "build_device")
+
+    def refit_device(self, d_pred: int, stream: int = 0):
+        L.check(self._lib.xrt_lbvh_refit_device(self._h, C.c_void_p(d_pred), self.n,
+                                                C.c_void_p(stream or None)), None, "refit_device")
 
     def export(self):
         n = self.n
