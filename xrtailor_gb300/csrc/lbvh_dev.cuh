@@ -66,10 +66,14 @@ __device__ __forceinline__ void lbvh_merge_upwards(uint32_t leaf_node, uint32_t 
       raise_error(err, kErrTreeWalk);
       return;
     }
-    __threadfence();
-    const uint32_t old = atomicAdd(&flags[parent], 1u);
+    // acq_rel: releases this thread's box stores with the arrival; the second arrival acquires
+    // the first's (one ordered atomic instead of two device-wide fences around a relaxed one)
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;"
+                 : "=r"(old)
+                 : "l"(flags + parent)
+                 : "memory");
     if ((old & 1u) == 0u) return;  // first arrival
-    __threadfence();
     const int4 nd = node[parent];
     const float4 la = __ldcg(&lo[nd.y]), ha = __ldcg(&hi[nd.y]);
     const float4 lb = __ldcg(&lo[nd.z]), hb = __ldcg(&hi[nd.z]);
