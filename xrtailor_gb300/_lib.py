@@ -138,6 +138,12 @@ SIGNATURES = {
     "xrt_set_obstacle_targets": (C.c_int32, [P, FP]),
     "xrt_set_obstacle_targets_device": (C.c_int32, [P, P]),
     "xrt_set_obstacle_skinning": (C.c_int32, [P, FP, UP, UP, FP, C.c_uint32]),
+    # include/xrt_cache.h
+    "xrt_cache_begin": (C.c_int32, [P, C.c_uint32, C.c_int32]),
+    "xrt_cache_count": (C.c_int32, [P, UP]),
+    "xrt_cache_read": (C.c_int32, [P, C.c_uint32, FP, FP, FP, FP]),
+    "xrt_cache_export_obj": (C.c_int32, [P, C.c_char_p, C.c_int32]),
+    "xrt_cache_end": (C.c_int32, [P]),
     "xrt_set_joint_transforms": (C.c_int32, [P, FP]),
     "xrt_set_joint_transforms_device": (C.c_int32, [P, P]),
     "xrt_step_frame": (C.c_int32, [P]),

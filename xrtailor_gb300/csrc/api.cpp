@@ -376,6 +376,7 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   c.gen_counter.release();
   c.skin.rest.release(); c.skin.outer.release(); c.skin.joint.release();
   c.skin.weight.release(); c.skin.transforms.release();
+  xrt::cache_release(c);
   for (xrt::TiledSet* t : {&c.s_tiles, &c.b_tiles}) {
     t->foot.release();
     t->meta.release();
@@ -1165,6 +1166,7 @@ xrt_status xrt_step_frame(xrt_ctx* h) {
     record_frame(c);
     XRT_CUDA(&c, cudaGetLastError());
   }
+  XRT_CUDA(&c, xrt::cache_frame(c));  // when recording: this frame into the frame cache
   c.frame_index++;
   return XRT_OK;
 }

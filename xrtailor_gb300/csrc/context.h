@@ -228,6 +228,20 @@ struct SkinState {
   DBuf<float> transforms;   // 12 per joint (3 x 4, row-major)
 };
 
+// Frame cache (cache.cu): device staging slots, a copy stream and a pinned host store.
+struct CacheState {
+  static constexpr int kSlots = 3;
+  bool on = false;
+  uint32_t flags = 0, capacity = 0, count = 0;
+  uint32_t per_frame = 0;            // floats per cached frame
+  float* host = nullptr;             // pinned, capacity x per_frame
+  DBuf<float> stage[kSlots];
+  cudaEvent_t staged[kSlots] = {};   // packing done (context stream)
+  cudaEvent_t copied[kSlots] = {};   // copy to the host done (copy stream)
+  bool used[kSlots] = {};
+  cudaStream_t copy = nullptr;
+};
+
 // Quality-mode self contact (proximity.cu): unified numbering, cloth first then obstacle.
 struct ProximityState {
   bool ready = false;
@@ -354,6 +368,7 @@ struct Context {
   Lbvh bvh;
   ProximityState prox;
   SkinState skin;
+  CacheState cache;
   DiffState diff;
   // host copies of the tile schedules (the adjoint regroups their slots by color)
   std::vector<int4> h_tile_meta[2];
@@ -470,6 +485,9 @@ void launch_generate_contacts(Context& c);
 void launch_obstacle_commit(Context& c);
 // Obstacle targets from the joint transforms (skin.cu), when skinning is on.
 void launch_skin(Context& c);
+// Frame cache (cache.cu): records the frame just issued, when recording; frees the store.
+cudaError_t cache_frame(Context& c);
+void cache_release(Context& c);
 void launch_vertex_normals(const float4* x, const int4* tri, const uint32_t* ptr,
                            const uint32_t* list, float4* out, uint32_t nv, cudaStream_t s);
 void launch_hash(Context& c);

@@ -284,6 +284,46 @@ class ClothSolver:
         t = _f32(transforms).reshape(-1)
         L.check(self._lib.xrt_set_joint_transforms(self._h, L.fptr(t)), self._h, "joints")
 
+    # -- frame cache (include/xrt_cache.h) ------------------------------------------------------
+    CACHE_CLOTH, CACHE_OBSTACLE, CACHE_NORMALS = 1, 2, 4
+
+    def cache_begin(self, capacity_frames: int, cloth=True, obstacle=False, normals=False):
+        """Records the following frames (SaveCache) into a pinned host store."""
+        flags = (self.CACHE_CLOTH if cloth else 0) | (self.CACHE_OBSTACLE if obstacle else 0) | \
+            (self.CACHE_NORMALS if normals else 0)
+        L.check(self._lib.xrt_cache_begin(self._h, int(capacity_frames), flags), self._h, "cache")
+        self._cache_flags = flags
+
+    def cache_count(self) -> int:
+        n = C.c_uint32()
+        L.check(self._lib.xrt_cache_count(self._h, C.byref(n)), self._h, "cache")
+        return n.value
+
+    def cache_read(self, frame: int) -> dict:
+        """Cached frame `frame`: the recorded arrays as (V, 3) float32 (absent ones None)."""
+        s = self.sizes()
+        out = dict(cloth_positions=np.empty((s.num_vertices, 3), np.float32),
+                   cloth_normals=np.empty((s.num_vertices, 3), np.float32),
+                   obstacle_positions=np.empty((s.num_obstacle_vertices, 3), np.float32),
+                   obstacle_normals=np.empty((s.num_obstacle_vertices, 3), np.float32))
+        L.check(self._lib.xrt_cache_read(self._h, int(frame),
+                                         *(L.fptr(a.reshape(-1)) for a in out.values())),
+                self._h, "cache_read")
+        f = getattr(self, "_cache_flags", 0)
+        cl, ob, nr = f & self.CACHE_CLOTH, f & self.CACHE_OBSTACLE, f & self.CACHE_NORMALS
+        present = dict(cloth_positions=cl, cloth_normals=cl and nr, obstacle_positions=ob,
+                       obstacle_normals=ob and nr)
+        return {k: (v if present[k] else None) for k, v in out.items()}
+
+    def cache_export_obj(self, directory: str, obstacle: bool = False):
+        """OBJ sequence of the cached cloth (or obstacle) frames: directory/000000.obj ..."""
+        which = self.CACHE_OBSTACLE if obstacle else self.CACHE_CLOTH
+        L.check(self._lib.xrt_cache_export_obj(self._h, str(directory).encode(), which),
+                self._h, "cache_export_obj")
+
+    def cache_end(self):
+        L.check(self._lib.xrt_cache_end(self._h), self._h, "cache_end")
+
     def set_joint_transforms_device(self, d_transforms: int):
         L.check(self._lib.xrt_set_joint_transforms_device(self._h, C.c_void_p(d_transforms)),
                 self._h, "joints")
