@@ -144,6 +144,11 @@ def bytes_per_substep(s, p, has_obstacle):
 # vertex's edge list entries are data dependent and not counted.
 BYTES_PER_UNIT = {"stretch": 88, "bend": 152, "collide": 48, "vf_solve": 64, "ee_apply": 32,
                   "predict_finalize": 64, "lra": 32}
+# The frame formula's per-unit terms for the tile-local stretch and bend launches: a constraint
+# record (stretch: 2 indices, rest, compliance + multiplier read and written; bend: 4 indices,
+# rest angle, compliance) and a vertex touched once (position read + written, inverse mass).
+RECORD_BYTES = 24
+VERTEX_BYTES = 28
 
 
 def run_ours(args, rank, local_rank, world):
@@ -238,6 +243,18 @@ def run_ours(args, rank, local_rank, world):
     d = phases[dom]
     peak, peak_src = _peaks()
     per_launch_bytes = BYTES_PER_UNIT[dom] * d["units"] / max(d["launches"], 1)
+    accounting = "per constraint: record + every vertex read and written (BYTES_PER_UNIT)"
+    tiles = {"stretch": (s.num_stretch_tile_colors, s.stretch_footprint_vertices),
+             "bend": (s.num_bend_tile_colors, s.bend_footprint_vertices)}.get(dom)
+    if tiles and tiles[0]:
+        # the frame formula's terms for one tile-color launch: the constraints' records (24 B
+        # each: indices, rest value, compliance, multiplier) and each footprint vertex once
+        # (28 B: position read and written, inverse mass read); a tile color's footprints are
+        # disjoint, so a launch touches footprint / tile colors vertices on average
+        per_launch_bytes = (RECORD_BYTES * d["units"] / max(d["launches"], 1) +
+                            VERTEX_BYTES * tiles[1] / tiles[0])
+        accounting = ("frame formula: 24 B per constraint record + 28 B per footprint vertex "
+                      "of the launch")
     per_launch_s = d["ms"] / 1e3 / max(d["launches"], 1)
     achieved = per_launch_bytes / per_launch_s / 1e9
     traffic = None
@@ -269,6 +286,7 @@ def run_ours(args, rank, local_rank, world):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_src, "bytes_per_launch": per_launch_bytes,
+                     "accounting": accounting,
                      "us_per_launch": per_launch_s * 1e6,
                      "share_of_frame": d["ms"] / total_ms if total_ms else None},
         "frame_bandwidth_gbs": frame_bytes / (t_dev / args.steps / world) / 1e9,
@@ -662,7 +680,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="garment",
                     choices=["garment", "small", "heavy", "batched", "diff", "lbvh"])
-    ap.add_argument("--cpu-frames", type=int, default=3)
+    ap.add_argument("--cpu-frames", type=int, default=24,
+                    help="frames of the CPU baseline sample (~10 s of the garment on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--instances", type=int, default=512, help="batched workload: garments")
     ap.add_argument("--plain-sample", type=int, default=512,

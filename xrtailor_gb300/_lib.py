@@ -95,7 +95,10 @@ class Sizes(C.Structure):
         ("num_stretch_colors", C.c_uint32), ("num_bend_colors", C.c_uint32),
         ("launches_per_frame", C.c_uint32), ("frame_index", C.c_uint32),
         ("particle_diameter", C.c_float), ("num_instances", C.c_uint32),
-        ("num_obstacle_bvh_nodes", C.c_uint32), ("reserved", C.c_uint32 * 5),
+        ("num_obstacle_bvh_nodes", C.c_uint32),
+        ("num_stretch_tile_colors", C.c_uint32), ("num_bend_tile_colors", C.c_uint32),
+        ("stretch_footprint_vertices", C.c_uint32), ("bend_footprint_vertices", C.c_uint32),
+        ("reserved", C.c_uint32 * 1),
     ]
 
 
