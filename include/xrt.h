@@ -165,7 +165,9 @@ xrt_status xrt_add_obstacle(xrt_ctx* ctx, const xrt_obstacle_desc* desc, int32_t
  * reference steps one solver per scene. */
 xrt_status xrt_add_instance(xrt_ctx* ctx, const xrt_cloth_desc* cloth,
                             const xrt_obstacle_desc* obstacle, int32_t* out_instance);
-/* Overrides the graph coloring of the stretch (kind 0) or bend (kind 1) constraints, in the
+/* Kinds 2 and 3 are the FEM fabric's strain (one per cloth face) and isometric bending (one per
+ * bend element) constraints (include/xrt_fem.h); xrt_get_coloring reports them after xrt_start.
+ * Overrides the graph coloring of the stretch (kind 0) or bend (kind 1) constraints, in the
  * constraint order reported by xrt_get_edges / xrt_get_bends.  Replaces
  * GraphColoring::Paint (src/physics/graph_coloring/Base.cu:163-317), whose randomized result
  * differs run to run; parity runs feed one coloring to both sides.  Before xrt_start. */

@@ -27,6 +27,7 @@ _SIG = {
     "orc_add_cloth": (C.c_int, [P, C.POINTER(L.ClothDesc)]),
     "orc_add_obstacle": (C.c_int, [P, C.POINTER(L.ObstacleDesc)]),
     "orc_set_coloring": (None, [P, C.c_int, UP, C.c_uint32]),
+    "orc_set_fem_material": (None, [P, C.POINTER(L.FemMaterial)]),
     "orc_set_compliance": (None, [P, C.c_int, FP, C.c_uint32]),
     "orc_set_inv_mass": (None, [P, FP, C.c_uint32]),
     "orc_start": (None, [P]), "orc_set_obstacle_targets": (None, [P, FP]),
@@ -107,8 +108,13 @@ class OracleSolver:
         return r
 
     def set_coloring(self, kind, colors):
+        """kind 0 stretch, 1 bend, 2 FEM strain, 3 FEM bending."""
         c = _u(colors)
         self._l.orc_set_coloring(self._h, kind, c.ctypes.data_as(UP), c.size)
+
+    def set_fem_material(self, material=None):
+        """The FEM fabric (an xrt_fem_material) or None for the Swift fabric; before start()."""
+        self._l.orc_set_fem_material(self._h, C.byref(material) if material is not None else None)
 
     def set_compliance(self, kind, values):
         v = _f(values)

@@ -29,6 +29,7 @@
 #endif
 
 #include "../include/xrt.h"
+#include "../include/xrt_fem.h"
 #include "oracle_lbvh.h"
 
 using namespace orc;
@@ -90,7 +91,14 @@ struct Oracle {
   std::vector<uint32_t> cell_start, cell_end;
   bool started = false;
   uint32_t frame_index = 0;
-  std::vector<uint32_t> pending_colors[2];
+  std::vector<uint32_t> pending_colors[4];  // stretch, bend, FEM strain, FEM bending
+  // FEM fabric (FEMHelper.cu): strain per cloth face, isometric bending per bend element
+  bool fem_on = false;
+  xrt_fem_material fem{};
+  std::vector<float> fem_area, fem_inv;     // per face: area, inverse material matrix (glm order)
+  std::vector<float> fem_q, fem_lambda;     // per bend element: row-major Hessian, multiplier
+  std::vector<uint32_t> fem_color[2];
+  uint32_t fem_ncolors[2] = {0, 0};
   // Quality-mode proximity repulsion / CCD impacts.  Unified numbering: cloth nodes, faces and
   // edges first, then the obstacle's (the reference addresses both through Node*/Face*/Edge*).
   std::vector<uint8_t> cfree;             // Node::is_free of cloth nodes (false when pinned)
@@ -535,6 +543,129 @@ void solve_bend(Oracle& o, uint32_t color, float dt) {
     o.x[i2] += c2;
     o.x[i3] += c3;
     o.x[i4] += c4;
+  }
+}
+
+// ---- FEM fabric ---------------------------------------------------------------------------
+// ComputeStrainMeta (FEMHelper.cu:10-39) per cloth face and ComputeHessianEnergy
+// (FEMHelper.cu:209-233) per bend element, from the initial world positions.  glm's matrices are
+// column-major: P[c][r]; the inverse of a 2x2 is [m11, -m01; -m10, m00] / det in that layout.
+void fem_setup(Oracle& o) {
+  const size_t nf = o.tri.size() / 3, nb = o.bends.size() / 4;
+  o.fem_area.assign(nf, 0.0f);
+  o.fem_inv.assign(4 * nf, 0.0f);
+  for (size_t f = 0; f < nf; ++f) {
+    const V3 p0 = o.x0[o.tri[3 * f]], p1 = o.x0[o.tri[3 * f + 1]], p2 = o.x0[o.tri[3 * f + 2]];
+    const V3 normal0 = cross(p1 - p0, p2 - p0);
+    o.fem_area[f] = 0.5f * length(normal0);
+    const V3 axis0_1 = normalize(p1 - p0);
+    const V3 axis0_2 = normalize(cross(normal0, axis0_1));
+    const float a0 = dot(p0, axis0_2), b0 = dot(p0, axis0_1);
+    const float a1 = dot(p1, axis0_2), b1 = dot(p1, axis0_1);
+    const float a2 = dot(p2, axis0_2), b2 = dot(p2, axis0_1);
+    const float P00 = a0 - a2, P10 = b0 - b2, P01 = a1 - a2, P11 = b1 - b2;
+    const float det = P00 * P11 - P10 * P01;
+    float* inv = &o.fem_inv[4 * f];
+    if (std::fabs(det) > kEps) {
+      const float r = 1.0f / det;
+      inv[0] = P11 * r;
+      inv[1] = (-P01) * r;
+      inv[2] = (-P10) * r;
+      inv[3] = P00 * r;
+    } else {
+      inv[0] = inv[3] = 1.0f;
+    }
+  }
+  o.fem_q.assign(16 * nb, 0.0f);
+  o.fem_lambda.assign(nb, 0.0f);
+  auto cot = [](V3 v, V3 w) { return dot(v, w) / length(cross(v, w)); };  // MathFunctions::CotTheta
+  for (size_t b = 0; b < nb; ++b) {
+    const V3 p0 = o.x0[o.bends[4 * b]], p1 = o.x0[o.bends[4 * b + 1]],
+             p2 = o.x0[o.bends[4 * b + 2]], p3 = o.x0[o.bends[4 * b + 3]];
+    const V3 e0 = p1 - p0, e1 = p2 - p0, e2 = p3 - p0, e3 = p2 - p1, e4 = p3 - p1;
+    const float c01 = cot(e0, e1), c02 = cot(e0, e2), c03 = cot(-e0, e3), c04 = cot(-e0, e4);
+    const float A0 = 0.5f * length(cross(p1 - p0, p2 - p0));
+    const float A1 = 0.5f * length(cross(p0 - p1, p3 - p1));
+    const float coeff = 3.0f / (A0 + A1);
+    const float K[4] = {c03 + c04, c01 + c02, -c01 - c03, -c02 - c04};
+    for (int j = 0; j < 4; ++j)
+      for (int i = 0; i < 4; ++i) o.fem_q[16 * b + 4 * j + i] = coeff * (K[i] * K[j]);
+  }
+}
+
+// SolveStrain_Kernel + ComputeStrainCorrection (FEMHelper.cu:96-207).
+void solve_fem_strain(Oracle& o, uint32_t color) {
+  const xrt_fem_material& m = o.fem;
+  const float d = 1.0f - m.xy_poisson_ratio * m.yx_poisson_ratio;
+  const float C00 = m.xx_stiffness / d, C01 = m.xx_stiffness * m.yx_poisson_ratio / d;
+  const float C11 = m.yy_stiffness / d, C10 = m.yy_stiffness * m.xy_poisson_ratio / d;
+  const float C22 = m.xy_stiffness;
+  const long nf = (long)o.tri.size() / 3;
+#pragma omp parallel for schedule(static)
+  for (long f = 0; f < nf; ++f) {
+    if (o.fem_color[0][f] != color) continue;
+    const uint32_t i0 = o.tri[3 * f], i1 = o.tri[3 * f + 1], i2 = o.tri[3 * f + 2];
+    const V3 p13 = o.x[i0] - o.x[i2], p23 = o.x[i1] - o.x[i2];
+    const float* inv = &o.fem_inv[4 * f];
+    const float F[3][2] = {{p13.x * inv[0] + p23.x * inv[2], p13.x * inv[1] + p23.x * inv[3]},
+                           {p13.y * inv[0] + p23.y * inv[2], p13.y * inv[1] + p23.y * inv[3]},
+                           {p13.z * inv[0] + p23.z * inv[2], p13.z * inv[1] + p23.z * inv[3]}};
+    const float E00 = 0.5f * (F[0][0] * F[0][0] + F[1][0] * F[1][0] + F[2][0] * F[2][0] - 1.0f);
+    const float E11 = 0.5f * (F[0][1] * F[0][1] + F[1][1] * F[1][1] + F[2][1] * F[2][1] - 1.0f);
+    const float E01 = 0.5f * (F[0][0] * F[0][1] + F[1][0] * F[1][1] + F[2][0] * F[2][1]);
+    const float S00 = C00 * E00 + C01 * E11, S11 = C10 * E00 + C11 * E11, S01 = C22 * E01;
+    float Pk[3][2];
+    for (int c = 0; c < 3; ++c) {
+      Pk[c][0] = S00 * F[c][0] + S01 * F[c][1];
+      Pk[c][1] = S01 * F[c][0] + S11 * F[c][1];
+    }
+    const float psi = 0.5f * (((E00 * S00 + E01 * S01) + E01 * S01) + E11 * S11);
+    const float area = o.fem_area[f];
+    const float energy = area * psi;
+    V3 g0, g1;
+    for (int c = 0; c < 3; ++c) {
+      set(g0, c, (inv[0] * Pk[c][0] + inv[1] * Pk[c][1]) * area);
+      set(g1, c, (inv[2] * Pk[c][0] + inv[3] * Pk[c][1]) * area);
+    }
+    const V3 g2 = -g0 - g1;
+    const float w0 = o.w[i0], w1 = o.w[i1], w2 = o.w[i2];
+    float sum = w0 * dot(g0, g0);
+    sum = sum + w1 * dot(g1, g1);
+    sum = sum + w2 * dot(g2, g2);
+    if (!(std::fabs(sum) > kEps)) continue;
+    const float s = energy / sum;
+    if (w0 > kEps) o.x[i0] = o.x[i0] + (-(s * w0)) * g0;
+    if (w1 > kEps) o.x[i1] = o.x[i1] + (-(s * w1)) * g1;
+    if (w2 > kEps) o.x[i2] = o.x[i2] + (-(s * w2)) * g2;
+  }
+}
+
+// SolveIsometricBending_Kernel (FEMHelper.cu:325-388).
+void solve_iso_bend(Oracle& o, uint32_t color, float dt, int iter) {
+  const float alpha = 1.0f / (o.fem.bending_stiffness * dt * dt);
+  const long nb = (long)o.bends.size() / 4;
+#pragma omp parallel for schedule(static)
+  for (long b = 0; b < nb; ++b) {
+    if (o.fem_color[1][b] != color) continue;
+    if (iter == 0) o.fem_lambda[b] = 0.0f;
+    const uint32_t id[4] = {o.bends[4 * b], o.bends[4 * b + 1], o.bends[4 * b + 2],
+                            o.bends[4 * b + 3]};
+    const float* Q = &o.fem_q[16 * b];
+    const V3 x[4] = {o.x[id[0]], o.x[id[1]], o.x[id[2]], o.x[id[3]]};
+    float energy = 0.0f;
+    for (int k = 0; k < 4; ++k)
+      for (int j = 0; j < 4; ++j) energy = energy + Q[4 * j + k] * dot(x[k], x[j]);
+    energy = energy * 0.5f;
+    if (std::fabs(energy) < kEps) continue;
+    V3 d[4] = {};
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) d[j] = d[j] + Q[4 * j + i] * x[i];
+    const float w[4] = {o.w[id[0]], o.w[id[1]], o.w[id[2]], o.w[id[3]]};
+    const float coeff = (w[0] * dot(d[0], d[0]) + w[1] * dot(d[1], d[1])) +
+                        (w[2] * dot(d[2], d[2]) + w[3] * dot(d[3], d[3]));
+    const float dl = (-energy - alpha * o.fem_lambda[b]) / (coeff + alpha);
+    for (int i = 0; i < 4; ++i) o.x[id[i]] = x[i] + (dl * w[i]) * d[i];
+    o.fem_lambda[b] = o.fem_lambda[b] + dl;
   }
 }
 
@@ -1245,9 +1376,15 @@ void step_frame(Oracle& o) {
         if (has_obstacle) generate_contacts(o);
         cnt++;
       }
-      for (uint32_t c = 0; c < o.n_s_colors; ++c) solve_stretch(o, c, substep_time, it);
-      if (p.solve_bending)
-        for (uint32_t c = 0; c < o.n_b_colors; ++c) solve_bend(o, c, substep_time);
+      if (o.fem_on) {  // SimulateQuality's fabric (ClothSolverBase.cpp:315-323)
+        for (uint32_t c = 0; c < o.fem_ncolors[0]; ++c) solve_fem_strain(o, c);
+        if (o.fem.solve_bending && !o.bends.empty())
+          for (uint32_t c = 0; c < o.fem_ncolors[1]; ++c) solve_iso_bend(o, c, substep_time, it);
+      } else {
+        for (uint32_t c = 0; c < o.n_s_colors; ++c) solve_stretch(o, c, substep_time, it);
+        if (p.solve_bending)
+          for (uint32_t c = 0; c < o.n_b_colors; ++c) solve_bend(o, c, substep_time);
+      }
       if (p.geodesic_lra) solve_lra(o);
       if (has_obstacle) {
         solve_contacts(o);
@@ -1287,6 +1424,21 @@ void start(Oracle& o) {
     } else {
       col = greedy_color(idx, arity, nv, nc);
     }
+  }
+  if (o.fem_on) {  // FEM fabric: strain over the faces (kind 2), bending over the bends (kind 3)
+    for (int kind = 0; kind < 2; ++kind) {
+      const std::vector<uint32_t>& idx = kind == 0 ? o.tri : o.bends;
+      std::vector<uint32_t>& col = o.fem_color[kind];
+      uint32_t& nc = o.fem_ncolors[kind];
+      if (!o.pending_colors[2 + kind].empty()) {
+        col = o.pending_colors[2 + kind];
+        nc = 0;
+        for (uint32_t c : col) nc = std::max(nc, c + 1);
+      } else {
+        col = greedy_color(idx, kind == 0 ? 3 : 4, nv, nc);
+      }
+    }
+    fem_setup(o);
   }
   o.s_lambda.assign(o.rest.size(), 0.0f);
   build_vf(o.tri, nv, o.vf_prefix, o.vf_list);
@@ -1451,7 +1603,12 @@ int orc_add_obstacle(void* h, const xrt_obstacle_desc* d) {
 
 void orc_set_coloring(void* h, int kind, const uint32_t* colors, uint32_t n) {
   Oracle& o = *static_cast<Oracle*>(h);
-  o.pending_colors[kind & 1].assign(colors, colors + n);
+  o.pending_colors[kind & 3].assign(colors, colors + n);
+}
+void orc_set_fem_material(void* h, const xrt_fem_material* m) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  o.fem_on = m != nullptr;
+  if (m) o.fem = *m;
 }
 void orc_set_compliance(void* h, int kind, const float* c, uint32_t n) {
   Oracle& o = *static_cast<Oracle*>(h);

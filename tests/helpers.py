@@ -30,11 +30,17 @@ def small_scene(n=16, obstacle="sphere", pins=True, attached=None, seed=1, size=
 
 
 def make_pair(params, cloths, obstacles=(), particle_diameter=0.0, colors_from_gpu=True,
-              inv_mass=None):
-    """Builds a ClothSolver (GPU) and an OracleSolver (CPU) with the same inputs."""
+              inv_mass=None, fem=None, tile_vertices=None):
+    """Builds a ClothSolver (GPU) and an OracleSolver (CPU) with the same inputs; `fem`: an
+    xrt_fem_material for both (the FEM fabric)."""
     from oracle.oracle import OracleSolver
     g = ClothSolver(params)
     o = OracleSolver(params)
+    if tile_vertices is not None:
+        g.set_tile_vertices(tile_vertices)
+    if fem is not None:
+        g.set_fem_material(fem)
+        o.set_fem_material(fem)
     for c in cloths:
         g.add_cloth(c, particle_diameter=particle_diameter)
         o.add_cloth(c, particle_diameter=particle_diameter)
@@ -49,6 +55,9 @@ def make_pair(params, cloths, obstacles=(), particle_diameter=0.0, colors_from_g
     if colors_from_gpu:
         o.set_coloring(0, g.coloring(0))
         o.set_coloring(1, g.coloring(1))
+        if fem is not None:
+            o.set_coloring(2, g.coloring(2))
+            o.set_coloring(3, g.coloring(3))
     o.start()
     return g, o
 

@@ -110,6 +110,14 @@ class Grads(C.Structure):
                 ("position", C.POINTER(C.c_float))]
 
 
+class FemMaterial(C.Structure):
+    """xrt_fem_material (include/xrt_fem.h)."""
+    _fields_ = [("xx_stiffness", C.c_float), ("yy_stiffness", C.c_float),
+                ("xy_stiffness", C.c_float), ("xy_poisson_ratio", C.c_float),
+                ("yx_poisson_ratio", C.c_float), ("bending_stiffness", C.c_float),
+                ("solve_bending", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
 class Profile(C.Structure):
     _fields_ = [("ms", C.c_double * 16), ("launches", C.c_uint64 * 16), ("units", C.c_uint64 * 16),
                 ("frames", C.c_uint32), ("reserved", C.c_uint32 * 7)]
@@ -141,6 +149,9 @@ SIGNATURES = {
     "xrt_set_obstacle_targets": (C.c_int32, [P, FP]),
     "xrt_set_obstacle_targets_device": (C.c_int32, [P, P]),
     "xrt_set_obstacle_skinning": (C.c_int32, [P, FP, UP, UP, FP, C.c_uint32]),
+    # include/xrt_fem.h
+    "xrt_default_fem_material": (C.c_int32, [C.POINTER(FemMaterial)]),
+    "xrt_set_fem_material": (C.c_int32, [P, C.POINTER(FemMaterial)]),
     # include/xrt_cache.h
     "xrt_cache_begin": (C.c_int32, [P, C.c_uint32, C.c_int32]),
     "xrt_cache_count": (C.c_int32, [P, UP]),

@@ -160,7 +160,10 @@ void record_frame(Context& c) {
         }
         cnt++;
       }
-      if (c.s_tiles.on) {
+      if (c.fem.on) {  // FEM fabric: strain colors, then isometric bending colors (profiled as
+                       // the stretch and bend phases)
+        xrt::launch_fem(c, k, it == 0, kStretch, kBend);
+      } else if (c.s_tiles.on) {
         for (size_t tc = 0; tc < c.s_tiles.tile_colors.size(); ++tc) {
           Timed t(c, kStretch, 1, c.s_tiles.tile_color_cons[tc]);
           xrt::launch_stretch_tiles(c, k, c.s_tiles.tile_colors[tc], it == 0);
@@ -171,7 +174,7 @@ void record_frame(Context& c) {
           xrt::launch_stretch(c, k, r, it == 0);
         }
       }
-      if (p.solve_bending) {
+      if (p.solve_bending && !c.fem.on) {
         if (c.b_tiles.on) {
           for (size_t tc = 0; tc < c.b_tiles.tile_colors.size(); ++tc) {
             Timed t(c, kBend, 1, c.b_tiles.tile_color_cons[tc]);
@@ -377,6 +380,7 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   c.skin.rest.release(); c.skin.outer.release(); c.skin.joint.release();
   c.skin.weight.release(); c.skin.transforms.release();
   xrt::cache_release(c);
+  xrt::fem_release(c);
   for (xrt::TiledSet* t : {&c.s_tiles, &c.b_tiles}) {
     t->foot.release();
     t->meta.release();
@@ -619,7 +623,7 @@ xrt_status xrt_add_instance(xrt_ctx* h, const xrt_cloth_desc* cloth,
 }
 
 xrt_status xrt_set_coloring(xrt_ctx* h, int32_t kind, const uint32_t* colors, uint32_t n) {
-  if (!h || (n && !colors) || (kind != 0 && kind != 1)) return XRT_ERR_INVALID_ARGUMENT;
+  if (!h || (n && !colors) || kind < 0 || kind > 3) return XRT_ERR_INVALID_ARGUMENT;
   if (h->c.started) {
     h->c.set_error("xrt_set_coloring after xrt_start");
     return XRT_ERR_STATE;
@@ -722,6 +726,88 @@ static void sort_by_color(const std::vector<uint32_t>& col, uint32_t ncolors,
   }
 }
 
+// One constraint kind's schedule, filled by schedule_kind.
+struct KindSchedule {
+  std::vector<uint32_t>& color;       // per constraint (input order)
+  uint32_t& ncolors;                  // colors (tile colors x local colors when tiled)
+  xrt::TiledSet& tiles;               // on when the tile-local schedule applies
+  std::vector<uint32_t>& perm;        // execution slot -> constraint
+  std::vector<uint32_t>& local;       // tiled: per slot and arity, footprint-local vertex index
+  std::vector<ColorRange>& ranges;    // per color (untiled)
+  std::vector<int4>& meta;            // tiled: host copy of the tile records
+  std::vector<uint32_t>& lofs;        // tiled: host copy of the local-color offsets
+};
+
+// The caller's coloring (validated), else the tile-local Gauss-Seidel schedule (tiles halved
+// until every footprint fits a block), else a greedy coloring.
+static xrt_status schedule_kind(Context& c, const std::vector<uint32_t>& idx, int arity,
+                                const std::vector<uint32_t>& pending,
+                                const std::vector<uint32_t>& segments, KindSchedule K) {
+  if (!pending.empty()) {
+    std::string why;
+    if (!xrt::setup::coloring_valid(idx, arity, pending, c.nv, why)) {
+      c.set_error("invalid coloring: " + why);
+      return XRT_ERR_COLORING;
+    }
+    K.color = pending;
+    K.ncolors = 0;
+    for (uint32_t v : K.color) K.ncolors = std::max(K.ncolors, v + 1);
+    sort_by_color(K.color, K.ncolors, K.perm, K.ranges);
+    return XRT_OK;
+  }
+  bool tiled = false;
+  if (c.tile_vertices > 0 && !idx.empty()) {
+    uint32_t tv = c.tile_vertices;
+    c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv, segments);
+    while (c.tmp_schedule.max_footprint > xrt::kTileMaxFootprint && tv > 32) {
+      tv /= 2;
+      c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv, segments);
+    }
+    tiled = c.tmp_schedule.num_tile_colors > 0 &&
+            c.tmp_schedule.max_footprint <= xrt::kTileMaxFootprint;
+  }
+  if (!tiled) {
+    K.color = xrt::setup::greedy_color(idx, arity, c.nv, K.ncolors);
+    sort_by_color(K.color, K.ncolors, K.perm, K.ranges);
+    return XRT_OK;
+  }
+  // tile-local Gauss-Seidel schedule (a coloring; see setup::TileSchedule)
+  xrt::TiledSet& T = K.tiles;
+  const xrt::setup::TileSchedule& S = c.tmp_schedule;
+  K.color = S.color;
+  K.ncolors = S.num_tile_colors * S.num_local;
+  T.on = true;
+  T.num_local = S.num_local;
+  T.max_foot = S.max_footprint;
+  T.max_cons = 0;
+  T.max_step = 0;
+  for (size_t tt = 0; tt + 1 < S.foot_ptr.size(); ++tt)
+    T.max_cons = std::max(T.max_cons, S.lc_ptr[(tt + 1) * S.num_local] - S.lc_ptr[tt * S.num_local]);
+  for (size_t k = 0; k + 1 < S.lc_ptr.size(); ++k)
+    T.max_step = std::max(T.max_step, S.lc_ptr[k + 1] - S.lc_ptr[k]);
+  T.tile_colors.clear();
+  T.tile_color_cons.clear();
+  for (uint32_t k = 0; k < S.num_tile_colors; ++k) {
+    T.tile_colors.push_back(ColorRange{S.tile_color_ptr[k], S.tile_color_ptr[k + 1]});
+    T.tile_color_cons.push_back(S.lc_ptr[S.tile_color_ptr[k + 1] * S.num_local] -
+                                S.lc_ptr[S.tile_color_ptr[k] * S.num_local]);
+  }
+  K.meta.clear();
+  K.lofs.clear();
+  for (size_t tt = 0; tt + 1 < S.foot_ptr.size(); ++tt) {
+    const uint32_t c0 = S.lc_ptr[tt * S.num_local], c1 = S.lc_ptr[(tt + 1) * S.num_local];
+    K.meta.push_back(make_int4((int)S.foot_ptr[tt], (int)(S.foot_ptr[tt + 1] - S.foot_ptr[tt]),
+                               (int)c0, (int)(c1 - c0)));
+    for (uint32_t l = 0; l <= S.num_local; ++l) K.lofs.push_back(S.lc_ptr[tt * S.num_local + l] - c0);
+  }
+  XRT_CUDA(&c, upload(T.foot, S.foot, c.stream));
+  XRT_CUDA(&c, upload(T.meta, K.meta, c.stream));
+  XRT_CUDA(&c, upload(T.lofs, K.lofs, c.stream));
+  K.perm = S.order;
+  K.local = S.local_slot;
+  return XRT_OK;
+}
+
 xrt_status xrt_start(xrt_ctx* h) {
   if (!h) return XRT_ERR_INVALID_ARGUMENT;
   Context& c = h->c;
@@ -786,71 +872,21 @@ xrt_status xrt_start(xrt_ctx* h) {
   // coloring
   for (int kind = 0; kind < 2; ++kind) {
     const std::vector<uint32_t>& idx = kind == 0 ? c.h_edges : c.h_bends;
-    const int arity = kind == 0 ? 2 : 4;
-    std::vector<uint32_t>& col = kind == 0 ? c.h_scolor : c.h_bcolor;
-    uint32_t& nc = kind == 0 ? c.n_scolors : c.n_bcolors;
-    if (!c.pending_colors[kind].empty()) {
-      std::string why;
-      if (!xrt::setup::coloring_valid(idx, arity, c.pending_colors[kind], c.nv, why)) {
-        c.set_error("invalid coloring: " + why);
-        return XRT_ERR_COLORING;
-      }
-      col = c.pending_colors[kind];
-      nc = 0;
-      for (uint32_t v : col) nc = std::max(nc, v + 1);
-    } else if (c.tile_vertices > 0 && !idx.empty() &&
-               [&] {
-                 uint32_t tv = c.tile_vertices;
-                 c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv, segments);
-                 while (c.tmp_schedule.max_footprint > xrt::kTileMaxFootprint && tv > 32) {
-                   tv /= 2;
-                   c.tmp_schedule = xrt::setup::build_tiles(idx, arity, c.nv, tv, segments);
-                 }
-                 return c.tmp_schedule.num_tile_colors > 0 &&
-                        c.tmp_schedule.max_footprint <= xrt::kTileMaxFootprint;
-               }()) {
-      // tile-local Gauss-Seidel schedule (a coloring; see setup::TileSchedule)
-      xrt::TiledSet& T = kind == 0 ? c.s_tiles : c.b_tiles;
-      const xrt::setup::TileSchedule& S = c.tmp_schedule;
-      col = S.color;
-      nc = S.num_tile_colors * S.num_local;
-      T.on = true;
-      T.num_local = S.num_local;
-      T.max_foot = S.max_footprint;
-      T.max_cons = 0;
-      T.max_step = 0;
-      for (size_t tt = 0; tt + 1 < S.foot_ptr.size(); ++tt)
-        T.max_cons = std::max(T.max_cons, S.lc_ptr[(tt + 1) * S.num_local] - S.lc_ptr[tt * S.num_local]);
-      for (size_t k = 0; k + 1 < S.lc_ptr.size(); ++k)
-        T.max_step = std::max(T.max_step, S.lc_ptr[k + 1] - S.lc_ptr[k]);
-      T.tile_colors.clear();
-      T.tile_color_cons.clear();
-      for (uint32_t k = 0; k < S.num_tile_colors; ++k) {
-        T.tile_colors.push_back(ColorRange{S.tile_color_ptr[k], S.tile_color_ptr[k + 1]});
-        T.tile_color_cons.push_back(S.lc_ptr[S.tile_color_ptr[k + 1] * S.num_local] -
-                                    S.lc_ptr[S.tile_color_ptr[k] * S.num_local]);
-      }
-      std::vector<int4> meta;
-      std::vector<uint32_t> lofs;
-      for (size_t tt = 0; tt + 1 < S.foot_ptr.size(); ++tt) {
-        const uint32_t c0 = S.lc_ptr[tt * S.num_local], c1 = S.lc_ptr[(tt + 1) * S.num_local];
-        meta.push_back(make_int4((int)S.foot_ptr[tt], (int)(S.foot_ptr[tt + 1] - S.foot_ptr[tt]),
-                                 (int)c0, (int)(c1 - c0)));
-        for (uint32_t l = 0; l <= S.num_local; ++l) lofs.push_back(S.lc_ptr[tt * S.num_local + l] - c0);
-      }
-      XRT_CUDA(&c, upload(T.foot, S.foot, c.stream));
-      XRT_CUDA(&c, upload(T.meta, meta, c.stream));
-      XRT_CUDA(&c, upload(T.lofs, lofs, c.stream));
-      c.h_tile_meta[kind] = meta;
-      c.h_tile_lofs[kind] = lofs;
-      (kind == 0 ? c.s_perm : c.b_perm) = S.order;
-      (kind == 0 ? c.s_local : c.b_local) = S.local_slot;
-      continue;
-    } else {
-      col = xrt::setup::greedy_color(idx, arity, c.nv, nc);
+    KindSchedule K{kind == 0 ? c.h_scolor : c.h_bcolor, kind == 0 ? c.n_scolors : c.n_bcolors,
+                   kind == 0 ? c.s_tiles : c.b_tiles, kind == 0 ? c.s_perm : c.b_perm,
+                   kind == 0 ? c.s_local : c.b_local, kind == 0 ? c.s_ranges : c.b_ranges,
+                   c.h_tile_meta[kind], c.h_tile_lofs[kind]};
+    xrt_status st = schedule_kind(c, idx, kind == 0 ? 2 : 4, c.pending_colors[kind], segments, K);
+    if (st != XRT_OK) return st;
+  }
+  if (c.fem.on) {  // the FEM fabric's strain (faces) and isometric bending (bend elements)
+    for (int kind = 0; kind < 2; ++kind) {
+      xrt::FemKind& F = kind == 0 ? c.fem.strain : c.fem.bend;
+      KindSchedule K{F.color, F.ncolors, F.tiles, F.perm, F.local, F.ranges, F.meta, F.lofs};
+      xrt_status st = schedule_kind(c, kind == 0 ? c.h_tri : c.h_bends, kind == 0 ? 3 : 4,
+                                    c.pending_colors[2 + kind], segments, K);
+      if (st != XRT_OK) return st;
     }
-    if (kind == 0) sort_by_color(c.h_scolor, c.n_scolors, c.s_perm, c.s_ranges);
-    else sort_by_color(c.h_bcolor, c.n_bcolors, c.b_perm, c.b_ranges);
   }
   if (c.s_tiles.on || c.b_tiles.on) {
     const size_t smem = std::max(xrt::tile_smem_bytes(c.s_tiles, sizeof(int4) + sizeof(float)),
@@ -862,6 +898,15 @@ xrt_status xrt_start(xrt_ctx* h) {
     XRT_CUDA(&c, xrt::configure_tile_kernels(std::max<size_t>(smem, 16)));
     if (c.s_tiles.on) XRT_CUDA(&c, xrt::choose_tile_block(c.s_tiles, false));
     if (c.b_tiles.on) XRT_CUDA(&c, xrt::choose_tile_block(c.b_tiles, true));
+  }
+  if (c.fem.on) {
+    for (const xrt::FemKind* K : {&c.fem.strain, &c.fem.bend})
+      if (K->tiles.on && xrt::tile_smem_bytes(K->tiles, sizeof(int4) + sizeof(float)) > 200 * 1024) {
+        c.set_error("FEM tile schedule needs more shared memory than a block has");
+        return XRT_ERR_INVALID_MESH;
+      }
+    XRT_CUDA(&c, xrt::fem_configure(c));
+    XRT_CUDA(&c, xrt::fem_upload(c));
   }
   xrt_status st = upload_constraints(c);
   if (st != XRT_OK) return st;
@@ -1362,8 +1407,11 @@ xrt_status xrt_get_bends(const xrt_ctx* h, uint32_t* out4, float* th) {
   return XRT_OK;
 }
 xrt_status xrt_get_coloring(const xrt_ctx* h, int32_t kind, uint32_t* colors) {
-  if (!h || !colors || (kind != 0 && kind != 1)) return XRT_ERR_INVALID_ARGUMENT;
-  const auto& col = kind == 0 ? h->c.h_scolor : h->c.h_bcolor;
+  if (!h || !colors || kind < 0 || kind > 3) return XRT_ERR_INVALID_ARGUMENT;
+  const auto& col = kind == 0   ? h->c.h_scolor
+                    : kind == 1 ? h->c.h_bcolor
+                    : kind == 2 ? h->c.fem.strain.color
+                                : h->c.fem.bend.color;
   std::copy(col.begin(), col.end(), colors);
   return XRT_OK;
 }

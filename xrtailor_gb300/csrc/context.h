@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/xrt.h"
+#include "../../include/xrt_fem.h"
 #include "setup.h"
 
 // Returns XRT_ERR_CUDA from the enclosing function, with the failing call in the context's error.
@@ -217,6 +218,31 @@ struct TiledSet {
   DBuf<uint32_t> lofs;                  // per executed tile: num_local + 1 offsets, tile-relative
 };
 
+// One constraint kind of the FEM fabric: its schedule (as the stretch / bend kinds') and the
+// slot-ordered vertex ids (footprint-local when tiled).
+struct FemKind {
+  std::vector<uint32_t> color;
+  uint32_t ncolors = 0;
+  TiledSet tiles;
+  std::vector<uint32_t> perm, local;
+  std::vector<ColorRange> ranges;
+  std::vector<int4> meta;
+  std::vector<uint32_t> lofs;
+  DBuf<int4> idx;
+};
+
+// The FEM fabric (fem.cu, include/xrt_fem.h).
+struct FemState {
+  bool on = false;
+  xrt_fem_material m{};
+  float c00 = 0, c01 = 0, c10 = 0, c11 = 0, c22 = 0;  // orthotropic tensor entries
+  FemKind strain, bend;            // strain: cloth faces; bend: the bend elements
+  DBuf<float4> s_inv;              // per strain slot: inverse material matrix (glm order)
+  DBuf<float> s_area;              // per strain slot
+  DBuf<float> b_q;                 // per bend slot: 16 floats, row-major Hessian
+  DBuf<float> b_lambda;            // per bend slot
+};
+
 // Obstacle skinning on the device (skin.cu): rest pose, CSR influences, joint transforms.
 struct SkinState {
   bool on = false;
@@ -311,7 +337,7 @@ struct Context {
   std::vector<uint32_t> h_bends;    // 4 per bend
   std::vector<float> h_theta, h_bcomp;
   std::vector<uint32_t> h_scolor, h_bcolor;
-  std::vector<uint32_t> pending_colors[2];
+  std::vector<uint32_t> pending_colors[4];  // stretch, bend, FEM strain, FEM bending
   std::vector<uint32_t> h_lra_src, h_lra_tgt;
   std::vector<float> h_lra_rest;
   struct HostBinding {
@@ -369,6 +395,7 @@ struct Context {
   ProximityState prox;
   SkinState skin;
   CacheState cache;
+  FemState fem;
   DiffState diff;
   // host copies of the tile schedules (the adjoint regroups their slots by color)
   std::vector<int4> h_tile_meta[2];
@@ -468,6 +495,17 @@ void launch_finalize_predict(Context& c, const FrameConst& k, bool predict_next,
 void launch_stretch(Context& c, const FrameConst& k, ColorRange r, bool reset_lambda);
 void launch_bend(Context& c, const FrameConst& k, ColorRange r);
 cudaError_t configure_tile_kernels(size_t max_smem_bytes);
+// Raises a kernel's dynamic shared-memory limit on the current device to at least `bytes`.  The
+// limit is process-wide, so it only ever grows (a context with smaller tiles must not lower it
+// under another's launches).
+cudaError_t raise_smem(const void* kern, size_t bytes);
+// FEM fabric (fem.cu): slot-ordered records after the schedules are built; the launch shapes;
+// one iteration's strain and bending launches (profiled under the given phases).
+cudaError_t fem_upload(Context& c);
+cudaError_t fem_configure(Context& c);
+void launch_fem(Context& c, const FrameConst& k, bool reset_lambda, int phase_strain,
+                int phase_bend);
+void fem_release(Context& c);
 size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes);
 // Sets T.block (256 / 512 threads) and T.resident; after configure_tile_kernels.
 cudaError_t choose_tile_block(TiledSet& T, bool bend);

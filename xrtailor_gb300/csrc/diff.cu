@@ -781,22 +781,6 @@ BendBwdKernel bend_bwd_kernel(const Context& c) {
   return bend_bwd_kernel(c.diff.b_block, c.diff.b_stage);
 }
 
-// The dynamic shared-memory limit of a kernel is process-wide: only ever raised, so a context
-// with smaller tiles does not lower it under another's launches.
-cudaError_t raise_smem(const void* kern, size_t bytes) {
-  static std::mutex mu;
-  static std::map<std::pair<int, const void*>, size_t> set;
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  std::lock_guard<std::mutex> lock(mu);
-  size_t& cur = set[{dev, kern}];
-  if (bytes <= cur) return cudaSuccess;
-  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e == cudaSuccess) cur = bytes;
-  return e;
-}
-
 // Launch shape of a tiled reverse: 128-thread blocks where the footprints fit (a local color of
 // a tile rarely has more elements, and four blocks per SM hold more tiles at once), else the
 // forward's; the tape slice is staged when the staged blocks still hold the largest tile color
@@ -1181,9 +1165,9 @@ void load_state(Context& c, const DiffState::Checkpoint& ck) {
 
 xrt_status diff_prepare(Context& c) {
   const xrt_swift_params& p = c.params;
-  if (p.enable_self_collision || p.pbd_repulsion || c.nbind > 0) {
-    c.set_error("the adjoint covers frames without particle self-collision, Quality repulsion "
-                "or bindings");
+  if (p.enable_self_collision || p.pbd_repulsion || c.nbind > 0 || c.fem.on) {
+    c.set_error("the adjoint covers frames of the Swift fabric without particle "
+                "self-collision, Quality repulsion or bindings");
     return XRT_ERR_INVALID_ARGUMENT;
   }
   if (p.geodesic_lra && c.nl && !c.lra_by_target) {

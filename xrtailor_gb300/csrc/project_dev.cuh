@@ -171,6 +171,89 @@ __device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float thet
   sx[half ? b.w : b.y] = make_float4(ab.x + cb.x, ab.y + cb.y, ab.z + cb.z, wb);
 }
 
+// ---- FEM fabric (FEMHelper.cu) -------------------------------------------------------------
+// The orthotropic elasticity tensor's non-zero entries (ComputeStrainCorrection's C, computed
+// once on the host): c00 = Ex/d, c01 = Ex nu_yx/d, c10 = Ey nu_xy/d, c11 = Ey/d, c22 = Es with
+// d = 1 - nu_xy nu_yx.
+struct FemTensor {
+  float c00, c01, c10, c11, c22;
+};
+
+// ComputeStrainCorrection + SolveStrain_Kernel (FEMHelper.cu:96-173, 175-207): inv holds the
+// rest triangle's inverse material matrix in glm's column-major order (inv[0][0], inv[0][1],
+// inv[1][0], inv[1][1]); the deformation gradient, Green strain, stress, first Piola stress and
+// H = inv^T P area are the reference's products in its order.  Moves the vertices with w > eps;
+// returns false when the gradient norm is too small.
+__device__ __forceinline__ bool fem_strain_project(float4& a0, float4& a1, float4& a2, float area,
+                                                   float4 inv, const FemTensor& C) {
+  const f3 p13 = mk3(a0) - mk3(a2);
+  const f3 p23 = mk3(a1) - mk3(a2);
+  const float i00 = inv.x, i01 = inv.y, i10 = inv.z, i11 = inv.w;
+  // F[c][r], c spatial, r material
+  const float F00 = p13.x * i00 + p23.x * i10, F01 = p13.x * i01 + p23.x * i11;
+  const float F10 = p13.y * i00 + p23.y * i10, F11 = p13.y * i01 + p23.y * i11;
+  const float F20 = p13.z * i00 + p23.z * i10, F21 = p13.z * i01 + p23.z * i11;
+  const float e00 = 0.5f * (F00 * F00 + F10 * F10 + F20 * F20 - 1.0f);
+  const float e11 = 0.5f * (F01 * F01 + F11 * F11 + F21 * F21 - 1.0f);
+  const float e01 = 0.5f * (F00 * F01 + F10 * F11 + F20 * F21);
+  const float s00 = C.c00 * e00 + C.c01 * e11;
+  const float s11 = C.c10 * e00 + C.c11 * e11;
+  const float s01 = C.c22 * e01;
+  // P = stress F: P[c][0] = s00 F[c][0] + s01 F[c][1], P[c][1] = s01 F[c][0] + s11 F[c][1]
+  const float P00 = s00 * F00 + s01 * F01, P01 = s01 * F00 + s11 * F01;
+  const float P10 = s00 * F10 + s01 * F11, P11 = s01 * F10 + s11 * F11;
+  const float P20 = s00 * F20 + s01 * F21, P21 = s01 * F20 + s11 * F21;
+  const float psi = 0.5f * (((e00 * s00 + e01 * s01) + e01 * s01) + e11 * s11);
+  const float energy = area * psi;
+  // H[c][0] = (i00 P[c][0] + i01 P[c][1]) area, H[c][1] = (i10 P[c][0] + i11 P[c][1]) area
+  const f3 g0 = mk3((i00 * P00 + i01 * P01) * area, (i00 * P10 + i01 * P11) * area,
+                    (i00 * P20 + i01 * P21) * area);
+  const f3 g1 = mk3((i10 * P00 + i11 * P01) * area, (i10 * P10 + i11 * P11) * area,
+                    (i10 * P20 + i11 * P21) * area);
+  const f3 g2 = -g0 - g1;
+  const float w0 = a0.w, w1 = a1.w, w2 = a2.w;
+  float sum = w0 * dot(g0, g0);
+  sum = sum + w1 * dot(g1, g1);
+  sum = sum + w2 * dot(g2, g2);
+  if (!(fabsf(sum) > kEps)) return false;
+  const float s = energy / sum;
+  if (w0 > kEps) a0 = mk4(mk3(a0) + (-(s * w0)) * g0, w0);
+  if (w1 > kEps) a1 = mk4(mk3(a1) + (-(s * w1)) * g1, w1);
+  if (w2 > kEps) a2 = mk4(mk3(a2) + (-(s * w2)) * g2, w2);
+  return true;
+}
+
+// SolveIsometricBending_Kernel (FEMHelper.cu:325-388): energy 1/2 sum_k sum_j Q[j][k] x_k.x_j,
+// derivatives d_j = sum_i Q[j][i] x_i, XPBD step with alpha = 1 / (stiffness dt^2) (passed in).
+// Q is row-major (Q[4 j + k] = Q[j][k]).  Returns false (nothing moves, lam unchanged) when
+// |energy| < eps.
+__device__ __forceinline__ bool iso_bend_project(float4& a0, float4& a1, float4& a2, float4& a3,
+                                                 const float* Q, float alpha, float& lam) {
+  const f3 x[4] = {mk3(a0), mk3(a1), mk3(a2), mk3(a3)};
+  float energy = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) energy = energy + Q[4 * j + k] * dot(x[k], x[j]);
+  energy = energy * 0.5f;
+  if (fabsf(energy) < kEps) return false;
+  f3 d[4] = {mk3(0, 0, 0), mk3(0, 0, 0), mk3(0, 0, 0), mk3(0, 0, 0)};
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) d[j] = d[j] + Q[4 * j + i] * x[i];
+  const float w[4] = {a0.w, a1.w, a2.w, a3.w};
+  const float coeff = (w[0] * dot(d[0], d[0]) + w[1] * dot(d[1], d[1])) +
+                      (w[2] * dot(d[2], d[2]) + w[3] * dot(d[3], d[3]));
+  const float dl = (-energy - alpha * lam) / (coeff + alpha);
+  a0 = mk4(x[0] + (dl * w[0]) * d[0], w[0]);
+  a1 = mk4(x[1] + (dl * w[1]) * d[1], w[1]);
+  a2 = mk4(x[2] + (dl * w[2]) * d[2], w[2]);
+  a3 = mk4(x[3] + (dl * w[3]) * d[3], w[3]);
+  lam = lam + dl;
+  return true;
+}
+
 __device__ __forceinline__ f3 lra_project(f3 xt, f3 xs, float w_t, float rest, float stretch) {
   const float target = rest * stretch;
   if (w_t < kEps && target > 0) return xt;

@@ -357,5 +357,61 @@ TileSchedule build_tiles(const std::vector<uint32_t>& idx, int arity, uint32_t n
   return S;
 }
 
+void fem_strain_rest(const std::vector<float>& x, const std::vector<uint32_t>& tri,
+                     std::vector<float>& area, std::vector<float>& inv) {
+  const size_t nf = tri.size() / 3;
+  area.assign(nf, 0.0f);
+  inv.assign(4 * nf, 0.0f);
+  auto P = [&](uint32_t v) { return V3{x[3 * v], x[3 * v + 1], x[3 * v + 2]}; };
+  for (size_t f = 0; f < nf; ++f) {
+    const V3 p0 = P(tri[3 * f]), p1 = P(tri[3 * f + 1]), p2 = P(tri[3 * f + 2]);
+    const V3 normal0 = cross(sub(p1, p0), sub(p2, p0));
+    area[f] = 0.5f * length(normal0);
+    const V3 axis0_1 = normalize(sub(p1, p0));
+    const V3 axis0_2 = normalize(cross(normal0, axis0_1));
+    // material coordinates (dot with axis0_2, dot with axis0_1); P[c][r] in glm's order
+    const float q0x = dot(p0, axis0_2), q0y = dot(p0, axis0_1);
+    const float q1x = dot(p1, axis0_2), q1y = dot(p1, axis0_1);
+    const float q2x = dot(p2, axis0_2), q2y = dot(p2, axis0_1);
+    const float m00 = q0x - q2x, m10 = q0y - q2y, m01 = q1x - q2x, m11 = q1y - q2y;
+    const float det = m00 * m11 - m10 * m01;
+    float* o = &inv[4 * f];
+    if (std::fabs(det) > 1e-6f) {
+      const float r = 1.0f / det;
+      o[0] = m11 * r;      // inv[0][0]
+      o[1] = (-m01) * r;   // inv[0][1]
+      o[2] = (-m10) * r;   // inv[1][0]
+      o[3] = m00 * r;      // inv[1][1]
+    } else {  // degenerate rest triangle: area ~0, its projection never moves anything
+      o[0] = o[3] = 1.0f;
+    }
+  }
+}
+
+static inline float cot_theta(V3 v, V3 w) { return dot(v, w) / length(cross(v, w)); }
+
+void iso_bend_hessian(const std::vector<float>& x, const std::vector<uint32_t>& bends,
+                      std::vector<float>& q) {
+  const size_t nb = bends.size() / 4;
+  q.assign(16 * nb, 0.0f);
+  auto P = [&](uint32_t v) { return V3{x[3 * v], x[3 * v + 1], x[3 * v + 2]}; };
+  for (size_t b = 0; b < nb; ++b) {
+    const V3 p0 = P(bends[4 * b]), p1 = P(bends[4 * b + 1]), p2 = P(bends[4 * b + 2]),
+             p3 = P(bends[4 * b + 3]);
+    const V3 e0 = sub(p1, p0), e1 = sub(p2, p0), e2 = sub(p3, p0), e3 = sub(p2, p1),
+             e4 = sub(p3, p1);
+    const V3 ne0 = V3{-e0.x, -e0.y, -e0.z};
+    const float c01 = cot_theta(e0, e1), c02 = cot_theta(e0, e2);
+    const float c03 = cot_theta(ne0, e3), c04 = cot_theta(ne0, e4);
+    const float A0 = 0.5f * length(cross(sub(p1, p0), sub(p2, p0)));  // TriangleArea(p0, p1, p2)
+    const float A1 = 0.5f * length(cross(sub(p0, p1), sub(p3, p1)));  // TriangleArea(p1, p0, p3)
+    const float coeff = 3.0f / (A0 + A1);
+    const float K[4] = {c03 + c04, c01 + c02, -c01 - c03, -c02 - c04};
+    float* o = &q[16 * b];
+    for (int j = 0; j < 4; ++j)
+      for (int i = 0; i < 4; ++i) o[4 * j + i] = coeff * (K[i] * K[j]);  // Q[j][i]
+  }
+}
+
 }  // namespace setup
 }  // namespace xrt

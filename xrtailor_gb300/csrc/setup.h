@@ -66,6 +66,16 @@ struct TileSchedule {
 // `segments`: ascending first vertex of each independent mesh (instance); tiles never cross a
 // segment and are numbered inside it exactly as for that mesh alone, so a batch of meshes gets
 // the schedule every mesh would get on its own.  Empty = one segment.
+// FEM fabric rest state from the initial world positions x (3 per vertex).
+// ComputeStrainMeta (FEMHelper.cu:10-39) per face of `tri`: area and the inverse 2x2 material
+// matrix in glm's column-major order (4 floats per face; identity for a degenerate face).
+void fem_strain_rest(const std::vector<float>& x, const std::vector<uint32_t>& tri,
+                     std::vector<float>& area, std::vector<float>& inv);
+// ComputeHessianEnergy (FEMHelper.cu:209-233) per bend element (4 ids): the 4x4 Hessian
+// 3 / (A0 + A1) K K^T with the cotangent weights K, row-major (16 floats per element).
+void iso_bend_hessian(const std::vector<float>& x, const std::vector<uint32_t>& bends,
+                      std::vector<float>& q);
+
 TileSchedule build_tiles(const std::vector<uint32_t>& idx, int arity, uint32_t nv,
                          uint32_t tile_vertices, const std::vector<uint32_t>& segments = {});
 

@@ -414,6 +414,20 @@ void launch_bend(Context& c, const FrameConst& k, ColorRange r) {
            r.end, k.dt);
 }
 
+cudaError_t raise_smem(const void* kern, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> set;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = set[{dev, kern}];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
 // The limit is a property of the kernel function on the current device, shared by every
 // context of the process, so it only ever grows: a context started later with smaller tiles
 // must not lower it under one that is already running.

@@ -266,6 +266,23 @@ class ClothSolver:
         p = _f32(positions).reshape(-1)
         L.check(self._lib.xrt_set_obstacle_targets(self._h, L.fptr(p)), self._h, "targets")
 
+    @staticmethod
+    def fem_material(**overrides):
+        """xrt_fem_material with the reference's defaults (FEMFabricSettings) and overrides."""
+        m = L.FemMaterial()
+        L.load().xrt_default_fem_material(C.byref(m))
+        for k, v in overrides.items():
+            setattr(m, k, v)
+        return m
+
+    def set_fem_material(self, material=None, **overrides):
+        """The FEM fabric (include/xrt_fem.h) in place of stretch + dihedral bend; before
+        start().  `material=None` with no overrides selects the Swift fabric again."""
+        m = material if material is not None else (self.fem_material(**overrides)
+                                                   if overrides else None)
+        L.check(self._lib.xrt_set_fem_material(self._h, C.byref(m) if m is not None else None),
+                self._h, "fem material")
+
     def set_obstacle_skinning(self, rest=None, outer=None, joints=None, weights=None,
                               num_joints: int = 0):
         """Obstacle targets by linear blend skinning on the device (xrt_set_obstacle_skinning);
@@ -413,8 +430,10 @@ class ClothSolver:
         return b, t
 
     def coloring(self, kind: int):
+        """kind 0 stretch (per edge), 1 bend (per bend element), 2 FEM strain (per cloth face),
+        3 FEM bending (per bend element)."""
         s = self.sizes()
-        n = s.num_edges if kind == 0 else s.num_bends
+        n = {0: s.num_edges, 1: s.num_bends, 2: s.num_triangles, 3: s.num_bends}[kind]
         c = np.empty(n, np.uint32)
         L.check(self._lib.xrt_get_coloring(self._h, kind, L.uptr(c)), self._h, "coloring")
         return c
