@@ -149,6 +149,10 @@ BYTES_PER_UNIT = {"stretch": 88, "bend": 152, "collide": 48, "vf_solve": 64, "ee
 # rest angle, compliance) and a vertex touched once (position read + written, inverse mass).
 RECORD_BYTES = 24
 VERTEX_BYTES = 28
+# FEM fabric (the phases keep the names stretch / bend): strain = 3 indices + inverse rest
+# matrix + area (36 B); isometric bending = 4 indices + 4x4 Hessian + multiplier read and
+# written (88 B).
+FEM_RECORD_BYTES = {"stretch": 36, "bend": 88}
 
 
 def run_ours(args, rank, local_rank, world):
@@ -161,6 +165,9 @@ def run_ours(args, rank, local_rank, world):
     solver = ClothSolver(p, device=local_rank)
     if args.tile_vertices is not None:
         solver.set_tile_vertices(args.tile_vertices)
+    fem = args.material == "fem"
+    if fem:
+        solver.set_fem_material(ClothSolver.fem_material())
     _setup(solver, sc)
     s = solver.sizes()
     V, S = s.num_vertices, p.num_substeps
@@ -251,17 +258,19 @@ def run_ours(args, rank, local_rank, world):
         # each: indices, rest value, compliance, multiplier) and each footprint vertex once
         # (28 B: position read and written, inverse mass read); a tile color's footprints are
         # disjoint, so a launch touches footprint / tile colors vertices on average
-        per_launch_bytes = (RECORD_BYTES * d["units"] / max(d["launches"], 1) +
+        record = FEM_RECORD_BYTES[dom] if fem else RECORD_BYTES
+        per_launch_bytes = (record * d["units"] / max(d["launches"], 1) +
                             VERTEX_BYTES * tiles[1] / tiles[0])
-        accounting = ("frame formula: 24 B per constraint record + 28 B per footprint vertex "
-                      "of the launch")
+        accounting = (f"frame formula: {record} B per constraint record + {VERTEX_BYTES} B per "
+                      "footprint vertex of the launch")
     per_launch_s = d["ms"] / 1e3 / max(d["launches"], 1)
     achieved = per_launch_bytes / per_launch_s / 1e9
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         try:
-            tr = json.load(open(tpath)).get(args.workload, {}).get(dom)
+            key = args.workload + ("_fem" if fem else "")
+            tr = json.load(open(tpath)).get(key, {}).get(dom)
             if tr:
                 traffic = tr["bytes_per_unit"] * d["units"] / max(d["launches"], 1)
         except Exception:
@@ -272,7 +281,10 @@ def run_ours(args, rank, local_rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded scene generators, xrtailor_gb300/scenes.py)",
-        "config": {"workload": f"plain_{args.workload}", "vertices": V, "edges": s.num_edges,
+        "config": {"workload": f"plain_{args.workload}" + ("_fem" if fem else ""),
+                   "fabric": "FEM strain + isometric bending" if fem else
+                             "XPBD stretch + dihedral bend",
+                   "vertices": V, "edges": s.num_edges,
                    "bends": s.num_bends, "lra": s.num_lra,
                    "obstacle_triangles": s.num_obstacle_triangles, "substeps": S,
                    "iterations": p.num_iterations, "collision_passes": p.num_collision_passes,
@@ -647,12 +659,14 @@ def run_lbvh(args, local_rank):
     }
 
 
-def run_cpu(workload, frames, warmup=1, threads=0):
+def run_cpu(workload, frames, warmup=1, threads=0, fem=False):
     from oracle.oracle import OracleSolver, lib
-    from xrtailor_gb300 import scenes
+    from xrtailor_gb300 import ClothSolver, scenes
     sc = _workload(workload)
     p = scenes.scene_params(sc)
     o = OracleSolver(p, threads=threads)
+    if fem:
+        o.set_fem_material(ClothSolver.fem_material())
     _setup(o, sc)
     tg = _targets(sc, warmup + frames)
     V = o.sizes()["num_vertices"]
@@ -693,6 +707,9 @@ def main():
     ap.add_argument("--diff-instances", type=int, default=16)
     ap.add_argument("--diff-n", type=int, default=128)
     ap.add_argument("--diff-frames", type=int, default=60)
+    ap.add_argument("--material", default="swift", choices=["swift", "fem"],
+                    help="plain workloads: the Swift fabric (XPBD stretch + dihedral bend) or "
+                         "the FEM fabric (strain + isometric bending, include/xrt_fem.h)")
     ap.add_argument("--tile-vertices", type=int, default=None,
                     help="tile size of the Gauss-Seidel schedule (library default if omitted)")
     args = ap.parse_args()
@@ -704,7 +721,8 @@ def main():
         if rank != 0:
             return
         frames = max(args.steps, 1)
-        value, cores, t = run_cpu(args.workload, frames, warmup=min(args.warmup, 1))
+        value, cores, t = run_cpu(args.workload, frames, warmup=min(args.warmup, 1),
+                                  fem=args.material == "fem")
         line = {"metric": METRIC, "value": value, "unit": "vertex-substeps/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / frames,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -735,7 +753,7 @@ def main():
         torch.distributed.init_process_group("nccl")
     res = run_ours(args, rank, local_rank, world)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, cores, t = run_cpu(args.workload, args.cpu_frames)
+        v, cores, t = run_cpu(args.workload, args.cpu_frames, fem=args.material == "fem")
         res["cpu_baseline"] = {"value": v, "unit": "vertex-substeps/s", "cores": cores,
                                "kind": "port",
                                "sample": f"{args.cpu_frames} frames of plain_{args.workload} "

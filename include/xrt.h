@@ -126,8 +126,9 @@ typedef struct xrt_sizes {
   float particle_diameter;         /* of instance 0 (merged mode: the last cloth added) */
   uint32_t num_instances;          /* 1 in merged mode */
   uint32_t num_obstacle_bvh_nodes; /* sum over instances of 2 F_i - 1 (F_i > 0) */
-  /* tile-local schedule (0 when the kind runs per color): tile colors (one launch each per
-   * iteration) and the summed footprint vertices of all tiles (a tile color's tiles have
+  /* tile-local schedule (0 when the kind runs per color) of the stretch and bend kinds, or of
+   * the FEM strain and bending kinds when the FEM fabric is on: tile colors (one launch each
+   * per iteration) and the summed footprint vertices of all tiles (a tile color's tiles have
    * disjoint footprints, so one launch touches footprint / tile colors vertices on average) */
   uint32_t num_stretch_tile_colors, num_bend_tile_colors;
   uint32_t stretch_footprint_vertices, bend_footprint_vertices;

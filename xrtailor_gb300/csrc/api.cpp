@@ -1322,12 +1322,13 @@ xrt_status xrt_get_sizes(const xrt_ctx* h, xrt_sizes* out) {
   out->num_obstacle_bvh_nodes = c.bvh.active ? c.bvh.nodes : 0u;
   uint32_t* tile_colors[2] = {&out->num_stretch_tile_colors, &out->num_bend_tile_colors};
   uint32_t* footprint[2] = {&out->stretch_footprint_vertices, &out->bend_footprint_vertices};
-  for (int kind = 0; kind < 2; ++kind) {
-    const xrt::TiledSet& T = kind == 0 ? c.s_tiles : c.b_tiles;
+  for (int kind = 0; kind < 2; ++kind) {  // the kinds the frame runs
+    const xrt::FemKind& F = kind == 0 ? c.fem.strain : c.fem.bend;
+    const xrt::TiledSet& T = c.fem.on ? F.tiles : (kind == 0 ? c.s_tiles : c.b_tiles);
     if (!T.on) continue;
     *tile_colors[kind] = (uint32_t)T.tile_colors.size();
     uint64_t f = 0;
-    for (const int4& m : c.h_tile_meta[kind]) f += (uint32_t)m.y;
+    for (const int4& m : (c.fem.on ? F.meta : c.h_tile_meta[kind])) f += (uint32_t)m.y;
     *footprint[kind] = (uint32_t)f;
   }
   return XRT_OK;
