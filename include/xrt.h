@@ -80,7 +80,13 @@ typedef struct xrt_swift_params {
   int32_t pbd_repulsion;
   float pbd_thickness;             /* REPULSION.PBD_THICKNESS (1e-4) */
   float repulsion_relaxation;      /* REPULSION.RELAXATION_RATE (0.25) */
-  int32_t reserved[5];
+  /* Quality-mode impact-zone collision step at the end of every substep, after the iterations
+   * and before the velocity update (ClothSolverBase.cpp:329-336, include/xrt_impact.h).  0 = off.
+   * Frames then run eagerly, not as a replayed graph. */
+  int32_t impact_zone;
+  float impact_zone_obstacle_mass; /* IMPACT_ZONE.OBSTACLE_MASS (1e3) */
+  float impact_zone_thickness;     /* IMPACT_ZONE.THICKNESS (1e-4) */
+  int32_t reserved[2];
 } xrt_swift_params;
 
 /* Cloth registration, mirrors ClothSolverUniversal::AddCloth(mesh, model_matrix, particle_diameter)

@@ -45,6 +45,7 @@ _SIG = {
     "orc_update_pairs": (C.c_uint32, [P, C.c_float]),
     "orc_solve_repulsion": (None, [P, C.c_float, C.c_float]),
     "orc_check_impacts": (None, [P, C.c_float]),
+    "orc_collision_step": (None, [P, C.c_float, C.c_float, IP]),
     "orc_get_pairs": (C.c_uint32, [P, UP]),
     "orc_get_impacts": (None, [P, FP, FP, FP, UP, IP]),
     "orc_set_positions_predicted": (None, [P, FP]), "orc_get_positions_predicted": (None, [P, FP]),
@@ -246,6 +247,13 @@ class OracleSolver:
 
     def check_impacts(self, thickness):
         self._l.orc_check_impacts(self._h, float(thickness))
+
+    def collision_step(self, obstacle_mass=1e3, thickness=1e-4):
+        st = np.zeros(8, np.int32)
+        self._l.orc_collision_step(self._h, float(obstacle_mass), float(thickness),
+                                   st.ctypes.data_as(IP))
+        return dict(zip(("success", "deform", "passes", "impacts", "zones", "solves"),
+                        (int(v) for v in st[:6])))
 
     def pairs(self):
         n = self._l.orc_get_pairs(self._h, None)

@@ -1343,6 +1343,389 @@ void face_topology(const std::vector<uint32_t>& tri, const std::vector<uint32_t>
 // ---------------------------------------------------------------------------------------------
 // frame — ClothSolverBase::SimulateSwift (ClothSolverBase.cpp:171-261)
 
+// ---------------------------------------------------------------------------------------------
+// impact-zone collision step — ImpactZoneOptimization::CollisionStep (impact_zone/Entry.cu:140-256)
+
+// The reference's reduction of a zone quantity (ReduceBaselineLocal/Global_Kernel,
+// ParallelOptimizer.cu:335-428): 256-element blocks summed by the stride tree
+// s[t] += s[t + d] (t % 2d == 0, d = 1 .. 128), then the block sums by the same tree.
+float blocked_sum(std::vector<float> v) {
+  do {
+    const size_t nb = std::max<size_t>(1, (v.size() + 255) / 256);
+    std::vector<float> next(nb);
+    for (size_t b = 0; b < nb; ++b) {
+      float s[256];
+      for (int t = 0; t < 256; ++t) s[t] = b * 256 + t < v.size() ? v[b * 256 + t] : 0.0f;
+      for (int d = 1; d < 256; d *= 2)
+        for (int t = 0; t < 256; t += 2 * d) s[t] += s[t + d];
+      next[b] = s[0];
+    }
+    v.swap(next);
+  } while (v.size() > 1);
+  return v[0];
+}
+
+struct IZone {
+  std::vector<uint32_t> impacts;  // ids into the step's impact list
+  std::set<uint32_t> nodes;
+  bool active = true, enabled = true;
+};
+
+struct IZStep {
+  Oracle& o;
+  int deform = 0;
+  float obstacle_mass = 1e3f, thickness = 1e-4f;
+  std::vector<Oracle::Impact> store;
+  std::vector<IZone> zones;
+  uint32_t V() const { return (uint32_t)o.x.size(); }
+  bool is_cloth(uint32_t v) const { return v < V(); }
+  bool is_free(uint32_t v) const { return is_cloth(v) && o.cfree[v] != 0; }
+  bool deformable(uint32_t v) const { return deform == 1 || is_free(v); }
+  // moved by the optimizer: free cloth nodes, and obstacle nodes at deform 1 (a pinned cloth node
+  // would enter with mass 1 / 0)
+  bool optimized(uint32_t v) const { return is_free(v) || (deform == 1 && !is_cloth(v)); }
+  V3 pos(uint32_t v) const { return is_cloth(v) ? o.x[v] : o.ox[v - V()]; }
+  void set_pos(uint32_t v, V3 p) {
+    if (is_cloth(v)) o.x[v] = p; else o.ox[v - V()] = p;
+  }
+};
+
+// independentImpacts (Entry.cu:25-63): impacts sorted by t; rounds of
+// InitializeImpactNodes / CollectRelativeImpacts / SetImpactMinIndices / CheckIndependentImpacts
+// (ImpactHelper.cu:234-343) until no impact is added.
+std::vector<Oracle::Impact> independent_impacts(IZStep& z, std::vector<Oracle::Impact> imp) {
+  std::stable_sort(imp.begin(), imp.end(),
+                   [](const Oracle::Impact& a, const Oracle::Impact& b) { return a.t < b.t; });
+  const int n = (int)imp.size();
+  std::map<uint32_t, bool> removed;
+  std::map<uint32_t, int> min_index;
+  for (const auto& im : imp)
+    for (uint32_t v : im.nodes)
+      if (z.deformable(v)) {
+        removed[v] = false;
+        min_index[v] = n;
+      }
+  std::vector<int> ans(n, 0);
+  int num, new_num = n;
+  do {
+    num = new_num;
+    std::map<uint32_t, int> mins;
+    for (int i = 0; i < n; ++i) {
+      bool flag = true;
+      for (uint32_t v : imp[i].nodes)
+        if (z.deformable(v) && removed[v]) flag = false;
+      if (!flag) continue;
+      for (uint32_t v : imp[i].nodes) {
+        if (!z.deformable(v)) continue;
+        auto it = mins.find(v);
+        if (it == mins.end() || i < it->second) mins[v] = i;
+      }
+    }
+    for (const auto& kv : mins) min_index[kv.first] = kv.second;
+    for (int i = 0; i < n; ++i) {
+      bool flag = true;
+      for (uint32_t v : imp[i].nodes)
+        if (z.deformable(v) && (removed[v] || min_index[v] != i)) flag = false;
+      if (!flag) continue;
+      ans[i] = 1;
+      for (uint32_t v : imp[i].nodes)
+        if (z.deformable(v)) removed[v] = true;
+    }
+    new_num = n - (int)std::count(ans.begin(), ans.end(), 1);
+  } while (num > new_num);
+  std::vector<Oracle::Impact> out;
+  for (int i = 0; i < n; ++i)
+    if (ans[i]) out.push_back(imp[i]);
+  return out;
+}
+
+// IsolateImpacts (ImpactZoneHelper.cu:214-304): FloodFillColoring_Kernel from the first uncolored
+// impact, WriteBackNodeColor_Kernel, repeated.  An impact that no fill reaches (every node a
+// pinned cloth node) is dropped.
+std::vector<IZone> isolate(IZStep& z, const std::vector<uint32_t>& ids) {
+  const int kOutside = -2, kInside = -1;
+  std::map<uint32_t, int> color;
+  auto col = [&](uint32_t v) {
+    auto it = color.find(v);
+    return it == color.end() ? kOutside : it->second;
+  };
+  for (uint32_t id : ids)
+    for (uint32_t v : z.store[id].nodes) color[v] = kInside;
+  std::vector<int> icol(ids.size(), -1);
+  std::vector<IZone> out;
+  for (int c = 0;; ++c) {
+    size_t first = 0;
+    while (first < ids.size() && icol[first] != -1) ++first;
+    if (first == ids.size()) break;
+    std::vector<uint32_t> stack(std::begin(z.store[ids[first]].nodes),
+                                std::end(z.store[ids[first]].nodes));
+    while (!stack.empty()) {
+      uint32_t v = stack.back();
+      stack.pop_back();
+      const bool cloth = z.is_cloth(v);
+      if (cloth && !z.is_free(v)) continue;
+      const uint32_t lv = cloth ? v : v - z.V();
+      const auto& pre = cloth ? z.o.vf_prefix : z.o.ovf_prefix;
+      const auto& lst = cloth ? z.o.vf_list : z.o.ovf_list;
+      const auto& tri = cloth ? z.o.tri : z.o.otri;
+      for (uint32_t q = pre[lv]; q < pre[lv + 1]; ++q)
+        for (int k = 0; k < 3; ++k) {
+          uint32_t u = (cloth ? 0 : z.V()) + tri[lst[q] * 3 + k];
+          if (col(u) == kInside) {
+            color[u] = c;
+            stack.push_back(u);
+          }
+        }
+    }
+    IZone zone;
+    for (size_t m = 0; m < ids.size(); ++m) {
+      if (icol[m] != -1) continue;
+      for (uint32_t v : z.store[ids[m]].nodes)
+        if (col(v) >= 0) {
+          icol[m] = c;
+          zone.impacts.push_back(ids[m]);
+          break;
+        }
+    }
+    if (icol[first] == -1) icol[first] = -2;
+    if (!zone.impacts.empty()) {
+      for (uint32_t id : zone.impacts)
+        for (uint32_t v : z.store[id].nodes) zone.nodes.insert(v);
+      out.push_back(zone);
+    }
+  }
+  return out;
+}
+
+bool share_node(const IZone& a, const IZone& b) {  // ImpactZone::Intersects
+  for (uint32_t v : b.nodes)
+    if (a.nodes.count(v)) return true;
+  return false;
+}
+
+void merge_into(IZone& a, IZone& b) {  // ImpactZone::Merge
+  a.impacts.insert(a.impacts.end(), b.impacts.begin(), b.impacts.end());
+  a.nodes.insert(b.nodes.begin(), b.nodes.end());
+  a.active = a.enabled = true;
+  b.enabled = false;
+}
+
+// AddImpacts (ImpactZoneHelper.cu:325-367), the merge pass repeated until no two zones share a
+// node, a disabled zone absorbing nothing.
+void add_impacts(IZStep& z, std::vector<IZone> fresh) {
+  const size_t n0 = z.zones.size();
+  for (auto& q : z.zones) q.active = false;
+  for (size_t i = 0; i < n0; ++i)
+    for (auto& f : fresh)
+      if (f.enabled && share_node(z.zones[i], f)) merge_into(z.zones[i], f);
+  for (auto& f : fresh)
+    if (f.enabled) z.zones.push_back(f);
+  for (bool changed = true; changed;) {
+    changed = false;
+    for (size_t i = 0; i < z.zones.size(); ++i)
+      for (size_t j = i + 1; j < z.zones.size(); ++j)
+        if (z.zones[i].enabled && z.zones[j].enabled && share_node(z.zones[i], z.zones[j])) {
+          merge_into(z.zones[i], z.zones[j]);
+          changed = true;
+        }
+  }
+  std::vector<IZone> keep;
+  for (auto& q : z.zones)
+    if (q.enabled) keep.push_back(q);
+  z.zones.swap(keep);
+}
+
+// ParallelImpactZoneOptimizer + ParallelOptimizer::Solve over the active zones
+// (ParallelImpactZoneOptimizer.cu:13-528, ParallelOptimizer.cu:513-880).
+void solve_zones(IZStep& z, const std::vector<V3>& cx1, const std::vector<V3>& ox1) {
+  const float mu = 1e3f, eps_s = 1e-12f, eps_f = 1e-10f, alpha = 0.5f;
+  struct Work {
+    std::vector<uint32_t> nodes, entries;
+    std::vector<int> loc;  // 4 per entry
+    std::vector<V3> X, Xt;
+    int conv;
+  };
+  std::vector<Work> ws;
+  std::vector<float> inv_all;
+  for (const IZone& q : z.zones) {
+    if (!q.active) continue;
+    Work w;
+    for (uint32_t v : q.nodes)
+      if (z.optimized(v)) w.nodes.push_back(v);
+    w.entries = q.impacts;
+    for (uint32_t id : w.entries)
+      for (uint32_t v : z.store[id].nodes) {
+        auto it = std::lower_bound(w.nodes.begin(), w.nodes.end(), v);
+        w.loc.push_back(it != w.nodes.end() && *it == v ? (int)(it - w.nodes.begin()) : -1);
+      }
+    for (uint32_t v : w.nodes)  // CollisionInv_Kernel
+      inv_all.push_back(z.is_cloth(v) ? z.o.w[v] : 1.0f / z.obstacle_mass);
+    ws.push_back(w);
+  }
+  if (ws.empty()) return;
+  const float inv = inv_all.empty() ? 0.0f : blocked_sum(inv_all) / (float)inv_all.size();
+  auto x1 = [&](uint32_t v) { return z.is_cloth(v) ? cx1[v] : ox1[v - z.V()]; };
+  auto mass = [&](uint32_t v) { return z.is_cloth(v) ? 1.0f / z.o.w[v] : z.obstacle_mass; };
+  for (Work& w : ws) {
+    const size_t nn = w.nodes.size(), ni = w.entries.size();
+    for (uint32_t v : w.nodes) w.X.push_back(z.pos(v));
+    w.Xt = w.X;
+    std::vector<float> lambda(ni, 0.0f), cc(ni);
+    auto constraint = [&](size_t e, const std::vector<V3>& Xs) {
+      const Oracle::Impact& im = z.store[w.entries[e]];
+      float c = -z.thickness;
+      for (int j = 0; j < 4; ++j) {
+        const int k = w.loc[4 * e + j];
+        c += im.w[j] * dot(im.n, k > -1 ? Xs[k] : z.pos(im.nodes[j]));
+      }
+      return c;
+    };
+    float s = 1e-3f * (float)nn;
+    w.conv = 100;
+    std::vector<V3> grad(nn);
+    for (int it = 0; it < 100; ++it) {
+      std::vector<float> c2(ni), l2(ni);
+      for (size_t e = 0; e < ni; ++e) {
+        const float q = constraint(e, w.X) + lambda[e] / mu;
+        cc[e] = q < 0.0f ? q : 0.0f;  // ClampViolation, sign 1
+        c2[e] = cc[e] * cc[e];
+        l2[e] = lambda[e] * lambda[e];
+      }
+      const float C2 = blocked_sum(c2), L2 = blocked_sum(l2);
+      std::vector<float> g2(nn), ob(nn);
+      for (size_t k = 0; k < nn; ++k) {  // ObjectiveGradient, then the constraint terms
+        const uint32_t v = w.nodes[k];
+        V3 g = (inv * mass(v)) * (w.X[k] - x1(v));
+        bool first = true;
+        V3 acc{0, 0, 0};
+        for (size_t e = 0; e < ni; ++e)
+          for (int j = 0; j < 4; ++j) {
+            if (w.loc[4 * e + j] != (int)k) continue;
+            const Oracle::Impact& im = z.store[w.entries[e]];
+            V3 t = ((mu * cc[e]) * im.w[j]) * im.n;
+            acc = first ? t : acc + t;
+            first = false;
+          }
+        g = g + acc;
+        grad[k] = g;
+        g2[k] = dot(g, g);
+        V3 d = w.X[k] - x1(v);
+        ob[k] = mass(v) * dot(d, d);
+      }
+      const float G2 = blocked_sum(g2), O = blocked_sum(ob);
+      const float f = (0.5f * inv) * O + (0.5f * mu) * C2 - (0.5f * L2) / mu;
+      s = s / 0.7f;
+      for (int ls = 0;; ++ls) {
+        s = s * 0.7f;
+        std::vector<float> ot(nn), ct(ni);
+        for (size_t k = 0; k < nn; ++k) {
+          w.Xt[k] = w.X[k] - s * grad[k];
+          V3 d = w.Xt[k] - x1(w.nodes[k]);
+          ot[k] = mass(w.nodes[k]) * dot(d, d);
+        }
+        for (size_t e = 0; e < ni; ++e) {
+          float q = constraint(e, w.Xt) + lambda[e] / mu;
+          q = q < 0.0f ? q : 0.0f;
+          ct[e] = q * q;
+        }
+        const float Ot = blocked_sum(ot), C2t = blocked_sum(ct);
+        const float ft = (0.5f * inv) * Ot + (0.5f * mu) * C2t - (0.5f * L2) / mu;
+        if (s < eps_s || ft < f - (alpha * s) * G2 || mabs(f - ft) < eps_f) break;
+        if (ls + 1 >= 1024) {
+          s = 0.0f;
+          break;
+        }
+      }
+      if (s < eps_s) {
+        w.conv = it;
+        break;
+      }
+      w.X = w.Xt;
+      for (size_t e = 0; e < ni; ++e) {  // UpdateMultiplier
+        const float q = lambda[e] + mu * constraint(e, w.X);
+        lambda[e] = q < 0.0f ? q : 0.0f;
+      }
+    }
+  }
+  int K = -1;
+  for (const Work& w : ws) K = std::max(K, w.conv);
+  for (const Work& w : ws) {  // Finalize: the last zones to converge keep X
+    const bool keep = w.conv == K && K < 100;
+    for (size_t k = 0; k < w.nodes.size(); ++k) z.set_pos(w.nodes[k], keep ? w.X[k] : w.Xt[k]);
+  }
+}
+
+// CollisionStep; stats8 in the layout of xrt_collision_stats.
+void collision_step(Oracle& o, float obstacle_mass, float thickness, int32_t* stats8) {
+  int32_t st[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const uint32_t F = (uint32_t)o.tri.size() / 3, OF = (uint32_t)o.otri.size() / 3;
+  if (F == 0) {
+    st[0] = 1;
+    if (stats8) std::copy(st, st + 8, stats8);
+    return;
+  }
+  const std::vector<V3> cx1 = o.x, ox1 = o.ox;  // SetupNode / SetupObstacleNode: x1 = x
+  auto ccd_tree = [](Lbvh& b, const std::vector<V3>& x, const std::vector<V3>& x0,
+                     const std::vector<V3>& n, const std::vector<uint32_t>& tri) {
+    b = Lbvh();
+    b.objects.resize(tri.size() / 3);
+    for (size_t f = 0; f < tri.size() / 3; ++f) {  // UpdateObjects_Kernel, ccd = true
+      Prim& pr = b.objects[f];
+      const uint32_t a = tri[3 * f], bb = tri[3 * f + 1], c = tri[3 * f + 2];
+      pr.idx1 = a; pr.idx2 = bb; pr.idx3 = c;
+      pr.v1 = x0[a] + 0.0f * n[a]; pr.v2 = x0[bb] + 0.0f * n[bb]; pr.v3 = x0[c] + 0.0f * n[c];
+      pr.pred1 = x[a] + 0.0f * n[a]; pr.pred2 = x[bb] + 0.0f * n[bb]; pr.pred3 = x[c] + 0.0f * n[c];
+    }
+    b.construct(0.0f);
+  };
+  Lbvh cbvh, obvh;
+  ccd_tree(cbvh, o.x, o.x0, o.n, o.tri);
+  if (OF) ccd_tree(obvh, o.ox, o.ox0, o.on, o.otri);
+  IZStep z{o};
+  z.obstacle_mass = obstacle_mass;
+  z.thickness = thickness;
+  bool success = false;
+  for (int deform = 0; deform < 2 && !success; ++deform) {
+    z.deform = deform;
+    z.store.clear();
+    z.zones.clear();
+    st[1] = deform;
+    st[2] = 0;
+    for (int pass = 0; pass < 100; ++pass) {
+      st[2] = pass + 1;
+      o.pairs.clear();  // FindImpacts: Traverse(cloth, obstacle), Traverse(cloth, cloth), CheckImpacts
+      traverse_pairs(cbvh, obvh, 0, F, thickness, o.pairs);
+      traverse_pairs(cbvh, cbvh, 0, 0, thickness, o.pairs);
+      check_impacts(o, thickness);
+      std::vector<Oracle::Impact> found;
+      for (const auto& im : o.impacts)
+        if (!(im.t < 0.0f)) found.push_back(im);
+      if (found.empty()) {
+        success = true;
+        break;
+      }
+      std::vector<Oracle::Impact> indep = independent_impacts(z, found);
+      std::vector<uint32_t> ids;
+      for (const auto& im : indep) {
+        ids.push_back((uint32_t)z.store.size());
+        z.store.push_back(im);
+      }
+      st[3] += (int32_t)indep.size();
+      add_impacts(z, isolate(z, ids));
+      for (const auto& q : z.zones) st[5] += q.active ? 1 : 0;
+      solve_zones(z, cx1, ox1);
+      update_bvh_ccd(cbvh, o.x, o.x0, o.tri);
+      if (deform == 1) {
+        if (OF) update_bvh_ccd(obvh, o.ox, o.ox0, o.otri);
+        z.obstacle_mass *= 0.5f;
+      }
+    }
+    st[4] = (int32_t)z.zones.size();
+  }
+  st[0] = success ? 1 : 0;
+  if (stats8) std::copy(st, st + 8, stats8);
+}
+
 void step_frame(Oracle& o) {
   const xrt_swift_params& p = o.p;
   const float substep_time = p.frame_time / (float)p.num_substeps;
@@ -1393,6 +1776,8 @@ void step_frame(Oracle& o) {
       }
       if (!o.otri.empty()) solve_binding(o);
     }
+    if (p.impact_zone)  // SimulateQuality's CollisionStep (ClothSolverBase.cpp:329-336)
+      collision_step(o, p.impact_zone_obstacle_mass, p.impact_zone_thickness, nullptr);
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < nv; ++i) {  // Finalize_Kernel
       V3 np = o.x[i];
@@ -1746,6 +2131,9 @@ void orc_solve_repulsion(void* h, float thickness, float relaxation) {
   solve_repulsion(*static_cast<Oracle*>(h), thickness, relaxation);
 }
 void orc_check_impacts(void* h, float thickness) { check_impacts(*static_cast<Oracle*>(h), thickness); }
+void orc_collision_step(void* h, float obstacle_mass, float thickness, int32_t* stats8) {
+  collision_step(*static_cast<Oracle*>(h), obstacle_mass, thickness, stats8);
+}
 uint32_t orc_get_pairs(void* h, uint32_t* out) {
   Oracle& o = *static_cast<Oracle*>(h);
   if (out) std::copy(o.pairs.begin(), o.pairs.end(), out);

@@ -1,0 +1,118 @@
+"""The impact-zone collision step on the GPU (xrt_collision_step, include/xrt_impact.h) against
+the CPU oracle's restatement of ImpactZoneOptimization::CollisionStep (impact_zone/Entry.cu).
+
+The pass structure (passes, impacts, zones, zone solves, deform level) must be equal.  Positions
+agree to 1e-5 of the scene size: the CCD narrow phase (a handful of Newton iterations per test)
+differs from the oracle's in the last place on rare tests, and the zone solve carries that."""
+import numpy as np
+import pytest
+
+from tests.helpers import bits, diag, make_pair, small_scene
+from xrtailor_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _params(**kw):
+    base = dict(num_substeps=2, num_iterations=3, solve_bending=0, num_collision_passes=2,
+                enable_self_collision=0)
+    base.update(kw)
+    return scenes._params(**base)
+
+
+def _close(a, b, scale):
+    err = float(np.abs(a.astype(np.float64) - b).max())
+    assert err <= 1e-5 * scale, err
+    return err
+
+
+def test_collision_step_through_the_obstacle_matches_oracle(xrt):
+    cloth, obs = small_scene(12)
+    g, o = make_pair(_params(), [cloth], [obs])
+    for _ in range(4):
+        g.step()
+        o.step()
+    x = o.host_positions()
+    np.testing.assert_array_equal(bits(g.host_positions()), bits(x))
+    pred = x.copy()
+    pred[:, 1] -= 0.12
+    g.set_predicted(pred)
+    o.set_predicted(pred)
+    sg, so = g.collision_step(), o.collision_step()
+    assert sg == so and sg["success"] == 1 and sg["impacts"] > 0, (sg, so)
+    a, b = g.predicted(), o.predicted()
+    err = _close(a, b, diag(b))
+    print(f"max |gpu - oracle| = {err:.3g}, bit-exact: {np.array_equal(bits(a), bits(b))}")
+    assert g.collision_step()["impacts"] == 0
+
+
+def test_collision_step_between_sheets_matches_oracle(xrt):
+    a = scenes.grid_cloth(16, 1.0, origin=(0.0, 0.50, 0.0), jitter=1e-3, seed=3)
+    b = scenes.grid_cloth(16, 1.0, origin=(0.05, 0.45, 0.05), jitter=1e-3, seed=4)
+    g, o = make_pair(_params(), [a, b], [])
+    x = o.host_positions()
+    nb = len(b.positions) // 3
+    pred = x.copy()
+    pred[-nb:, 1] += 0.1
+    g.set_predicted(pred)
+    o.set_predicted(pred)
+    sg, so = g.collision_step(), o.collision_step()
+    assert sg == so and sg["success"] == 1 and sg["impacts"] > 0, (sg, so)
+    _close(g.predicted(), o.predicted(), diag(x))
+    assert g.collision_step()["impacts"] == 0
+
+
+def test_collision_step_at_deform_1_matches_oracle(xrt):
+    cloth, obs = small_scene(8)
+    g, o = make_pair(_params(), [cloth], [obs])
+    g.step()
+    o.step()
+    x = o.host_positions()
+    pin = x[cloth.fixed_indices[0]]
+    tgt = (o.obstacle_positions() + np.array([pin[0] - 0.5, pin[1] + 0.05, pin[2] - 0.5])).astype(np.float32)
+    for s in (g, o):
+        s.set_obstacle_targets(tgt)
+        s.set_predicted(x)
+    sg, so = g.collision_step(), o.collision_step()
+    assert sg == so and sg["deform"] == 1 and sg["success"] == 1, (sg, so)
+    _close(g.predicted(), o.predicted(), diag(x))
+
+
+def test_frames_with_impact_zone_match_oracle(xrt):
+    cloth, obs = small_scene(12)
+    p = _params(impact_zone=1, num_substeps=4, num_iterations=4)
+    p.gravity[1] = -60.0  # the cloth reaches the sphere within a few frames
+    g, o = make_pair(p, [cloth], [obs])
+    for _ in range(6):
+        g.step()
+        o.step()
+        _close(g.host_positions(), o.host_positions(), diag(o.host_positions()))
+    g.synchronize()
+
+
+def test_large_sheet_ends_crossing_free(xrt):
+    from xrtailor_gb300 import ClothSolver
+    cloth, obs = small_scene(64)
+    g = ClothSolver(_params())
+    g.add_cloth(cloth)
+    g.add_obstacle(obs)
+    g.start()
+    g.step()
+    x = g.host_positions()
+    pred = x.copy()
+    pred[:, 1] -= 0.15
+    g.set_predicted(pred)
+    st = g.collision_step()
+    assert st["success"] == 1 and st["impacts"] > 100, st
+    g.synchronize()
+    assert np.isfinite(g.predicted()).all()
+    assert g.collision_step()["impacts"] == 0
+
+
+def test_rejected_in_batched_context(xrt):
+    from xrtailor_gb300 import ClothSolver
+    cloth, obs = small_scene(8)
+    s = ClothSolver(_params(impact_zone=1))
+    s.add_instance(cloth, obs)
+    with pytest.raises(RuntimeError):
+        s.start()

@@ -52,7 +52,23 @@ class SwiftParams(C.Structure):
         ("pbd_repulsion", C.c_int32),
         ("pbd_thickness", C.c_float),
         ("repulsion_relaxation", C.c_float),
-        ("reserved", C.c_int32 * 5),
+        ("impact_zone", C.c_int32),
+        ("impact_zone_obstacle_mass", C.c_float),
+        ("impact_zone_thickness", C.c_float),
+        ("reserved", C.c_int32 * 2),
+    ]
+
+
+class CollisionStats(C.Structure):
+    """xrt_collision_stats (include/xrt_impact.h)."""
+    _fields_ = [
+        ("success", C.c_int32),
+        ("deform", C.c_int32),
+        ("passes", C.c_int32),
+        ("impacts", C.c_uint32),
+        ("zones", C.c_uint32),
+        ("solves", C.c_uint32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -202,6 +218,7 @@ SIGNATURES = {
     "xrt_proximity_update_pairs": (C.c_int32, [P, C.c_float, UP]),
     "xrt_proximity_solve": (C.c_int32, [P, C.c_float, C.c_float]),
     "xrt_impacts_check": (C.c_int32, [P, C.c_float, UP]),
+    "xrt_collision_step": (C.c_int32, [P, C.c_float, C.c_float, C.POINTER(CollisionStats)]),
     "xrt_export_pairs": (C.c_int32, [P, UP]),
     "xrt_export_impacts": (C.c_int32, [P, FP, FP, FP, UP, IP]),
     "xrt_export_cloth_bvh": (C.c_int32, [P, UP, UP, UP, FP, IP, IP]),

@@ -87,6 +87,10 @@ xrt_status validate_params(const xrt_swift_params& p, std::string& why) {
   else if (p.max_neighbor_size < 1) why = "max_neighbor_size must be >= 1";
   else if (!(p.frame_time > 0.0f)) why = "frame_time must be > 0";
   else if (!(p.hash_cell_size > 0.0f)) why = "hash_cell_size must be > 0";
+  else if (p.impact_zone && !(p.impact_zone_obstacle_mass > 0.0f))
+    why = "impact_zone_obstacle_mass must be > 0";
+  else if (p.impact_zone && !(p.impact_zone_thickness >= 0.0f))
+    why = "impact_zone_thickness must be >= 0";
   else return XRT_OK;
   return XRT_ERR_INVALID_CONFIG;
 }
@@ -211,6 +215,11 @@ void record_frame(Context& c) {
         swap_x();
       }
     }
+    if (p.impact_zone) {  // CollisionStep after the iterations (ClothSolverBase.cpp:329-336)
+      const xrt_status r = xrt::collision_step(c, p.impact_zone_obstacle_mass,
+                                               p.impact_zone_thickness, nullptr);
+      if (r != XRT_OK && c.frame_status == XRT_OK) c.frame_status = r;
+    }
     const bool last = s + 1 == p.num_substeps;
     Timed t(c, kPredict, 1, c.nv);
     xrt::launch_finalize_predict(c, k, !last, last);
@@ -325,6 +334,9 @@ xrt_status xrt_default_params(xrt_swift_params* p) {
   p->pbd_repulsion = 0;
   p->pbd_thickness = 1e-4f;         // RepulsionSettings (config/Base.hpp:102-108)
   p->repulsion_relaxation = 0.25f;
+  p->impact_zone = 0;
+  p->impact_zone_obstacle_mass = 1e3f;  // ImpactZoneSettings (config/Base.hpp:115-118)
+  p->impact_zone_thickness = 1e-4f;
   return XRT_OK;
 }
 
@@ -381,6 +393,7 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   c.skin.weight.release(); c.skin.transforms.release();
   xrt::cache_release(c);
   xrt::fem_release(c);
+  xrt::izone_release(c);
   for (xrt::TiledSet* t : {&c.s_tiles, &c.b_tiles}) {
     t->foot.release();
     t->meta.release();
@@ -833,8 +846,9 @@ xrt_status xrt_start(xrt_ctx* h) {
       c.set_error("binding refers to a missing obstacle vertex");
       return XRT_ERR_INVALID_MESH;
     }
-  if (c.instanced && c.params.pbd_repulsion) {
-    c.set_error("pbd_repulsion (Quality-mode self contact) is not available in a batched context");
+  if (c.instanced && (c.params.pbd_repulsion || c.params.impact_zone)) {
+    c.set_error("pbd_repulsion and impact_zone (Quality-mode self contact) are not available in a "
+                "batched context");
     return XRT_ERR_INVALID_ARGUMENT;
   }
   // instances: merged mode is one instance holding every cloth and obstacle
@@ -1191,17 +1205,19 @@ xrt_status xrt_step_frame(xrt_ctx* h) {
   Context& c = h->c;
   if (require_started(c) != XRT_OK) return XRT_ERR_STATE;
   cudaSetDevice(c.device);
-  if (c.params.pbd_repulsion) {
+  const bool eager = c.params.pbd_repulsion || c.params.impact_zone;  // host reads in the frame
+  if (eager) {
     xrt_status st = xrt::prox_prepare(c);
     if (st != XRT_OK) return st;
   }
   xrt::launch_skin(c);  // obstacle targets from the joint transforms, when skinning is on
   if (c.diff.active) xrt::diff_checkpoint(c);  // state at the frame start, for xrt_backward
+  c.frame_status = XRT_OK;
   if (c.profiling) {
     record_frame(c);
     XRT_CUDA(&c, cudaGetLastError());
     collect_profile(c);
-  } else if (c.graph_enabled && !c.params.pbd_repulsion) {
+  } else if (c.graph_enabled && !eager) {
     if (c.graph_dirty || !c.graph_exec) {
       xrt_status st = capture_frame(c);
       if (st != XRT_OK) return st;
@@ -1211,6 +1227,7 @@ xrt_status xrt_step_frame(xrt_ctx* h) {
     record_frame(c);
     XRT_CUDA(&c, cudaGetLastError());
   }
+  if (c.frame_status != XRT_OK) return c.frame_status;
   XRT_CUDA(&c, xrt::cache_frame(c));  // when recording: this frame into the frame cache
   c.frame_index++;
   return XRT_OK;
@@ -1233,7 +1250,8 @@ xrt_status xrt_synchronize(xrt_ctx* h) {
   XRT_CUDA(&c, cudaMemcpy(&err, c.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
   if (err) {
     c.set_error("device error word 0x" + std::to_string(err) +
-                " (1: traversal bound, 2: tree-walk bound, 4: index range)");
+                " (1: traversal bound, 2: tree-walk bound, 4: index range, 8: impact zone size, "
+                "16: line-search bound)");
     return XRT_ERR_DEVICE_FLAG;
   }
   return XRT_OK;

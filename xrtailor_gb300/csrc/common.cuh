@@ -71,6 +71,8 @@ enum : uint32_t {
   kErrTraversal = 1u << 0,  // a traversal exceeded its visit bound
   kErrTreeWalk = 1u << 1,   // a bottom-up / escape walk exceeded its depth bound
   kErrIndex = 1u << 2,      // an index was out of range
+  kErrZoneSize = 1u << 3,   // an impact zone exceeded 65,536 nodes or impacts
+  kErrLineSearch = 1u << 4, // a zone's backtracking line search exceeded its step bound
 };
 
 __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit) { atomicOr(err, bit); }

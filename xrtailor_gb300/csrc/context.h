@@ -9,6 +9,7 @@
 
 #include "../../include/xrt.h"
 #include "../../include/xrt_fem.h"
+#include "../../include/xrt_impact.h"
 #include "setup.h"
 
 // Returns XRT_ERR_CUDA from the enclosing function, with the failing call in the context's error.
@@ -289,10 +290,46 @@ struct ProximityState {
   uint32_t nimpacts = 0;
 };
 
+// Impact-zone collision step (impact.cu).  An impact zone: impacts (ids into the step's impact
+// store) solved together, and the set of every unified node they touch.
+struct HostZone {
+  std::vector<uint32_t> impacts;
+  std::vector<uint32_t> nodes;  // sorted, unique
+  bool active = true, enabled = true;
+};
+
+struct ImpactZoneState {
+  bool ready = false;
+  Lbvh cbvh, obvh;                  // the step's own LBVHs over x0 -> x boxes
+  DBuf<float4> cx1, ox1;            // Node::x1: positions at the start of the step
+  DBuf<uint32_t> hits, hit_incl, hit_total;
+  DBuf<float> new_t;                // impacts of this pass in (pair, test) order
+  DBuf<uint4> new_nodes;
+  DBuf<uint32_t> new_src;           // their slot in the CheckImpacts output
+  DBuf<uint32_t> pick;              // compacted ids of the independent impacts
+  DBuf<float4> sw, sn;              // impact store: weights, normal
+  DBuf<uint4> snodes;
+  uint32_t nstore = 0;
+  // optimizer layout of the active zones
+  DBuf<int4> zone;                  // entry begin, entry end, node begin, node end
+  DBuf<uint32_t> zimp;              // store id per entry
+  DBuf<int32_t> zloc;               // 4 per entry: node position, -1 = not optimized
+  DBuf<uint32_t> znode;             // unified node per node position
+  DBuf<uint32_t> gptr, gslot;       // per node position: its (4 entry + k) slots, ascending
+  DBuf<float4> X, Xt, grad;
+  DBuf<float> lambda, cc, inv_avg, partial;
+  DBuf<int32_t> conv;
+  // host side
+  std::vector<uint32_t> cvf_ptr, cvf_list, ovf_ptr, ovf_list;  // node -> incident faces
+  std::vector<uint4> h_snodes;
+  std::vector<HostZone> zones;
+};
+
 struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string last_error;
+  xrt_status frame_status = XRT_OK;  // first failure of an eagerly recorded frame's host steps
   xrt_swift_params params{};
   bool started = false;
   bool graph_enabled = true;
@@ -393,6 +430,7 @@ struct Context {
   DBuf<uint32_t> ovf_ptr, ovf_list;
   Lbvh bvh;
   ProximityState prox;
+  ImpactZoneState izone;
   SkinState skin;
   CacheState cache;
   FemState fem;
@@ -551,8 +589,18 @@ void launch_cloth_bvh_build(Context& c);
 void launch_update_ccd(Lbvh& b, const float4* x, const float4* x0, const int4* tri, cudaStream_t s,
                        uint32_t* err);
 cudaError_t prox_update_pairs(Context& c, float thickness);
+cudaError_t prox_face_pairs(Context& c, const Lbvh& cloth, const Lbvh& obstacle, float thickness);
+// inclusive scan of n counts by one block; total[0] = sum
+void launch_scan_inclusive(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total,
+                           cudaStream_t s);
 void prox_solve(Context& c, float thickness, float relaxation);
 cudaError_t prox_check_impacts(Context& c, float thickness);
+// prims with ccd boxes: v_k = x0[idx_k] + tol * n[idx_k], pred_k = x[idx_k] + tol * n[idx_k]
+void launch_prims_ccd(Lbvh& b, const float4* x, const float4* x0, const float4* nrm,
+                      const int4* tri, uint32_t nf, float tol, cudaStream_t s);
+// ImpactZoneOptimization::CollisionStep on the current cloth and obstacle x0 -> x (impact.cu)
+xrt_status collision_step(Context& c, float obstacle_mass, float thickness, xrt_collision_stats* out);
+void izone_release(Context& c);
 
 }  // namespace xrt
 

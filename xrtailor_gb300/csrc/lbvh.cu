@@ -325,6 +325,23 @@ __global__ void k_prims_mesh(const float4* __restrict__ x, const float4* __restr
   }
 }
 
+// UpdateObjects_Kernel with ccd = true (BVH.cu:382-418): v from x0, pred from x.
+__global__ void k_prims_ccd(const float4* __restrict__ x, const float4* __restrict__ x0,
+                            const float4* __restrict__ nrm, const int4* __restrict__ tri,
+                            uint32_t nf, float tol, float4* __restrict__ v,
+                            float4* __restrict__ pred) {
+  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int4 t = tri[f];
+  const int id[3] = {t.x, t.y, t.z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const f3 n = mk3(nrm[id[k]]);
+    v[3 * f + k] = mk4(mk3(x0[id[k]]) + tol * n, 0.0f);
+    pred[3 * f + k] = mk4(mk3(x[id[k]]) + tol * n, 0.0f);
+  }
+}
+
 // Forest node of the leaf at sorted position i, and its global primitive (from the leaf's
 // local object).
 __device__ __forceinline__ uint32_t leaf_node_of(const LbvhForest& F, uint32_t i, uint32_t& base) {
@@ -522,6 +539,12 @@ void launch_prims_from_mesh(Lbvh& b, const float4* x, const float4* nrm, const i
                             uint32_t nf, float tol, cudaStream_t s) {
   if (nf == 0) return;
   k_prims_mesh<<<grid_for(nf), kBlock, 0, s>>>(x, nrm, tri, nf, tol, b.v.p, b.pred.p);
+}
+
+void launch_prims_ccd(Lbvh& b, const float4* x, const float4* x0, const float4* nrm,
+                      const int4* tri, uint32_t nf, float tol, cudaStream_t s) {
+  if (nf == 0) return;
+  k_prims_ccd<<<grid_for(nf), kBlock, 0, s>>>(x, x0, nrm, tri, nf, tol, b.v.p, b.pred.p);
 }
 
 void launch_refit_midstep(Lbvh& b, const float4* x1, const float4* n1, const int4* tri, float tol,

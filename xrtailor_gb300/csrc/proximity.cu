@@ -529,6 +529,11 @@ PTopo topo_of(const Context& c) {
 
 }  // namespace
 
+void launch_scan_inclusive(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total,
+                           cudaStream_t s) {
+  k_scan_inclusive<<<1, 1024, 0, s>>>(in, out, n, total);
+}
+
 void launch_cloth_bvh_build(Context& c) {
   Lbvh& b = c.prox.cbvh;
   b.n = c.nf;
@@ -543,20 +548,25 @@ void launch_update_ccd(Lbvh& b, const float4* x, const float4* x0, const int4* t
                                                 b.flags.p, err);
 }
 
-// UpdatePairs: cloth BVH Update(ccd), then cloth x obstacle and cloth x cloth pairs.  The pair
-// count is read back to size the list (the reference reads num.back() the same way).
+// UpdatePairs: cloth BVH Update(ccd), then cloth x obstacle and cloth x cloth pairs.
 cudaError_t prox_update_pairs(Context& c, float thickness) {
+  launch_update_ccd(c.prox.cbvh, c.x.p, c.x0.p, c.tri.p, c.stream, c.err.p);
+  return prox_face_pairs(c, c.prox.cbvh, c.bvh, thickness);
+}
+
+// Traverse(cloth, obstacle) followed by Traverse(cloth, cloth) into the pair list.  The pair
+// count is read back to size the list (the reference reads num.back() the same way).
+cudaError_t prox_face_pairs(Context& c, const Lbvh& cloth, const Lbvh& obstacle, float thickness) {
   ProximityState& P = c.prox;
-  launch_update_ccd(P.cbvh, c.x.p, c.x0.p, c.tri.p, c.stream, c.err.p);
   P.npairs = 0;
-  if (!P.cbvh.active) return cudaGetLastError();
-  const LbvhView lhs = P.cbvh.view();
+  if (!cloth.active) return cudaGetLastError();
+  const LbvhView lhs = cloth.view();
   const uint32_t nq = lhs.n;
   struct Side {
     LbvhView rhs;
     uint32_t base;
     bool on;
-  } sides[2] = {{c.bvh.view(), c.nf, c.bvh.active}, {lhs, 0u, true}};
+  } sides[2] = {{obstacle.view(), c.nf, obstacle.active}, {lhs, 0u, true}};
   uint32_t totals[2] = {0, 0};
   for (int s = 0; s < 2; ++s) {
     if (!sides[s].on) continue;

@@ -546,6 +546,14 @@ class ClothSolver:
         a = _f32(x).reshape(-1)
         L.check(self._lib.xrt_set_predicted(self._h, L.fptr(a)), self._h, "set predicted")
 
+    def collision_step(self, obstacle_mass: float = 1e3, thickness: float = 1e-4) -> dict:
+        """ImpactZoneOptimization::CollisionStep on the current state (include/xrt_impact.h)."""
+        st = L.CollisionStats()
+        L.check(self._lib.xrt_collision_step(self._h, float(obstacle_mass), float(thickness),
+                                             C.byref(st)), self._h, "collision step")
+        return {k: getattr(st, k) for k in ("success", "deform", "passes", "impacts", "zones",
+                                            "solves")}
+
     # -- adjoint (include/xrt_diff.h) ----------------------------------------------------------
     def diff_begin(self):
         """Checkpoint the following frames for backward()."""
