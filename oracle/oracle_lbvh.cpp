@@ -530,8 +530,10 @@ static int solve_quadratic(float a, float b, float c, float x[2]) {
   if (i == 2 && x[0] > x[1]) std::swap(x[0], x[1]);
   return i;
 }
+// xc[0] starts at 0: the reference leaves it uninitialized when SolveQuadratic accepts no root
+// with a non-negative discriminant (a = b = 0), and starts Newton's method from it.
 int solve_cubic(float a, float b, float c, float d, float x[3]) {
-  float xc[2];
+  float xc[2] = {0.0f, 0.0f};
   int n = solve_quadratic(3.0f * a, 2.0f * b, c, xc);
   if (n == 0) {
     x[0] = newtons_method(a, b, c, d, xc[0], 0);

@@ -97,6 +97,10 @@ def test_solve_cubic_roots(oracle_lib):
     assert n == 3 and np.allclose(np.sort(x), [0.2, 0.5, 0.8], atol=1e-5)
     n, x = orc.solve_cubic(1.0, 0.0, 1.0, -2.0)  # one real root at 1
     assert n == 1 and abs(x[0] - 1.0) < 1e-5
+    # a = b = 0 (parallel motion): Newton's method from 0 on 0.4 x - 0.1, the same every call
+    for _ in range(3):
+        n, x = orc.solve_cubic(0.0, 0.0, 0.4, -0.1)
+        assert n == 1 and x[0] == np.float32(0.1) / np.float32(0.4)
 
 
 def _check_tree(t, n):

@@ -379,8 +379,11 @@ __device__ int solve_quadratic(float a, float b, float c, float x[2]) {
   return i;
 }
 
+// SolveCubic (MathFunctions.cu:128-150).  When the derivative quadratic has a non-negative
+// discriminant but no accepted root (a = b = 0: a linear coplanarity polynomial, e.g. parallel
+// motion), the reference starts Newton's method from an uninitialized xc[0]; here it starts from 0.
 __device__ int solve_cubic(float a, float b, float c, float d, float x[3]) {
-  float xc[2];
+  float xc[2] = {0.0f, 0.0f};
   const int n = solve_quadratic(3.0f * a, 2.0f * b, c, xc);
   if (n == 0) {
     x[0] = newtons_method(a, b, c, d, xc[0], 0);
