@@ -659,6 +659,88 @@ def run_lbvh(args, local_rank):
     }
 
 
+def _impact_state(n, solver):
+    """The impact-zone workload: an n x n sheet (two pinned corners) draped for 4 frames over the
+    radius-0.3 icosphere, then predicted positions 0.12 below: every vertex over the sphere's cap
+    crosses it within the step."""
+    from xrtailor_gb300 import scenes
+    cloth = scenes.grid_cloth(n, 1.0, origin=(0.0, 0.35, 0.0), jitter=1e-3, seed=1)
+    cloth.fixed_indices = scenes.two_corner_pins(n)
+    solver.add_cloth(cloth)
+    solver.add_obstacle(scenes.icosphere(2, 0.3, center=(0.5, 0.0, 0.5)))
+    solver.start()
+    for _ in range(4):
+        solver.step()
+    x = solver.host_positions()
+    pred = x.copy()
+    pred[:, 1] -= 0.12
+    return pred
+
+
+def _impact_params():
+    from xrtailor_gb300 import scenes
+    return scenes._params(num_substeps=2, num_iterations=3, solve_bending=0,
+                          num_collision_passes=2, enable_self_collision=0)
+
+
+def run_impact(args, local_rank):
+    """ImpactZoneOptimization::CollisionStep (xrt_collision_step): one step = restore the crossing
+    predicted positions, then the whole collision step (passes of pairs + CCD + zone solves until
+    no impact remains).  Host-driven (impact counts are read back per pass, as in the reference),
+    so it is timed on the wall clock around synchronised calls."""
+    import torch
+    from xrtailor_gb300 import ClothSolver, build as xb
+    xb.build()
+    torch.cuda.set_device(local_rank)
+    g = ClothSolver(_impact_params(), device=local_rank)
+    pred = _impact_state(args.impact_n, g)
+    for _ in range(args.warmup):
+        g.set_predicted(pred)
+        st = g.collision_step()
+    g.synchronize()
+    times = []
+    with ClockSampler(local_rank) as clocks:
+        for _ in range(args.steps):
+            g.set_predicted(pred)
+            g.synchronize()
+            t0 = time.perf_counter()
+            st = g.collision_step()
+            g.synchronize()
+            times.append(time.perf_counter() - t0)
+    # end to end: host positions in, collision step, host positions out
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        g.set_predicted(pred)
+        g.collision_step()
+        out = g.predicted()
+    e2e_s = (time.perf_counter() - e0) / args.steps
+    step_s = sum(times) / len(times)
+    V = g.sizes().num_vertices
+    res = {"metric": "impact-zone collision steps per second", "value": 1.0 / step_s,
+           "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "replicas only",
+           "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded sheet and icosphere, bench.py _impact_state)",
+           "config": {"workload": f"impact_zone_sheet{args.impact_n}", "vertices": V,
+                      "obstacle": "icosphere(2), r = 0.3", "crossing": "0.12 below x0",
+                      "stats": st},
+           "e2e": {"value": 1.0 / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": int(pred.nbytes),
+                   "d2h_bytes_per_step": int(out.nbytes)},
+           "gpu_launches": None, "roofline": None, "clocks": clocks.summary()}
+    if not args.no_cpu_baseline:
+        from oracle.oracle import OracleSolver, lib
+        o = OracleSolver(_impact_params())
+        opred = _impact_state(args.impact_n, o)
+        o.set_predicted(opred)
+        c0 = time.perf_counter()
+        so = o.collision_step()
+        ct = time.perf_counter() - c0
+        res["cpu_baseline"] = {"value": 1.0 / ct, "unit": "steps/s", "cores": 1, "kind": "port",
+                               "sample": f"1 collision step of the same state ({ct:.1f} s)",
+                               "same_stats": so == st}
+    return res
+
+
 def run_cpu(workload, frames, warmup=1, threads=0, fem=False):
     from oracle.oracle import OracleSolver, lib
     from xrtailor_gb300 import ClothSolver, scenes
@@ -693,7 +775,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="garment",
-                    choices=["garment", "small", "heavy", "batched", "diff", "lbvh"])
+                    choices=["garment", "small", "heavy", "batched", "diff", "lbvh", "impact"])
+    ap.add_argument("--impact-n", type=int, default=128, help="impact workload: sheet size")
     ap.add_argument("--cpu-frames", type=int, default=24,
                     help="frames of the CPU baseline sample (~10 s of the garment on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -747,6 +830,10 @@ def main():
     if args.workload == "lbvh":
         if rank == 0:
             print(json.dumps(run_lbvh(args, local_rank)))
+        return
+    if args.workload == "impact":
+        if rank == 0:
+            print(json.dumps(run_impact(args, local_rank)))
         return
     if world > 1:
         import torch

@@ -1583,6 +1583,9 @@ void solve_zones(IZStep& z, const std::vector<V3>& cx1, const std::vector<V3>& o
     float s = 1e-3f * (float)nn;
     w.conv = 100;
     std::vector<V3> grad(nn);
+    std::vector<std::vector<uint32_t>> slots(nn);  // per node: 4 entry + j, ascending
+    for (size_t q = 0; q < w.loc.size(); ++q)
+      if (w.loc[q] > -1) slots[w.loc[q]].push_back((uint32_t)q);
     for (int it = 0; it < 100; ++it) {
       std::vector<float> c2(ni), l2(ni);
       for (size_t e = 0; e < ni; ++e) {
@@ -1598,14 +1601,14 @@ void solve_zones(IZStep& z, const std::vector<V3>& cx1, const std::vector<V3>& o
         V3 g = (inv * mass(v)) * (w.X[k] - x1(v));
         bool first = true;
         V3 acc{0, 0, 0};
-        for (size_t e = 0; e < ni; ++e)
-          for (int j = 0; j < 4; ++j) {
-            if (w.loc[4 * e + j] != (int)k) continue;
-            const Oracle::Impact& im = z.store[w.entries[e]];
-            V3 t = ((mu * cc[e]) * im.w[j]) * im.n;
-            acc = first ? t : acc + t;
-            first = false;
-          }
+        for (uint32_t q : slots[k]) {  // reduce_by_key over the slots of the node
+          const size_t e = q / 4;
+          const int j = (int)(q % 4);
+          const Oracle::Impact& im = z.store[w.entries[e]];
+          V3 t = ((mu * cc[e]) * im.w[j]) * im.n;
+          acc = first ? t : acc + t;
+          first = false;
+        }
         g = g + acc;
         grad[k] = g;
         g2[k] = dot(g, g);

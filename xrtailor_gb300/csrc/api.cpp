@@ -403,6 +403,7 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   P.cbvh.release();
   P.face.release(); P.fedge.release(); P.fn0.release(); P.edge.release(); P.eadj.release();
   P.cfree.release(); P.counts.release(); P.incl.release(); P.total.release(); P.pairs.release();
+  P.scan.sums.release(); P.scan.incl.release();
   P.deltas.release(); P.rcounts.release(); P.imp_t.release(); P.imp_w.release(); P.imp_n.release();
   P.imp_nodes.release();
   if (c.stream) cudaStreamDestroy(c.stream);

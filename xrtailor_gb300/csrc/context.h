@@ -270,8 +270,13 @@ struct CacheState {
 };
 
 // Quality-mode self contact (proximity.cu): unified numbering, cloth first then obstacle.
+struct ScanScratch {               // tile sums of the multi-block scan (proximity.cu)
+  DBuf<uint32_t> sums, incl;
+};
+
 struct ProximityState {
   bool ready = false;
+  ScanScratch scan;
   Lbvh cbvh;                       // cloth LBVH
   DBuf<int4> face;                 // nodes (unified) + r-triangle mask
   DBuf<int4> fedge;                // unified edge of (v_i, v_i+1)
@@ -318,7 +323,7 @@ struct ImpactZoneState {
   DBuf<uint32_t> gptr, gslot;       // per node position: its (4 entry + k) slots, ascending
   DBuf<float4> X, Xt, grad;
   DBuf<float> lambda, cc, inv_avg, partial;
-  DBuf<int32_t> conv;
+  DBuf<int32_t> conv, zid;          // per zone: convergence iteration; zones in launch order
   // host side
   std::vector<uint32_t> cvf_ptr, cvf_list, ovf_ptr, ovf_list;  // node -> incident faces
   std::vector<uint4> h_snodes;
@@ -590,9 +595,9 @@ void launch_update_ccd(Lbvh& b, const float4* x, const float4* x0, const int4* t
                        uint32_t* err);
 cudaError_t prox_update_pairs(Context& c, float thickness);
 cudaError_t prox_face_pairs(Context& c, const Lbvh& cloth, const Lbvh& obstacle, float thickness);
-// inclusive scan of n counts by one block; total[0] = sum
-void launch_scan_inclusive(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total,
-                           cudaStream_t s);
+// inclusive scan of n counts (multi-block); total[0] = sum
+cudaError_t scan_inclusive(ScanScratch& w, const uint32_t* in, uint32_t* out, uint32_t n,
+                           uint32_t* total, cudaStream_t s);
 void prox_solve(Context& c, float thickness, float relaxation);
 cudaError_t prox_check_impacts(Context& c, float thickness);
 // prims with ccd boxes: v_k = x0[idx_k] + tol * n[idx_k], pred_k = x[idx_k] + tol * n[idx_k]

@@ -24,16 +24,22 @@
 // ParallelOptimizer.cu:335-428): 256-element blocks summed by the stride tree s[t] += s[t + d],
 // d = 1, 2, ..., 128, then the block sums by the same tree.  With --fmad=false every value is the
 // IEEE result of the reference's expression order.
+#include <cooperative_groups.h>
+
 #include <algorithm>
+#include <iterator>
 #include <numeric>
 
 #include "common.cuh"
 #include "context.h"
 
+namespace cg = cooperative_groups;
+
 namespace xrt {
 namespace {
 
 constexpr int kZT = 256;              // threads of a zone block = IZO_BLOCK_SIZE
+constexpr int kZoneCluster = 8;       // blocks per zone of more than 256 nodes or impacts
 constexpr int kMaxChunks = 256;       // 256 x 256 nodes / impacts per zone (the reduction's reach)
 constexpr int kMaxOptIters = 100;     // MAX_ITERATIONS (ParallelOptimizer.cuh)
 constexpr int kMaxLineSearch = 1024;  // the reference's search ends by s < 1e-12 within ~110 steps
@@ -125,66 +131,81 @@ __device__ __forceinline__ float constraint_at(const ZoneArgs& a, int e, const f
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int k = a.zloc[4 * e + j];
-    const f3 x = k > -1 ? mk3(Xs[k]) : pos_of(a, nds[j]);
+    const f3 x = k > -1 ? mk3(__ldcg(&Xs[k])) : pos_of(a, nds[j]);
     c += comp4(w, j) * dot(n, x);
   }
   return c;
 }
 
-__global__ void __launch_bounds__(kZT) k_zone_solve(ZoneArgs a) {
+// One zone per cluster of C blocks (C = 1 for zones of at most 256 nodes and impacts).  Block r
+// of the cluster owns the 256-element chunks ch = r, r + C, ...: it computes their values and
+// chunk sums and writes the sums into block 0's shared memory (distributed shared memory); after
+// a cluster barrier every block reads the chunk sums from block 0 and sums them by the same
+// tree, so every block of the cluster holds the same totals and takes the same branches.  Zone
+// arrays written by one block and read by others go through L2 (ld/st .cg).
+template <int C>
+__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
+    k_zone_solve(ZoneArgs a, const int32_t* __restrict__ zid) {
   __shared__ float pa[kMaxChunks], pb[kMaxChunks];
   __shared__ float ws[9];
+  cg::cluster_group cl = cg::this_cluster();
   const int tid = threadIdx.x;
-  const int4 z = a.zone[blockIdx.x];
+  const int rank = (int)cl.block_rank();
+  const int zi = zid[blockIdx.x / C];
+  float* lpa = cl.map_shared_rank(pa, 0);
+  float* lpb = cl.map_shared_rank(pb, 0);
+  const int4 z = a.zone[zi];
   const int eb = z.x, ni = z.y - z.x, nb = z.z, nn = z.w - z.z;
   if (ni > kZT * kMaxChunks || nn > kZT * kMaxChunks) {
-    if (tid == 0) {
+    if (tid == 0 && rank == 0) {
       raise_error(a.err, kErrZoneSize);
-      a.conv[blockIdx.x] = -1;  // positions stay
+      a.conv[zi] = -1;  // positions stay
     }
     return;
   }
   const int nce = (ni + kZT - 1) / kZT, ncn = (nn + kZT - 1) / kZT;
-  for (int k = tid; k < nn; k += kZT) {  // Initialize_Kernel
+  const int first = rank * kZT + tid, stride = C * kZT;  // this block's elements
+  for (int k = first; k < nn; k += stride) {  // Initialize_Kernel
     const float4 p = mk4(pos_of(a, a.znode[nb + k]), 0.0f);
-    a.X[nb + k] = p;
-    a.Xt[nb + k] = p;
+    __stcg(&a.X[nb + k], p);
+    __stcg(&a.Xt[nb + k], p);
   }
-  for (int e = tid; e < ni; e += kZT) a.lambda[eb + e] = 0.0f;
-  __syncthreads();
+  for (int e = first; e < ni; e += stride) __stcg(&a.lambda[eb + e], 0.0f);
+  cl.sync();
   const float inv = *a.inv_avg;
   float s = kStepCoeff * (float)nn;  // InitStepLength_Kernel
   int conv_it = kMaxOptIters;
   for (int it = 0; it < kMaxOptIters; ++it) {
     // constraints at X: coefficients min(c + lambda / mu, 0), C2 and lambda2
-    for (int ch = 0; ch < nce; ++ch) {
+    for (int ch = rank; ch < nce; ch += C) {
       const int e = ch * kZT + tid;
       float c2 = 0.0f, l2 = 0.0f;
       if (e < ni) {
-        const float lam = a.lambda[eb + e];
+        const float lam = __ldcg(&a.lambda[eb + e]);
         const float q = tmin(constraint_at(a, eb + e, a.X) + lam / kMu, 0.0f);
-        a.cc[eb + e] = q;
+        __stcg(&a.cc[eb + e], q);
         c2 = q * q;
         l2 = lam * lam;
       }
       c2 = tree256(c2, ws);
       l2 = tree256(l2, ws);
       if (tid == 0) {
-        pa[ch] = c2;
-        pb[ch] = l2;
+        lpa[ch] = c2;
+        lpb[ch] = l2;
       }
     }
-    __syncthreads();
-    const float C2 = tree256(tid < nce ? pa[tid] : 0.0f, ws);
-    const float L2 = tree256(tid < nce ? pb[tid] : 0.0f, ws);
+    cl.sync();
+    const float C2 = tree256(tid < nce ? lpa[tid] : 0.0f, ws);
+    const float L2 = tree256(tid < nce ? lpb[tid] : 0.0f, ws);
+    cl.sync();
     // gradient at X: inv * m * (x - x1) + sum of mu * coefficient * w_j * n (slot order); G2, O
-    for (int ch = 0; ch < ncn; ++ch) {
+    for (int ch = rank; ch < ncn; ch += C) {
       const int k = ch * kZT + tid;
       float g2 = 0.0f, o = 0.0f;
       if (k < nn) {
         const int idx = nb + k;
         const uint32_t v = a.znode[idx];
-        const f3 x = mk3(a.X[idx]), x1 = x1_of(a, v);
+        const f3 x = mk3(__ldcg(&a.X[idx])), x1 = x1_of(a, v);
         const float m = mass_of(a, v);
         f3 g = (inv * m) * (x - x1);
         f3 acc = mk3(0.0f, 0.0f, 0.0f);
@@ -192,11 +213,11 @@ __global__ void __launch_bounds__(kZT) k_zone_solve(ZoneArgs a) {
           const uint32_t slot = a.gslot[q];
           const int e = (int)(slot >> 2), j = (int)(slot & 3u);
           const uint32_t id = a.zimp[e];
-          const f3 t = ((kMu * a.cc[e]) * comp4(a.sw[id], j)) * mk3(a.sn[id]);
+          const f3 t = ((kMu * __ldcg(&a.cc[e])) * comp4(a.sw[id], j)) * mk3(a.sn[id]);
           acc = q == a.gptr[idx] ? t : acc + t;
         }
         g = g + acc;
-        a.grad[idx] = mk4(g, 0.0f);
+        __stcg(&a.grad[idx], mk4(g, 0.0f));
         g2 = dot(g, g);
         const f3 d = x - x1;
         o = m * dot(d, d);
@@ -204,50 +225,53 @@ __global__ void __launch_bounds__(kZT) k_zone_solve(ZoneArgs a) {
       g2 = tree256(g2, ws);
       o = tree256(o, ws);
       if (tid == 0) {
-        pa[ch] = g2;
-        pb[ch] = o;
+        lpa[ch] = g2;
+        lpb[ch] = o;
       }
     }
-    __syncthreads();
-    const float G2 = tree256(tid < ncn ? pa[tid] : 0.0f, ws);
-    const float O = tree256(tid < ncn ? pb[tid] : 0.0f, ws);
+    cl.sync();
+    const float G2 = tree256(tid < ncn ? lpa[tid] : 0.0f, ws);
+    const float O = tree256(tid < ncn ? lpb[tid] : 0.0f, ws);
+    cl.sync();
     const float f = (0.5f * inv) * O + (0.5f * kMu) * C2 - (0.5f * L2) / kMu;
     s = s / 0.7f;  // PreconditionStepLength_Kernel
     for (int ls = 0;; ++ls) {
       s = s * 0.7f;  // AdjustStepLength_Kernel
-      for (int ch = 0; ch < ncn; ++ch) {  // NextX_Kernel + CollisionObjective_Kernel
+      for (int ch = rank; ch < ncn; ch += C) {  // NextX_Kernel + CollisionObjective_Kernel
         const int k = ch * kZT + tid;
         float o = 0.0f;
         if (k < nn) {
           const int idx = nb + k;
           const uint32_t v = a.znode[idx];
-          const f3 xt = mk3(a.X[idx]) - s * mk3(a.grad[idx]);
-          a.Xt[idx] = mk4(xt, 0.0f);
+          const f3 xt = mk3(__ldcg(&a.X[idx])) - s * mk3(__ldcg(&a.grad[idx]));
+          __stcg(&a.Xt[idx], mk4(xt, 0.0f));
           const f3 d = xt - x1_of(a, v);
           o = mass_of(a, v) * dot(d, d);
         }
         o = tree256(o, ws);
-        if (tid == 0) pa[ch] = o;
+        if (tid == 0) lpa[ch] = o;
       }
-      __syncthreads();
-      const float Ot = tree256(tid < ncn ? pa[tid] : 0.0f, ws);
-      for (int ch = 0; ch < nce; ++ch) {
+      cl.sync();
+      const float Ot = tree256(tid < ncn ? lpa[tid] : 0.0f, ws);
+      for (int ch = rank; ch < nce; ch += C) {
         const int e = ch * kZT + tid;
         float c2 = 0.0f;
         if (e < ni) {
-          const float q = tmin(constraint_at(a, eb + e, a.Xt) + a.lambda[eb + e] / kMu, 0.0f);
+          const float q = tmin(constraint_at(a, eb + e, a.Xt) + __ldcg(&a.lambda[eb + e]) / kMu,
+                               0.0f);
           c2 = q * q;
         }
         c2 = tree256(c2, ws);
-        if (tid == 0) pb[ch] = c2;
+        if (tid == 0) lpb[ch] = c2;
       }
-      __syncthreads();
-      const float C2t = tree256(tid < nce ? pb[tid] : 0.0f, ws);
+      cl.sync();
+      const float C2t = tree256(tid < nce ? lpb[tid] : 0.0f, ws);
+      cl.sync();
       // BacktrackingLineSearchAdvanced_Kernel (ParallelImpactZoneOptimizer.cu:413-497)
       const float ft = (0.5f * inv) * Ot + (0.5f * kMu) * C2t - (0.5f * L2) / kMu;
       if (s < kEpsS || ft < f - (kAlpha * s) * G2 || tabs(f - ft) < kEpsF) break;
       if (ls + 1 >= kMaxLineSearch) {  // only a non-finite objective gets here
-        if (tid == 0) raise_error(a.err, kErrLineSearch);
+        if (tid == 0 && rank == 0) raise_error(a.err, kErrLineSearch);
         s = 0.0f;
         break;
       }
@@ -256,15 +280,16 @@ __global__ void __launch_bounds__(kZT) k_zone_solve(ZoneArgs a) {
       conv_it = it;
       break;
     }
-    for (int k = tid; k < nn; k += kZT) a.X[nb + k] = a.Xt[nb + k];  // current_X = next_X
-    __syncthreads();
-    for (int e = tid; e < ni; e += kZT) {  // UpdateMultiplier_Kernel
+    for (int k = first; k < nn; k += stride)  // current_X = next_X
+      __stcg(&a.X[nb + k], __ldcg(&a.Xt[nb + k]));
+    cl.sync();
+    for (int e = first; e < ni; e += stride) {  // UpdateMultiplier_Kernel
       const float c = constraint_at(a, eb + e, a.X);
-      a.lambda[eb + e] = tmin(a.lambda[eb + e] + kMu * c, 0.0f);
+      __stcg(&a.lambda[eb + e], tmin(__ldcg(&a.lambda[eb + e]) + kMu * c, 0.0f));
     }
-    __syncthreads();
+    cl.sync();
   }
-  if (tid == 0) a.conv[blockIdx.x] = conv_it;
+  if (tid == 0 && rank == 0) a.conv[zi] = conv_it;
 }
 
 // Finalize_Kernel.  The reference's iteration loop stops once every zone has converged, before
@@ -621,7 +646,7 @@ xrt_status find_impacts(Context& c, float thickness, std::vector<float>& t,
   XRT_CUDA(&c, z.hits.reserve(np));
   XRT_CUDA(&c, z.hit_incl.reserve(np));
   k_count_hits<<<grid_for(np), kBlock, 0, s>>>(c.prox.imp_t.p, np, z.hits.p);
-  launch_scan_inclusive(z.hits.p, z.hit_incl.p, np, z.hit_total.p, s);
+  XRT_CUDA(&c, scan_inclusive(c.prox.scan, z.hits.p, z.hit_incl.p, np, z.hit_total.p, s));
   uint32_t total = 0;
   XRT_CUDA(&c, cudaMemcpyAsync(&total, z.hit_total.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   XRT_CUDA(&c, cudaStreamSynchronize(s));
@@ -700,7 +725,14 @@ xrt_status solve_zones(Context& c, const Graph& g, float obstacle_mass, float th
   ZoneArgs a{z.zone.p, z.zimp.p, z.zloc.p, z.znode.p, z.gptr.p, z.gslot.p, z.sw.p, z.sn.p,
              z.snodes.p, c.x.p, c.ox.p, z.cx1.p, z.ox1.p, z.X.p, z.Xt.p, z.grad.p, z.lambda.p,
              z.cc.p, z.conv.p, z.inv_avg.p, c.nv, obstacle_mass, thickness, c.err.p};
-  k_zone_solve<<<nz, kZT, 0, s>>>(a);
+  std::vector<int32_t> small, large;  // zones by size: one block, or a cluster of blocks
+  for (uint32_t q = 0; q < nz; ++q)
+    (std::max(zone[q].y - zone[q].x, zone[q].w - zone[q].z) <= kZT ? small : large).push_back((int32_t)q);
+  const uint32_t ns = (uint32_t)small.size(), nl = (uint32_t)large.size();
+  small.insert(small.end(), large.begin(), large.end());
+  XRT_CUDA(&c, put(z.zid, small, s));
+  if (ns) k_zone_solve<1><<<ns, kZT, 0, s>>>(a, z.zid.p);
+  if (nl) k_zone_solve<kZoneCluster><<<nl * kZoneCluster, kZT, 0, s>>>(a, z.zid.p + ns);
   k_zone_finalize<<<nz, kZT, 0, s>>>(z.zone.p, z.conv.p, nz, z.znode.p, z.X.p, z.Xt.p, c.x.p,
                                      c.ox.p, c.nv);
   XRT_CUDA(&c, cudaGetLastError());
@@ -806,6 +838,7 @@ void izone_release(Context& c) {
   z.zone.release();
   z.zloc.release();
   z.conv.release();
+  z.zid.release();
   z.zones.clear();
   z.ready = false;
 }

@@ -13,6 +13,8 @@
 // Nodes, faces and edges of the cloth and of the obstacle share one numbering (cloth first), the
 // device counterpart of the reference's Node*/Face*/Edge* pointers.  Repulsion deltas are summed
 // with float atomics in launch order, as in the reference; every other output is deterministic.
+#include <algorithm>
+
 #include "common.cuh"
 #include "context.h"
 #include "lbvh_dev.cuh"
@@ -275,6 +277,50 @@ __global__ void k_pairs(LbvhView lhs, LbvhView rhs, float thickness, uint32_t* _
   if (!FILL) counts[id] = found;
 }
 
+// Inclusive scan of a 1024-element tile by one block: warp shuffles, then the warp totals.
+__device__ uint32_t block_scan1024(uint32_t v, uint32_t* sw /* 32 */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t o = __shfl_up_sync(0xFFFFFFFFu, v, d);
+    if (lane >= d) v += o;
+  }
+  if (lane == 31) sw[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t t = sw[lane];
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t o = __shfl_up_sync(0xFFFFFFFFu, t, d);
+      if (lane >= d) t += o;
+    }
+    sw[lane] = t;
+  }
+  __syncthreads();
+  return v + (warp ? sw[warp - 1] : 0u);
+}
+
+// Phase 1 of the multi-block scan: the sum of each 1024-element tile.
+__global__ void __launch_bounds__(1024) k_tile_sums(const uint32_t* __restrict__ in, uint32_t n,
+                                                    uint32_t* __restrict__ sums) {
+  __shared__ uint32_t sw[32];
+  const uint32_t i = blockIdx.x * 1024u + threadIdx.x;
+  const uint32_t v = block_scan1024(i < n ? in[i] : 0u, sw);
+  if (threadIdx.x == 1023) sums[blockIdx.x] = v;
+}
+
+// Phase 3: each tile scanned, plus the inclusive scan of the tile sums before it.
+__global__ void __launch_bounds__(1024) k_tile_scan(const uint32_t* __restrict__ in, uint32_t n,
+                                                    const uint32_t* __restrict__ sums,
+                                                    const uint32_t* __restrict__ sums_incl,
+                                                    uint32_t* __restrict__ out) {
+  __shared__ uint32_t sw[32];
+  const uint32_t i = blockIdx.x * 1024u + threadIdx.x;
+  const uint32_t base = sums_incl[blockIdx.x] - sums[blockIdx.x];
+  const uint32_t v = block_scan1024(i < n ? in[i] : 0u, sw);
+  if (i < n) out[i] = base + v;
+}
+
 // Inclusive scan of `n` counts by one block of 1024 threads; total[0] = sum.
 __global__ void __launch_bounds__(1024) k_scan_inclusive(const uint32_t* __restrict__ in,
                                                          uint32_t* __restrict__ out, uint32_t n,
@@ -470,57 +516,52 @@ __device__ bool overlap_dilated(const float* alo, const float* ahi, const float*
   return true;
 }
 
+// One thread per test: test k of pair p writes slot 15 p + k.  k = 3 side + i (side 0: vertex i of
+// the first face against the second face, side 1: the reverse), then k = 6 + 3 i + j (edge i of
+// the first face against edge j of the second), the reference's order.
 __global__ void k_check_impacts(PNodes u, PTopo t, const uint2* __restrict__ pairs, uint32_t np,
                                 float thickness, ImpactOut out) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= np) return;
+  const size_t index = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (index >= 15 * (size_t)np) return;
+  const uint32_t p = (uint32_t)(index / 15), k = (uint32_t)(index % 15);
   const uint2 pr = pairs[p];
-  size_t index = 15 * (size_t)p;
-  for (int side = 0; side < 2; ++side) {
-    const uint32_t f0 = side == 0 ? pr.x : pr.y, f1 = side == 0 ? pr.y : pr.x;
-    const int4 a = t.face[f0], b = t.face[f1];
-    const uint32_t an[3] = {(uint32_t)a.x, (uint32_t)a.y, (uint32_t)a.z};
-    for (int i = 0; i < 3; ++i, ++index) {
-      const uint32_t nd[4] = {an[i], (uint32_t)b.x, (uint32_t)b.y, (uint32_t)b.z};
-      float w[4] = {0, 0, 0, 0};
-      f3 n = mk3(0, 0, 0);
-      float tt = 0;
-      bool ok = false;
-      if (!(nd[0] == nd[1] || nd[0] == nd[2] || nd[0] == nd[3])) {
-        float alo[3], ahi[3], blo[3], bhi[3];
-        ccd_bounds(u, nd, 0, 1, alo, ahi);
-        ccd_bounds(u, nd, 1, 3, blo, bhi);
-        if (overlap_dilated(alo, ahi, blo, bhi, thickness)) ok = check_impact(u, true, nd, tt, w, n);
-      }
-      out.t[index] = ok ? tt : -1.0f;
-      out.w[index] = make_float4(w[0], w[1], w[2], w[3]);
-      out.n[index] = make_float4(n.x, n.y, n.z, 1.0f);
-      out.nodes[index] = make_uint4(nd[0], nd[1], nd[2], nd[3]);
-    }
+  const bool vf = k < 6;
+  uint32_t nd[4];
+  bool distinct;
+  if (vf) {
+    const uint32_t side = k / 3, i = k % 3;
+    const int4 a = t.face[side == 0 ? pr.x : pr.y], b = t.face[side == 0 ? pr.y : pr.x];
+    nd[0] = (uint32_t)(i == 0 ? a.x : (i == 1 ? a.y : a.z));
+    nd[1] = (uint32_t)b.x;
+    nd[2] = (uint32_t)b.y;
+    nd[3] = (uint32_t)b.z;
+    distinct = !(nd[0] == nd[1] || nd[0] == nd[2] || nd[0] == nd[3]);
+  } else {
+    const uint32_t i = (k - 6) / 3, j = (k - 6) % 3;
+    const int4 ea = t.fedge[pr.x], eb = t.fedge[pr.y];
+    const uint2 e0 = t.edge[i == 0 ? ea.x : (i == 1 ? ea.y : ea.z)];
+    const uint2 e1 = t.edge[j == 0 ? eb.x : (j == 1 ? eb.y : eb.z)];
+    nd[0] = e0.x;
+    nd[1] = e0.y;
+    nd[2] = e1.x;
+    nd[3] = e1.y;
+    distinct = !(nd[0] == nd[2] || nd[0] == nd[3] || nd[1] == nd[2] || nd[1] == nd[3]);
   }
-  const int4 ea = t.fedge[pr.x], eb = t.fedge[pr.y];
-  const uint32_t eas[3] = {(uint32_t)ea.x, (uint32_t)ea.y, (uint32_t)ea.z};
-  const uint32_t ebs[3] = {(uint32_t)eb.x, (uint32_t)eb.y, (uint32_t)eb.z};
-  for (int i = 0; i < 3; ++i) {
-    for (int j = 0; j < 3; ++j, ++index) {
-      const uint2 e0 = t.edge[eas[i]], e1 = t.edge[ebs[j]];
-      const uint32_t nd[4] = {e0.x, e0.y, e1.x, e1.y};
-      float w[4] = {0, 0, 0, 0};
-      f3 n = mk3(0, 0, 0);
-      float tt = 0;
-      bool ok = false;
-      if (!(nd[0] == nd[2] || nd[0] == nd[3] || nd[1] == nd[2] || nd[1] == nd[3])) {
-        float alo[3], ahi[3], blo[3], bhi[3];
-        ccd_bounds(u, nd, 0, 2, alo, ahi);
-        ccd_bounds(u, nd, 2, 2, blo, bhi);
-        if (overlap_dilated(alo, ahi, blo, bhi, thickness)) ok = check_impact(u, false, nd, tt, w, n);
-      }
-      out.t[index] = ok ? tt : -1.0f;
-      out.w[index] = make_float4(w[0], w[1], w[2], w[3]);
-      out.n[index] = make_float4(n.x, n.y, n.z, 0.0f);
-      out.nodes[index] = make_uint4(nd[0], nd[1], nd[2], nd[3]);
-    }
+  float w[4] = {0, 0, 0, 0};
+  f3 n = mk3(0, 0, 0);
+  float tt = 0;
+  bool ok = false;
+  if (distinct) {
+    const int na = vf ? 1 : 2;
+    float alo[3], ahi[3], blo[3], bhi[3];
+    ccd_bounds(u, nd, 0, na, alo, ahi);
+    ccd_bounds(u, nd, na, 4 - na, blo, bhi);
+    if (overlap_dilated(alo, ahi, blo, bhi, thickness)) ok = check_impact(u, vf, nd, tt, w, n);
   }
+  out.t[index] = ok ? tt : -1.0f;
+  out.w[index] = make_float4(w[0], w[1], w[2], w[3]);
+  out.n[index] = make_float4(n.x, n.y, n.z, vf ? 1.0f : 0.0f);
+  out.nodes[index] = make_uint4(nd[0], nd[1], nd[2], nd[3]);
 }
 
 PNodes nodes_of(const Context& c) {
@@ -532,9 +573,18 @@ PTopo topo_of(const Context& c) {
 
 }  // namespace
 
-void launch_scan_inclusive(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total,
-                           cudaStream_t s) {
-  k_scan_inclusive<<<1, 1024, 0, s>>>(in, out, n, total);
+// Tiles of 1024 summed, the tile sums scanned by one block, the tiles scanned with their offsets.
+cudaError_t scan_inclusive(ScanScratch& w, const uint32_t* in, uint32_t* out, uint32_t n,
+                           uint32_t* total, cudaStream_t s) {
+  const uint32_t nt = std::max(1u, (n + 1023) / 1024);
+  cudaError_t e = w.sums.reserve(nt);
+  if (e == cudaSuccess) e = w.incl.reserve(nt);
+  if (e != cudaSuccess) return e;
+  if (n == 0) return cudaMemsetAsync(total, 0, sizeof(uint32_t), s);
+  k_tile_sums<<<nt, 1024, 0, s>>>(in, n, w.sums.p);
+  k_scan_inclusive<<<1, 1024, 0, s>>>(w.sums.p, w.incl.p, nt, total);
+  k_tile_scan<<<nt, 1024, 0, s>>>(in, n, w.sums.p, w.incl.p, out);
+  return cudaGetLastError();
 }
 
 void launch_cloth_bvh_build(Context& c) {
@@ -575,7 +625,9 @@ cudaError_t prox_face_pairs(Context& c, const Lbvh& cloth, const Lbvh& obstacle,
     if (!sides[s].on) continue;
     k_pairs<false><<<grid_for(nq), kBlock, 0, c.stream>>>(lhs, sides[s].rhs, thickness, P.counts.p,
                                                           nullptr, 0, 0, 0, nullptr, c.err.p);
-    k_scan_inclusive<<<1, 1024, 0, c.stream>>>(P.counts.p, P.incl.p + (size_t)s * nq, nq, P.total.p + s);
+    const cudaError_t e = scan_inclusive(P.scan, P.counts.p, P.incl.p + (size_t)s * nq, nq,
+                                         P.total.p + s, c.stream);
+    if (e != cudaSuccess) return e;
   }
   cudaError_t e = cudaMemcpyAsync(totals, P.total.p, sizeof(totals), cudaMemcpyDeviceToHost, c.stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
@@ -619,7 +671,7 @@ cudaError_t prox_check_impacts(Context& c, float thickness) {
   }
   P.nimpacts = (uint32_t)ni;
   if (P.npairs)
-    k_check_impacts<<<grid_for(P.npairs), kBlock, 0, c.stream>>>(
+    k_check_impacts<<<grid_for((uint32_t)ni), kBlock, 0, c.stream>>>(
         nodes_of(c), topo_of(c), P.pairs.p, P.npairs, thickness,
         ImpactOut{P.imp_t.p, P.imp_w.p, P.imp_n.p, P.imp_nodes.p});
   return cudaGetLastError();
