@@ -40,6 +40,7 @@ namespace {
 
 constexpr int kZT = 256;              // threads of a zone block = IZO_BLOCK_SIZE
 constexpr int kZoneCluster = 8;       // blocks per zone of more than 256 nodes or impacts
+constexpr int kZoneClusterWide = 16;  // blocks per zone of more than 2,048 (non-portable size)
 constexpr int kMaxChunks = 256;       // 256 x 256 nodes / impacts per zone (the reduction's reach)
 constexpr int kMaxOptIters = 100;     // MAX_ITERATIONS (ParallelOptimizer.cuh)
 constexpr int kMaxLineSearch = 1024;  // the reference's search ends by s < 1e-12 within ~110 steps
@@ -52,6 +53,45 @@ constexpr float kStepCoeff = 1e-3f;   // STEP_LENGTH_COEFF_SCALAR
 
 __device__ __forceinline__ float comp4(float4 v, int j) {
   return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+
+// Two sums of one value per thread each, every thread getting both; the tree256 order.  ws: 18
+// floats; callers alternate two ws buffers, so a call needs no barrier after its reads.
+__device__ __forceinline__ void tree256_2(float& a, float& b, float* ws) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const float oa = __shfl_down_sync(0xFFFFFFFFu, a, d);
+    const float ob = __shfl_down_sync(0xFFFFFFFFu, b, d);
+    if ((lane & (2 * d - 1)) == 0) {
+      a += oa;
+      b += ob;
+    }
+  }
+  if (lane == 0) {
+    ws[warp] = a;
+    ws[9 + warp] = b;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    float u = lane < 8 ? ws[lane] : 0.0f, w = lane < 8 ? ws[9 + lane] : 0.0f;
+#pragma unroll
+    for (int d = 1; d < 8; d <<= 1) {
+      const float ou = __shfl_down_sync(0xFFFFFFFFu, u, d);
+      const float ow = __shfl_down_sync(0xFFFFFFFFu, w, d);
+      if ((lane & (2 * d - 1)) == 0) {
+        u += ou;
+        w += ow;
+      }
+    }
+    if (lane == 0) {
+      ws[8] = u;
+      ws[17] = w;
+    }
+  }
+  __syncthreads();
+  a = ws[8];
+  b = ws[17];
 }
 
 // Sum of one value per thread of a 256-thread block in the order of the reference's stride tree:
@@ -137,23 +177,46 @@ __device__ __forceinline__ float constraint_at(const ZoneArgs& a, int e, const f
   return c;
 }
 
+template <int C>
+__device__ __forceinline__ void zone_sync(cg::cluster_group& cl) {
+  if constexpr (C == 1) {
+    __syncthreads();
+  } else {
+    cl.sync();
+  }
+}
+
 // One zone per cluster of C blocks (C = 1 for zones of at most 256 nodes and impacts).  Block r
 // of the cluster owns the 256-element chunks ch = r, r + C, ...: it computes their values and
 // chunk sums and writes the sums into block 0's shared memory (distributed shared memory); after
 // a cluster barrier every block reads the chunk sums from block 0 and sums them by the same
-// tree, so every block of the cluster holds the same totals and takes the same branches.  Zone
-// arrays written by one block and read by others go through L2 (ld/st .cg).
+// tree, so every block of the cluster holds the same totals and takes the same branches.  The
+// chunk sums alternate between two buffer sets: a set is written again only after a later
+// barrier that every block reaches after its reads.  Zone arrays written by one block and read
+// by others go through L2 (ld/st .cg) and are published by a barrier before they are read.
 template <int C>
 __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
     k_zone_solve(ZoneArgs a, const int32_t* __restrict__ zid) {
-  __shared__ float pa[kMaxChunks], pb[kMaxChunks];
-  __shared__ float ws[9];
+  __shared__ float part[2 * 2 * kMaxChunks];  // [buffer set][quantity][chunk], read in block 0
+  __shared__ float wsb[2 * 18];
   cg::cluster_group cl = cg::this_cluster();
   const int tid = threadIdx.x;
   const int rank = (int)cl.block_rank();
   const int zi = zid[blockIdx.x / C];
-  float* lpa = cl.map_shared_rank(pa, 0);
-  float* lpb = cl.map_shared_rank(pb, 0);
+  float* lead = cl.map_shared_rank(part, 0);
+  int set = 0, wsp = 0;
+  auto buf = [&](int q) { return lead + (2 * set + q) * kMaxChunks; };
+  auto tree2 = [&](float& x, float& y) {
+    tree256_2(x, y, wsb + 18 * wsp);
+    wsp ^= 1;
+  };
+  // chunk sums of this block's chunks of a quantity pair, then the totals of both
+  auto totals = [&](int nch, float& x, float& y) {
+    x = tid < nch ? buf(0)[tid] : 0.0f;
+    y = tid < nch ? buf(1)[tid] : 0.0f;
+    tree2(x, y);
+    set ^= 1;
+  };
   const int4 z = a.zone[zi];
   const int eb = z.x, ni = z.y - z.x, nb = z.z, nn = z.w - z.z;
   if (ni > kZT * kMaxChunks || nn > kZT * kMaxChunks) {
@@ -171,10 +234,11 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
     __stcg(&a.Xt[nb + k], p);
   }
   for (int e = first; e < ni; e += stride) __stcg(&a.lambda[eb + e], 0.0f);
-  cl.sync();
+  zone_sync<C>(cl);
   const float inv = *a.inv_avg;
   float s = kStepCoeff * (float)nn;  // InitStepLength_Kernel
   int conv_it = kMaxOptIters;
+  float zero = 0.0f;
   for (int it = 0; it < kMaxOptIters; ++it) {
     // constraints at X: coefficients min(c + lambda / mu, 0), C2 and lambda2
     for (int ch = rank; ch < nce; ch += C) {
@@ -187,17 +251,15 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
         c2 = q * q;
         l2 = lam * lam;
       }
-      c2 = tree256(c2, ws);
-      l2 = tree256(l2, ws);
+      tree2(c2, l2);
       if (tid == 0) {
-        lpa[ch] = c2;
-        lpb[ch] = l2;
+        buf(0)[ch] = c2;
+        buf(1)[ch] = l2;
       }
     }
-    cl.sync();
-    const float C2 = tree256(tid < nce ? lpa[tid] : 0.0f, ws);
-    const float L2 = tree256(tid < nce ? lpb[tid] : 0.0f, ws);
-    cl.sync();
+    zone_sync<C>(cl);
+    float C2, L2;
+    totals(nce, C2, L2);
     // gradient at X: inv * m * (x - x1) + sum of mu * coefficient * w_j * n (slot order); G2, O
     for (int ch = rank; ch < ncn; ch += C) {
       const int k = ch * kZT + tid;
@@ -222,17 +284,15 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
         const f3 d = x - x1;
         o = m * dot(d, d);
       }
-      g2 = tree256(g2, ws);
-      o = tree256(o, ws);
+      tree2(g2, o);
       if (tid == 0) {
-        lpa[ch] = g2;
-        lpb[ch] = o;
+        buf(0)[ch] = g2;
+        buf(1)[ch] = o;
       }
     }
-    cl.sync();
-    const float G2 = tree256(tid < ncn ? lpa[tid] : 0.0f, ws);
-    const float O = tree256(tid < ncn ? lpb[tid] : 0.0f, ws);
-    cl.sync();
+    zone_sync<C>(cl);
+    float G2, O;
+    totals(ncn, G2, O);
     const float f = (0.5f * inv) * O + (0.5f * kMu) * C2 - (0.5f * L2) / kMu;
     s = s / 0.7f;  // PreconditionStepLength_Kernel
     for (int ls = 0;; ++ls) {
@@ -248,11 +308,10 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
           const f3 d = xt - x1_of(a, v);
           o = mass_of(a, v) * dot(d, d);
         }
-        o = tree256(o, ws);
-        if (tid == 0) lpa[ch] = o;
+        tree2(o, zero);
+        if (tid == 0) buf(0)[ch] = o;
       }
-      cl.sync();
-      const float Ot = tree256(tid < ncn ? lpa[tid] : 0.0f, ws);
+      zone_sync<C>(cl);  // also publishes Xt
       for (int ch = rank; ch < nce; ch += C) {
         const int e = ch * kZT + tid;
         float c2 = 0.0f;
@@ -261,12 +320,14 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
                                0.0f);
           c2 = q * q;
         }
-        c2 = tree256(c2, ws);
-        if (tid == 0) lpb[ch] = c2;
+        tree2(c2, zero);
+        if (tid == 0) buf(1)[ch] = c2;
       }
-      cl.sync();
-      const float C2t = tree256(tid < nce ? lpb[tid] : 0.0f, ws);
-      cl.sync();
+      zone_sync<C>(cl);
+      // Ot over the nodes' chunks, C2t over the impacts' chunks
+      float Ot = tid < ncn ? buf(0)[tid] : 0.0f, C2t = tid < nce ? buf(1)[tid] : 0.0f;
+      tree2(Ot, C2t);
+      set ^= 1;
       // BacktrackingLineSearchAdvanced_Kernel (ParallelImpactZoneOptimizer.cu:413-497)
       const float ft = (0.5f * inv) * Ot + (0.5f * kMu) * C2t - (0.5f * L2) / kMu;
       if (s < kEpsS || ft < f - (kAlpha * s) * G2 || tabs(f - ft) < kEpsF) break;
@@ -282,14 +343,32 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
     }
     for (int k = first; k < nn; k += stride)  // current_X = next_X
       __stcg(&a.X[nb + k], __ldcg(&a.Xt[nb + k]));
-    cl.sync();
-    for (int e = first; e < ni; e += stride) {  // UpdateMultiplier_Kernel
+    zone_sync<C>(cl);
+    for (int e = first; e < ni; e += stride) {  // UpdateMultiplier_Kernel (own impacts only)
       const float c = constraint_at(a, eb + e, a.X);
       __stcg(&a.lambda[eb + e], tmin(__ldcg(&a.lambda[eb + e]) + kMu * c, 0.0f));
     }
-    cl.sync();
   }
   if (tid == 0 && rank == 0) a.conv[zi] = conv_it;
+}
+
+// 16-block clusters need the non-portable cluster size opt-in; they are used once the device
+// reports that it can hold one (else zones stay on 8-block clusters).
+bool wide_clusters() {
+  static int state = -1;
+  if (state < 0) {
+    state = 0;
+    const void* k = (const void*)k_zone_solve<kZoneClusterWide>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(kZoneClusterWide);
+      cfg.blockDim = dim3(kZT);
+      int n = 0;
+      if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) == cudaSuccess && n > 0) state = 1;
+    }
+    (void)cudaGetLastError();  // a refused opt-in is not an error of the step
+  }
+  return state == 1;
 }
 
 // Finalize_Kernel.  The reference's iteration loop stops once every zone has converged, before
@@ -725,14 +804,22 @@ xrt_status solve_zones(Context& c, const Graph& g, float obstacle_mass, float th
   ZoneArgs a{z.zone.p, z.zimp.p, z.zloc.p, z.znode.p, z.gptr.p, z.gslot.p, z.sw.p, z.sn.p,
              z.snodes.p, c.x.p, c.ox.p, z.cx1.p, z.ox1.p, z.X.p, z.Xt.p, z.grad.p, z.lambda.p,
              z.cc.p, z.conv.p, z.inv_avg.p, c.nv, obstacle_mass, thickness, c.err.p};
-  std::vector<int32_t> small, large;  // zones by size: one block, or a cluster of blocks
-  for (uint32_t q = 0; q < nz; ++q)
-    (std::max(zone[q].y - zone[q].x, zone[q].w - zone[q].z) <= kZT ? small : large).push_back((int32_t)q);
-  const uint32_t ns = (uint32_t)small.size(), nl = (uint32_t)large.size();
-  small.insert(small.end(), large.begin(), large.end());
-  XRT_CUDA(&c, put(z.zid, small, s));
-  if (ns) k_zone_solve<1><<<ns, kZT, 0, s>>>(a, z.zid.p);
-  if (nl) k_zone_solve<kZoneCluster><<<nl * kZoneCluster, kZT, 0, s>>>(a, z.zid.p + ns);
+  // zones by size: one block (<= 1 chunk), a cluster of 8 (<= 8 chunks) or of 16 blocks
+  const bool wide = wide_clusters();
+  std::vector<int32_t> group[3];
+  for (uint32_t q = 0; q < nz; ++q) {
+    const int n = std::max(zone[q].y - zone[q].x, zone[q].w - zone[q].z);
+    group[n <= kZT ? 0 : (n <= kZoneCluster * kZT || !wide ? 1 : 2)].push_back((int32_t)q);
+  }
+  const uint32_t n0 = (uint32_t)group[0].size(), n1 = (uint32_t)group[1].size(),
+                 n2 = (uint32_t)group[2].size();
+  std::vector<int32_t> order = group[0];
+  order.insert(order.end(), group[1].begin(), group[1].end());
+  order.insert(order.end(), group[2].begin(), group[2].end());
+  XRT_CUDA(&c, put(z.zid, order, s));
+  if (n0) k_zone_solve<1><<<n0, kZT, 0, s>>>(a, z.zid.p);
+  if (n1) k_zone_solve<kZoneCluster><<<n1 * kZoneCluster, kZT, 0, s>>>(a, z.zid.p + n0);
+  if (n2) k_zone_solve<kZoneClusterWide><<<n2 * kZoneClusterWide, kZT, 0, s>>>(a, z.zid.p + n0 + n1);
   k_zone_finalize<<<nz, kZT, 0, s>>>(z.zone.p, z.conv.p, nz, z.znode.p, z.X.p, z.Xt.p, c.x.p,
                                      c.ox.p, c.nv);
   XRT_CUDA(&c, cudaGetLastError());
