@@ -86,7 +86,11 @@ typedef struct xrt_swift_params {
   int32_t impact_zone;
   float impact_zone_obstacle_mass; /* IMPACT_ZONE.OBSTACLE_MASS (1e3) */
   float impact_zone_thickness;     /* IMPACT_ZONE.THICKNESS (1e-4) */
-  int32_t reserved[2];
+  /* Quality-mode imminent repulsion (ImminentRepulsion, 0 = off): once per frame the cloth x
+   * cloth and cloth x obstacle face pairs of the x0 boxes give vertex-face and edge-edge
+   * quadratures; every iteration starts with their impulses (ClothSolverBase.cpp:280-300). */
+  int32_t imminent_repulsion;
+  float imminent_thickness;        /* REPULSION.IMMINENT_THICKNESS (1e-3) */
 } xrt_swift_params;
 
 /* Cloth registration, mirrors ClothSolverUniversal::AddCloth(mesh, model_matrix, particle_diameter)

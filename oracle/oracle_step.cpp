@@ -120,6 +120,12 @@ struct Oracle {
     int32_t is_vf;
   };
   std::vector<Impact> impacts;
+  struct Quad {  // imminent-repulsion quadrature
+    uint32_t nodes[4];
+    float bary[4];
+  };
+  std::vector<Quad> quads;
+  std::vector<V3> ov;  // obstacle Node::v: 0 until a collision step sets (x - x0) / dt
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -1212,6 +1218,101 @@ void solve_repulsion(Oracle& o, float h, float relaxation) {
   }
 }
 
+// ImminentRepulsion::UpdateProximity + Generate (ImminentRepulsion.cu:21-102,
+// ImminentRepulsionHelper.cu:10-66): pairs cloth x cloth then cloth x obstacle (thickness 1e-6),
+// edge-edge quadratures of every pair, then vertex-face ones, at x0.
+void imminent_generate(Oracle& o) {
+  UNodes u(o);
+  std::vector<uint32_t> pairs;
+  traverse_pairs(o.cloth_bvh, o.cloth_bvh, 0, 0, 1e-6f, pairs);
+  traverse_pairs(o.cloth_bvh, o.bvh, 0, u.F(), 1e-6f, pairs);
+  o.quads.clear();
+  const size_t np = pairs.size() / 2;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (size_t p = 0; p < np; ++p) {
+      const uint32_t f0 = pairs[2 * p], f1 = pairs[2 * p + 1];
+      if (f0 == f1) continue;
+      const uint32_t r0 = u.frtri(f0), r1 = u.frtri(f1);
+      if (pass == 0) {  // CheckImminentEEQuadrature
+        for (int i = 0; i < 3; ++i) {
+          if (!((r0 >> (i + 3)) & 1u)) continue;
+          for (int j = 0; j < 3; ++j) {
+            if (!((r1 >> (j + 3)) & 1u)) continue;
+            const uint32_t e0 = u.fedge(f0, i), e1 = u.fedge(f1, j);
+            const uint32_t nd[4] = {u.enode(e0, 0), u.enode(e0, 1), u.enode(e1, 0), u.enode(e1, 1)};
+            if (nd[0] == nd[2] || nd[0] == nd[3] || nd[1] == nd[2] || nd[1] == nd[3]) continue;
+            V3 fn;
+            float w[4] = {0, 0, 0, 0};
+            signed_ee_distance(u.x0(nd[0]), u.x0(nd[1]), u.x0(nd[2]), u.x0(nd[3]), fn, w);
+            if (!(mmin(mmin(w[0], w[1]), mmin(-w[2], -w[3])) >= 1e-6f && in_edge(u, w[1], e0, e1) &&
+                  in_edge(u, -w[3], e1, e0)))
+              continue;
+            o.quads.push_back(Oracle::Quad{{nd[0], nd[1], nd[2], nd[3]}, {w[0], w[1], w[2], w[3]}});
+          }
+        }
+      } else {  // CheckImminentVFQuadrature
+        for (int i = 0; i < 3; ++i) {
+          if (!((r0 >> i) & 1u)) continue;
+          const uint32_t node = u.fnode(f0, i);
+          const uint32_t a = u.fnode(f1, 0), b = u.fnode(f1, 1), c = u.fnode(f1, 2);
+          if (node == a || node == b || node == c) continue;
+          V3 fn;
+          float w[4] = {0, 0, 0, 0};
+          signed_vf_distance(u.x0(node), u.x0(a), u.x0(b), u.x0(c), fn, w);
+          if (!(mmin(-w[1], mmin(-w[2], -w[3])) >= 1e-6f)) continue;
+          o.quads.push_back(Oracle::Quad{{a, b, c, node}, {w[1], w[2], w[3], w[0]}});
+        }
+      }
+    }
+  }
+}
+
+// ImminentRepulsion::Solve (ImminentRepulsion.cu:104-169) with add_repulsion = true: cloth
+// velocities (x - x0) / dt, EvaluateImminentImpulse of every quadrature, deltas summed in
+// quadrature order, ApplyImminentImpulse.
+void imminent_solve(Oracle& o, float h, float relaxation, float dt) {
+  UNodes u(o);
+  const uint32_t V = u.V;
+  if (o.ov.size() != o.ox.size()) o.ov.assign(o.ox.size(), V3{0, 0, 0});
+  for (uint32_t i = 0; i < V; ++i) o.v[i] = (o.x[i] - o.x0[i]) / dt;
+  o.rep_deltas.assign(V, V3{0, 0, 0});
+  o.rep_counts.assign(V, 0);
+  for (const Oracle::Quad& q : o.quads) {
+    V3 pr{0, 0, 0}, vr{0, 0, 0};
+    for (int i = 0; i < 4; ++i) {
+      pr = pr + q.bary[i] * u.x0(q.nodes[i]);
+      vr = vr + q.bary[i] * (q.nodes[i] < V ? o.v[q.nodes[i]] : o.ov[q.nodes[i] - V]);
+    }
+    const float npr = length(pr);
+    if (npr > h || npr < 1e-5f) continue;
+    pr = normalize(pr);
+    const float vr_nrm = dot(vr, pr);
+    if (vr_nrm > (h - npr) * 0.1f) continue;
+    V3 I = (vr_nrm * dt) * pr;
+    const V3 vr_tan = vr - vr_nrm * pr;
+    if (length(vr_tan) > h * 0.01f) {  // friction coefficient 0
+      const float imp_norm = length(I), coeff = 0.0f;
+      const V3 dir = normalize(vr_tan);
+      const V3 friction = imp_norm * coeff > length(vr_tan) ? -vr_tan : (-dir * imp_norm) * coeff;
+      I = I + friction * 1.0f;
+    }
+    float inv_cm = 0.0f;
+    for (int i = 0; i < 4; ++i) inv_cm += (q.bary[i] * q.bary[i]) * u.w(q.nodes[i]);
+    if (inv_cm < 1e-5f) continue;
+    for (int i = 0; i < 4; ++i) {  // AccumulateImpulses
+      const V3 corr = I * ((-u.w(q.nodes[i]) * q.bary[i]) / inv_cm);
+      if (length(corr) < kEps || !u.free_(q.nodes[i])) continue;
+      o.rep_deltas[q.nodes[i]] += corr;
+      o.rep_counts[q.nodes[i]] += 1;
+    }
+  }
+  for (uint32_t i = 0; i < V; ++i) {
+    float count = (float)o.rep_counts[i];
+    if (count <= kEps) continue;
+    o.x[i] = o.x[i] + o.rep_deltas[i] / count * relaxation;
+  }
+}
+
 // CheckImpact (ImpactHelper.cu:34-87)
 bool check_impact(const UNodes& u, bool vf, const uint32_t* nd, Oracle::Impact& im) {
   for (int k = 0; k < 4; ++k) im.nodes[k] = nd[k];
@@ -1668,6 +1769,9 @@ void collision_step(Oracle& o, float obstacle_mass, float thickness, int32_t* st
     return;
   }
   const std::vector<V3> cx1 = o.x, ox1 = o.ox;  // SetupNode / SetupObstacleNode: x1 = x
+  const float dt = o.p.frame_time / (float)o.p.num_substeps;
+  o.ov.assign(o.ox.size(), V3{0, 0, 0});
+  for (size_t i = 0; i < o.ox.size(); ++i) o.ov[i] = (o.ox[i] - o.ox0[i]) / dt;
   auto ccd_tree = [](Lbvh& b, const std::vector<V3>& x, const std::vector<V3>& x0,
                      const std::vector<V3>& n, const std::vector<uint32_t>& tri) {
     b = Lbvh();
@@ -1737,9 +1841,11 @@ void step_frame(Oracle& o) {
   if (obstacle_updated) rebuild_obstacle_bvh(o, 0.0f);
   const bool has_obstacle = o.bvh.active;
   const bool repulsion = p.pbd_repulsion != 0;
-  if (repulsion) {  // SimulateQuality (ClothSolverBase.cpp:276-293)
-    if (!o.otri.empty()) update_bvh_ccd(o.bvh, o.ox, o.ox0, o.otri);
+  const bool imminent = p.imminent_repulsion != 0;
+  if (repulsion || imminent) {  // SimulateQuality (ClothSolverBase.cpp:276-293)
     build_cloth_bvh(o);
+    if (imminent) imminent_generate(o);
+    if (!o.otri.empty()) update_bvh_ccd(o.bvh, o.ox, o.ox0, o.otri);
   }
   const int frequency = (p.num_substeps * p.num_iterations) / p.num_collision_passes;
   int cnt = 0;
@@ -1751,6 +1857,8 @@ void step_frame(Oracle& o) {
     }
     if (p.enable_self_collision && substep % p.inter_leaved_hash == 0) hash_particles(o);
     for (int it = 0; it < p.num_iterations; ++it) {
+      if (imminent)  // ClothSolverBase.cpp:296-301
+        imminent_solve(o, p.imminent_thickness, p.repulsion_relaxation, substep_time);
       if (repulsion) {  // ClothSolverBase.cpp:303-313
         if (it % 10 == 0) update_pairs(o, 1e-6f);
         solve_repulsion(o, p.pbd_thickness, p.repulsion_relaxation);

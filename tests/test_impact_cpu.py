@@ -88,3 +88,15 @@ def test_frames_with_impact_zone_stay_finite():
         o.step()
     assert np.isfinite(o.host_positions()).all()
     assert np.isfinite(o.host_velocities()).all()
+
+
+def test_imminent_repulsion_acts_and_stays_finite():
+    xs = []
+    for on in (0, 1):
+        o, _ = _oracle(n=10, imminent_repulsion=on, imminent_thickness=0.05)
+        for _ in range(8):  # the sheet reaches the sphere at frame 6
+            o.step()
+        x = o.host_positions()
+        assert np.isfinite(x).all() and np.isfinite(o.host_velocities()).all()
+        xs.append(x)
+    assert np.abs(xs[1] - xs[0]).max() > 1e-6  # the impulses moved the cloth

@@ -120,3 +120,36 @@ def test_rejected_in_batched_context(xrt):
     s.add_instance(cloth, obs)
     with pytest.raises(RuntimeError):
         s.start()
+
+
+def _diag(x):
+    return float(np.linalg.norm(x.max(axis=0) - x.min(axis=0)))
+
+
+def test_frames_with_imminent_repulsion_match_oracle(xrt):
+    # impulses are summed with float atomics, as in the reference: 1e-4 of the diagonal
+    cloth, obs = small_scene(12)
+    p = _params(imminent_repulsion=1, imminent_thickness=0.05)
+    g, o = make_pair(p, [cloth], [obs])
+    for _ in range(8):  # the sheet reaches the sphere at frame 6
+        g.step()
+        o.step()
+        xo = o.host_positions()
+        err = float(np.abs(g.host_positions().astype(np.float64) - xo).max())
+        assert err <= 1e-4 * _diag(xo), err
+
+
+def test_quality_frames_match_oracle(xrt):
+    # SimulateQuality's pieces together: FEM fabric, imminent and PBD repulsion, impact zones
+    from xrtailor_gb300 import ClothSolver
+    cloth, obs = small_scene(12)
+    p = _params(imminent_repulsion=1, imminent_thickness=0.02, pbd_repulsion=1, impact_zone=1,
+                num_substeps=2, num_iterations=4)
+    g, o = make_pair(p, [cloth], [obs], fem=ClothSolver.fem_material())
+    for _ in range(8):
+        g.step()
+        o.step()
+        xo = o.host_positions()
+        err = float(np.abs(g.host_positions().astype(np.float64) - xo).max())
+        assert err <= 1e-4 * _diag(xo), err
+    g.synchronize()

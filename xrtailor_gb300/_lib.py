@@ -55,7 +55,8 @@ class SwiftParams(C.Structure):
         ("impact_zone", C.c_int32),
         ("impact_zone_obstacle_mass", C.c_float),
         ("impact_zone_thickness", C.c_float),
-        ("reserved", C.c_int32 * 2),
+        ("imminent_repulsion", C.c_int32),
+        ("imminent_thickness", C.c_float),
     ]
 
 

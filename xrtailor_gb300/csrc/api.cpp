@@ -125,9 +125,18 @@ void record_frame(Context& c) {
   const bool has_obstacle = c.onf > 0;
   const bool bindings = c.nbind > 0;
   const bool repulsion = p.pbd_repulsion != 0;
-  if (repulsion) {  // SimulateQuality: cloth LBVH per frame, obstacle Update(ccd) (:276-293)
-    if (has_obstacle) xrt::launch_update_ccd(c.bvh, c.ox.p, c.ox0.p, c.otri.p, c.stream, c.err.p);
+  const bool imminent = p.imminent_repulsion != 0;
+  if (repulsion || imminent) {  // SimulateQuality: cloth LBVH per frame, the imminent
+                                // quadratures, obstacle Update(ccd) (ClothSolverBase.cpp:276-293)
     xrt::launch_cloth_bvh_build(c);
+    if (imminent) {
+      const cudaError_t e = xrt::prox_imminent_generate(c);
+      if (e != cudaSuccess && c.frame_status == XRT_OK) {
+        c.set_error(std::string("imminent repulsion: ") + cudaGetErrorString(e));
+        c.frame_status = XRT_ERR_CUDA;
+      }
+    }
+    if (has_obstacle) xrt::launch_update_ccd(c.bvh, c.ox.p, c.ox0.p, c.otri.p, c.stream, c.err.p);
   }
   const int frequency = (p.num_substeps * p.num_iterations) / p.num_collision_passes;
   int cnt = 0;
@@ -141,6 +150,8 @@ void record_frame(Context& c) {
       xrt::launch_hash(c);
     }
     for (int it = 0; it < p.num_iterations; ++it) {
+      if (imminent)  // ImminentRepulsion::Solve first (ClothSolverBase.cpp:296-301)
+        xrt::prox_imminent_solve(c, p.imminent_thickness, p.repulsion_relaxation, k.dt);
       if (repulsion) {  // PBD repulsion at the start of the iteration (ClothSolverBase.cpp:303-313)
         if (it % 10 == 0) xrt::prox_update_pairs(c, 1e-6f);
         xrt::prox_solve(c, p.pbd_thickness, p.repulsion_relaxation);
@@ -337,6 +348,8 @@ xrt_status xrt_default_params(xrt_swift_params* p) {
   p->impact_zone = 0;
   p->impact_zone_obstacle_mass = 1e3f;  // ImpactZoneSettings (config/Base.hpp:115-118)
   p->impact_zone_thickness = 1e-4f;
+  p->imminent_repulsion = 0;
+  p->imminent_thickness = 1e-3f;        // RepulsionSettings (config/Base.hpp:102-108)
   return XRT_OK;
 }
 
@@ -404,6 +417,7 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   P.face.release(); P.fedge.release(); P.fn0.release(); P.edge.release(); P.eadj.release();
   P.cfree.release(); P.counts.release(); P.incl.release(); P.total.release(); P.pairs.release();
   P.scan.sums.release(); P.scan.incl.release();
+  P.qnodes.release(); P.qbary.release(); P.ov.release();
   P.deltas.release(); P.rcounts.release(); P.imp_t.release(); P.imp_w.release(); P.imp_n.release();
   P.imp_nodes.release();
   if (c.stream) cudaStreamDestroy(c.stream);
@@ -847,9 +861,9 @@ xrt_status xrt_start(xrt_ctx* h) {
       c.set_error("binding refers to a missing obstacle vertex");
       return XRT_ERR_INVALID_MESH;
     }
-  if (c.instanced && (c.params.pbd_repulsion || c.params.impact_zone)) {
-    c.set_error("pbd_repulsion and impact_zone (Quality-mode self contact) are not available in a "
-                "batched context");
+  if (c.instanced && (c.params.pbd_repulsion || c.params.impact_zone || c.params.imminent_repulsion)) {
+    c.set_error("pbd_repulsion, imminent_repulsion and impact_zone (Quality-mode self contact) are "
+                "not available in a batched context");
     return XRT_ERR_INVALID_ARGUMENT;
   }
   // instances: merged mode is one instance holding every cloth and obstacle
@@ -1206,7 +1220,8 @@ xrt_status xrt_step_frame(xrt_ctx* h) {
   Context& c = h->c;
   if (require_started(c) != XRT_OK) return XRT_ERR_STATE;
   cudaSetDevice(c.device);
-  const bool eager = c.params.pbd_repulsion || c.params.impact_zone;  // host reads in the frame
+  const bool eager = c.params.pbd_repulsion || c.params.impact_zone ||  // host reads in the frame
+                     c.params.imminent_repulsion;
   if (eager) {
     xrt_status st = xrt::prox_prepare(c);
     if (st != XRT_OK) return st;

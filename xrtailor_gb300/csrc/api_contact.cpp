@@ -105,6 +105,8 @@ xrt_status xrt::prox_prepare(Context& c) {
   XRT_CUDA(&c, put(c.prox.edge, uedge, s));
   XRT_CUDA(&c, put(c.prox.eadj, eadj, s));
   XRT_CUDA(&c, put(c.prox.cfree, c.h_cfree, s));
+  XRT_CUDA(&c, c.prox.ov.reserve(std::max(c.onv, 1u)));  // obstacle Node::v starts at 0
+  XRT_CUDA(&c, cudaMemsetAsync(c.prox.ov.p, 0, sizeof(float4) * std::max(c.onv, 1u), s));
   XRT_CUDA(&c, c.prox.counts.reserve(std::max(c.nf, 1u)));
   XRT_CUDA(&c, c.prox.incl.reserve(2 * (size_t)std::max(c.nf, 1u)));
   XRT_CUDA(&c, c.prox.total.reserve(2));

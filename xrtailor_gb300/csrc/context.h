@@ -293,6 +293,12 @@ struct ProximityState {
   DBuf<float4> imp_w, imp_n;
   DBuf<uint4> imp_nodes;
   uint32_t nimpacts = 0;
+  // imminent repulsion: 12 quadrature slots per face pair (9 edge-edge, 3 vertex-face) of the
+  // frame; nodes.x = kNone marks an empty slot
+  DBuf<uint4> qnodes;
+  DBuf<float4> qbary;
+  uint32_t nquads = 0;
+  DBuf<float4> ov;                 // obstacle Node::v (set by the collision step; 0 before)
 };
 
 // Impact-zone collision step (impact.cu).  An impact zone: impacts (ids into the step's impact
@@ -594,7 +600,14 @@ void launch_cloth_bvh_build(Context& c);
 void launch_update_ccd(Lbvh& b, const float4* x, const float4* x0, const int4* tri, cudaStream_t s,
                        uint32_t* err);
 cudaError_t prox_update_pairs(Context& c, float thickness);
-cudaError_t prox_face_pairs(Context& c, const Lbvh& cloth, const Lbvh& obstacle, float thickness);
+cudaError_t prox_face_pairs(Context& c, const Lbvh& cloth, const Lbvh& obstacle, float thickness,
+                            bool self_first = false);
+// ImminentRepulsion::UpdateProximity + Generate (once per frame) and Solve (per iteration)
+cudaError_t prox_imminent_generate(Context& c);
+// v = (x - x0) / dt of n nodes (UpdateVelocity_Kernel, SetupObstacleNode_Kernel)
+void launch_node_velocity(const float4* x, const float4* x0, float4* v, uint32_t n, float dt,
+                          cudaStream_t s);
+void prox_imminent_solve(Context& c, float thickness, float relaxation, float dt);
 // inclusive scan of n counts (multi-block); total[0] = sum
 cudaError_t scan_inclusive(ScanScratch& w, const uint32_t* in, uint32_t* out, uint32_t n,
                            uint32_t* total, cudaStream_t s);

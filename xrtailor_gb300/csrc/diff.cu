@@ -1165,7 +1165,8 @@ void load_state(Context& c, const DiffState::Checkpoint& ck) {
 
 xrt_status diff_prepare(Context& c) {
   const xrt_swift_params& p = c.params;
-  if (p.enable_self_collision || p.pbd_repulsion || p.impact_zone || c.nbind > 0 || c.fem.on) {
+  if (p.enable_self_collision || p.pbd_repulsion || p.impact_zone || p.imminent_repulsion ||
+      c.nbind > 0 || c.fem.on) {
     c.set_error("the adjoint covers frames of the Swift fabric without particle "
                 "self-collision, Quality repulsion, impact zones or bindings");
     return XRT_ERR_INVALID_ARGUMENT;

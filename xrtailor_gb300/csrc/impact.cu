@@ -840,10 +840,13 @@ xrt_status collision_step(Context& c, float obstacle_mass, float thickness, xrt_
   if ((r = izone_prepare(c)) != XRT_OK) return r;
   ImpactZoneState& z = c.izone;
   const cudaStream_t s = c.stream;
-  // SetupNode_Kernel / SetupObstacleNode_Kernel: x1 = x
+  // SetupNode_Kernel / SetupObstacleNode_Kernel: x1 = x; obstacle v = (x - x0) / substep time
   XRT_CUDA(&c, cudaMemcpyAsync(z.cx1.p, c.x.p, sizeof(float4) * c.nv, cudaMemcpyDeviceToDevice, s));
-  if (c.onv)
+  if (c.onv) {
     XRT_CUDA(&c, cudaMemcpyAsync(z.ox1.p, c.ox.p, sizeof(float4) * c.onv, cudaMemcpyDeviceToDevice, s));
+    launch_node_velocity(c.ox.p, c.ox0.p, c.prox.ov.p, c.onv,
+                         c.params.frame_time / (float)c.params.num_substeps, s);
+  }
   // UpdateData(faces, 0, ccd = true) + Construct(0) of both meshes
   z.cbvh.n = c.nf;
   launch_prims_ccd(z.cbvh, c.x.p, c.x0.p, c.n.p, c.tri.p, c.nf, 0.0f, s);

@@ -564,6 +564,129 @@ __global__ void k_check_impacts(PNodes u, PTopo t, const uint2* __restrict__ pai
   out.nodes[index] = make_uint4(nd[0], nd[1], nd[2], nd[3]);
 }
 
+// ---- imminent repulsion (ImminentRepulsion.cu, ImminentRepulsionHelper.cu) ---------------------
+
+// CheckImminentVFQuadrature (ImminentRepulsionHelper.cu:10-38): the vertex inside the face at x0;
+// nodes (face 0, 1, 2, vertex), weights rotated to match.
+__device__ bool imminent_vf(const PNodes& u, uint32_t node, int4 fc, uint4& qn, float4& qb) {
+  const uint32_t f0 = (uint32_t)fc.x, f1 = (uint32_t)fc.y, f2 = (uint32_t)fc.z;
+  if (node == f0 || node == f1 || node == f2) return false;
+  f3 fn;
+  float w[4] = {0, 0, 0, 0};
+  signed_vf_distance(u.x0(node), u.x0(f0), u.x0(f1), u.x0(f2), fn, w);
+  if (!(tmin(-w[1], tmin(-w[2], -w[3])) >= 1e-6f)) return false;
+  qn = make_uint4(f0, f1, f2, node);
+  qb = make_float4(w[1], w[2], w[3], w[0]);
+  return true;
+}
+
+// CheckImminentEEQuadrature (ImminentRepulsionHelper.cu:40-66)
+__device__ bool imminent_ee(const PNodes& u, const PTopo& t, uint32_t e0, uint32_t e1, uint4& qn,
+                            float4& qb) {
+  const uint2 a = t.edge[e0], b = t.edge[e1];
+  if (a.x == b.x || a.x == b.y || a.y == b.x || a.y == b.y) return false;
+  f3 fn;
+  float w[4] = {0, 0, 0, 0};
+  signed_ee_distance(u.x0(a.x), u.x0(a.y), u.x0(b.x), u.x0(b.y), fn, w);
+  if (!(tmin(tmin(w[0], w[1]), tmin(-w[2], -w[3])) >= 1e-6f && in_edge(u, t, w[1], e0, e1) &&
+        in_edge(u, t, -w[3], e1, e0)))
+    return false;
+  qn = make_uint4(a.x, a.y, b.x, b.y);
+  qb = make_float4(w[0], w[1], w[2], w[3]);
+  return true;
+}
+
+// EvaluateEE/VFQuadrature_Kernel: slot 12 p + 3 i + j edge i of the first face against edge j
+// of the second (both owned by their r-triangles), slot 12 p + 9 + i vertex i of the first face
+// (owned) against the second face; a face paired with itself gives nothing.
+__global__ void k_imminent_quads(PNodes u, PTopo t, const uint2* __restrict__ pairs, uint32_t np,
+                                 uint4* __restrict__ qnodes, float4* __restrict__ qbary) {
+  const size_t slot = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= 12 * (size_t)np) return;
+  const uint32_t p = (uint32_t)(slot / 12), k = (uint32_t)(slot % 12);
+  const uint2 pr = pairs[p];
+  uint4 qn = make_uint4(kNone, kNone, kNone, kNone);
+  float4 qb = make_float4(0, 0, 0, 0);
+  if (pr.x != pr.y) {
+    const int4 fa = t.face[pr.x], fb = t.face[pr.y];
+    const uint32_t r0 = (uint32_t)fa.w, r1 = (uint32_t)fb.w;
+    if (k < 9) {
+      const uint32_t i = k / 3, j = k % 3;
+      if (((r0 >> (i + 3)) & 1u) && ((r1 >> (j + 3)) & 1u)) {
+        const int4 ea = t.fedge[pr.x], eb = t.fedge[pr.y];
+        const uint32_t e0 = (uint32_t)(i == 0 ? ea.x : (i == 1 ? ea.y : ea.z));
+        const uint32_t e1 = (uint32_t)(j == 0 ? eb.x : (j == 1 ? eb.y : eb.z));
+        if (!imminent_ee(u, t, e0, e1, qn, qb)) qn.x = kNone;
+      }
+    } else {
+      const uint32_t i = k - 9;
+      if ((r0 >> i) & 1u) {
+        const uint32_t node = (uint32_t)(i == 0 ? fa.x : (i == 1 ? fa.y : fa.z));
+        if (!imminent_vf(u, node, fb, qn, qb)) qn.x = kNone;
+      }
+    }
+  }
+  qnodes[slot] = qn;
+  qbary[slot] = qb;
+}
+
+// UpdateVelocity_Kernel (ImminentRepulsion.cu:147-151): v = (x - x0) / dt for the cloth
+__global__ void k_imminent_velocity(const float4* __restrict__ x, const float4* __restrict__ x0,
+                                    float4* __restrict__ v, uint32_t n, float dt) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  v[i] = mk4((mk3(x[i]) - mk3(x0[i])) / dt, v[i].w);
+}
+
+// ComputeImminentImpulse_Kernel + EvaluateImminentImpulse (ImminentRepulsionHelper.cu:68-131)
+// with add_repulsion = true; AccumulateImpulses (float atomics, as the reference).
+__global__ void k_imminent_impulse(PNodes u, const float4* __restrict__ cv,
+                                   const float4* __restrict__ ov, const uint4* __restrict__ qnodes,
+                                   const float4* __restrict__ qbary, uint32_t nq, float h, float dt,
+                                   float* deltas, int* counts) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const uint4 qn = qnodes[q];
+  if (qn.x == kNone) return;
+  const float4 qb = qbary[q];
+  const uint32_t nd[4] = {qn.x, qn.y, qn.z, qn.w};
+  const float b[4] = {qb.x, qb.y, qb.z, qb.w};
+  f3 pr = mk3(0.0f, 0.0f, 0.0f), vr = mk3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    pr = pr + b[i] * u.x0(nd[i]);
+    vr = vr + b[i] * (nd[i] < u.V ? mk3(cv[nd[i]]) : mk3(ov[nd[i] - u.V]));
+  }
+  const float npr = length(pr);
+  if (npr > h) return;
+  if (npr < 1e-5f) return;
+  pr = normalize(pr);
+  const float vr_nrm = dot(vr, pr);
+  const float target = (h - npr) * 0.1f;
+  if (vr_nrm > target) return;
+  f3 I = (vr_nrm * dt) * pr;
+  const f3 vr_tan = vr - vr_nrm * pr;
+  if (length(vr_tan) > h * 0.01f) {  // friction coefficient 0: the term adds signed zeros
+    const float imp_norm = length(I);
+    const f3 dir = normalize(vr_tan);
+    const float coeff = 0.0f;
+    const f3 friction = imp_norm * coeff > length(vr_tan) ? -vr_tan : (-dir * imp_norm) * coeff;
+    I = I + friction * 1.0f;
+  }
+  float inv_cm = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) inv_cm += (b[i] * b[i]) * u.w(nd[i]);
+  if (inv_cm < 1e-5f) return;
+  Impulse imp;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float beta = (-u.w(nd[i]) * b[i]) / inv_cm;
+    imp.corr[i] = I * beta;
+    imp.nodes[i] = nd[i];
+  }
+  accumulate(u, imp, deltas, counts);
+}
+
 PNodes nodes_of(const Context& c) {
   return PNodes{c.x.p, c.x0.p, c.ox.p, c.ox0.p, c.prox.cfree.p, c.nv};
 }
@@ -609,7 +732,8 @@ cudaError_t prox_update_pairs(Context& c, float thickness) {
 
 // Traverse(cloth, obstacle) followed by Traverse(cloth, cloth) into the pair list.  The pair
 // count is read back to size the list (the reference reads num.back() the same way).
-cudaError_t prox_face_pairs(Context& c, const Lbvh& cloth, const Lbvh& obstacle, float thickness) {
+cudaError_t prox_face_pairs(Context& c, const Lbvh& cloth, const Lbvh& obstacle, float thickness,
+                            bool self_first) {
   ProximityState& P = c.prox;
   P.npairs = 0;
   if (!cloth.active) return cudaGetLastError();
@@ -620,6 +744,7 @@ cudaError_t prox_face_pairs(Context& c, const Lbvh& cloth, const Lbvh& obstacle,
     uint32_t base;
     bool on;
   } sides[2] = {{obstacle.view(), c.nf, obstacle.active}, {lhs, 0u, true}};
+  if (self_first) std::swap(sides[0], sides[1]);
   uint32_t totals[2] = {0, 0};
   for (int s = 0; s < 2; ++s) {
     if (!sides[s].on) continue;
@@ -632,7 +757,8 @@ cudaError_t prox_face_pairs(Context& c, const Lbvh& cloth, const Lbvh& obstacle,
   cudaError_t e = cudaMemcpyAsync(totals, P.total.p, sizeof(totals), cudaMemcpyDeviceToHost, c.stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return e;
-  if (!sides[0].on) totals[0] = 0;
+  for (int s = 0; s < 2; ++s)
+    if (!sides[s].on) totals[s] = 0;
   const uint32_t np = totals[0] + totals[1];
   if (np > P.pairs.n) {
     e = P.pairs.reserve((size_t)np + np / 4 + 1024);
@@ -656,6 +782,41 @@ void prox_solve(Context& c, float thickness, float relaxation) {
     k_evaluate_rep<<<grid_for(P.npairs), kBlock, 0, c.stream>>>(nodes_of(c), topo_of(c), P.pairs.p,
                                                                 P.npairs, thickness, P.deltas.p,
                                                                 P.rcounts.p);
+  k_apply_rep<<<grid_for(c.nv), kBlock, 0, c.stream>>>(c.x.p, P.deltas.p, P.rcounts.p, c.nv,
+                                                       relaxation);
+}
+
+void launch_node_velocity(const float4* x, const float4* x0, float4* v, uint32_t n, float dt,
+                          cudaStream_t s) {
+  if (n) k_imminent_velocity<<<grid_for(n), kBlock, 0, s>>>(x, x0, v, n, dt);
+}
+
+// UpdateProximity (Traverse cloth x cloth, then cloth x obstacle, thickness 1e-6, on the trees as
+// they are) + Generate: the quadrature slots of the frame.
+cudaError_t prox_imminent_generate(Context& c) {
+  ProximityState& P = c.prox;
+  cudaError_t e = prox_face_pairs(c, P.cbvh, c.bvh, 1e-6f, /*self_first=*/true);
+  if (e != cudaSuccess) return e;
+  const size_t nq = 12 * (size_t)P.npairs;
+  if (nq > P.qnodes.n) {
+    if ((e = P.qnodes.reserve(nq + nq / 4)) || (e = P.qbary.reserve(nq + nq / 4))) return e;
+  }
+  P.nquads = (uint32_t)nq;
+  if (nq)
+    k_imminent_quads<<<grid_for((uint32_t)nq), kBlock, 0, c.stream>>>(nodes_of(c), topo_of(c),
+                                                                      P.pairs.p, P.npairs,
+                                                                      P.qnodes.p, P.qbary.p);
+  return cudaGetLastError();
+}
+
+// ImminentRepulsion::Solve: cloth velocities, impulses of every quadrature, ApplyImminentImpulse.
+void prox_imminent_solve(Context& c, float thickness, float relaxation, float dt) {
+  ProximityState& P = c.prox;
+  launch_node_velocity(c.x.p, c.x0.p, c.v.p, c.nv, dt, c.stream);
+  if (P.nquads)
+    k_imminent_impulse<<<grid_for(P.nquads), kBlock, 0, c.stream>>>(
+        nodes_of(c), c.v.p, P.ov.p, P.qnodes.p, P.qbary.p, P.nquads, thickness, dt, P.deltas.p,
+        P.rcounts.p);
   k_apply_rep<<<grid_for(c.nv), kBlock, 0, c.stream>>>(c.x.p, P.deltas.p, P.rcounts.p, c.nv,
                                                        relaxation);
 }
