@@ -162,10 +162,12 @@ def run_ours(args, rank, local_rank, world):
     torch.cuda.set_device(local_rank)
     sc = _workload(args.workload)
     p = scenes.scene_params(sc)
+    if args.quality:
+        _quality(p)
     solver = ClothSolver(p, device=local_rank)
     if args.tile_vertices is not None:
         solver.set_tile_vertices(args.tile_vertices)
-    fem = args.material == "fem"
+    fem = args.material == "fem" or args.quality
     if fem:
         solver.set_fem_material(ClothSolver.fem_material())
     _setup(solver, sc)
@@ -281,7 +283,10 @@ def run_ours(args, rank, local_rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded scene generators, xrtailor_gb300/scenes.py)",
-        "config": {"workload": f"plain_{args.workload}" + ("_fem" if fem else ""),
+        "config": {"workload": f"plain_{args.workload}" +
+                               ("_quality" if args.quality else ("_fem" if fem else "")),
+                   "quality": ("FEM fabric, imminent + PBD repulsion, impact-zone collision step "
+                               "per substep, no particle hash") if args.quality else None,
                    "fabric": "FEM strain + isometric bending" if fem else
                              "XPBD stretch + dihedral bend",
                    "vertices": V, "edges": s.num_edges,
@@ -741,11 +746,23 @@ def run_impact(args, local_rank):
     return res
 
 
-def run_cpu(workload, frames, warmup=1, threads=0, fem=False):
+def _quality(p):
+    """SimulateQuality's configuration on top of a workload's parameters (the FEM fabric is set
+    by the caller): imminent + PBD repulsion, the impact-zone step, no particle hash."""
+    p.enable_self_collision = 0
+    p.imminent_repulsion = 1
+    p.pbd_repulsion = 1
+    p.impact_zone = 1
+
+
+def run_cpu(workload, frames, warmup=1, threads=0, fem=False, quality=False):
     from oracle.oracle import OracleSolver, lib
     from xrtailor_gb300 import ClothSolver, scenes
     sc = _workload(workload)
     p = scenes.scene_params(sc)
+    if quality:
+        _quality(p)
+        fem = True
     o = OracleSolver(p, threads=threads)
     if fem:
         o.set_fem_material(ClothSolver.fem_material())
@@ -777,6 +794,9 @@ def main():
     ap.add_argument("--workload", default="garment",
                     choices=["garment", "small", "heavy", "batched", "diff", "lbvh", "impact"])
     ap.add_argument("--impact-n", type=int, default=128, help="impact workload: sheet size")
+    ap.add_argument("--quality", action="store_true",
+                    help="plain workloads in SimulateQuality's configuration: FEM fabric, "
+                         "imminent + PBD repulsion, impact zones per substep, no particle hash")
     ap.add_argument("--cpu-frames", type=int, default=24,
                     help="frames of the CPU baseline sample (~10 s of the garment on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -805,7 +825,7 @@ def main():
             return
         frames = max(args.steps, 1)
         value, cores, t = run_cpu(args.workload, frames, warmup=min(args.warmup, 1),
-                                  fem=args.material == "fem")
+                                  fem=args.material == "fem", quality=args.quality)
         line = {"metric": METRIC, "value": value, "unit": "vertex-substeps/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / frames,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -840,10 +860,12 @@ def main():
         torch.distributed.init_process_group("nccl")
     res = run_ours(args, rank, local_rank, world)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, cores, t = run_cpu(args.workload, args.cpu_frames, fem=args.material == "fem")
+        frames = 1 if args.quality else args.cpu_frames
+        v, cores, t = run_cpu(args.workload, frames, fem=args.material == "fem",
+                              quality=args.quality)
         res["cpu_baseline"] = {"value": v, "unit": "vertex-substeps/s", "cores": cores,
                                "kind": "port",
-                               "sample": f"{args.cpu_frames} frames of plain_{args.workload} "
+                               "sample": f"{frames} frames of {res['config']['workload']} "
                                          f"({t:.1f} s)"}
     if rank == 0:
         print(json.dumps(res))
