@@ -519,7 +519,8 @@ __device__ bool overlap_dilated(const float* alo, const float* ahi, const float*
 // One thread per test: test k of pair p writes slot 15 p + k.  k = 3 side + i (side 0: vertex i of
 // the first face against the second face, side 1: the reverse), then k = 6 + 3 i + j (edge i of
 // the first face against edge j of the second), the reference's order.
-__global__ void k_check_impacts(PNodes u, PTopo t, const uint2* __restrict__ pairs, uint32_t np,
+__global__ void __launch_bounds__(kBlock, 3) k_check_impacts(PNodes u, PTopo t,
+                                                             const uint2* __restrict__ pairs, uint32_t np,
                                 float thickness, ImpactOut out) {
   const size_t index = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (index >= 15 * (size_t)np) return;
