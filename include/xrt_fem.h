@@ -8,7 +8,8 @@
  * stretch and dihedral bend constraints; everything else in the frame is unchanged.  The
  * reference runs this fabric inside SimulateQuality (src/pipeline/base/ClothSolverBase.cpp:
  * 263-345: strain colors, bending colors, LRA, bindings per iteration) together with its
- * impact-zone collision step, which is not part of this library.
+ * repulsions and its impact-zone collision step, which xrt_swift_params switches on
+ * (imminent_repulsion, pbd_repulsion, impact_zone; include/xrt_impact.h).
  *
  * Strain (ComputeStrainCorrection, FEMHelper.cu:96-173): Green strain from the deformation
  * gradient against the rest triangle's inverse 2x2 material matrix, orthotropic stress
