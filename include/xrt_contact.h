@@ -29,6 +29,16 @@ xrt_status xrt_proximity_update_pairs(xrt_ctx* ctx, float thickness, uint32_t* o
  * proximity constraints of every pair (EvaluateRep_Kernel), averaged impulses applied to the
  * cloth's predicted positions x with `relaxation` (ApplyPBDImpulse_Kernel). */
 xrt_status xrt_proximity_solve(xrt_ctx* ctx, float thickness, float relaxation);
+/* ImminentRepulsion::UpdateProximity + Generate (ImminentRepulsion.cu:21-102): face pairs cloth x
+ * cloth then cloth x obstacle (thickness 1e-6) on the cloth LBVH as built and the obstacle LBVH
+ * as it stands, then the edge-edge and vertex-face quadratures at x0.  Synchronises. */
+xrt_status xrt_imminent_generate(xrt_ctx* ctx, uint32_t* out_num_quads);
+/* the quadratures in Generate's order (edge-edge of every pair, then vertex-face): 4 unified
+ * nodes and 4 weights each; either pointer may be NULL */
+xrt_status xrt_export_quads(xrt_ctx* ctx, uint32_t* nodes, float* bary);
+/* ImminentRepulsion::Solve (ImminentRepulsion.cu:153-169): cloth velocities (x - x0) / dt, the
+ * quadratures' impulses (float atomics), ApplyImminentImpulse with `relaxation` */
+xrt_status xrt_imminent_solve(xrt_ctx* ctx, float thickness, float relaxation, float dt);
 /* CheckImpacts (ImpactHelper.cu:116-177) over the current pairs: 15 tests per pair (3 + 3
  * vertex-face, 9 edge-edge), coplanarity cubic over t in [0, 1] from x0 to x. */
 xrt_status xrt_impacts_check(xrt_ctx* ctx, float thickness, uint32_t* out_num_impacts);

@@ -46,6 +46,9 @@ _SIG = {
     "orc_solve_repulsion": (None, [P, C.c_float, C.c_float]),
     "orc_check_impacts": (None, [P, C.c_float]),
     "orc_collision_step": (None, [P, C.c_float, C.c_float, IP]),
+    "orc_imminent_generate": (C.c_uint32, [P]),
+    "orc_get_quads": (None, [P, UP, FP]),
+    "orc_imminent_solve": (None, [P, C.c_float, C.c_float, C.c_float]),
     "orc_get_pairs": (C.c_uint32, [P, UP]),
     "orc_get_impacts": (None, [P, FP, FP, FP, UP, IP]),
     "orc_set_positions_predicted": (None, [P, FP]), "orc_get_positions_predicted": (None, [P, FP]),
@@ -247,6 +250,20 @@ class OracleSolver:
 
     def check_impacts(self, thickness):
         self._l.orc_check_impacts(self._h, float(thickness))
+
+    def imminent_generate(self):
+        self._nquads = int(self._l.orc_imminent_generate(self._h))
+        return self._nquads
+
+    def quads(self):
+        n = getattr(self, "_nquads", 0)
+        nodes = np.zeros((n, 4), np.uint32)
+        bary = np.zeros((n, 4), np.float32)
+        self._l.orc_get_quads(self._h, nodes.ctypes.data_as(UP), bary.ctypes.data_as(FP))
+        return nodes, bary
+
+    def imminent_solve(self, thickness, relaxation, dt):
+        self._l.orc_imminent_solve(self._h, float(thickness), float(relaxation), float(dt))
 
     def collision_step(self, obstacle_mass=1e3, thickness=1e-4):
         st = np.zeros(8, np.int32)

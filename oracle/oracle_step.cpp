@@ -2242,6 +2242,22 @@ void orc_solve_repulsion(void* h, float thickness, float relaxation) {
   solve_repulsion(*static_cast<Oracle*>(h), thickness, relaxation);
 }
 void orc_check_impacts(void* h, float thickness) { check_impacts(*static_cast<Oracle*>(h), thickness); }
+uint32_t orc_imminent_generate(void* h) {
+  Oracle& o = *static_cast<Oracle*>(h);
+  imminent_generate(o);
+  return (uint32_t)o.quads.size();
+}
+void orc_get_quads(void* h, uint32_t* nodes, float* bary) {
+  const Oracle& o = *static_cast<Oracle*>(h);
+  for (size_t q = 0; q < o.quads.size(); ++q)
+    for (int k = 0; k < 4; ++k) {
+      nodes[4 * q + k] = o.quads[q].nodes[k];
+      bary[4 * q + k] = o.quads[q].bary[k];
+    }
+}
+void orc_imminent_solve(void* h, float thickness, float relaxation, float dt) {
+  imminent_solve(*static_cast<Oracle*>(h), thickness, relaxation, dt);
+}
 void orc_collision_step(void* h, float obstacle_mass, float thickness, int32_t* stats8) {
   collision_step(*static_cast<Oracle*>(h), obstacle_mass, thickness, stats8);
 }

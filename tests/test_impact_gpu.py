@@ -153,3 +153,28 @@ def test_quality_frames_match_oracle(xrt):
         err = float(np.abs(g.host_positions().astype(np.float64) - xo).max())
         assert err <= 1e-4 * _diag(xo), err
     g.synchronize()
+
+
+def test_imminent_quadratures_match_oracle(xrt):
+    # the quadratures involve no atomics: bit-exact; then solves (float atomics) to 1e-4
+    cloth, obs = small_scene(12)
+    g, o = make_pair(_params(), [cloth], [obs])
+    for _ in range(7):  # the sheet on the sphere
+        g.step()
+        o.step()
+    x = o.host_positions()
+    pred = (x + np.random.default_rng(5).normal(0, 0.01, x.shape)).astype(np.float32)
+    for s in (g, o):
+        s.set_predicted(pred)
+        s.cloth_bvh_build()
+    ng, no = g.imminent_generate(), o.imminent_generate()
+    assert ng == no > 0, (ng, no)
+    (an, ab), (bn, bb) = g.quads(), o.quads()
+    np.testing.assert_array_equal(an, bn)
+    _same(ab, bb)
+    for _ in range(3):
+        g.imminent_solve(0.05, 0.25, 1.0 / 120)
+        o.imminent_solve(0.05, 0.25, 1.0 / 120)
+    err = float(np.abs(g.predicted().astype(np.float64) - o.predicted()).max())
+    assert err <= 1e-4 * _diag(x), err
+    assert np.abs(o.predicted() - pred).max() > 0  # the impulses acted

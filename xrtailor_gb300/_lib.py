@@ -219,6 +219,9 @@ SIGNATURES = {
     "xrt_proximity_update_pairs": (C.c_int32, [P, C.c_float, UP]),
     "xrt_proximity_solve": (C.c_int32, [P, C.c_float, C.c_float]),
     "xrt_impacts_check": (C.c_int32, [P, C.c_float, UP]),
+    "xrt_imminent_generate": (C.c_int32, [P, UP]),
+    "xrt_export_quads": (C.c_int32, [P, UP, FP]),
+    "xrt_imminent_solve": (C.c_int32, [P, C.c_float, C.c_float, C.c_float]),
     "xrt_collision_step": (C.c_int32, [P, C.c_float, C.c_float, C.POINTER(CollisionStats)]),
     "xrt_export_pairs": (C.c_int32, [P, UP]),
     "xrt_export_impacts": (C.c_int32, [P, FP, FP, FP, UP, IP]),

@@ -183,6 +183,70 @@ xrt_status xrt_impacts_check(xrt_ctx* h, float thickness, uint32_t* out_n) {
   return XRT_OK;
 }
 
+xrt_status xrt_imminent_generate(xrt_ctx* h, uint32_t* out_n) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  cudaSetDevice(c.device);
+  xrt_status st = prox_prepare(c);
+  if (st != XRT_OK) return st;
+  if (!c.prox.cbvh.active) {
+    c.set_error("build the cloth LBVH first (xrt_cloth_bvh_build)");
+    return XRT_ERR_STATE;
+  }
+  XRT_CUDA(&c, xrt::prox_imminent_generate(c));
+  std::vector<uint4> q(c.prox.nquads);
+  if (!q.empty())
+    XRT_CUDA(&c, cudaMemcpyAsync(q.data(), c.prox.qnodes.p, sizeof(uint4) * q.size(),
+                                 cudaMemcpyDeviceToHost, c.stream));
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  uint32_t n = 0;
+  for (const uint4& v : q) n += v.x != 0xFFFFFFFFu;
+  if (out_n) *out_n = n;
+  return XRT_OK;
+}
+
+// Slots are 12 per pair (9 edge-edge, then 3 vertex-face); exported compacted in Generate's
+// order: the edge-edge quadratures of every pair, then the vertex-face ones.
+xrt_status xrt_export_quads(xrt_ctx* h, uint32_t* nodes, float* bary) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  cudaSetDevice(c.device);
+  const size_t ns = c.prox.nquads;
+  std::vector<uint4> q(ns);
+  std::vector<float4> b(ns);
+  if (ns) {
+    XRT_CUDA(&c, cudaMemcpyAsync(q.data(), c.prox.qnodes.p, sizeof(uint4) * ns,
+                                 cudaMemcpyDeviceToHost, c.stream));
+    XRT_CUDA(&c, cudaMemcpyAsync(b.data(), c.prox.qbary.p, sizeof(float4) * ns,
+                                 cudaMemcpyDeviceToHost, c.stream));
+  }
+  XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+  size_t o = 0;
+  for (int vf = 0; vf < 2; ++vf)
+    for (size_t s = 0; s < ns; ++s) {
+      if (q[s].x == 0xFFFFFFFFu || ((s % 12) >= 9) != (vf == 1)) continue;
+      const uint32_t qn[4] = {q[s].x, q[s].y, q[s].z, q[s].w};
+      const float qb[4] = {b[s].x, b[s].y, b[s].z, b[s].w};
+      for (int k = 0; k < 4; ++k) {
+        if (nodes) nodes[4 * o + k] = qn[k];
+        if (bary) bary[4 * o + k] = qb[k];
+      }
+      ++o;
+    }
+  return XRT_OK;
+}
+
+xrt_status xrt_imminent_solve(xrt_ctx* h, float thickness, float relaxation, float dt) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  cudaSetDevice(c.device);
+  xrt_status st = prox_prepare(c);
+  if (st != XRT_OK) return st;
+  xrt::prox_imminent_solve(c, thickness, relaxation, dt);
+  XRT_CUDA(&c, cudaGetLastError());
+  return XRT_OK;
+}
+
 xrt_status xrt_export_pairs(xrt_ctx* h, uint32_t* pairs) {
   if (!h || !pairs) return XRT_ERR_INVALID_ARGUMENT;
   Context& c = h->c;

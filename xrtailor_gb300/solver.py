@@ -505,6 +505,25 @@ class ClothSolver:
         L.check(self._lib.xrt_proximity_solve(self._h, float(thickness), float(relaxation)),
                 self._h, "proximity solve")
 
+    def imminent_generate(self) -> int:
+        """ImminentRepulsion::UpdateProximity + Generate; returns the number of quadratures."""
+        n = C.c_uint32()
+        L.check(self._lib.xrt_imminent_generate(self._h, C.byref(n)), self._h, "imminent")
+        self._nquads = n.value
+        return n.value
+
+    def quads(self):
+        n = getattr(self, "_nquads", 0)
+        nodes = np.zeros((n, 4), np.uint32)
+        bary = np.zeros((n, 4), np.float32)
+        L.check(self._lib.xrt_export_quads(self._h, nodes.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                           L.fptr(bary)), self._h, "quads")
+        return nodes, bary
+
+    def imminent_solve(self, thickness: float, relaxation: float, dt: float):
+        L.check(self._lib.xrt_imminent_solve(self._h, float(thickness), float(relaxation),
+                                             float(dt)), self._h, "imminent solve")
+
     def check_impacts(self, thickness: float) -> int:
         n = C.c_uint32()
         L.check(self._lib.xrt_impacts_check(self._h, float(thickness), C.byref(n)), self._h,
