@@ -41,6 +41,7 @@ namespace {
 constexpr int kZT = 256;              // threads of a zone block = IZO_BLOCK_SIZE
 constexpr int kZoneCluster = 8;       // blocks per zone of more than 256 nodes or impacts
 constexpr int kZoneClusterWide = 16;  // blocks per zone of more than 2,048 (non-portable size)
+constexpr int kWideGroups = 4;        // 256-thread groups per block of those clusters
 constexpr int kMaxChunks = 256;       // 256 x 256 nodes / impacts per zone (the reduction's reach)
 constexpr int kMaxOptIters = 100;     // MAX_ITERATIONS (ParallelOptimizer.cuh)
 constexpr int kMaxLineSearch = 1024;  // the reference's search ends by s < 1e-12 within ~110 steps
@@ -55,10 +56,12 @@ __device__ __forceinline__ float comp4(float4 v, int j) {
   return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
 }
 
-// Two sums of one value per thread each, every thread getting both; the tree256 order.  ws: 18
-// floats; callers alternate two ws buffers, so a call needs no barrier after its reads.
-__device__ __forceinline__ void tree256_2(float& a, float& b, float* ws) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// Two sums of one value per thread each, every thread getting both; the tree256 order, taken
+// separately by every group of 256 threads of the block.  ws: 18 floats per group; callers
+// alternate two ws buffers, so a call needs no barrier after its reads.
+__device__ __forceinline__ void tree256_2(float& a, float& b, float* wsg) {
+  const int lane = threadIdx.x & 31, warp = (threadIdx.x >> 5) & 7;
+  float* ws = wsg + 18 * (threadIdx.x >> 8);
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const float oa = __shfl_down_sync(0xFFFFFFFFu, a, d);
@@ -194,26 +197,28 @@ __device__ __forceinline__ void zone_sync(cg::cluster_group& cl) {
 // chunk sums alternate between two buffer sets: a set is written again only after a later
 // barrier that every block reaches after its reads.  Zone arrays written by one block and read
 // by others go through L2 (ld/st .cg) and are published by a barrier before they are read.
-template <int C>
-__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
+// A block has G groups of 256 threads; group g of block r owns chunks r G + g, (r + C) G + g, ...
+template <int C, int G>
+__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT * G)
     k_zone_solve(ZoneArgs a, const int32_t* __restrict__ zid) {
   __shared__ float part[2 * 2 * kMaxChunks];  // [buffer set][quantity][chunk], read in block 0
-  __shared__ float wsb[2 * 18];
+  __shared__ float wsb[2 * 18 * G];
   cg::cluster_group cl = cg::this_cluster();
   const int tid = threadIdx.x;
+  const int grp = tid >> 8, lt = tid & (kZT - 1);  // group, thread of the group
   const int rank = (int)cl.block_rank();
   const int zi = zid[blockIdx.x / C];
   float* lead = cl.map_shared_rank(part, 0);
   int set = 0, wsp = 0;
   auto buf = [&](int q) { return lead + (2 * set + q) * kMaxChunks; };
   auto tree2 = [&](float& x, float& y) {
-    tree256_2(x, y, wsb + 18 * wsp);
+    tree256_2(x, y, wsb + 18 * G * wsp);
     wsp ^= 1;
   };
-  // chunk sums of this block's chunks of a quantity pair, then the totals of both
+  // the chunk sums of a quantity pair, then the totals of both (every group takes the same tree)
   auto totals = [&](int nch, float& x, float& y) {
-    x = tid < nch ? buf(0)[tid] : 0.0f;
-    y = tid < nch ? buf(1)[tid] : 0.0f;
+    x = lt < nch ? buf(0)[lt] : 0.0f;
+    y = lt < nch ? buf(1)[lt] : 0.0f;
     tree2(x, y);
     set ^= 1;
   };
@@ -227,7 +232,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
     return;
   }
   const int nce = (ni + kZT - 1) / kZT, ncn = (nn + kZT - 1) / kZT;
-  const int first = rank * kZT + tid, stride = C * kZT;  // this block's elements
+  const int first = rank * G * kZT + tid, stride = C * G * kZT;  // this block's elements
   for (int k = first; k < nn; k += stride) {  // Initialize_Kernel
     const float4 p = mk4(pos_of(a, a.znode[nb + k]), 0.0f);
     __stcg(&a.X[nb + k], p);
@@ -241,8 +246,8 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
   float zero = 0.0f;
   for (int it = 0; it < kMaxOptIters; ++it) {
     // constraints at X: coefficients min(c + lambda / mu, 0), C2 and lambda2
-    for (int ch = rank; ch < nce; ch += C) {
-      const int e = ch * kZT + tid;
+    for (int cb = rank * G; cb < nce; cb += C * G) {
+      const int ch = cb + grp, e = ch * kZT + lt;
       float c2 = 0.0f, l2 = 0.0f;
       if (e < ni) {
         const float lam = __ldcg(&a.lambda[eb + e]);
@@ -252,7 +257,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
         l2 = lam * lam;
       }
       tree2(c2, l2);
-      if (tid == 0) {
+      if (lt == 0 && ch < nce) {
         buf(0)[ch] = c2;
         buf(1)[ch] = l2;
       }
@@ -261,8 +266,8 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
     float C2, L2;
     totals(nce, C2, L2);
     // gradient at X: inv * m * (x - x1) + sum of mu * coefficient * w_j * n (slot order); G2, O
-    for (int ch = rank; ch < ncn; ch += C) {
-      const int k = ch * kZT + tid;
+    for (int cb = rank * G; cb < ncn; cb += C * G) {
+      const int ch = cb + grp, k = ch * kZT + lt;
       float g2 = 0.0f, o = 0.0f;
       if (k < nn) {
         const int idx = nb + k;
@@ -285,7 +290,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
         o = m * dot(d, d);
       }
       tree2(g2, o);
-      if (tid == 0) {
+      if (lt == 0 && ch < ncn) {
         buf(0)[ch] = g2;
         buf(1)[ch] = o;
       }
@@ -297,8 +302,8 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
     s = s / 0.7f;  // PreconditionStepLength_Kernel
     for (int ls = 0;; ++ls) {
       s = s * 0.7f;  // AdjustStepLength_Kernel
-      for (int ch = rank; ch < ncn; ch += C) {  // NextX_Kernel + CollisionObjective_Kernel
-        const int k = ch * kZT + tid;
+      for (int cb = rank * G; cb < ncn; cb += C * G) {  // NextX_Kernel + CollisionObjective_Kernel
+        const int ch = cb + grp, k = ch * kZT + lt;
         float o = 0.0f;
         if (k < nn) {
           const int idx = nb + k;
@@ -309,11 +314,11 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
           o = mass_of(a, v) * dot(d, d);
         }
         tree2(o, zero);
-        if (tid == 0) buf(0)[ch] = o;
+        if (lt == 0 && ch < ncn) buf(0)[ch] = o;
       }
       zone_sync<C>(cl);  // also publishes Xt
-      for (int ch = rank; ch < nce; ch += C) {
-        const int e = ch * kZT + tid;
+      for (int cb = rank * G; cb < nce; cb += C * G) {
+        const int ch = cb + grp, e = ch * kZT + lt;
         float c2 = 0.0f;
         if (e < ni) {
           const float q = tmin(constraint_at(a, eb + e, a.Xt) + __ldcg(&a.lambda[eb + e]) / kMu,
@@ -321,11 +326,11 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
           c2 = q * q;
         }
         tree2(c2, zero);
-        if (tid == 0) buf(1)[ch] = c2;
+        if (lt == 0 && ch < nce) buf(1)[ch] = c2;
       }
       zone_sync<C>(cl);
       // Ot over the nodes' chunks, C2t over the impacts' chunks
-      float Ot = tid < ncn ? buf(0)[tid] : 0.0f, C2t = tid < nce ? buf(1)[tid] : 0.0f;
+      float Ot = lt < ncn ? buf(0)[lt] : 0.0f, C2t = lt < nce ? buf(1)[lt] : 0.0f;
       tree2(Ot, C2t);
       set ^= 1;
       // BacktrackingLineSearchAdvanced_Kernel (ParallelImpactZoneOptimizer.cu:413-497)
@@ -354,21 +359,27 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT)
 
 // 16-block clusters need the non-portable cluster size opt-in; they are used once the device
 // reports that it can hold one (else zones stay on 8-block clusters).
-bool wide_clusters() {
+// Which 16-block clusters the device holds: bit 0 with blocks of 256 threads, bit 1 with blocks
+// of 1,024 (kWideGroups groups).
+int wide_clusters() {
   static int state = -1;
   if (state < 0) {
     state = 0;
-    const void* k = (const void*)k_zone_solve<kZoneClusterWide>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+    auto fits = [](const void* k, int threads) {
+      if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+        return false;
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(kZoneClusterWide);
-      cfg.blockDim = dim3(kZT);
+      cfg.blockDim = dim3(threads);
       int n = 0;
-      if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) == cudaSuccess && n > 0) state = 1;
-    }
+      return cudaOccupancyMaxActiveClusters(&n, k, &cfg) == cudaSuccess && n > 0;
+    };
+    if (fits((const void*)k_zone_solve<kZoneClusterWide, 1>, kZT)) state |= 1;
+    if (fits((const void*)k_zone_solve<kZoneClusterWide, kWideGroups>, kWideGroups * kZT))
+      state |= 2;
     (void)cudaGetLastError();  // a refused opt-in is not an error of the step
   }
-  return state == 1;
+  return state;
 }
 
 // Finalize_Kernel.  The reference's iteration loop stops once every zone has converged, before
@@ -804,22 +815,32 @@ xrt_status solve_zones(Context& c, const Graph& g, float obstacle_mass, float th
   ZoneArgs a{z.zone.p, z.zimp.p, z.zloc.p, z.znode.p, z.gptr.p, z.gslot.p, z.sw.p, z.sn.p,
              z.snodes.p, c.x.p, c.ox.p, z.cx1.p, z.ox1.p, z.X.p, z.Xt.p, z.grad.p, z.lambda.p,
              z.cc.p, z.conv.p, z.inv_avg.p, c.nv, obstacle_mass, thickness, c.err.p};
-  // zones by size: one block (<= 1 chunk), a cluster of 8 (<= 8 chunks) or of 16 blocks
-  const bool wide = wide_clusters();
-  std::vector<int32_t> group[3];
+  // zones by size: one block (<= 1 chunk), a cluster of 8 (<= 8 chunks), of 16 blocks
+  // (<= 16 chunks), of 16 blocks of 4 groups (more)
+  const int wg = wide_clusters();
+  std::vector<int32_t> group[4];
   for (uint32_t q = 0; q < nz; ++q) {
     const int n = std::max(zone[q].y - zone[q].x, zone[q].w - zone[q].z);
-    group[n <= kZT ? 0 : (n <= kZoneCluster * kZT || !wide ? 1 : 2)].push_back((int32_t)q);
+    int g = n <= kZT ? 0 : (n <= kZoneCluster * kZT ? 1 : (n <= kZoneClusterWide * kZT ? 2 : 3));
+    if (g == 3 && !(wg & 2)) g = 2;
+    if (g == 2 && !(wg & 1)) g = 1;
+    group[g].push_back((int32_t)q);
   }
-  const uint32_t n0 = (uint32_t)group[0].size(), n1 = (uint32_t)group[1].size(),
-                 n2 = (uint32_t)group[2].size();
-  std::vector<int32_t> order = group[0];
-  order.insert(order.end(), group[1].begin(), group[1].end());
-  order.insert(order.end(), group[2].begin(), group[2].end());
+  std::vector<int32_t> order;
+  uint32_t off[5] = {0, 0, 0, 0, 0};
+  for (int g = 0; g < 4; ++g) {
+    order.insert(order.end(), group[g].begin(), group[g].end());
+    off[g + 1] = (uint32_t)order.size();
+  }
   XRT_CUDA(&c, put(z.zid, order, s));
-  if (n0) k_zone_solve<1><<<n0, kZT, 0, s>>>(a, z.zid.p);
-  if (n1) k_zone_solve<kZoneCluster><<<n1 * kZoneCluster, kZT, 0, s>>>(a, z.zid.p + n0);
-  if (n2) k_zone_solve<kZoneClusterWide><<<n2 * kZoneClusterWide, kZT, 0, s>>>(a, z.zid.p + n0 + n1);
+  const uint32_t n0 = off[1], n1 = off[2] - off[1], n2 = off[3] - off[2], n3 = off[4] - off[3];
+  if (n0) k_zone_solve<1, 1><<<n0, kZT, 0, s>>>(a, z.zid.p);
+  if (n1) k_zone_solve<kZoneCluster, 1><<<n1 * kZoneCluster, kZT, 0, s>>>(a, z.zid.p + off[1]);
+  if (n2)
+    k_zone_solve<kZoneClusterWide, 1><<<n2 * kZoneClusterWide, kZT, 0, s>>>(a, z.zid.p + off[2]);
+  if (n3)
+    k_zone_solve<kZoneClusterWide, kWideGroups><<<n3 * kZoneClusterWide, kWideGroups * kZT, 0, s>>>(
+        a, z.zid.p + off[3]);
   k_zone_finalize<<<nz, kZT, 0, s>>>(z.zone.p, z.conv.p, nz, z.znode.p, z.X.p, z.Xt.p, c.x.p,
                                      c.ox.p, c.nv);
   XRT_CUDA(&c, cudaGetLastError());
