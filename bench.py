@@ -2,20 +2,24 @@
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
-One step = one frame = ClothSolverBase::SimulateSwift (num_substeps substeps) over the whole
-garment; the default workload is the garment-scale plain step: a 256x256 cloth (65,536 vertices)
-on the animated 6,890-vertex tube body, 20 substeps x 15 iterations, stretch + bend + LRA,
-obstacle and particle self contact.  Inputs are synthetic and seeded (xrtailor_gb300/scenes.py).
+One step = one frame = ClothSolverBase::SimulateSwift (num_substeps substeps).  The default
+workload is the batched configuration: 512 garments (vertex counts log-uniform in [2k, 100k],
+14.19 M vertices in all), each draped on its own animated 6,890-vertex tube body, stepped by one
+context in one launch per phase, 10 substeps x 10 iterations, stretch + bend + LRA, obstacle and
+particle self contact.  Inputs are synthetic and seeded (xrtailor_gb300/scenes.py).
 
 Output: one JSON line (rank 0).  `value` times K frames with CUDA events on the library's stream,
 inputs resident in HBM, L2 flushed (a 512 MiB write) between frames outside the timed events;
-`e2e` times K frames through the public C ABI with host buffers (obstacle targets in, cloth
-positions out, per frame) by wall clock; `roofline` is the dominant phase's algorithmic bytes per
-launch over its CUDA-event launch time (a profiled pass after the timed region);
-`cpu_baseline` is the oracle (OpenMP CPU restatement) on the host cores on a bounded sample.
-`--impl reference` times that CPU restatement alone: the reference's own path is CUDA-only and
-cannot be built here (no glm / vcglib / GLFW sources), so the oracle port stands in for it.
-Several GPUs (torchrun) run independent replicas (the plain step does not shard).
+`e2e` times K frames through the public API with host buffers (obstacle targets in from pinned
+memory, cloth positions out, per frame) by wall clock; `roofline` is the dominant phase's
+algorithmic bytes per launch over its launch time, timed by CUDA event-record nodes inside a
+replayed frame graph; `plain_per_garment` / `batched_over_plain` time a sample of the same
+garments each alone in its own context; `cpu_baseline` is the oracle (OpenMP CPU restatement)
+on a bounded garment sample; `plain_garment` holds the 256 x 256 garment's numbers.
+`--impl reference` times that CPU restatement alone on a garment sample per step: the reference's
+own path is CUDA-only and cannot be built here (no glm / vcglib / GLFW sources), so the oracle
+port stands in for it.  Other workloads: --workload garment|small|heavy|diff|lbvh|impact.
+Several GPUs (torchrun) run independent replicas.
 """
 import argparse
 import json
@@ -54,6 +58,52 @@ def _workload(name):
     if name == "heavy":
         return scenes.plain_heavy(1024)
     raise SystemExit(f"unknown workload {name}")
+
+
+def _mesh_counts(mesh):
+    """(vertices, edges, bend elements) of a triangle mesh: undirected edges, and one bend
+    element per edge shared by two triangles."""
+    t = np.asarray(mesh.triangles, np.int64)
+    e = np.sort(np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]]), axis=1)
+    _, cnt = np.unique(e[:, 0] * (int(t.max()) + 1) + e[:, 1], return_counts=True)
+    return len(mesh.positions), len(cnt), int((cnt == 2).sum())
+
+
+L2_NOTE = "flushed between frames (512 MiB write, outside the timed events)"
+
+
+def _plain_config(workload, p, quality=False, fem=False):
+    """The workload's description, the same for both arms (a function of the scene only)."""
+    sc = _workload(workload)
+    V, E, B = _mesh_counts(sc.cloth)
+    att = sc.cloth.attached_indices
+    slots = 0 if att is None else len(att)
+    return {"workload": f"plain_{workload}" + ("_quality" if quality else ("_fem" if fem else "")),
+            "quality": ("FEM fabric, imminent + PBD repulsion, impact-zone collision step "
+                        "per substep, no particle hash") if quality else None,
+            "fabric": "FEM strain + isometric bending" if fem else "XPBD stretch + dihedral bend",
+            "vertices": V, "edges": E, "bends": B, "lra": slots * V,
+            "obstacle_triangles": len(sc.obstacle.triangles) if sc.obstacle is not None else 0,
+            "substeps": p.num_substeps, "iterations": p.num_iterations,
+            "collision_passes": p.num_collision_passes,
+            "self_collision": bool(p.enable_self_collision), "l2": L2_NOTE}
+
+
+def _batched_config(instances, p):
+    """The batched workload's description, the same for both arms (a function of the seeded
+    draw only)."""
+    from xrtailor_gb300 import scenes
+    rng_sizes = scenes.batched_sizes(instances)
+    nxy = scenes.batched_grid_dims(instances)
+    E = int(sum(nx * (ny - 1) + ny * (nx - 1) + (nx - 1) * (ny - 1) for nx, ny in nxy))
+    B = E - int(sum(2 * (nx - 1) + 2 * (ny - 1) for nx, ny in nxy))
+    V = int(rng_sizes.sum())
+    return {"workload": f"batched_{instances}", "instances": instances, "vertices": V,
+            "edges": E, "bends": B, "lra": 2 * V,
+            "obstacle_triangles": instances * len(scenes.TubeBody().triangles),
+            "substeps": p.num_substeps, "iterations": p.num_iterations,
+            "collision_passes": p.num_collision_passes,
+            "self_collision": bool(p.enable_self_collision), "l2": L2_NOTE}
 
 
 def _setup(solver, sc):
@@ -283,20 +333,9 @@ def run_ours(args, rank, local_rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded scene generators, xrtailor_gb300/scenes.py)",
-        "config": {"workload": f"plain_{args.workload}" +
-                               ("_quality" if args.quality else ("_fem" if fem else "")),
-                   "quality": ("FEM fabric, imminent + PBD repulsion, impact-zone collision step "
-                               "per substep, no particle hash") if args.quality else None,
-                   "fabric": "FEM strain + isometric bending" if fem else
-                             "XPBD stretch + dihedral bend",
-                   "vertices": V, "edges": s.num_edges,
-                   "bends": s.num_bends, "lra": s.num_lra,
-                   "obstacle_triangles": s.num_obstacle_triangles, "substeps": S,
-                   "iterations": p.num_iterations, "collision_passes": p.num_collision_passes,
-                   "self_collision": bool(p.enable_self_collision),
-                   "stretch_colors": s.num_stretch_colors, "bend_colors": s.num_bend_colors,
-                   "l2": "flushed between frames (512 MiB write, outside the timed events)",
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": dict(_plain_config(args.workload, p, args.quality, fem),
+                       parallelism="replicas" if world > 1 else "single"),
+        "schedule": {"stretch_colors": s.num_stretch_colors, "bend_colors": s.num_bend_colors},
         "e2e": {"value": e2e, "unit": "vertex-substeps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(out.nbytes)},
         "gpu_launches": int(s.launches_per_frame) * args.steps,
@@ -314,26 +353,67 @@ def run_ours(args, rank, local_rank, world):
     return result
 
 
+def _phase_roofline(prof, sz, fem=False):
+    """The dominant phase of a per-phase profile (xrt_get_profile) and its roofline terms:
+    algorithmic bytes per launch over the launch's average time.  Tile-local stretch and bend
+    launches are accounted in the frame formula's terms (record bytes per constraint + 28 B per
+    footprint vertex of the launch); other phases by BYTES_PER_UNIT."""
+    phases = {k: v for k, v in prof.items() if k != "frames" and v["launches"]}
+    total_ms = sum(v["ms"] for v in phases.values())
+    dom = max((k for k in phases if k in BYTES_PER_UNIT), key=lambda k: phases[k]["ms"])
+    d = phases[dom]
+    per_launch_bytes = BYTES_PER_UNIT[dom] * d["units"] / max(d["launches"], 1)
+    accounting = "per constraint: record + every vertex read and written (BYTES_PER_UNIT)"
+    tiles = {"stretch": (sz.num_stretch_tile_colors, sz.stretch_footprint_vertices),
+             "bend": (sz.num_bend_tile_colors, sz.bend_footprint_vertices)}.get(dom)
+    if tiles and tiles[0]:
+        # a tile color's footprints are disjoint, so one launch touches footprint / tile colors
+        # vertices; its records are the launch's constraints
+        record = FEM_RECORD_BYTES[dom] if fem else RECORD_BYTES
+        per_launch_bytes = (record * d["units"] / max(d["launches"], 1) +
+                            VERTEX_BYTES * tiles[1] / tiles[0])
+        accounting = (f"frame formula: {record} B per constraint record + {VERTEX_BYTES} B per "
+                      "footprint vertex of the launch")
+    per_launch_s = d["ms"] / 1e3 / max(d["launches"], 1)
+    return dom, d, per_launch_bytes, per_launch_s, accounting, (d["ms"] / total_ms if total_ms else None)
+
+
+def _traffic(key, dom, units_per_launch):
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        tr = json.load(open(tpath)).get(key, {}).get(dom)
+        if tr:
+            return tr["bytes_per_unit"] * units_per_launch
+    except Exception:
+        pass
+    return None
+
+
 def run_batched(args, local_rank):
     """The batched workload: `--instances` garments (default 512), each on its own body, stepped
-    by one context in one launch per phase; then the same garments stepped one context each
-    (the plain step per garment) on the same GPU, frames timed the same way."""
+    by one context in one launch per phase; then a sample of the same garments stepped one
+    context each (the plain step per garment) on the same GPU, frames timed the same way."""
     import torch
     from xrtailor_gb300 import ClothSolver, build as xb, scenes
     xb.build()
     torch.cuda.set_device(local_rank)
     dev = f"cuda:{local_rank}"
     from xrtailor_gb300 import autotune
+    t_gen = time.perf_counter()
     gs = scenes.batched_garments(args.instances)
     p = scenes._params(**scenes.BATCHED_PARAMS)
     S = p.num_substeps
-    nframes = args.warmup + args.steps + 1
+    nframes = args.warmup + 2 * args.steps + 4
     ov = [len(g.body.rest) for g in gs]
     obase = np.concatenate([[0], np.cumsum(ov)])
-    tg = torch.empty((nframes, int(obase[-1]), 3), dtype=torch.float32, device=dev)
+    # obstacle targets of every frame, on the device (timed frames) and in pinned host memory
+    # (frames through the public API with host buffers)
+    tg_host = torch.empty((nframes, int(obase[-1]), 3), dtype=torch.float32).pin_memory()
     for f in range(nframes):
-        tg[f] = torch.from_numpy(np.concatenate([g.body.pose((f + 1) / 60.0) for g in gs]))
+        tg_host[f] = torch.from_numpy(np.concatenate([g.body.pose((f + 1) / 60.0) for g in gs]))
+    tg = tg_host.to(dev)
     torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t_gen
 
     def comps(idx):
         return np.concatenate([np.full(gs[i].num_edges, gs[i].stretch_compliance, np.float32)
@@ -381,6 +461,7 @@ def run_batched(args, local_rank):
           for _ in range(args.steps)]
     torch.cuda.synchronize()
     with ClockSampler(local_rank) as clocks:
+        wall0 = time.perf_counter()
         with torch.cuda.stream(stream):
             for a, b in ev:
                 lib.xrt_set_obstacle_targets_device(s._h, tg[fi].data_ptr())
@@ -390,24 +471,51 @@ def run_batched(args, local_rank):
                 b.record(stream)
                 flush.zero_()
         torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
     s.synchronize()
     t_batch = sum(a.elapsed_time(b) for a, b in ev) / 1e3
     value = V * S * args.steps / t_batch
     launches = s.sizes().launches_per_frame
-    # per-phase profile (one eager frame with CUDA events around every launch)
-    s.set_profiling(True)
-    lib.xrt_set_obstacle_targets_device(s._h, tg[fi % nframes].data_ptr())
-    s.step()
-    prof = s.profile()
-    s.set_profiling(False)
-    phases = {k: round(v["ms"] / max(prof["frames"], 1), 3) for k, v in prof.items()
-              if k != "frames" and v["launches"]}
+    sz = s.sizes()
+
+    # end to end through the public API: the frame's obstacle targets from pinned host memory,
+    # the step, the cloth positions back into host memory, every frame
+    out = np.empty((V, 3), np.float32)
+    h2d = int(tg_host[0].numel() * 4)
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.set_obstacle_targets(tg_host[fi].numpy())
+        fi += 1
+        s.step()
+        L_ = s._lib
+        from xrtailor_gb300 import _lib as L
+        L.check(L_.xrt_get_positions(s._h, L.fptr(out)), s._h, "read")
+    e2e_t = time.perf_counter() - e0
+    e2e = V * S * args.steps / e2e_t
+
+    # per-phase profiles of one frame each: replayed graph with an event pair per phase group
+    # (the roofline's launch time) and eager frames with an event pair per launch
+    prof = {}
+    for mode, graph in (("graph", True), ("eager", False)):
+        s.set_profiling(True, graph=graph)
+        lib.xrt_set_obstacle_targets_device(s._h, tg[fi % nframes].data_ptr())
+        fi += 1
+        s.step()
+        prof[mode] = s.profile()
+        s.set_profiling(False)
+    dom, d, per_launch_bytes, per_launch_s, accounting, share = _phase_roofline(prof["graph"], sz)
+    peak, peak_src = _peaks()
+    achieved = per_launch_bytes / per_launch_s / 1e9
+    units_per_launch = d["units"] / max(d["launches"], 1)
+    phases = {m: {k: round(v["ms"] / max(pr["frames"], 1), 3) for k, v in pr.items()
+                  if k != "frames" and v["launches"]} for m, pr in prof.items()}
     s.close()
     del s
     torch.cuda.empty_cache()
+
     # the plain step per garment: one context per garment, frames timed with events on its stream
-    step_idx = max(1, len(gs) // max(1, args.plain_sample))
-    sample = list(range(0, len(gs), step_idx))[: args.plain_sample] if args.plain_sample > 0 else []
+    sample = autotune.subset(len(gs), args.plain_sample) if args.plain_sample > 0 else []
     plain_t, plain_units = 0.0, 0
     t_plain_wall = time.perf_counter()
     for i in sample:
@@ -439,34 +547,77 @@ def run_batched(args, local_rank):
         q.close()
     plain_wall = time.perf_counter() - t_plain_wall
     plain_value = plain_units / plain_t if plain_t > 0 else None
-    return {
+    res = {
         "metric": METRIC, "value": value, "unit": "vertex-substeps/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t_batch / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded: xrtailor_gb300/scenes.py batched_garments)",
-        "config": {"workload": f"batched_{len(gs)}", "instances": len(gs), "vertices": V,
-                   "edges": sz.num_edges, "bends": sz.num_bends,
-                   "obstacle_triangles": sz.num_obstacle_triangles, "substeps": S,
-                   "iterations": p.num_iterations, "collision_passes": p.num_collision_passes,
-                   "self_collision": bool(p.enable_self_collision),
-                   "l2": "flushed between frames (512 MiB write, outside the timed events)",
-                   "setup_s": round(setup_s, 1), "parallelism": "single",
-                   "launch": tuned or {"tile_vertices": tile},
-                   "autotune": {"instances": args.tune_instances, "seconds": round(tune_s, 1),
-                                "trials_ms_per_frame": [[t, d, round(ms, 2)]
-                                                        for t, d, ms in trials]}},
+        "config": dict(_batched_config(len(gs), p), parallelism="single"),
+        "launch": tuned or {"tile_vertices": tile},
+        "e2e": {"value": e2e, "unit": "vertex-substeps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": int(out.nbytes),
+                "path": "ClothSolver.set_obstacle_targets (pinned host) + step + xrt_get_positions"},
         "gpu_launches": int(launches) * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": _traffic(f"batched_{len(gs)}", dom, units_per_launch),
+                     "peak_source": peak_src, "bytes_per_launch": per_launch_bytes,
+                     "accounting": accounting, "us_per_launch": per_launch_s * 1e6,
+                     "timing": "replayed frame graph, CUDA event-record nodes around each "
+                               "iteration's launches of the phase",
+                     "share_of_frame": share},
+        "frame_bandwidth_gbs": bytes_per_substep(sz, p, True) * S / (t_batch / args.steps) / 1e9,
         "plain_per_garment": {
             "value": plain_value, "unit": "vertex-substeps/s",
             "garments_timed": len(sample), "frames_each": args.plain_frames,
             "wall_s": round(plain_wall, 1),
-            "method": "each garment alone in its own context (graph replay), CUDA events per "
-                      "frame; throughput = sum of vertex-substeps / sum of frame times"},
+            "method": "evenly spaced garments, each alone in its own context (graph replay), "
+                      "CUDA events per frame; throughput = sum of vertex-substeps / sum of "
+                      "frame times"},
         "batched_over_plain": value / plain_value if plain_value else None,
         "phase_ms_per_frame": phases,
+        "setup_s": {"scenes": round(gen_s, 1), "autotune": round(tune_s, 1),
+                    "context": round(setup_s, 1), "plain_sample": round(plain_wall, 1)},
+        "autotune_trials_ms_per_frame": [[t, dd, round(ms, 2)] for t, dd, ms in trials],
         "clocks": clocks.summary(),
+        "wall_s": wall,
     }
+    return res
+
+
+def _cpu_garment_sample(count):
+    """Evenly spaced garments of the batched draw for the CPU legs (indices)."""
+    from xrtailor_gb300 import autotune
+    return autotune.subset(512, count)
+
+
+def run_cpu_batched(args, frames_per_garment=1, threads=0, sample=8):
+    """The oracle (OpenMP port of the plain step) on `sample` evenly spaced garments of the
+    batched draw, each in its own oracle solver, `frames_per_garment` frames each after one
+    warm-up frame: the sum of vertex-substeps over the sum of frame times."""
+    from oracle.oracle import OracleSolver, default_params, lib
+    from xrtailor_gb300 import scenes
+    idx = _cpu_garment_sample(sample)
+    gs = scenes.batched_garments(args.instances, only=idx)
+    p = default_params(**scenes.BATCHED_PARAMS)
+    t_sum, units = 0.0, 0
+    for g in gs:
+        o = OracleSolver(p, threads=threads)
+        o.add_cloth(g.cloth)
+        o.add_obstacle(g.body.mesh)
+        o.set_compliance(0, np.full(g.num_edges, g.stretch_compliance, np.float32))
+        o.start()
+        o.set_obstacle_targets(g.body.pose(1 / 60.0))
+        o.step()
+        t0 = time.perf_counter()
+        for f in range(frames_per_garment):
+            o.set_obstacle_targets(g.body.pose((f + 2) / 60.0))
+            o.step()
+        t_sum += time.perf_counter() - t0
+        units += len(g.cloth.positions) * p.num_substeps * frames_per_garment
+        o.close()
+    return units / t_sum, lib().orc_num_threads(), t_sum, idx
 
 
 def run_diff(args, local_rank):
@@ -755,17 +906,24 @@ def _quality(p):
     p.impact_zone = 1
 
 
-def run_cpu(workload, frames, warmup=1, threads=0, fem=False, quality=False):
-    from oracle.oracle import OracleSolver, lib
-    from xrtailor_gb300 import ClothSolver, scenes
-    sc = _workload(workload)
-    p = scenes.scene_params(sc)
+def _oracle_params(sc, quality=False):
+    """The scene's parameters over the oracle's own restatement of the reference defaults, so a
+    CPU-only run loads nothing from the CUDA library."""
+    from oracle.oracle import default_params
+    p = default_params(**sc.params)
     if quality:
         _quality(p)
-        fem = True
+    return p
+
+
+def run_cpu(workload, frames, warmup=1, threads=0, fem=False, quality=False):
+    from oracle.oracle import OracleSolver, default_fem_material, lib
+    sc = _workload(workload)
+    p = _oracle_params(sc, quality)
+    fem = fem or quality
     o = OracleSolver(p, threads=threads)
     if fem:
-        o.set_fem_material(ClothSolver.fem_material())
+        o.set_fem_material(default_fem_material())
     _setup(o, sc)
     tg = _targets(sc, warmup + frames)
     V = o.sizes()["num_vertices"]
@@ -785,13 +943,82 @@ def run_cpu(workload, frames, warmup=1, threads=0, fem=False, quality=False):
     return V * p.num_substeps * frames / t, lib().orc_num_threads(), t
 
 
+def _garment_summary(args, local_rank):
+    """The 256 x 256 garment (plain step) as extra keys of the batched line."""
+    import copy
+    a = copy.copy(args)
+    a.workload, a.quality, a.material, a.tile_vertices = "garment", False, "swift", None
+    a.steps = min(args.steps, 20)
+    r = run_ours(a, 0, local_rank, 1)
+    keep = ("value", "ms_per_step", "e2e", "roofline", "frame_bandwidth_gbs", "clocks", "config")
+    out = {k: r[k] for k in keep}
+    out["steps"] = a.steps
+    return out
+
+
+def run_reference(args):
+    """The reference arm: the oracle (OpenMP port of the reference's plain step; the reference's
+    own path is CUDA-only and cannot be built here) on the host cores, each step a bounded sample
+    of the workload.  Batched: one frame of each of 8 evenly spaced garments of the batch, each in
+    its own solver (the reference steps one scene per solver)."""
+    from oracle.oracle import OracleSolver, default_params, lib
+    from xrtailor_gb300 import scenes
+    steps, warmup = max(args.steps, 1), max(args.warmup, 0)
+    if args.workload == "batched":
+        idx = _cpu_garment_sample(8)
+        gs = scenes.batched_garments(args.instances, only=idx)
+        p = default_params(**scenes.BATCHED_PARAMS)
+        solvers = []
+        for g in gs:
+            o = OracleSolver(p)
+            o.add_cloth(g.cloth)
+            o.add_obstacle(g.body.mesh)
+            o.set_compliance(0, np.full(g.num_edges, g.stretch_compliance, np.float32))
+            o.start()
+            solvers.append(o)
+        poses = [[g.body.pose((f + 1) / 60.0) for f in range(warmup + steps)] for g in gs]
+        units_step = sum(len(g.cloth.positions) for g in gs) * p.num_substeps
+        for f in range(warmup):
+            for o, ps in zip(solvers, poses):
+                o.set_obstacle_targets(ps[f])
+                o.step()
+        t0 = time.perf_counter()
+        for f in range(warmup, warmup + steps):
+            for o, ps in zip(solvers, poses):
+                o.set_obstacle_targets(ps[f])
+                o.step()
+        t = time.perf_counter() - t0
+        value = units_step * steps / t
+        sample = (f"each step one frame of each of 8 evenly spaced garments of the batch "
+                  f"(garments {idx}, {units_step // p.num_substeps} vertices), one oracle "
+                  f"solver per garment")
+        config = dict(_batched_config(args.instances, p), parallelism="single")
+    else:
+        fem = args.material == "fem" or args.quality
+        value, cores_, t = run_cpu(args.workload, steps, warmup=warmup, fem=fem,
+                                   quality=args.quality)
+        cfg_p = _oracle_params(_workload(args.workload), args.quality)
+        config = dict(_plain_config(args.workload, cfg_p, args.quality, fem), parallelism="single")
+        sample = f"{steps} full frames of {config['workload']}"
+    cores = lib().orc_num_threads()
+    return {"metric": METRIC, "value": value, "unit": "vertex-substeps/s", "n_gpus": 0,
+            "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * t / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scene generators, xrtailor_gb300/scenes.py)",
+            "config": config, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "vertex-substeps/s", "cores": cores,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "vertex-substeps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="garment",
+    ap.add_argument("--workload", default="batched",
                     choices=["garment", "small", "heavy", "batched", "diff", "lbvh", "impact"])
     ap.add_argument("--impact-n", type=int, default=128, help="impact workload: sheet size")
     ap.add_argument("--quality", action="store_true",
@@ -801,7 +1028,9 @@ def main():
                     help="frames of the CPU baseline sample (~10 s of the garment on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--instances", type=int, default=512, help="batched workload: garments")
-    ap.add_argument("--plain-sample", type=int, default=512,
+    ap.add_argument("--no-garment", action="store_true",
+                    help="batched workload: skip the 256 x 256 garment's extra keys")
+    ap.add_argument("--plain-sample", type=int, default=128,
                     help="batched workload: garments timed alone (evenly spaced)")
     ap.add_argument("--plain-frames", type=int, default=2)
     ap.add_argument("--tune-instances", type=int, default=32,
@@ -823,25 +1052,37 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        frames = max(args.steps, 1)
-        value, cores, t = run_cpu(args.workload, frames, warmup=min(args.warmup, 1),
-                                  fem=args.material == "fem", quality=args.quality)
-        line = {"metric": METRIC, "value": value, "unit": "vertex-substeps/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / frames,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded scene generators, xrtailor_gb300/scenes.py)",
-                "config": {"workload": f"plain_{args.workload}"}, "impl": "reference",
-                "cpu_baseline": {"value": value, "unit": "vertex-substeps/s", "cores": cores,
-                                 "kind": "port",
-                                 "sample": f"{frames} full frames of plain_{args.workload}"},
-                "e2e": {"value": value, "unit": "vertex-substeps/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        print(json.dumps(run_reference(args)))
         return
 
     if args.workload == "batched":
+        if world > 1:
+            # independent replicas of the batch, one per GPU (instances would shard with no
+            # exchange step; every GPU runs the whole batch here)
+            import torch
+            torch.distributed.init_process_group("nccl")
+        res = run_batched(args, local_rank)
+        if world > 1:
+            import torch
+            tt = torch.tensor([res["ms_per_step"]], device=f"cuda:{local_rank}")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            res["ms_per_step"] = float(tt.item())
+            res["value"] = (res["config"]["vertices"] * res["config"]["substeps"] * world /
+                            (res["ms_per_step"] / 1e3))
+            res["n_gpus"] = world
+            res["config"]["parallelism"] = f"replicas x{world}"
+            torch.distributed.destroy_process_group()
+        if rank == 0 and not args.no_cpu_baseline:
+            v, cores, t, idx = run_cpu_batched(args, frames_per_garment=3, sample=16)
+            res["cpu_baseline"] = {"value": v, "unit": "vertex-substeps/s", "cores": cores,
+                                   "kind": "port",
+                                   "sample": f"3 frames each of 16 evenly spaced garments of the "
+                                             f"batch (garments {idx}), one oracle solver per "
+                                             f"garment ({t:.1f} s)"}
+        if rank == 0 and not args.no_garment:
+            res["plain_garment"] = _garment_summary(args, local_rank)
         if rank == 0:
-            print(json.dumps(run_batched(args, local_rank)))
+            print(json.dumps(res))
         return
     if args.workload == "diff":
         if rank == 0:

@@ -242,8 +242,12 @@ typedef struct xrt_profile {
   uint32_t frames;      /* frames accumulated */
   uint32_t reserved[7];
 } xrt_profile;
-/* enabled != 0: frames run eagerly with a CUDA-event pair around every launch, accumulating
- * per phase; 0: back to graph replay.  Resets the accumulators. */
+/* enabled = 1: frames run eagerly with a CUDA-event pair around every launch, accumulating per
+ * phase; 2: each frame is captured as a graph with an event-record node pair around every phase
+ * group (one iteration's stretch launches, its bend launches, and each single launch of the
+ * other phases) and replayed, so the launches inside a group keep their dependent-launch edges
+ * (frames that read results back on the host run as in mode 1); 0: back to graph replay.
+ * Resets the accumulators. */
 xrt_status xrt_set_profiling(xrt_ctx* ctx, int32_t enabled);
 xrt_status xrt_get_profile(xrt_ctx* ctx, xrt_profile* out);
 /* Phase names: 0 predict_finalize, 1 hash, 2 collide, 3 bvh_build, 4 obstacle_pass, 5 generate,
@@ -326,7 +330,10 @@ xrt_status xrt_lbvh_sizes(const xrt_lbvh* bvh, uint32_t* num_objects);
  * at most 65,536 primitives (larger n -> XRT_ERR_FACE_CAPACITY).  All calls on a GPU share that
  * array; calls whose device work overlaps race, so order them on one stream.  The first call on
  * each GPU looks up the array's device address (cudaGetSymbolAddress) with that GPU current;
- * make it before any stream capture starts. */
+ * make it before any stream capture starts.  The status covers argument checks and launch
+ * errors only: the build's bounded tree walks, which can trip only on a corrupt tree (for
+ * instance NaN coordinates), record their error in the scratch array and are not reported;
+ * pass finite coordinates. */
 xrt_status xrt_lbvh_build_noalloc(const float* d_prims, const float* d_pred, uint32_t n, float scr,
                                   uint32_t* d_sorted_morton, uint32_t* d_sorted_objects,
                                   uint32_t* d_nodes, float* d_aabbs, int32_t* d_i_esc,

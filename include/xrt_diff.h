@@ -6,12 +6,17 @@
  * obstacle VF / EE responses with the contact set held as recorded in the forward pass, and
  * finalize.  Frames with particle self-collision, Quality repulsion or bindings are rejected.
  *
- * Usage:  xrt_diff_begin(ctx);  then any number of xrt_step_frame calls (obstacle targets as
- * usual);  then xrt_backward(ctx, dL/dx of the final positions, ...).  Every frame start is
- * checkpointed (cloth and obstacle state, 48 B per cloth vertex); the reverse pass replays one
- * frame at a time from its checkpoint with taping kernels and walks the tape back, so memory is
- * the checkpoints plus one frame of tape.  The context's state after xrt_backward is the state
- * before it.  The arithmetic is fp32, like the forward.
+ * Usage:  xrt_diff_begin(ctx) (or xrt_diff_begin_interval);  then any number of xrt_step_frame
+ * calls (obstacle targets as usual);  then xrt_backward(ctx, dL/dx of the final positions, ...).
+ * The state at every k-th substep boundary (k a multiple of the frame's substeps; k = one frame
+ * by default) is checkpointed (cloth and obstacle state, 48 B per cloth vertex), and every
+ * frame's obstacle targets are kept (16 B per obstacle vertex).  The reverse pass walks the
+ * checkpoint segments newest first: it recomputes a segment's frames from its checkpoint, then
+ * replays each of them, newest first, with taping kernels and walks the tape back.  Memory is
+ * the checkpoints, one segment of frame states and one frame of tape; a longer interval trades
+ * checkpoint memory for one more forward frame per recorded frame.  The recomputation is the
+ * forward itself, so the gradients do not depend on the interval.  The context's state after
+ * xrt_backward is the state before it.  The arithmetic is fp32, like the forward.
  */
 #ifndef XRT_DIFF_H
 #define XRT_DIFF_H
@@ -32,8 +37,11 @@ typedef struct xrt_grads {
   float* position;           /* 3 x num_vertices: dL / d initial position */
 } xrt_grads;
 
-/* Starts recording: the following frames are checkpointed for xrt_backward. */
+/* Starts recording: the following frames are checkpointed for xrt_backward, every frame. */
 xrt_status xrt_diff_begin(xrt_ctx* ctx);
+/* The same with a checkpoint every `substeps` substeps: a positive multiple of num_substeps
+ * (XRT_ERR_INVALID_ARGUMENT otherwise). */
+xrt_status xrt_diff_begin_interval(xrt_ctx* ctx, int32_t substeps);
 /* Reverse pass over the frames recorded since xrt_diff_begin.  dL_dx: 3 x num_vertices
  * (gradient of the loss with respect to the final positions); dL_dv: the same for the final
  * velocities, or NULL. */

@@ -39,7 +39,9 @@ typedef struct xrt_collision_stats {
   uint32_t impacts;       /* independent impacts solved, over both levels */
   uint32_t zones;         /* zones at the end of the last level */
   uint32_t solves;        /* zone solves launched (sum of active zones over the passes) */
-  int32_t reserved[2];
+  uint32_t wide_solves[2]; /* of those, zones too large for an 8-block cluster: solved by
+                              16-block clusters of 256-thread blocks ([0]) or of 1,024-thread
+                              blocks ([1]); a launch-shape record, not part of the algorithm */
 } xrt_collision_stats;
 
 /* One CollisionStep on the context's current state.  `out` may be NULL.  Synchronises (impact

@@ -21,6 +21,8 @@ _lib = None
 FP, UP, IP, P = C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.POINTER(C.c_int32), C.c_void_p
 
 _SIG = {
+    "orc_default_params": (None, [C.POINTER(L.SwiftParams)]),
+    "orc_default_fem_material": (None, [C.POINTER(L.FemMaterial)]),
     "orc_create": (P, []), "orc_destroy": (None, [P]), "orc_num_threads": (C.c_int, []),
     "orc_set_threads": (None, [C.c_int]),
     "orc_set_params": (None, [P, C.POINTER(L.SwiftParams)]),
@@ -86,6 +88,22 @@ def _f(a):
 
 def _u(a):
     return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def default_params(**overrides) -> L.SwiftParams:
+    """The reference's effective Swift-mode defaults (orc_default_params) with overrides; needs
+    nothing from the CUDA library."""
+    from xrtailor_gb300.scenes import apply_overrides
+    p = L.SwiftParams()
+    lib().orc_default_params(C.byref(p))
+    return apply_overrides(p, **overrides)
+
+
+def default_fem_material() -> L.FemMaterial:
+    """FEMFabricSettings' defaults (orc_default_fem_material)."""
+    m = L.FemMaterial()
+    lib().orc_default_fem_material(C.byref(m))
+    return m
 
 
 class OracleSolver:

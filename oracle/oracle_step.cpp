@@ -1981,6 +1981,64 @@ void start(Oracle& o) {
 
 extern "C" {
 
+// The reference's effective Swift-mode defaults, restated field by field so that a CPU-only run
+// needs nothing from the CUDA library:
+//   SolverSettings (config/Base.hpp:91-97): 1 substep, 200 iterations, max speed 1e6,
+//     gravity (0, -9.8, 0), damping 0.98;
+//   BasicFabricSettings (config/Base.hpp:38-45): stretch 0, bend 1e2, relaxation 0.25,
+//     long-range stretchiness 1.1, solve bending; GEODESIC_LRA is parsed but never applied, the
+//     solver always runs the geodesic form (LongRangeAttachments.cu:5-26);
+//   SwiftModeCollisionSettings (config/Base.hpp:128-133): 10 passes, SDF margin 1e-2, BVH
+//     tolerance 0.003; ParticleCollisionSettings (config/Base.hpp:59-66): friction 0.1, 64
+//     neighbors, hash every 3 substeps, self collision on, diameter 1.3 x first edge, cell 1.5;
+//   frame time 1/60 (utils/Timer.hpp:177), obstacle animation on (core/Common.hpp:81);
+//   RepulsionSettings (config/Base.hpp:108-114) and ImpactZoneSettings (:116-119) for the
+//     Quality stages, which are off in the Swift frame.
+void orc_default_params(xrt_swift_params* p) {
+  std::memset(p, 0, sizeof(*p));
+  p->num_substeps = 1;
+  p->num_iterations = 200;
+  p->max_speed = 1e6f;
+  p->gravity[0] = 0.0f;
+  p->gravity[1] = -9.8f;
+  p->gravity[2] = 0.0f;
+  p->damping = 0.98f;
+  p->stretch_compliance = 0.0f;
+  p->bend_compliance = 1e2f;
+  p->relaxation_factor = 0.25f;
+  p->long_range_stretchiness = 1.1f;
+  p->geodesic_lra = 1;
+  p->solve_bending = 1;
+  p->num_collision_passes = 10;
+  p->sdf_collision_margin = 1e-2f;
+  p->bvh_tolerance = 0.003f;
+  p->friction = 0.1f;
+  p->max_neighbor_size = 64;
+  p->inter_leaved_hash = 3;
+  p->enable_self_collision = 1;
+  p->particle_diameter = 1.3f;
+  p->hash_cell_size = 1.5f;
+  p->frame_time = 1.0f / 60.0f;
+  p->update_obstacle_animation = 1;
+  p->pbd_repulsion = 0;
+  p->pbd_thickness = 1e-4f;
+  p->repulsion_relaxation = 0.25f;
+  p->impact_zone = 0;
+  p->impact_zone_obstacle_mass = 1e3f;
+  p->impact_zone_thickness = 1e-4f;
+  p->imminent_repulsion = 0;
+  p->imminent_thickness = 1e-3f;
+}
+
+// FEMFabricSettings (config/Base.hpp:47-57).
+void orc_default_fem_material(xrt_fem_material* m) {
+  std::memset(m, 0, sizeof(*m));
+  m->xx_stiffness = m->yy_stiffness = m->xy_stiffness = 1.0f;
+  m->xy_poisson_ratio = m->yx_poisson_ratio = 0.3f;
+  m->bending_stiffness = 1.0f;
+  m->solve_bending = 1;
+}
+
 void* orc_create() { return new Oracle(); }
 void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
 int orc_num_threads() {

@@ -78,6 +78,19 @@ def test_default_params_are_the_reference_effective_defaults(xrt):
     assert xrt.xrt_get_version(C.byref(v)) == 0 and v.value == 1
 
 
+def test_oracle_defaults_equal_the_library_defaults(xrt, oracle_lib):
+    """The oracle restates the defaults itself (CPU runs load nothing from libxrt.so); both
+    restatements must agree field for field, bit for bit."""
+    from oracle.oracle import default_fem_material, default_params
+    from xrtailor_gb300 import _lib
+    a, b = _lib.SwiftParams(), default_params()
+    assert xrt.xrt_default_params(C.byref(a)) == 0
+    assert bytes(a) == bytes(b)
+    m = _lib.FemMaterial()
+    assert xrt.xrt_default_fem_material(C.byref(m)) == 0
+    assert bytes(m) == bytes(default_fem_material())
+
+
 def _gpu_present():
     try:
         import torch

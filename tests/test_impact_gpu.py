@@ -113,6 +113,33 @@ def test_large_sheet_ends_crossing_free(xrt):
     assert g.collision_step()["impacts"] == 0
 
 
+def test_one_large_zone_matches_oracle(xrt):
+    """A 192 x 192 sheet crossing the icosphere by 0.12: one zone of about 5,600 impacts, more
+    than sixteen 256-element chunks, so it is solved by 16-block clusters of 1,024 threads (four
+    chunk trees at once) where the device holds them.  Sums keep the blocked order, so the pass
+    statistics and positions equal the oracle's bit for bit."""
+    n = 192
+    cloth = scenes.grid_cloth(n, 1.0, origin=(0.0, 0.35, 0.0), jitter=1e-3, seed=1)
+    cloth.fixed_indices = scenes.two_corner_pins(n)
+    sphere = scenes.icosphere(2, 0.3, center=(0.5, 0.0, 0.5))
+    g, o = make_pair(_params(), [cloth], [sphere])
+    for _ in range(4):
+        g.step()
+        o.step()
+    x = o.host_positions()
+    _same(g.host_positions(), x)
+    pred = x.copy()
+    pred[:, 1] -= 0.12
+    g.set_predicted(pred)
+    o.set_predicted(pred)
+    sg = g.collision_step(launch_shapes=True)
+    so = o.collision_step()
+    shapes = sg.pop("wide_solves")
+    assert sg == so and sg["success"] == 1 and sg["impacts"] > 4096, (sg, so)
+    assert shapes[0] + shapes[1] > 0, shapes  # the zone outgrew the 8-block clusters
+    _same(g.predicted(), o.predicted())
+
+
 def test_rejected_in_batched_context(xrt):
     from xrtailor_gb300 import ClothSolver
     cloth, obs = small_scene(8)

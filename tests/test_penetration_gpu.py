@@ -65,3 +65,79 @@ def test_no_penetration_over_the_run(xrt):
         assert _edges_crossing(x, edges, n, off, near=0.05) == 0, f
     # the sheet did reach the sphere (contact was exercised, not avoided)
     assert worst < 0.01, worst
+
+
+def _tube_margin(body, time, x):
+    """How far each point lies inside the posed tube body (positive inside), from its shape: the
+    point is taken into the rest frame of every bone, where the tube is a surface of revolution
+    (rings of radius prof(y) between 0.08 and 0.92 of the height, cones to the two poles), and
+    compared with the radius there.  Bone b covers rest heights [b L, (b + 1) L), widened by half
+    a bone at each joint so that a point near a joint is in the range of a bone on either side."""
+    T = body.joint_transforms(time).astype(np.float64).reshape(-1, 3, 4)
+    R, tr = T[:, :, :3], T[:, :, 3]
+    h, L = body.height, body.height / body.bones
+    base = np.asarray(body.base, np.float64)
+    ys = np.linspace(0.08 * h, 0.92 * h, body.rings)
+    prof = body.radius * (1.0 + 0.15 * np.sin(ys / h * 3 * np.pi))
+    inscribed = np.cos(np.pi / body.slices)  # a polygon ring lies within its circle
+    out = np.full(len(x), -np.inf)
+    for b in range(body.bones):
+        q = (x - tr[b]) @ R[b] - base  # R_b^T (x - t_b): the rest position under bone b
+        y = q[:, 1]
+        lo = -np.inf if b == 0 else (b - 0.5) * L  # half a bone of overlap at each joint
+        hi = np.inf if b == body.bones - 1 else (b + 1.5) * L
+        sel = (y >= lo) & (y < hi) & (y >= 0.0) & (y <= h)
+        yy = y[sel]
+        rad = np.interp(yy, ys, prof) * inscribed
+        bot, top = yy < ys[0], yy > ys[-1]
+        rad[bot] = prof[0] * inscribed * yy[bot] / ys[0]
+        rad[top] = prof[-1] * inscribed * (h - yy[top]) / (h - ys[-1])
+        m = rad - np.hypot(q[sel, 0], q[sel, 2])
+        out[sel] = np.maximum(out[sel], m)
+    return out
+
+
+def _body_signed_distance(x, verts, sdf, body, time, near=0.03):
+    """Signed distance (positive outside) of cloth vertices to the posed tube body: exact on the
+    mesh for vertices within `near` of a body vertex; for the others (at least `near` from the
+    surface's vertices) the tube's own shape flags the ones inside or within 5 mm of its surface
+    (_tube_margin), and those get the exact distance too."""
+    from scipy.spatial import cKDTree
+    d0, _ = cKDTree(verts).query(x)
+    out = d0.copy()
+    close = d0 < near
+    if close.any():
+        out[close] = sdf(x[close], verts)
+    far = np.nonzero(~close)[0]
+    if len(far):
+        # the tube's shape flags candidates; the exact distance decides for them
+        flagged = far[_tube_margin(body, time, x[far]) > -5e-3]
+        if len(flagged):
+            out[flagged] = sdf(x[flagged], verts)
+    return out
+
+
+def test_garment_run_keeps_the_cloth_outside_the_body(xrt):
+    """The garment (256 x 256 on the animated tube body, 20 substeps x 15 iterations, the
+    configured compliances) over its whole 240-frame run: after every frame no cloth vertex lies
+    inside the posed body (vertex-face signed distance >= 0)."""
+    sc = scenes.plain_garment(256)
+    p = scenes.scene_params(sc)
+    s = ClothSolver(p)
+    s.add_cloth(sc.cloth, particle_diameter=sc.particle_diameter)
+    s.add_obstacle(sc.obstacle)
+    s.start()
+    from tests.helpers import MeshSignedDistance
+    sdf = MeshSignedDistance(sc.body.triangles)
+    worst, touching = np.inf, 0
+    for f in range(sc.frames):
+        t = sc.body.pose((f + 1) / 60.0)
+        s.set_obstacle_targets(t)
+        s.step()
+        x = s.host_positions().astype(np.float64)
+        assert np.isfinite(x).all(), f
+        sd = _body_signed_distance(x, t.astype(np.float64), sdf, sc.body, (f + 1) / 60.0)
+        worst = min(worst, float(sd.min()))
+        touching = max(touching, int((sd < 5e-3).sum()))
+        assert (sd >= 0).all(), (f, int((sd < 0).sum()), float(sd.min()))
+    assert touching > 100, touching  # the garment rests on the body

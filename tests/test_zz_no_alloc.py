@@ -38,11 +38,12 @@ def _noalloc(xrt, prims, pred, scr):
                iesc=torch.empty(max(n - 1, 1), dtype=torch.int32, device=dev),
                eesc=torch.empty(n, dtype=torch.int32, device=dev))
     stream = torch.cuda.current_stream(dev)
+    # one primitive has no internal node: the internal escape table may then be NULL
+    iesc = None if n == 1 else out["iesc"].data_ptr()
     rc = xrt.xrt_lbvh_build_noalloc(
         d_prims.data_ptr(), None if d_pred is None else d_pred.data_ptr(), n, float(scr),
         out["morton"].data_ptr(), out["objects"].data_ptr(), out["nodes"].data_ptr(),
-        out["aabbs"].data_ptr(), out["iesc"].data_ptr(), out["eesc"].data_ptr(),
-        stream.cuda_stream)
+        out["aabbs"].data_ptr(), iesc, out["eesc"].data_ptr(), stream.cuda_stream)
     assert rc == 0, rc
     torch.cuda.synchronize(dev)
     h = {k: v.cpu().numpy() for k, v in out.items()}
@@ -73,6 +74,17 @@ def test_noalloc_build_matches_allocating_build_on_consecutive_calls(xrt):
         if first is None:
             first = got
     _same(got, first)  # the last call repeats the first input
+
+
+def test_noalloc_build_at_the_limit_and_at_one_primitive(xrt):
+    # the largest accepted input fills the fixed layout (32 radix tiles of the histogram); one
+    # primitive has a single leaf and no internal node; the two calls in a row share the array
+    rng = np.random.default_rng(43)
+    full = prim_soup(MAX_PRIMS, seed=43)
+    full_pred = (full + rng.normal(0, 0.01, full.shape)).astype(np.float32)
+    one = prim_soup(1, seed=44)
+    for prims, pred, scr in ((full, full_pred, 0.002), (one, None, 0.0), (full, full_pred, 0.002)):
+        _same(_noalloc(xrt, prims, pred, scr), _allocating(prims, pred, scr))
 
 
 def test_noalloc_build_rejects_more_than_the_limit(xrt):

@@ -69,7 +69,7 @@ class CollisionStats(C.Structure):
         ("impacts", C.c_uint32),
         ("zones", C.c_uint32),
         ("solves", C.c_uint32),
-        ("reserved", C.c_int32 * 2),
+        ("wide_solves", C.c_uint32 * 2),
     ]
 
 
@@ -230,6 +230,7 @@ SIGNATURES = {
     "xrt_set_predicted": (C.c_int32, [P, FP]),
     # include/xrt_diff.h
     "xrt_diff_begin": (C.c_int32, [P]),
+    "xrt_diff_begin_interval": (C.c_int32, [P, C.c_int32]),
     "xrt_backward": (C.c_int32, [P, FP, FP, C.POINTER(Grads)]),
     "xrt_diff_end": (C.c_int32, [P]),
 }

@@ -179,25 +179,29 @@ void record_frame(Context& c) {
                        // the stretch and bend phases)
         xrt::launch_fem(c, k, it == 0, kStretch, kBend);
       } else if (c.s_tiles.on) {
+        Timed g(c, kStretch, (uint32_t)c.s_tiles.tile_colors.size(), c.ne, Timed::kGroup);
         for (size_t tc = 0; tc < c.s_tiles.tile_colors.size(); ++tc) {
-          Timed t(c, kStretch, 1, c.s_tiles.tile_color_cons[tc]);
+          Timed t(c, kStretch, 1, c.s_tiles.tile_color_cons[tc], Timed::kMember);
           xrt::launch_stretch_tiles(c, k, c.s_tiles.tile_colors[tc], it == 0);
         }
       } else {
+        Timed g(c, kStretch, (uint32_t)c.s_ranges.size(), c.ne, Timed::kGroup);
         for (const ColorRange& r : c.s_ranges) {
-          Timed t(c, kStretch, 1, r.end - r.begin);
+          Timed t(c, kStretch, 1, r.end - r.begin, Timed::kMember);
           xrt::launch_stretch(c, k, r, it == 0);
         }
       }
       if (p.solve_bending && !c.fem.on) {
         if (c.b_tiles.on) {
+          Timed g(c, kBend, (uint32_t)c.b_tiles.tile_colors.size(), c.nb, Timed::kGroup);
           for (size_t tc = 0; tc < c.b_tiles.tile_colors.size(); ++tc) {
-            Timed t(c, kBend, 1, c.b_tiles.tile_color_cons[tc]);
+            Timed t(c, kBend, 1, c.b_tiles.tile_color_cons[tc], Timed::kMember);
             xrt::launch_bend_tiles(c, k, c.b_tiles.tile_colors[tc]);
           }
         } else {
+          Timed g(c, kBend, (uint32_t)c.b_ranges.size(), c.nb, Timed::kGroup);
           for (const ColorRange& r : c.b_ranges) {
-            Timed t(c, kBend, 1, r.end - r.begin);
+            Timed t(c, kBend, 1, r.end - r.begin, Timed::kMember);
             xrt::launch_bend(c, k, r);
           }
         }
@@ -276,6 +280,28 @@ xrt_status capture_frame(Context& c) {
     return XRT_ERR_CUDA;
   }
   c.graph_dirty = false;
+  return XRT_OK;
+}
+
+// One frame captured with the profiling events of mode 2 as event-record nodes, replayed once
+// and discarded; the frame graph of normal stepping is left as it is.
+xrt_status profile_frame_graph(Context& c) {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  XRT_CUDA(&c, cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+  record_frame(c);
+  cudaError_t e = cudaStreamEndCapture(c.stream, &graph);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (e != cudaSuccess) {
+    c.prof_used = 0;
+    c.set_error(std::string("profiled frame graph failed: ") + cudaGetErrorString(e));
+    return XRT_ERR_CUDA;
+  }
+  collect_profile(c);
   return XRT_OK;
 }
 
@@ -391,7 +417,8 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   for (auto* b : f4) b->release();
   DBuf<uint32_t>* u[] = {&c.vf_ptr, &c.vf_list, &c.lra_ptr, &c.lra_src, &c.lra_l_src, &c.lra_l_tgt,
                          &c.bind_ptr, &c.ve_ptr, &c.ve_list, &c.hash_key, &c.hash_val,
-                         &c.cell_start, &c.cell_end, &c.neighbors, &c.ovf_ptr, &c.ovf_list, &c.err};
+                         &c.cell_start, &c.cell_end, &c.neighbors, &c.nb_count, &c.ovf_ptr,
+                         &c.ovf_list, &c.err};
   for (auto* b : u) b->release();
   c.tri.release(); c.s_con.release(); c.b_idx.release(); c.bind_b.release(); c.otri.release();
   c.s_lambda.release(); c.lra_rest.release(); c.lra_l_rest.release(); c.b_tc.release();
@@ -736,6 +763,38 @@ static xrt_status upload_constraints(Context& c) {
   XRT_CUDA(&c, upload(c.s_con, scon, c.stream));
   XRT_CUDA(&c, upload(c.b_idx, bidx, c.stream));
   XRT_CUDA(&c, upload(c.b_tc, btc, c.stream));
+  // the forward tile kernels' per-tile record blocks (TiledSet::rec); footprint-local ids fit
+  // 16 bits
+  static_assert(xrt::kTileMaxFootprint <= 65536, "16-bit footprint-local vertex ids");
+  for (int kind = 0; kind < 2; ++kind) {
+    xrt::TiledSet& T = kind == 0 ? c.s_tiles : c.b_tiles;
+    if (!T.on) continue;
+    const int arity = kind == 0 ? 2 : 4;
+    const std::vector<uint32_t>& local = kind == 0 ? c.s_local : c.b_local;
+    const std::vector<int4>& meta = c.h_tile_meta[kind];
+    std::vector<uint4> rec;
+    std::vector<uint32_t> ofs(meta.size());
+    for (size_t t = 0; t < meta.size(); ++t) {
+      const uint32_t c0 = (uint32_t)meta[t].z, nc = (uint32_t)meta[t].w;
+      const uint32_t n16 = xrt::tile_rec16(nc, arity), ids16 = (2 * arity * nc + 15) / 16;
+      ofs[t] = (uint32_t)rec.size();
+      rec.resize(rec.size() + n16, make_uint4(0, 0, 0, 0));
+      uint16_t* ids = reinterpret_cast<uint16_t*>(rec.data() + ofs[t]);
+      float2* vals = reinterpret_cast<float2*>(rec.data() + ofs[t] + ids16);
+      for (uint32_t j = 0; j < nc; ++j) {
+        const uint32_t slot = c0 + j;
+        for (int a = 0; a < arity; ++a) ids[arity * j + a] = (uint16_t)local[arity * slot + a];
+        vals[j] = kind == 0 ? make_float2(c.h_rest[c.s_perm[slot]], c.h_scomp[c.s_perm[slot]])
+                            : btc[slot];
+      }
+    }
+    if (rec.size() >= (1ull << 32)) {
+      c.set_error("tile record blocks exceed 2^32 x 16 bytes");
+      return XRT_ERR_EDGE_CAPACITY;
+    }
+    XRT_CUDA(&c, upload(T.rec, rec, c.stream));
+    XRT_CUDA(&c, upload(T.rec_ofs, ofs, c.stream));
+  }
   XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
   return XRT_OK;
 }
@@ -828,6 +887,8 @@ static xrt_status schedule_kind(Context& c, const std::vector<uint32_t>& idx, in
                                (int)c0, (int)(c1 - c0)));
     for (uint32_t l = 0; l <= S.num_local; ++l) K.lofs.push_back(S.lc_ptr[tt * S.num_local + l] - c0);
   }
+  T.max_rec16 = 0;  // the largest record block of the forward tile kernels (TiledSet::rec)
+  for (const int4& m : K.meta) T.max_rec16 = std::max(T.max_rec16, xrt::tile_rec16((uint32_t)m.w, arity));
   XRT_CUDA(&c, upload(T.foot, S.foot, c.stream));
   XRT_CUDA(&c, upload(T.meta, K.meta, c.stream));
   XRT_CUDA(&c, upload(T.lofs, K.lofs, c.stream));
@@ -918,8 +979,10 @@ xrt_status xrt_start(xrt_ctx* h) {
     }
   }
   if (c.s_tiles.on || c.b_tiles.on) {
-    const size_t smem = std::max(xrt::tile_smem_bytes(c.s_tiles, sizeof(int4) + sizeof(float)),
-                                 xrt::tile_smem_bytes(c.b_tiles, sizeof(int4) + sizeof(float2)));
+    const size_t smem = std::max(
+        std::max(xrt::tile_smem_bytes(c.s_tiles, sizeof(int4) + sizeof(float)),
+                 xrt::tile_smem_bytes(c.b_tiles, sizeof(int4) + sizeof(float2))),
+        std::max(xrt::tile_smem_fwd(c.s_tiles, true), xrt::tile_smem_fwd(c.b_tiles, false)));
     if (smem > 200 * 1024) {
       c.set_error("tile schedule needs more shared memory than a block has");
       return XRT_ERR_INVALID_MESH;
@@ -1029,6 +1092,8 @@ xrt_status xrt_start(xrt_ctx* h) {
     XRT_CUDA(&c, c.neighbors.reserve(nbs));
     XRT_CUDA(&c, cudaMemsetAsync(c.cell_end.p, 0, sizeof(uint32_t) * table, c.stream));
     XRT_CUDA(&c, cudaMemsetAsync(c.neighbors.p, 0, sizeof(uint32_t) * nbs, c.stream));
+    XRT_CUDA(&c, c.nb_count.reserve(c.nv));
+    XRT_CUDA(&c, cudaMemsetAsync(c.nb_count.p, 0, sizeof(uint32_t) * c.nv, c.stream));
     XRT_CUDA(&c, c.hash_sorter.reserve(c.nv));
   }
   // bindings: GenerateBinding_Kernel (BindingConstraint.cu:20-44) rest lengths from x0
@@ -1228,8 +1293,23 @@ xrt_status xrt_step_frame(xrt_ctx* h) {
   }
   xrt::launch_skin(c);  // obstacle targets from the joint transforms, when skinning is on
   if (c.diff.active) xrt::diff_checkpoint(c);  // state at the frame start, for xrt_backward
+  xrt_status st = xrt::frame_core(c, eager);
+  if (st != XRT_OK) return st;
+  XRT_CUDA(&c, xrt::cache_frame(c));  // when recording: this frame into the frame cache
+  c.frame_index++;
+  return XRT_OK;
+}
+
+}  // extern "C"
+
+// The frame's launches on the current state: a profiled frame, the replayed frame graph or an
+// eager frame.  Also the adjoint's plain recomputation of the frames between checkpoints.
+xrt_status xrt::frame_core(Context& c, bool eager) {
   c.frame_status = XRT_OK;
-  if (c.profiling) {
+  if (c.profiling == 2 && !eager) {
+    xrt_status st = profile_frame_graph(c);
+    if (st != XRT_OK) return st;
+  } else if (c.profiling) {
     record_frame(c);
     XRT_CUDA(&c, cudaGetLastError());
     collect_profile(c);
@@ -1243,11 +1323,10 @@ xrt_status xrt_step_frame(xrt_ctx* h) {
     record_frame(c);
     XRT_CUDA(&c, cudaGetLastError());
   }
-  if (c.frame_status != XRT_OK) return c.frame_status;
-  XRT_CUDA(&c, xrt::cache_frame(c));  // when recording: this frame into the frame cache
-  c.frame_index++;
-  return XRT_OK;
+  return c.frame_status;
 }
+
+extern "C" {
 
 xrt_status xrt_step_frames(xrt_ctx* h, int32_t n) {
   for (int32_t i = 0; i < n; ++i) {
@@ -1307,7 +1386,8 @@ xrt_status xrt_set_profiling(xrt_ctx* h, int32_t enabled) {
   Context& c = h->c;
   cudaSetDevice(c.device);
   XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
-  c.profiling = enabled != 0;
+  if (enabled < 0 || enabled > 2) return XRT_ERR_INVALID_ARGUMENT;
+  c.profiling = enabled;
   c.prof_used = 0;
   c.prof_frames = 0;
   for (int i = 0; i < 16; ++i) {

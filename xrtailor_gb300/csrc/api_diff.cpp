@@ -17,7 +17,22 @@ xrt_status xrt_diff_begin(xrt_ctx* h) {
   }
   cudaSetDevice(c.device);
   if (c.diff.active) xrt::diff_release(c);
-  return xrt::diff_prepare(c);
+  xrt_status st = xrt::diff_prepare(c);
+  c.diff.interval = 1;
+  return st;
+}
+
+xrt_status xrt_diff_begin_interval(xrt_ctx* h, int32_t substeps) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  const int32_t S = c.params.num_substeps;
+  if (substeps <= 0 || S <= 0 || substeps % S != 0) {
+    c.set_error("the checkpoint interval must be a positive multiple of num_substeps");
+    return XRT_ERR_INVALID_ARGUMENT;
+  }
+  const xrt_status st = xrt_diff_begin(h);
+  if (st == XRT_OK) c.diff.interval = (uint32_t)(substeps / S);
+  return st;
 }
 
 xrt_status xrt_backward(xrt_ctx* h, const float* dL_dx, const float* dL_dv,

@@ -73,6 +73,7 @@ enum : uint32_t {
   kErrIndex = 1u << 2,      // an index was out of range
   kErrZoneSize = 1u << 3,   // an impact zone exceeded 65,536 nodes or impacts
   kErrLineSearch = 1u << 4, // a zone's backtracking line search exceeded its step bound
+  kErrBulkCopy = 1u << 5,   // a bulk copy into shared memory did not complete within its bound
 };
 
 __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit) { atomicOr(err, bit); }
@@ -93,6 +94,49 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 __device__ __forceinline__ void pdl_release() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
+
+// Bulk copy global -> shared memory completed on an mbarrier (cp.async.bulk with complete_tx,
+// sm_90 and later).  Source and destination must be 16-byte aligned and the size a multiple of
+// 16 bytes.  One thread initialises the barrier, announces the byte count and issues the copy;
+// the block then waits on phase 0.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+  // make the initialised barrier visible to the async proxy that completes it
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_load_g2s(void* dst, const void* src, uint32_t bytes,
+                                              uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// Waits for the barrier's phase `parity` to complete, polling at most `limit` times; returns
+// false when the limit ran out (the caller reports it and leaves without using the data).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  const uint32_t a = smem_u32(bar);
+  for (uint32_t k = 0; k < limit; ++k) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+constexpr uint32_t kBulkWaitLimit = 1u << 22;
 
 template <typename... P, typename... A>
 inline cudaError_t launch_k(bool pdl, void (*kern)(P...), unsigned grid, unsigned block,

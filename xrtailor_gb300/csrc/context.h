@@ -51,6 +51,19 @@ struct DBuf {
 
 // ---- radix sort (radix.cu) --------------------------------------------------------------------
 struct RadixSort {
+  // Keys per histogram / scatter tile, digits per pass, and histogram entries per block of the
+  // multi-block scan.  Histograms of at most kSingleBlockScan entries are scanned by one block
+  // and never touch `sums`.
+  static constexpr uint32_t kTileKeys = 2048;
+  static constexpr uint32_t kDigits = 256;
+  static constexpr uint32_t kScanChunk = 4096;
+  static constexpr uint32_t kSingleBlockScan = 4 * kScanChunk;
+  static constexpr size_t hist_entries(size_t n) {
+    return (size_t)kDigits * (n ? (n + kTileKeys - 1) / kTileKeys : 1);
+  }
+  static constexpr size_t sums_entries(size_t n) {
+    return (hist_entries(n) + kScanChunk - 1) / kScanChunk;
+  }
   DBuf<uint32_t> keys_tmp, vals_tmp, hist, sums;
   cudaError_t reserve(uint32_t n);
   // Stable LSD sort of (keys, vals) by the low `bits` bits of keys.  The result is left in
@@ -154,17 +167,23 @@ struct ColorRange {
 };
 
 // ---- hand-written adjoint (diff.cu) --------------------------------------------------------------
-// Between xrt_diff_begin and xrt_backward every frame start is checkpointed; the reverse pass
-// replays each frame from its checkpoint (same colors, same order: the same bits) while taping
-// the inputs of every projection, then walks the tape backwards.
+// Between xrt_diff_begin and xrt_backward the state at every `interval`-th frame start is
+// checkpointed, and every frame's obstacle targets are kept; the reverse pass walks the
+// segments of `interval` frames newest first: it restores the segment's checkpoint, recomputes
+// the segment's frames plainly (keeping each frame's start state), then replays each frame,
+// newest first, while taping the inputs of every projection (same colors, same order: the same
+// bits) and walks the tape backwards.
 struct DiffState {
   bool active = false;
-  uint32_t frames = 0;  // frames checkpointed since xrt_diff_begin
+  uint32_t frames = 0;    // frames stepped since xrt_diff_begin
+  uint32_t interval = 1;  // frames per checkpoint
   struct Checkpoint {
     DBuf<float4> x, x0, v, ox0, ox, on;
     uint32_t frame_index = 0;
   };
-  std::vector<Checkpoint> ck;
+  std::vector<Checkpoint> ck;        // one per segment
+  std::vector<DBuf<float4>> targets; // per frame: the obstacle targets at its start
+  std::vector<Checkpoint> seg;       // the reverse pass's recomputed frame starts of a segment
   // execution slots grouped by color, colors in forward order
   std::vector<ColorRange> s_colors, b_colors;
   DBuf<uint32_t> s_order, b_order;
@@ -217,7 +236,19 @@ struct TiledSet {
   DBuf<int4> meta;                      // per executed tile {first footprint, footprint size,
                                         //  first constraint, constraint count}
   DBuf<uint32_t> lofs;                  // per executed tile: num_local + 1 offsets, tile-relative
+  // Records of the forward tile kernels, one 16-byte aligned block per executed tile, copied
+  // into shared memory in one bulk copy: the constraints' footprint-local vertex ids as 16-bit
+  // values (2 per stretch constraint, 4 per bend element), padded to 16 bytes, then their float2
+  // values (rest length and compliance / rest angle and compliance), padded to 16 bytes.
+  DBuf<uint4> rec;
+  DBuf<uint32_t> rec_ofs;               // per executed tile: first uint4 of its block
+  uint32_t max_rec16 = 0;               // largest block, in uint4
 };
+
+// uint4 units of a tile's record block: `arity` 16-bit ids and a float2 per constraint.
+__host__ __device__ inline uint32_t tile_rec16(uint32_t nc, uint32_t arity) {
+  return (2 * arity * nc + 15) / 16 + (8 * nc + 15) / 16;
+}
 
 // One constraint kind of the FEM fabric: its schedule (as the stretch / bend kinds') and the
 // slot-ordered vertex ids (footprint-local when tiled).
@@ -434,6 +465,7 @@ struct Context {
   DBuf<float4> ee_a, ee_b, ee_c;     // {dist, p2}, {q2, s}, {fn, t}
   // particle hash
   DBuf<uint32_t> hash_key, hash_val, cell_start, cell_end, neighbors;
+  DBuf<uint32_t> nb_count;  // entries of each vertex's neighbor list (before its terminator)
   RadixSort hash_sorter;
   // obstacle
   DBuf<float4> ox0, ox, ox1, on, on1;
@@ -451,14 +483,17 @@ struct Context {
   std::vector<uint32_t> h_tile_lofs[2];
   // error word
   DBuf<uint32_t> err;
-  // per-phase profiling (eager frames only)
+  // per-phase profiling: 1 = eager frames, an event pair around every launch; 2 = the frame
+  // captured as a graph with an event-record node pair around each phase group (a phase's
+  // launches of one iteration) and replayed, so the launches inside a group keep their
+  // programmatic dependent launch edges
   struct ProfEvent {
     cudaEvent_t a, b;
     int phase;
     uint32_t kernels;
     uint64_t units;
   };
-  bool profiling = false;
+  int profiling = 0;
   std::vector<ProfEvent> prof_events;
   size_t prof_used = 0;
   double prof_ms[16] = {};
@@ -472,12 +507,17 @@ struct Context {
 // Profile phases of the reverse pass (after the frame's, which api.cpp names).
 enum AdjointPhase { kAdjReplay = 12, kAdjStretch, kAdjBend, kAdjVertex };
 
-// CUDA-event pair around one launch group when profiling (eager frames only).
+// CUDA-event pair around one launch when profiling eagerly (mode 1), or around a whole phase
+// group inside a captured frame (mode 2).  A launch inside a group (`member`) is timed only in
+// mode 1; a group scope only in mode 2; any other scope in both.
 struct Timed {
+  enum Kind { kLaunch, kMember, kGroup };
   Context& c;
   size_t idx = (size_t)-1;
-  Timed(Context& ctx, int phase, uint32_t kernels, uint64_t units) : c(ctx) {
+  Timed(Context& ctx, int phase, uint32_t kernels, uint64_t units, Kind kind = kLaunch) : c(ctx) {
     if (!c.profiling) return;
+    if (kind == kMember && c.profiling != 1) return;
+    if (kind == kGroup && c.profiling != 2) return;
     if (c.prof_used == c.prof_events.size()) {
       Context::ProfEvent e{};
       cudaEventCreate(&e.a);
@@ -489,10 +529,19 @@ struct Timed {
     e.phase = phase;
     e.kernels = kernels;
     e.units = units;
-    cudaEventRecord(e.a, c.stream);
+    record(e.a);
   }
   ~Timed() {
-    if (idx != (size_t)-1) cudaEventRecord(c.prof_events[idx].b, c.stream);
+    if (idx != (size_t)-1) record(c.prof_events[idx].b);
+  }
+  void record(cudaEvent_t e) {
+    // under stream capture (mode 2) the record becomes an event-record node of the graph
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (c.profiling == 2 && cudaStreamIsCapturing(c.stream, &cs) == cudaSuccess &&
+        cs == cudaStreamCaptureStatusActive)
+      cudaEventRecordWithFlags(e, c.stream, cudaEventRecordExternal);
+    else
+      cudaEventRecord(e, c.stream);
   }
 };
 
@@ -556,6 +605,7 @@ void launch_fem(Context& c, const FrameConst& k, bool reset_lambda, int phase_st
                 int phase_bend);
 void fem_release(Context& c);
 size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes);
+size_t tile_smem_fwd(const TiledSet& T, bool stretch);  // the forward stretch / bend kernels
 // Sets T.block (256 / 512 threads) and T.resident; after configure_tile_kernels.
 cudaError_t choose_tile_block(TiledSet& T, bool bend);
 // tile-local Gauss-Seidel: all tiles of one tile color (range of executed tiles)
@@ -589,6 +639,8 @@ xrt_status export_lbvh(Lbvh& b, cudaStream_t s, std::string& err, uint32_t* mort
 // ---- adjoint (diff.cu) ---------------------------------------------------------------------------
 xrt_status diff_prepare(Context& c);     // schedule, tape and adjoint buffers
 void diff_checkpoint(Context& c);        // state at the start of the next frame
+// The frame's launches on the current state (api.cpp): profiled, replayed graph or eager.
+xrt_status frame_core(Context& c, bool eager);
 // Reverse pass over the checkpointed frames; host outputs may be null (sizes: E, B, V, 3V, 3V).
 xrt_status diff_backward(Context& c, const float* dLdx, const float* dLdv, float* d_compliance,
                          float* d_bend_compliance, float* d_mass, float* d_velocity,

@@ -1235,8 +1235,16 @@ xrt_status diff_prepare(Context& c) {
 
 void diff_checkpoint(Context& c) {
   DiffState& D = c.diff;
-  if (D.ck.size() <= D.frames) D.ck.emplace_back();
-  save_state(c, D.ck[D.frames]);
+  const uint32_t k = D.frames / D.interval;
+  if (D.frames % D.interval == 0) {
+    if (D.ck.size() <= k) D.ck.emplace_back();
+    save_state(c, D.ck[k]);
+  }
+  if (D.targets.size() <= D.frames) D.targets.emplace_back();
+  if (c.onv) {
+    D.targets[D.frames].reserve(c.onv);
+    copy_d(D.targets[D.frames].p, c.ox.p, sizeof(float4) * c.onv, c.stream);
+  }
   D.frames++;
 }
 
@@ -1263,8 +1271,31 @@ xrt_status diff_backward(Context& c, const float* dLdx, const float* dLdv, float
   XRT_CUDA(&c, cudaMemcpyAsync(D.Gv.p, gv.data(), sizeof(float4) * V, cudaMemcpyHostToDevice, s));
   XRT_CUDA(&c, cudaMemsetAsync(D.comp_bar.p, 0, sizeof(float) * std::max(c.ne, 1u), s));
   XRT_CUDA(&c, cudaMemsetAsync(D.bcomp_bar.p, 0, sizeof(float) * std::max(c.nb, 1u), s));
+  const uint32_t m = D.interval;
+  if (m > 1 && D.seg.size() < m) D.seg.resize(m);
   for (int f = (int)D.frames - 1; f >= 0; --f) {
-    load_state(c, D.ck[f]);
+    const uint32_t k = (uint32_t)f / m, first = k * m;
+    if (m > 1 && ((uint32_t)f == D.frames - 1 || (uint32_t)f % m == m - 1)) {
+      // a new segment (newest first): recompute its frames from its checkpoint, keeping the
+      // start state of each
+      load_state(c, D.ck[k]);
+      for (uint32_t j = first; j <= (uint32_t)f; ++j) {
+        if (c.onv) copy_d(c.ox.p, D.targets[j].p, sizeof(float4) * c.onv, c.stream);
+        save_state(c, D.seg[j - first]);
+        if (j == (uint32_t)f) break;  // the segment's last frame is replayed with taping below
+        const int prof = c.profiling;
+        c.profiling = 0;  // the recomputation is not part of the reverse pass's profile
+        const xrt_status st = frame_core(c, false);
+        c.profiling = prof;
+        if (st != XRT_OK) {
+          destroy_frame_graphs(D);
+          load_state(c, now);
+          return st;
+        }
+        c.frame_index++;
+      }
+    }
+    load_state(c, m > 1 ? D.seg[(uint32_t)f - first] : D.ck[f]);
     if (c.graph_enabled && !c.profiling) {
       const cudaError_t e = run_frame_graph(c);
       if (e != cudaSuccess) {
@@ -1326,6 +1357,11 @@ void diff_release(Context& c) {
   for (auto& ck : D.ck)
     for (DBuf<float4>* b : {&ck.x, &ck.x0, &ck.v, &ck.ox0, &ck.ox, &ck.on}) b->release();
   D.ck.clear();
+  for (auto& t : D.targets) t.release();
+  D.targets.clear();
+  for (auto& ck : D.seg)
+    for (DBuf<float4>* b : {&ck.x, &ck.x0, &ck.v, &ck.ox0, &ck.ox, &ck.on}) b->release();
+  D.seg.clear();
   D.s_order.release(); D.b_order.release(); D.s_gidx.release(); D.b_gidx.release();
   for (DBuf<float4>* b : {&D.t_sx, &D.t_bx, &D.t_stage, &D.t_ee, &D.t_vf_qs, &D.t_rt_qc,
                           &D.t_ee_a, &D.t_ee_b, &D.t_ee_c, &D.t_pred, &D.G, &D.G2, &D.Gv, &D.H,

@@ -24,6 +24,7 @@
 // ParallelOptimizer.cu:335-428): 256-element blocks summed by the stride tree s[t] += s[t + d],
 // d = 1, 2, ..., 128, then the block sums by the same tree.  With --fmad=false every value is the
 // IEEE result of the reference's expression order.
+#include <mutex>
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -359,12 +360,19 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kZT * G)
 
 // 16-block clusters need the non-portable cluster size opt-in; they are used once the device
 // reports that it can hold one (else zones stay on 8-block clusters).
-// Which 16-block clusters the device holds: bit 0 with blocks of 256 threads, bit 1 with blocks
-// of 1,024 (kWideGroups groups).
+// Which 16-block clusters the current device holds: bit 0 with blocks of 256 threads, bit 1 with
+// blocks of 1,024 (kWideGroups groups).  The opt-in is a per-device function attribute, so the
+// answer is established and cached once per device, under a lock.
 int wide_clusters() {
-  static int state = -1;
-  if (state < 0) {
-    state = 0;
+  constexpr int kMaxDevices = 256;
+  static std::mutex lock;
+  static int state[kMaxDevices];
+  static bool known[kMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 0;
+  std::lock_guard<std::mutex> guard(lock);
+  if (!known[dev]) {
+    int st = 0;
     auto fits = [](const void* k, int threads) {
       if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
         return false;
@@ -374,12 +382,14 @@ int wide_clusters() {
       int n = 0;
       return cudaOccupancyMaxActiveClusters(&n, k, &cfg) == cudaSuccess && n > 0;
     };
-    if (fits((const void*)k_zone_solve<kZoneClusterWide, 1>, kZT)) state |= 1;
+    if (fits((const void*)k_zone_solve<kZoneClusterWide, 1>, kZT)) st |= 1;
     if (fits((const void*)k_zone_solve<kZoneClusterWide, kWideGroups>, kWideGroups * kZT))
-      state |= 2;
+      st |= 2;
     (void)cudaGetLastError();  // a refused opt-in is not an error of the step
+    state[dev] = st;
+    known[dev] = true;
   }
-  return state;
+  return state[dev];
 }
 
 // Finalize_Kernel.  The reference's iteration loop stops once every zone has converged, before
@@ -758,7 +768,7 @@ xrt_status find_impacts(Context& c, float thickness, std::vector<float>& t,
 
 // ParallelImpactZoneOptimizer over the active zones (list order), then Finalize.
 xrt_status solve_zones(Context& c, const Graph& g, float obstacle_mass, float thickness,
-                       uint32_t& nsolved) {
+                       uint32_t& nsolved, uint32_t* by_group) {
   ImpactZoneState& z = c.izone;
   const cudaStream_t s = c.stream;
   std::vector<int4> zone;
@@ -834,6 +844,8 @@ xrt_status solve_zones(Context& c, const Graph& g, float obstacle_mass, float th
   }
   XRT_CUDA(&c, put(z.zid, order, s));
   const uint32_t n0 = off[1], n1 = off[2] - off[1], n2 = off[3] - off[2], n3 = off[4] - off[3];
+  by_group[0] += n2;
+  by_group[1] += n3;
   if (n0) k_zone_solve<1, 1><<<n0, kZT, 0, s>>>(a, z.zid.p);
   if (n1) k_zone_solve<kZoneCluster, 1><<<n1 * kZoneCluster, kZT, 0, s>>>(a, z.zid.p + off[1]);
   if (n2)
@@ -917,7 +929,7 @@ xrt_status collision_step(Context& c, float obstacle_mass, float thickness, xrt_
       std::vector<HostZone> fresh = isolate(g, ids);
       add_impacts(z.zones, fresh);
       uint32_t nsolved = 0;
-      if ((r = solve_zones(c, g, mass, thickness, nsolved)) != XRT_OK) return r;
+      if ((r = solve_zones(c, g, mass, thickness, nsolved, st.wide_solves)) != XRT_OK) return r;
       st.solves += nsolved;
       launch_update_ccd(z.cbvh, c.x.p, c.x0.p, c.tri.p, s, c.err.p);
       if (deform == 1) {

@@ -32,8 +32,8 @@ constexpr uint32_t kNoAllocMaxPrims = 65536;
 constexpr size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct Layout {
-  size_t v, pred, leaf_lo, leaf_hi, lo, hi, node, morton, index, keys_tmp, vals_tmp, hist, key64,
-      flags, iesc, eesc, root, dup, err, total;
+  size_t v, pred, leaf_lo, leaf_hi, lo, hi, node, morton, index, keys_tmp, vals_tmp, hist, sums,
+      key64, flags, iesc, eesc, root, dup, err, total;
 };
 
 constexpr Layout make_layout(size_t n) {
@@ -50,7 +50,8 @@ constexpr Layout make_layout(size_t n) {
   L.index = o;    o += al(n * 4);
   L.keys_tmp = o; o += al(n * 4);
   L.vals_tmp = o; o += al(n * 4);
-  L.hist = o;     o += al(256 * ((n + 2047) / 2048) * 4);
+  L.hist = o;     o += al(RadixSort::hist_entries(n) * 4);
+  L.sums = o;     o += al(RadixSort::sums_entries(n) * 4);
   L.key64 = o;    o += al(n * 8);
   L.flags = o;    o += al(n * 4);
   L.iesc = o;     o += al(n * 4);
@@ -63,6 +64,13 @@ constexpr Layout make_layout(size_t n) {
 }
 
 constexpr Layout kLayout = make_layout(kNoAllocMaxPrims);
+
+// The sort's histogram at the cap is scanned by one block, so the build stays within the layout
+// whatever the radix sort's tile size; `sums` is carved out all the same, so a larger cap or a
+// smaller scan chunk cannot send the multi-block scan through a null pointer.
+static_assert(RadixSort::hist_entries(kNoAllocMaxPrims) <= RadixSort::kSingleBlockScan,
+              "the no-allocation cap must keep the radix histogram in the single-block scan");
+static_assert(kLayout.total < (size_t(64) << 20), "the fixed scratch array stays modest");
 
 // The fixed working memory of xrt_lbvh_build_noalloc (see the header comment of this file).
 static __device__ __align__(256) unsigned char g_lbvh_scratch[kLayout.total];
@@ -134,7 +142,8 @@ extern "C" xrt_status xrt_lbvh_build_noalloc(const float* d_prims, const float* 
   point_at(b.index, base, kLayout.index, N);
   point_at(b.sorter.keys_tmp, base, kLayout.keys_tmp, N);
   point_at(b.sorter.vals_tmp, base, kLayout.vals_tmp, N);
-  point_at(b.sorter.hist, base, kLayout.hist, 256 * ((N + 2047) / 2048));
+  point_at(b.sorter.hist, base, kLayout.hist, RadixSort::hist_entries(N));
+  point_at(b.sorter.sums, base, kLayout.sums, RadixSort::sums_entries(N));
   point_at(b.key64, base, kLayout.key64, N);
   point_at(b.flags, base, kLayout.flags, N);
   point_at(b.iesc, base, kLayout.iesc, N);

@@ -21,6 +21,8 @@ constexpr int kThreads = 256;
 constexpr int kTile = kItems * kThreads;
 constexpr int kWarps = kThreads / 32;
 constexpr int kRadix = 256;
+static_assert(kTile == (int)RadixSort::kTileKeys && kRadix == (int)RadixSort::kDigits,
+              "tile and digit counts are shared with the fixed layouts of other files");
 
 __global__ void __launch_bounds__(kThreads) k_histogram(const uint32_t* __restrict__ keys,
                                                         uint32_t n, int shift, uint32_t num_tiles,
@@ -43,6 +45,7 @@ __global__ void __launch_bounds__(kThreads) k_histogram(const uint32_t* __restri
 // the totals; each block adds its offset.  Integer sums, so the result does not depend on the
 // split.
 constexpr int kScanChunk = 4096;
+static_assert(kScanChunk == (int)RadixSort::kScanChunk, "scan chunk shared through context.h");
 
 __device__ __forceinline__ uint32_t block_exclusive_scan_1024(uint32_t v, uint32_t* s_warp,
                                                              uint32_t* total) {
@@ -193,10 +196,8 @@ __global__ void __launch_bounds__(kThreads) k_scatter(const uint32_t* __restrict
 cudaError_t RadixSort::reserve(uint32_t n) {
   cudaError_t e = keys_tmp.reserve(n);
   if (e == cudaSuccess) e = vals_tmp.reserve(n);
-  const uint32_t tiles = (n + kTile - 1) / kTile;
-  const size_t entries = (size_t)kRadix * (tiles ? tiles : 1);
-  if (e == cudaSuccess) e = hist.reserve(entries);
-  if (e == cudaSuccess) e = sums.reserve((entries + kScanChunk - 1) / kScanChunk);
+  if (e == cudaSuccess) e = hist.reserve(hist_entries(n));
+  if (e == cudaSuccess) e = sums.reserve(sums_entries(n));
   return e;
 }
 
@@ -211,7 +212,7 @@ void RadixSort::sort(uint32_t* keys, uint32_t* vals, uint32_t n, int bits, cudaS
     for (int shift = 0; shift < bits; shift += 8) {
       k_histogram<<<tiles, kThreads, 0, s>>>(k_in, n, shift, tiles, hist.p);
       const uint32_t entries = kRadix * tiles;
-      if (entries <= 4 * kScanChunk) {
+      if (entries <= kSingleBlockScan) {
         k_scan<<<1, 1024, 0, s>>>(hist.p, entries);
       } else {
         const uint32_t chunks = (entries + kScanChunk - 1) / kScanChunk;

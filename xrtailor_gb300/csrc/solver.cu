@@ -100,49 +100,104 @@ __global__ void k_stretch(const int4* __restrict__ con, float* __restrict__ lamb
 // prologue / gather / scatter helpers in project_dev.cuh).  The tile's footprint is staged in
 // shared memory, its local colors run in order with a block barrier between them, and the
 // footprint is written back.  Tiles of one tile color have disjoint footprints.
-// Shared memory of a tile launch: footprint positions, the tile's constraint records, the
-// multipliers (stretch) or rest angles (bend), then the num_local + 1 local-color offsets.
-// Prologue before pdl_wait (setup-time data only): the tile's metadata, offsets, records and
-// footprint vertex ids, the ids held in registers (kFootPerThread per thread) so the gather and
-// the write-back each issue all their loads and stores at once.  NT threads per block: 512 for
-// footprints up to 4,096 vertices, 256 (twice the resident blocks per SM) up to 2,048.
+// Shared memory of a tile launch: footprint positions, the tile's record block, its mbarrier,
+// the multipliers (stretch), then the num_local + 1 local-color offsets and the footprint ids.
+// Prologue before pdl_wait (setup-time data only): the tile's metadata, offsets and footprint
+// vertex ids (kFootPerThread per thread in registers, so the gather and the write-back each
+// issue all their loads and stores at once), and one bulk copy of the tile's record block
+// (TiledSet::rec: 16-bit footprint-local ids, then float2 values) into shared memory, completed
+// on an mbarrier while the predecessor grid drains and the footprint is gathered.  NT threads
+// per block: 512 for footprints up to 4,096 vertices, 256 (twice the resident blocks per SM) up
+// to 2,048.
+struct TileSmem {
+  float4* sx;
+  uint4* srec;
+  uint64_t* bar;
+  float* sl;
+  uint32_t* so;
+  uint32_t* sf;
+};
+
+__device__ __forceinline__ TileSmem tile_smem(float4* smem, uint32_t max_foot, uint32_t max_rec16,
+                                              uint32_t max_lambda, uint32_t num_local) {
+  TileSmem m;
+  m.sx = smem;
+  m.srec = reinterpret_cast<uint4*>(m.sx + max_foot);
+  m.bar = reinterpret_cast<uint64_t*>(m.srec + max_rec16);
+  m.sl = reinterpret_cast<float*>(m.bar + 2);
+  m.so = reinterpret_cast<uint32_t*>(m.sl + max_lambda);
+  m.sf = m.so + num_local + 1;
+  return m;
+}
+
+// Thread 0 starts the copy of tile t's record block (n16 uint4).
+__device__ __forceinline__ void tile_records_start(const TileSmem& m, const uint4* __restrict__ rec,
+                                                   const uint32_t* __restrict__ rec_ofs,
+                                                   uint32_t t, uint32_t n16) {
+  if (threadIdx.x != 0) return;
+  mbar_init(m.bar, 1);
+  if (n16)
+    bulk_load_g2s(m.srec, rec + __ldg(&rec_ofs[t]), 16u * n16, m.bar);
+  else
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m.bar)) : "memory");
+}
+
+// After a __syncthreads that follows tile_records_start: every thread waits for the records
+// (bounded).  False (the same in every thread) when the copy did not complete: the error is
+// raised, the copy waited for once more, and the block must leave.
+__device__ __forceinline__ bool tile_records_ready(const TileSmem& m, uint32_t* err) {
+  const bool ok = mbar_wait_bounded(m.bar, 0, kBulkWaitLimit);
+  if (__syncthreads_or(!ok)) {
+    if (threadIdx.x == 0) {
+      raise_error(err, kErrBulkCopy);
+      mbar_wait_bounded(m.bar, 0, kBulkWaitLimit);
+    }
+    __syncthreads();
+    return false;
+  }
+  return true;
+}
+
 template <bool RESET, int NT>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_stretch_tiles(
-    const int4* __restrict__ con, float* __restrict__ lambda, float4* __restrict__ x,
-    const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
-    const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
-    uint32_t max_foot, uint32_t max_cons, float dt) {
+    const uint4* __restrict__ rec, const uint32_t* __restrict__ rec_ofs,
+    float* __restrict__ lambda, float4* __restrict__ x, const uint32_t* __restrict__ foot,
+    const int4* __restrict__ meta, const uint32_t* __restrict__ lofs, uint32_t tile_begin,
+    uint32_t num_local, uint32_t max_foot, uint32_t max_rec16, uint32_t max_cons, float dt,
+    uint32_t* err) {
   extern __shared__ float4 smem[];
-  float4* sx = smem;
-  int4* sc = reinterpret_cast<int4*>(sx + max_foot);
-  float* sl = reinterpret_cast<float*>(sc + max_cons);
-  uint32_t* so = reinterpret_cast<uint32_t*>(sl + max_cons);
-  uint32_t* sf = so + num_local + 1;
-  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
+  const TileSmem m = tile_smem(smem, max_foot, max_rec16, max_cons, num_local);
+  const uint32_t t = tile_begin + blockIdx.x;
+  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, t, num_local, m.so);
   const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
-#pragma unroll 4
-  for (uint32_t j = threadIdx.x; j < nc; j += NT) sc[j] = __ldg(&con[c0 + j]);
+  tile_records_start(m, rec, rec_ofs, t, tile_rec16(nc, 2));
   pdl_wait();
 #pragma unroll 4
-  for (uint32_t j = threadIdx.x; j < nc; j += NT) sl[j] = RESET ? 0.0f : lambda[c0 + j];
-  tile_gather<NT>(f, x, sx, sf);
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) m.sl[j] = RESET ? 0.0f : lambda[c0 + j];
+  tile_gather<NT>(f, x, m.sx, m.sf);
   __syncthreads();
+  if (!tile_records_ready(m, err)) return;
+  const ushort2* sid = reinterpret_cast<const ushort2*>(m.srec);
+  const float2* sval = reinterpret_cast<const float2*>(m.srec + (4 * nc + 15) / 16);
+  float4* sx = m.sx;
+  float* sl = m.sl;
   for (uint32_t l = 0; l < num_local; ++l) {
-    const uint32_t ce = so[l + 1];
-    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
-      const int4 c = sc[j];
+    const uint32_t ce = m.so[l + 1];
+    for (uint32_t j = m.so[l] + threadIdx.x; j < ce; j += NT) {
+      const ushort2 ab = sid[j];
+      const float2 rc = sval[j];
       float lam = sl[j];
-      float4 a = sx[c.x], b = sx[c.y];
-      if (stretch_project(a, b, __int_as_float(c.z), __int_as_float(c.w), dt, lam)) {
-        sx[c.x] = a;
-        sx[c.y] = b;
+      float4 a = sx[ab.x], b = sx[ab.y];
+      if (stretch_project(a, b, rc.x, rc.y, dt, lam)) {
+        sx[ab.x] = a;
+        sx[ab.y] = b;
         sl[j] = lam;
       }
     }
     __syncthreads();
   }
   pdl_release();  // late: the successor's blocks arrive as this one drains (measured faster)
-  tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
+  tile_scatter<NT>((uint32_t)f.m.y, x, sx, m.sf);
 #pragma unroll 4
   for (uint32_t j = threadIdx.x; j < nc; j += NT) lambda[c0 + j] = sl[j];
 }
@@ -168,26 +223,24 @@ __global__ void k_bend(const int4* __restrict__ idx, const float2* __restrict__ 
 // (fewer instructions in total, for launches with many waves of tiles).
 template <int NT, bool PAIR>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
-    const int4* __restrict__ idx, const float2* __restrict__ tc, float4* __restrict__ x,
+    const uint4* __restrict__ rec, const uint32_t* __restrict__ rec_ofs, float4* __restrict__ x,
     const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
     const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
-    uint32_t max_foot, uint32_t max_cons, float dt) {
+    uint32_t max_foot, uint32_t max_rec16, float dt, uint32_t* err) {
   extern __shared__ float4 smem[];
-  float4* sx = smem;
-  int4* sc = reinterpret_cast<int4*>(sx + max_foot);
-  float2* st = reinterpret_cast<float2*>(sc + max_cons);
-  uint32_t* so = reinterpret_cast<uint32_t*>(st + max_cons);
-  uint32_t* sf = so + num_local + 1;
-  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
-  const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
-#pragma unroll 4
-  for (uint32_t j = threadIdx.x; j < nc; j += NT) {
-    sc[j] = __ldg(&idx[c0 + j]);
-    st[j] = __ldg(&tc[c0 + j]);
-  }
+  const TileSmem m = tile_smem(smem, max_foot, max_rec16, 0, num_local);
+  const uint32_t t = tile_begin + blockIdx.x;
+  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, t, num_local, m.so);
+  const uint32_t nc = (uint32_t)f.m.w;
+  tile_records_start(m, rec, rec_ofs, t, tile_rec16(nc, 4));
   pdl_wait();
-  tile_gather<NT>(f, x, sx, sf);
+  tile_gather<NT>(f, x, m.sx, m.sf);
   __syncthreads();
+  if (!tile_records_ready(m, err)) return;
+  const ushort4* sid = reinterpret_cast<const ushort4*>(m.srec);
+  const float2* st = reinterpret_cast<const float2*>(m.srec + (8 * nc + 15) / 16);
+  float4* sx = m.sx;
+  const uint32_t* so = m.so;
   if (PAIR) {
     // the loop trip count is warp-uniform so the pair exchanges run with full warps
     const uint32_t lane0 = threadIdx.x & ~31u;
@@ -197,7 +250,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
         const uint32_t s = base + (threadIdx.x & 31u);
         const bool active = s < ce;
         const uint32_t j = active ? s >> 1 : cb >> 1;
-        const int4 b = sc[j];
+        const ushort4 q = sid[j];
+        const int4 b = make_int4(q.x, q.y, q.z, q.w);
         const float2 th = st[j];
         bend_project_pair(sx, b, th.x, th.y, dt, s & 1u, active);
       }
@@ -207,7 +261,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
     for (uint32_t l = 0; l < num_local; ++l) {
       const uint32_t ce = so[l + 1];
       for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
-        const int4 b = sc[j];
+        const ushort4 b = sid[j];
         const float2 th = st[j];
         float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
         bend_project(a1, a2, a3, a4, th.x, th.y, dt);
@@ -220,7 +274,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
     }
   }
   pdl_release();
-  tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
+  tile_scatter<NT>((uint32_t)f.m.y, x, sx, m.sf);
 }
 
 
@@ -462,6 +516,14 @@ size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes) {
          sizeof(uint32_t) * (T.num_local + 1) + sizeof(uint32_t) * T.max_foot;
 }
 
+// Shared memory of the forward tile kernels (TileSmem): footprint, record block, mbarrier slot,
+// the stretch multipliers, offsets and footprint ids.
+size_t tile_smem_fwd(const TiledSet& T, bool stretch) {
+  return sizeof(float4) * T.max_foot + 16 * (size_t)T.max_rec16 + 16 +
+         (stretch ? sizeof(float) * T.max_cons : 0) + sizeof(uint32_t) * (T.num_local + 1) +
+         sizeof(uint32_t) * T.max_foot;
+}
+
 // Block size of a tile set: 256 threads when the footprint fits 256 x kFootPerThread and a local
 // color's elements (two lanes each for bend) fill at most one pass, else 512; and how many of its
 // bend blocks the GPU holds at once.
@@ -472,8 +534,7 @@ cudaError_t choose_tile_block(TiledSet& T, bool bend) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
-  const size_t smem = tile_smem_bytes(T, bend ? sizeof(int4) + sizeof(float2)
-                                              : sizeof(int4) + sizeof(float));
+  const size_t smem = tile_smem_fwd(T, !bend);
   const void* kern = bend ? (T.block == 256 ? (const void*)k_bend_tiles<256, true>
                                             : (const void*)k_bend_tiles<512, true>)
                           : (T.block == 256 ? (const void*)k_stretch_tiles<false, 256>
@@ -488,11 +549,12 @@ void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, boo
   const uint32_t nt = tiles.end - tiles.begin;
   if (nt == 0) return;
   const TiledSet& T = c.s_tiles;
-  const size_t smem = tile_smem_bytes(T, sizeof(int4) + sizeof(float));
+  const size_t smem = tile_smem_fwd(T, true);
   auto kern = T.block == 256 ? (reset_lambda ? k_stretch_tiles<true, 256> : k_stretch_tiles<false, 256>)
                              : (reset_lambda ? k_stretch_tiles<true, 512> : k_stretch_tiles<false, 512>);
-  launch_k(c.pdl, kern, nt, T.block, smem, c.stream, c.s_con.p, c.s_lambda.p, c.x.p, T.foot.p,
-           T.meta.p, T.lofs.p, tiles.begin, T.num_local, T.max_foot, T.max_cons, k.dt);
+  launch_k(c.pdl, kern, nt, T.block, smem, c.stream, T.rec.p, T.rec_ofs.p, c.s_lambda.p, c.x.p,
+           T.foot.p, T.meta.p, T.lofs.p, tiles.begin, T.num_local, T.max_foot, T.max_rec16,
+           T.max_cons, k.dt, c.err.p);
 }
 
 void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles) {
@@ -502,9 +564,9 @@ void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles) {
   const bool pair = nt <= T.resident;  // one wave: latency-bound, halve the chain
   auto kern = T.block == 256 ? (pair ? k_bend_tiles<256, true> : k_bend_tiles<256, false>)
                              : (pair ? k_bend_tiles<512, true> : k_bend_tiles<512, false>);
-  launch_k(c.pdl, kern, nt, T.block, tile_smem_bytes(T, sizeof(int4) + sizeof(float2)), c.stream,
-           c.b_idx.p, c.b_tc.p, c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin, T.num_local,
-           T.max_foot, T.max_cons, k.dt);
+  launch_k(c.pdl, kern, nt, T.block, tile_smem_fwd(T, false), c.stream, T.rec.p, T.rec_ofs.p,
+           c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin, T.num_local, T.max_foot, T.max_rec16,
+           k.dt, c.err.p);
 }
 
 // LRA phase with a free slot vertex: one launch per slot block in list order.  (With every slot

@@ -203,11 +203,8 @@ class Scene:
     frames: int = 1
 
 
-def _params(**kw):
-    from . import _lib as L
-    import ctypes as C
-    p = L.SwiftParams()
-    L.load().xrt_default_params(C.byref(p))
+def apply_overrides(p, **kw):
+    """Sets the named fields of an xrt_swift_params (gravity as a 3-sequence); returns p."""
     for k, v in kw.items():
         if k == "gravity":
             for i in range(3):
@@ -215,6 +212,15 @@ def _params(**kw):
         else:
             setattr(p, k, v)
     return p
+
+
+def _params(**kw):
+    """xrt_swift_params: the library's defaults (xrt_default_params) with overrides."""
+    from . import _lib as L
+    import ctypes as C
+    p = L.SwiftParams()
+    L.load().xrt_default_params(C.byref(p))
+    return apply_overrides(p, **kw)
 
 
 def plain_small(n: int = 64, frames: int = 120) -> Scene:
@@ -277,17 +283,18 @@ class Garment:
 BATCHED_PARAMS = dict(num_substeps=10, num_iterations=10, bend_compliance=1e-6)
 
 
-def batched_garments(count: int = 512, seed: int = 4) -> list:
+def batched_garments(count: int = 512, seed: int = 4, only=None) -> list:
     """`count` independent garments: vertex counts log-uniform in [2,000, 100,000], aspect
     (x : z) uniform in [0.5, 2], square cells, 1 m wide, draped 5 cm above their own tube body
     (joint motion seeded with seed + i), two corners pinned and LRA-attached; stretch compliance
-    log-uniform in [1e-9, 1e-5] per instance."""
+    log-uniform in [1e-9, 1e-5] per instance.  `only`: build just these garment indices of the
+    same draw (in that order)."""
     rng = np.random.default_rng(seed)
     V = np.exp(rng.uniform(np.log(2000.0), np.log(100000.0), count))
     aspect = rng.uniform(0.5, 2.0, count)
     comp = np.exp(rng.uniform(np.log(1e-9), np.log(1e-5), count))
     out = []
-    for i in range(count):
+    for i in (range(count) if only is None else only):
         ny = max(2, int(round(np.sqrt(V[i] / aspect[i]))))
         nx = max(2, int(round(V[i] / ny)))
         body = TubeBody(seed=seed + i)
@@ -298,6 +305,24 @@ def batched_garments(count: int = 512, seed: int = 4) -> list:
         cloth.attached_indices = np.array([0, nx - 1], np.uint32)
         out.append(Garment(cloth, body, nx, ny, float(comp[i])))
     return out
+
+
+def batched_grid_dims(count: int = 512, seed: int = 4) -> list:
+    """(nx, ny) of each garment of batched_garments(count, seed), without building the meshes."""
+    rng = np.random.default_rng(seed)
+    V = np.exp(rng.uniform(np.log(2000.0), np.log(100000.0), count))
+    aspect = rng.uniform(0.5, 2.0, count)
+    out = []
+    for i in range(count):
+        ny = max(2, int(round(np.sqrt(V[i] / aspect[i]))))
+        nx = max(2, int(round(V[i] / ny)))
+        out.append((nx, ny))
+    return out
+
+
+def batched_sizes(count: int = 512, seed: int = 4) -> np.ndarray:
+    """Vertex counts nx * ny of batched_garments(count, seed), without building the meshes."""
+    return np.array([nx * ny for nx, ny in batched_grid_dims(count, seed)], np.int64)
 
 
 # 10 substeps x 10 iterations, one collision pass per substep, no particle self-collision.

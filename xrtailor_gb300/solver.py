@@ -367,9 +367,12 @@ class ClothSolver:
         L.check(self._lib.xrt_set_dependent_launch(self._h, int(bool(enabled))), self._h,
                 "dependent launch")
 
-    def set_profiling(self, enabled: bool):
-        """Per-launch CUDA-event timing of every phase (eager frames); resets the totals."""
-        L.check(self._lib.xrt_set_profiling(self._h, int(bool(enabled))), self._h, "profiling")
+    def set_profiling(self, enabled, graph: bool = False):
+        """CUDA-event timing of every phase; resets the totals.  Eager frames with an event pair
+        around every launch, or with `graph` replayed frame graphs with an event-record node
+        pair around every phase group (include/xrt.h xrt_set_profiling)."""
+        mode = 0 if not enabled else (2 if graph else 1)
+        L.check(self._lib.xrt_set_profiling(self._h, mode), self._h, "profiling")
 
     def profile(self) -> dict:
         pr = L.Profile()
@@ -565,18 +568,29 @@ class ClothSolver:
         a = _f32(x).reshape(-1)
         L.check(self._lib.xrt_set_predicted(self._h, L.fptr(a)), self._h, "set predicted")
 
-    def collision_step(self, obstacle_mass: float = 1e3, thickness: float = 1e-4) -> dict:
-        """ImpactZoneOptimization::CollisionStep on the current state (include/xrt_impact.h)."""
+    def collision_step(self, obstacle_mass: float = 1e3, thickness: float = 1e-4,
+                       launch_shapes: bool = False) -> dict:
+        """ImpactZoneOptimization::CollisionStep on the current state (include/xrt_impact.h).
+        With `launch_shapes`, the dict also holds `wide_solves`: how many zone solves ran on
+        16-block clusters of 256- and of 1,024-thread blocks."""
         st = L.CollisionStats()
         L.check(self._lib.xrt_collision_step(self._h, float(obstacle_mass), float(thickness),
                                              C.byref(st)), self._h, "collision step")
-        return {k: getattr(st, k) for k in ("success", "deform", "passes", "impacts", "zones",
-                                            "solves")}
+        out = {k: getattr(st, k) for k in ("success", "deform", "passes", "impacts", "zones",
+                                           "solves")}
+        if launch_shapes:
+            out["wide_solves"] = (int(st.wide_solves[0]), int(st.wide_solves[1]))
+        return out
 
     # -- adjoint (include/xrt_diff.h) ----------------------------------------------------------
-    def diff_begin(self):
-        """Checkpoint the following frames for backward()."""
-        L.check(self._lib.xrt_diff_begin(self._h), self._h, "diff_begin")
+    def diff_begin(self, interval_substeps=None):
+        """Checkpoint the following frames for backward(): every frame, or every
+        `interval_substeps` substeps (a multiple of the frame's substeps)."""
+        if interval_substeps is None:
+            L.check(self._lib.xrt_diff_begin(self._h), self._h, "diff_begin")
+        else:
+            L.check(self._lib.xrt_diff_begin_interval(self._h, int(interval_substeps)), self._h,
+                    "diff_begin")
 
     def backward(self, dL_dx, dL_dv=None) -> dict:
         """Gradients of a loss on the final positions (and velocities) with respect to per-edge
