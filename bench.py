@@ -273,9 +273,12 @@ def run_ours(args, rank, local_rank, world):
     units = V * S * args.steps * world
     value = units / t_dev
 
-    # end to end through the C ABI with host buffers
-    host_targets = tg
-    out = np.empty((V, 3), np.float32)
+    # end to end through the C ABI with host buffers (pinned)
+    from xrtailor_gb300 import _lib as L
+    host_targets = None
+    if tg is not None:
+        host_targets = torch.from_numpy(np.stack(tg)).pin_memory().numpy()
+    out = torch.empty((V, 3), dtype=torch.float32).pin_memory().numpy()
     h2d = (host_targets[0].nbytes if host_targets is not None else 0)
     torch.cuda.synchronize()
     e0 = time.perf_counter()
@@ -284,7 +287,7 @@ def run_ours(args, rank, local_rank, world):
             solver.set_obstacle_targets(host_targets[fi % len(host_targets)])
         fi += 1
         solver.step()
-        out = solver.host_positions()
+        L.check(lib.xrt_get_positions(solver._h, L.fptr(out)), solver._h, "read")
     e2e_t = time.perf_counter() - e0
     e2e = V * S * args.steps / e2e_t
 
@@ -480,7 +483,8 @@ def run_batched(args, local_rank):
 
     # end to end through the public API: the frame's obstacle targets from pinned host memory,
     # the step, the cloth positions back into host memory, every frame
-    out = np.empty((V, 3), np.float32)
+    from xrtailor_gb300 import _lib as L
+    out = torch.empty((V, 3), dtype=torch.float32).pin_memory().numpy()
     h2d = int(tg_host[0].numel() * 4)
     torch.cuda.synchronize()
     e0 = time.perf_counter()
@@ -488,9 +492,7 @@ def run_batched(args, local_rank):
         s.set_obstacle_targets(tg_host[fi].numpy())
         fi += 1
         s.step()
-        L_ = s._lib
-        from xrtailor_gb300 import _lib as L
-        L.check(L_.xrt_get_positions(s._h, L.fptr(out)), s._h, "read")
+        L.check(lib.xrt_get_positions(s._h, L.fptr(out)), s._h, "read")
     e2e_t = time.perf_counter() - e0
     e2e = V * S * args.steps / e2e_t
 
@@ -557,7 +559,8 @@ def run_batched(args, local_rank):
         "launch": tuned or {"tile_vertices": tile},
         "e2e": {"value": e2e, "unit": "vertex-substeps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(out.nbytes),
-                "path": "ClothSolver.set_obstacle_targets (pinned host) + step + xrt_get_positions"},
+                "path": "ClothSolver.set_obstacle_targets + step + xrt_get_positions, pinned "
+                        "host buffers"},
         "gpu_launches": int(launches) * args.steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,

@@ -329,8 +329,11 @@ def test_checkpoint_interval_must_be_a_multiple_of_the_frame(xrt):
 def test_adjoint_matches_fp64_central_differences_on_a_smooth_rollout(xrt):
     """A well-conditioned rollout (soft stretch, compliance 1e-4 to 1e-3, no bend, no contact):
     two frames of 3 substeps x 4 iterations with LRA.  The library's float32 gradients, projected
-    on 50 random directions, match FP64 central differences (h = 1e-6, relative for mass and
-    compliance, absolute for velocity) of the reference program within 1e-4 relative."""
+    on 50 random directions r (relative for mass and compliance, absolute for velocity), match
+    FP64 central differences (h = 1e-6) of the reference program within 1e-4 of the directional
+    derivative's scale: |fd - g.r| <= 1e-4 * ||g * s||, where s is the per-component scale of r
+    (so ||g * s|| is the RMS of g.r over such directions; a single direction can be nearly
+    orthogonal to g, and then |g.r| itself is no measure of the error)."""
     s, p, obs, pinned, a = _setup(n=12, bending=False)
     rng = np.random.default_rng(21)
     E = s.sizes().num_edges
@@ -365,6 +368,9 @@ def test_adjoint_matches_fp64_central_differences_on_a_smooth_rollout(xrt):
         ad = float((g["velocity"].astype(np.float64) * rv).sum() +
                    (g["mass"].astype(np.float64) * rm).sum() +
                    (g["stretch_compliance"].astype(np.float64) * rc).sum())
-        err = abs(fd - ad) / max(abs(fd), 1e-3)
+        scale = float(np.sqrt((g["velocity"].astype(np.float64) ** 2).sum() +
+                              ((g["mass"].astype(np.float64) * mass * free) ** 2).sum() +
+                              ((g["stretch_compliance"].astype(np.float64) * comp64) ** 2).sum()))
+        err = abs(fd - ad) / scale
         worst = max(worst, err)
-        assert err <= 1e-4, (k, fd, ad, err)
+        assert err <= 1e-4, (k, fd, ad, scale, err)

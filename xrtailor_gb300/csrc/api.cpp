@@ -318,15 +318,12 @@ xrt_status read_f4(Context& c, const DBuf<float4>& d, uint32_t n, float* out) {
     c.set_error("null output pointer");
     return XRT_ERR_INVALID_ARGUMENT;
   }
-  std::vector<float4> h(n);
-  if (n) {
-    XRT_CUDA(&c, cudaMemcpyAsync(h.data(), d.p, n * sizeof(float4), cudaMemcpyDeviceToHost, c.stream));
+  if (n) {  // packed on the device, then one copy straight into the caller's buffer
+    XRT_CUDA(&c, c.stage3.reserve(3 * (size_t)n));
+    xrt::launch_pack_xyz(d.p, c.stage3.p, n, c.stream);
+    XRT_CUDA(&c, cudaMemcpyAsync(out, c.stage3.p, 3 * sizeof(float) * (size_t)n,
+                                 cudaMemcpyDeviceToHost, c.stream));
     XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
-  }
-  for (uint32_t i = 0; i < n; ++i) {
-    out[3 * i] = h[i].x;
-    out[3 * i + 1] = h[i].y;
-    out[3 * i + 2] = h[i].z;
   }
   return XRT_OK;
 }
@@ -417,11 +414,12 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   for (auto* b : f4) b->release();
   DBuf<uint32_t>* u[] = {&c.vf_ptr, &c.vf_list, &c.lra_ptr, &c.lra_src, &c.lra_l_src, &c.lra_l_tgt,
                          &c.bind_ptr, &c.ve_ptr, &c.ve_list, &c.hash_key, &c.hash_val,
-                         &c.cell_start, &c.cell_end, &c.neighbors, &c.nb_count, &c.ovf_ptr,
+                         &c.cell_start, &c.cell_end, &c.neighbors, &c.ovf_ptr,
                          &c.ovf_list, &c.err};
   for (auto* b : u) b->release();
   c.tri.release(); c.s_con.release(); c.b_idx.release(); c.bind_b.release(); c.otri.release();
   c.s_lambda.release(); c.lra_rest.release(); c.lra_l_rest.release(); c.b_tc.release();
+  c.stage3.release();
   c.edge.release(); c.vf_idx.release(); c.rt_idx.release();
   c.hash_sorter.keys_tmp.release(); c.hash_sorter.vals_tmp.release(); c.hash_sorter.hist.release();
   c.hash_sorter.sums.release();
@@ -1092,8 +1090,6 @@ xrt_status xrt_start(xrt_ctx* h) {
     XRT_CUDA(&c, c.neighbors.reserve(nbs));
     XRT_CUDA(&c, cudaMemsetAsync(c.cell_end.p, 0, sizeof(uint32_t) * table, c.stream));
     XRT_CUDA(&c, cudaMemsetAsync(c.neighbors.p, 0, sizeof(uint32_t) * nbs, c.stream));
-    XRT_CUDA(&c, c.nb_count.reserve(c.nv));
-    XRT_CUDA(&c, cudaMemsetAsync(c.nb_count.p, 0, sizeof(uint32_t) * c.nv, c.stream));
     XRT_CUDA(&c, c.hash_sorter.reserve(c.nv));
   }
   // bindings: GenerateBinding_Kernel (BindingConstraint.cu:20-44) rest lengths from x0
@@ -1179,9 +1175,12 @@ xrt_status xrt_set_obstacle_targets(xrt_ctx* h, const float* pos) {
     return XRT_ERR_STATE;
   }
   cudaSetDevice(c.device);
-  std::vector<float4> t(c.onv);
-  for (uint32_t i = 0; i < c.onv; ++i) t[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0);
-  XRT_CUDA(&c, cudaMemcpyAsync(c.ox.p, t.data(), sizeof(float4) * c.onv, cudaMemcpyHostToDevice, c.stream));
+  // one copy of the caller's packed xyz, unpacked on the device; the call returns once the
+  // caller's buffer has been read
+  XRT_CUDA(&c, c.stage3.reserve(3 * (size_t)c.onv));
+  XRT_CUDA(&c, cudaMemcpyAsync(c.stage3.p, pos, 3 * sizeof(float) * (size_t)c.onv,
+                               cudaMemcpyHostToDevice, c.stream));
+  xrt::launch_unpack_xyz(c.stage3.p, c.ox.p, c.onv, 0.0f, c.stream);
   XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
   return XRT_OK;
 }

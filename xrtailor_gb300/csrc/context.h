@@ -465,7 +465,7 @@ struct Context {
   DBuf<float4> ee_a, ee_b, ee_c;     // {dist, p2}, {q2, s}, {fn, t}
   // particle hash
   DBuf<uint32_t> hash_key, hash_val, cell_start, cell_end, neighbors;
-  DBuf<uint32_t> nb_count;  // entries of each vertex's neighbor list (before its terminator)
+  DBuf<float> stage3;  // packed xyz staging of the C ABI's host copies
   RadixSort hash_sorter;
   // obstacle
   DBuf<float4> ox0, ox, ox1, on, on1;
@@ -606,6 +606,9 @@ void launch_fem(Context& c, const FrameConst& k, bool reset_lambda, int phase_st
 void fem_release(Context& c);
 size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes);
 size_t tile_smem_fwd(const TiledSet& T, bool stretch);  // the forward stretch / bend kernels
+// float4 -> packed xyz (12 B per element) and back (w set to `w`), for host copies.
+void launch_pack_xyz(const float4* in, float* out, uint32_t n, cudaStream_t s);
+void launch_unpack_xyz(const float* in, float4* out, uint32_t n, float w, cudaStream_t s);
 // Sets T.block (256 / 512 threads) and T.resident; after configure_tile_kernels.
 cudaError_t choose_tile_block(TiledSet& T, bool bend);
 // tile-local Gauss-Seidel: all tiles of one tile color (range of executed tiles)

@@ -56,8 +56,7 @@ __global__ void k_cache_neighbors(const uint32_t* __restrict__ sidx,
                                   const uint32_t* __restrict__ cell_end,
                                   const float4* __restrict__ x, const float4* __restrict__ x_init,
                                   uint32_t nv, InstView I, uint32_t maxnb,
-                                  uint32_t* __restrict__ neighbors,
-                                  uint32_t* __restrict__ nb_count) {
+                                  uint32_t* __restrict__ neighbors) {
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= nv) return;
   const uint32_t id = sidx[tid];
@@ -84,15 +83,11 @@ __global__ void k_cache_neighbors(const uint32_t* __restrict__ sidx,
           if (nb != id && dot(dp, dp) < spacing2 && dot(d0, d0) > d2) {
             neighbors[ni] = nb;
             ni += nv;
-            if (ni >= limit) {
-              nb_count[id] = maxnb;
-              return;
-            }
+            if (ni >= limit) return;
           }
         }
       }
   if (ni < limit) neighbors[ni] = kNone;
-  nb_count[id] = (uint32_t)((ni - id) / nv);  // entries before the terminator
 }
 
 __device__ __forceinline__ f3 friction_of(float mu, f3 correction, f3 rel_vel) {
@@ -108,123 +103,60 @@ __device__ __forceinline__ f3 friction_of(float mu, f3 correction, f3 rel_vel) {
   return fr;
 }
 
-// CollideParticles_Kernel + ApplyDeltas, one warp per 32 consecutive vertices.  The warp
-// flattens its vertices' neighbor slots (slot order within a vertex, vertices in order) and
-// evaluates them kRound pairs at a time, kRound / 32 per lane with all their loads in flight
-// (neighbor ids, then the neighbors' positions), so the pair arithmetic runs on full warps
-// whatever the spread of neighbor counts (0 to 64) and a round costs two dependent memory
-// trips; each vertex then folds its own pairs' terms in slot order, the reference's summation
-// order, from shared memory.
-constexpr int kCollideWarps = 8;
-constexpr int kPairsPerLane = 4;
-constexpr uint32_t kRound = 32u * kPairsPerLane;
-
-struct CollidePair {
-  float ax, ay, az, bx, by, bz;  // w_i * common and w_i * friction of the pair
-  int hit;                       // within the diameter (counted)
-};
-
-__global__ void __launch_bounds__(32 * kCollideWarps, 3) k_collide(
-    const float4* __restrict__ x_in, float4* __restrict__ x_out, const float4* __restrict__ x0,
-    const uint32_t* __restrict__ neighbors, const uint32_t* __restrict__ nb_count, uint32_t nv,
-    InstView I, float mu, float relaxation) {
-  __shared__ float4 s_p[kCollideWarps][32];        // predicted position, inverse mass
-  __shared__ float4 s_v[kCollideWarps][32];        // x - x0, diameter
-  __shared__ uint32_t s_off[kCollideWarps][33];    // first flattened pair of each lane; total
-  __shared__ CollidePair s_pair[kCollideWarps][kRound];
+__global__ void k_collide(const float4* __restrict__ x_in, float4* __restrict__ x_out,
+                          const float4* __restrict__ x0, const uint32_t* __restrict__ neighbors,
+                          uint32_t nv, uint32_t maxnb, InstView I, float mu, float relaxation) {
   pdl_release();
   pdl_wait();
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t base = (blockIdx.x * kCollideWarps + warp) * 32u;
-  if (base >= nv) return;  // whole warps only: every lane below stays to the end
-  const uint32_t id = base + lane;
-  const bool mine = id < nv;
-  float4 pi = make_float4(0, 0, 0, 0);
-  f3 vel_i = mk3(0, 0, 0);
-  float diameter = 0.0f;
-  uint32_t c = 0;
-  if (mine) {
-    pi = x_in[id];
-    vel_i = mk3(pi) - mk3(x0[id]);
-    diameter = inst_rec(I, inst_index(I, id)).diameter;
-    c = nb_count[id];
-  }
-  uint32_t off = c;  // inclusive scan, then exclusive
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, off, d);
-    if (lane >= (uint32_t)d) off += y;
-  }
-  const uint32_t total = __shfl_sync(0xFFFFFFFFu, off, 31);
-  off -= c;
-  s_p[warp][lane] = pi;
-  s_v[warp][lane] = mk4(vel_i, diameter);
-  s_off[warp][lane] = off;
-  if (lane == 0) s_off[warp][32] = total;
-  __syncwarp();
+  const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= nv) return;
+  const float diameter = inst_rec(I, inst_index(I, id)).diameter;
+  const float4 pi = x_in[id];
+  const f3 pred_i = mk3(pi);
+  const f3 vel_i = pred_i - mk3(x0[id]);
+  const float w_i = pi.w;
   f3 pd = mk3(0, 0, 0);
   int cnt = 0;
-  for (uint32_t start = 0; start < total; start += kRound) {
-    uint32_t own[kPairsPerLane], nb[kPairsPerLane];
+  // Neighbor slots are read a batch at a time (ids, then positions, all loads of a batch in
+  // flight); the list ends at the first id >= nv (reference: j > num_particles; j == nv never
+  // occurs) and the batch is then processed in slot order.
+  constexpr uint32_t kBatch = 8;
+  bool done = false;
+  for (uint32_t base = 0; base < maxnb && !done; base += kBatch) {
+    uint32_t nb[kBatch];
 #pragma unroll
-    for (int r = 0; r < kPairsPerLane; ++r) {  // owners and neighbor ids
-      const uint32_t p = start + (uint32_t)r * 32u + lane;
-      uint32_t o = 0;  // the last lane whose pairs start at or before p
+    for (uint32_t r = 0; r < kBatch; ++r)
+      nb[r] = base + r < maxnb ? neighbors[(uint64_t)(base + r) * nv + id] : nv;
+    float4 pj[kBatch];
 #pragma unroll
-      for (uint32_t step = 16; step > 0; step >>= 1)
-        if (s_off[warp][o + step] <= p) o += step;
-      own[r] = o;
-      nb[r] = p < total ? neighbors[(uint64_t)(p - s_off[warp][o]) * nv + base + o] : nv;
-    }
-    float4 pj[kPairsPerLane], qj[kPairsPerLane];
+    for (uint32_t r = 0; r < kBatch; ++r) pj[r] = nb[r] < nv ? x_in[nb[r]] : make_float4(0, 0, 0, 0);
 #pragma unroll
-    for (int r = 0; r < kPairsPerLane; ++r) {  // the neighbors' positions, all in flight
-      pj[r] = nb[r] < nv ? x_in[nb[r]] : make_float4(0, 0, 0, 0);
-      qj[r] = nb[r] < nv ? x0[nb[r]] : make_float4(0, 0, 0, 0);
-    }
-#pragma unroll
-    for (int r = 0; r < kPairsPerLane; ++r) {
-      CollidePair out{0, 0, 0, 0, 0, 0, 0};
-      if (nb[r] < nv) {
-        const float4 po = s_p[warp][own[r]];
-        const float4 vo = s_v[warp][own[r]];
-        const float w_i = po.w;
-        const float denom = w_i + pj[r].w;
-        if (denom > 0) {
-          const f3 pred_i = mk3(po), pred_j = mk3(pj[r]);
-          const f3 diff = pred_i - pred_j;
-          const float distance = length(diff);
-          if (distance < vo.w) {
-            const f3 gradient = diff / (distance + kEps);
-            const float lambda = (distance - vo.w) / denom;
-            const f3 common = lambda * gradient;
-            const f3 a = w_i * common;
-            const f3 rel = mk3(vo) - (pred_j - mk3(qj[r]));
-            const f3 b = w_i * friction_of(mu, common, rel);
-            out = CollidePair{a.x, a.y, a.z, b.x, b.y, b.z, 1};
-          }
-        }
+    for (uint32_t r = 0; r < kBatch; ++r) {
+      if (done) break;
+      const uint32_t j = nb[r];
+      if (j >= nv) {
+        done = true;
+        break;
       }
-      s_pair[warp][(uint32_t)r * 32u + lane] = out;
+      const float denom = w_i + pj[r].w;
+      if (denom <= 0) continue;
+      const f3 pred_j = mk3(pj[r]);
+      const f3 diff = pred_i - pred_j;
+      const float distance = length(diff);
+      if (distance >= diameter) continue;
+      const f3 gradient = diff / (distance + kEps);
+      const float lambda = (distance - diameter) / denom;
+      const f3 common = lambda * gradient;
+      ++cnt;
+      pd = pd - w_i * common;
+      const f3 rel = vel_i - (pred_j - mk3(x0[j]));
+      pd = pd + w_i * friction_of(mu, common, rel);
     }
-    __syncwarp();
-    const uint32_t lo = off > start ? off : start;
-    const uint32_t hi = min(off + c, start + kRound);
-    for (uint32_t q = lo; q < hi; ++q) {
-      const CollidePair& r = s_pair[warp][q - start];
-      if (r.hit) {
-        ++cnt;
-        pd = pd - mk3(r.ax, r.ay, r.az);
-        pd = pd + mk3(r.bx, r.by, r.bz);
-      }
-    }
-    __syncwarp();
   }
-  if (!mine) return;
-  f3 q = mk3(pi);
+  f3 q = pred_i;
   const float count = (float)cnt;
   if (count > 0.0f) q = q + pd / count * relaxation;
-  x_out[id] = mk4(q, pi.w);
+  x_out[id] = mk4(q, w_i);
 }
 
 }  // namespace
@@ -243,12 +175,12 @@ void launch_hash(Context& c) {
   k_cell_bounds<<<grid_for(nv), kBlock, 0, c.stream>>>(skey, nv, c.cell_start.p, c.cell_end.p);
   k_cache_neighbors<<<grid_for(nv), kBlock, 0, c.stream>>>(
       sidx, c.cell_start.p, c.cell_end.p, c.x.p, c.x_init.p, nv, I,
-      (uint32_t)c.params.max_neighbor_size, c.neighbors.p, c.nb_count.p);
+      (uint32_t)c.params.max_neighbor_size, c.neighbors.p);
 }
 
 void launch_collide(Context& c, const FrameConst& k) {
-  launch_k(c.pdl, k_collide, grid_for(c.nv, 32 * kCollideWarps), 32 * kCollideWarps, 0, c.stream,
-           c.x.p, c.x_alt.p, c.x0.p, c.neighbors.p, c.nb_count.p, c.nv, c.inst_view(), k.friction,
+  launch_k(c.pdl, k_collide, grid_for(c.nv), kBlock, 0, c.stream, c.x.p, c.x_alt.p, c.x0.p,
+           c.neighbors.p, c.nv, (uint32_t)c.params.max_neighbor_size, c.inst_view(), k.friction,
            k.relaxation);
 }
 

@@ -545,6 +545,33 @@ cudaError_t choose_tile_block(TiledSet& T, bool bend) {
   return cudaSuccess;
 }
 
+// float4 {x, y, z, w} <-> packed xyz, for the host copies of the C ABI (one DMA of 12 B per
+// element instead of 16 B and a host-side repacking loop).
+static __global__ void k_pack_xyz(const float4* __restrict__ in, float* __restrict__ out,
+                                  uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 v = in[i];
+  out[3 * (size_t)i] = v.x;
+  out[3 * (size_t)i + 1] = v.y;
+  out[3 * (size_t)i + 2] = v.z;
+}
+
+static __global__ void k_unpack_xyz(const float* __restrict__ in, float4* __restrict__ out,
+                                    uint32_t n, float w) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = make_float4(in[3 * (size_t)i], in[3 * (size_t)i + 1], in[3 * (size_t)i + 2], w);
+}
+
+void launch_pack_xyz(const float4* in, float* out, uint32_t n, cudaStream_t s) {
+  if (n) k_pack_xyz<<<grid_for(n), kBlock, 0, s>>>(in, out, n);
+}
+
+void launch_unpack_xyz(const float* in, float4* out, uint32_t n, float w, cudaStream_t s) {
+  if (n) k_unpack_xyz<<<grid_for(n), kBlock, 0, s>>>(in, out, n, w);
+}
+
 void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, bool reset_lambda) {
   const uint32_t nt = tiles.end - tiles.begin;
   if (nt == 0) return;
