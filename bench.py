@@ -447,6 +447,7 @@ def run_batched(args, local_rank):
     s = make(tile, range(len(gs)))
     if tuned is not None:
         s.set_dependent_launch(tuned["dependent_launch"])
+        s.set_vertex_block(tuned["vertex_block"])
     setup_s = time.perf_counter() - t_setup
     sz = s.sizes()
     V = sz.num_vertices
@@ -582,7 +583,7 @@ def run_batched(args, local_rank):
         "phase_ms_per_frame": phases,
         "setup_s": {"scenes": round(gen_s, 1), "autotune": round(tune_s, 1),
                     "context": round(setup_s, 1), "plain_sample": round(plain_wall, 1)},
-        "autotune_trials_ms_per_frame": [[t, dd, round(ms, 2)] for t, dd, ms in trials],
+        "autotune_trials_ms_per_frame": [[t, dd, vb, round(ms, 2)] for t, dd, vb, ms in trials],
         "clocks": clocks.summary(),
         "wall_s": wall,
     }

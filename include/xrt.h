@@ -232,6 +232,11 @@ xrt_status xrt_set_dependent_launch(xrt_ctx* ctx, int32_t enabled);
  * (xrt_set_coloring) always runs as per-color launches.  No reference counterpart (the
  * reference launches one kernel per color, BasicSolver.cu:131-134). */
 xrt_status xrt_set_tile_vertices(xrt_ctx* ctx, uint32_t tile_vertices);
+/* Threads per block of the per-vertex substep kernels (predict / finalize, particle collide,
+ * LRA + VF and EE + ApplyDeltas): 64 to 512, a multiple of 32 (default 256).  Results are
+ * identical for every value.  No reference counterpart (a launch option of this library; the
+ * reference launches its per-vertex kernels with fixed 256-thread blocks). */
+xrt_status xrt_set_vertex_block(xrt_ctx* ctx, uint32_t threads);
 
 /* ---- per-phase GPU timing (replaces Timer / ScopedTimerGPU, utils/Timer.hpp:67-114) -------- */
 #define XRT_NUM_PHASES 16

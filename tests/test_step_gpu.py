@@ -208,6 +208,25 @@ def test_dependent_launch_is_bit_identical(xrt, graph):
     np.testing.assert_array_equal(bits(runs[0]), bits(runs[1]))
 
 
+def test_vertex_block_is_bit_identical(xrt):
+    """The per-vertex kernels' block size (xrt_set_vertex_block, an autotuner knob) changes only
+    how vertices are grouped into blocks: every block size gives the oracle's bits."""
+    cloth, obs = small_scene(40, attached=scenes.two_corner_pins(40))
+    p = _params(num_substeps=3, num_iterations=5, num_collision_passes=3)
+    runs = []
+    for block in (64, 128, 512):
+        g, o = make_pair(p, [cloth], [obs], particle_diameter=0.02)
+        g.set_vertex_block(block)
+        for _ in range(3):
+            g.step()
+            o.step()
+        _close(g, o, exact=True)
+        runs.append(g.host_positions())
+    np.testing.assert_array_equal(bits(runs[0]), bits(runs[2]))
+    with pytest.raises(XrtError):
+        g.set_vertex_block(100)
+
+
 def test_pbd_repulsion_frame(xrt):
     cloth, obs = small_scene(14)
     p = _params(solve_bending=0, pbd_repulsion=1, pbd_thickness=1e-3, repulsion_relaxation=0.25,

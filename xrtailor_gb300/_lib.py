@@ -183,6 +183,7 @@ SIGNATURES = {
     "xrt_set_graph_mode": (C.c_int32, [P, C.c_int32]),
     "xrt_set_dependent_launch": (C.c_int32, [P, C.c_int32]),
     "xrt_set_tile_vertices": (C.c_int32, [P, C.c_uint32]),
+    "xrt_set_vertex_block": (C.c_int32, [P, C.c_uint32]),
     "xrt_get_sizes": (C.c_int32, [P, C.POINTER(Sizes)]),
     "xrt_set_profiling": (C.c_int32, [P, C.c_int32]),
     "xrt_get_profile": (C.c_int32, [P, C.POINTER(Profile)]),

@@ -1,13 +1,17 @@
 """Launch-configuration autotuner for the Swift step.
 
-The two knobs that change the frame time without changing what the step computes (every
-candidate is a valid coloring of the same constraints; results are then those of that coloring):
+The knobs that change the frame time without changing what the step computes (every candidate
+is a valid coloring of the same constraints; results are then those of that coloring):
   * tile size of the tile-local Gauss-Seidel schedule (xrt_set_tile_vertices): small tiles keep
     more SMs busy when one garment is latency-bound, large tiles cut halo traffic and barriers
     per constraint when a batch of garments is throughput-bound;
-  * programmatic dependent launch (xrt_set_dependent_launch).
+  * programmatic dependent launch (xrt_set_dependent_launch);
+  * threads per block of the per-vertex kernels (xrt_set_vertex_block), tuned at the chosen tile
+    size and launch mode; results are identical for every value.
 The block size of the tile kernels (256 / 512 threads) and their one- or two-lane bend
-projection follow from the tile schedule inside the library.
+projection follow from the tile schedule inside the library.  The LBVH keeps one triangle per
+leaf, as the reference builds it (BVH.cu:689-694): the candidate lists must equal the
+reference's leaf-by-leaf traversal, so the leaf size is not a free knob here.
 
 Each candidate is built by the caller's `make(tile_vertices)` (a started ClothSolver), stepped
 `warmup` frames, then `frames` frames timed with CUDA events on the library's stream; the
@@ -16,7 +20,8 @@ instances (see `subset`), which is what the batched benchmark does.
 """
 import numpy as np
 
-DEFAULT_TILES = (256, 512, 1024, 2048)
+DEFAULT_TILES = (256, 512, 768, 1024, 2048)
+DEFAULT_VERTEX_BLOCKS = (128, 256, 512)
 
 
 def time_frames(solver, frames, targets=None, first=0):
@@ -43,8 +48,11 @@ def time_frames(solver, frames, targets=None, first=0):
     return sum(a.elapsed_time(b) for a, b in ev) / frames
 
 
-def tune(make, tiles=DEFAULT_TILES, pdl=(True, False), frames=3, warmup=1, targets=None):
-    """Returns ({"tile_vertices": t, "dependent_launch": d}, [(tile, pdl, ms_per_frame), ...])."""
+def tune(make, tiles=DEFAULT_TILES, pdl=(True, False), frames=3, warmup=1, targets=None,
+         vertex_blocks=DEFAULT_VERTEX_BLOCKS):
+    """Returns ({"tile_vertices": t, "dependent_launch": d, "vertex_block": b},
+    [(tile, pdl, vertex block, ms_per_frame), ...]).  Tile size and launch mode are tuned at the
+    default vertex block (256), then the vertex block at the chosen pair."""
     trials = []
     for t in tiles:
         s = make(t)
@@ -52,10 +60,20 @@ def tune(make, tiles=DEFAULT_TILES, pdl=(True, False), frames=3, warmup=1, targe
             s.set_dependent_launch(d)
             time_frames(s, warmup, targets, first=0)
             ms = time_frames(s, frames, targets, first=warmup)
-            trials.append((t, d, ms))
+            trials.append((t, d, 256, ms))
         s.close()
-    t, d, _ = min(trials, key=lambda r: r[2])
-    return {"tile_vertices": t, "dependent_launch": d}, trials
+    t, d, _, _ = min(trials, key=lambda r: r[3])
+    s = make(t)
+    s.set_dependent_launch(d)
+    for b in vertex_blocks:
+        if b == 256:
+            continue
+        s.set_vertex_block(b)
+        time_frames(s, warmup, targets, first=0)
+        trials.append((t, d, b, time_frames(s, frames, targets, first=warmup)))
+    s.close()
+    best = min((r for r in trials if r[0] == t and r[1] == d), key=lambda r: r[3])
+    return {"tile_vertices": t, "dependent_launch": d, "vertex_block": best[2]}, trials
 
 
 def subset(n_items, count):

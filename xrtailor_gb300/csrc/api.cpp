@@ -1365,6 +1365,18 @@ xrt_status xrt_set_dependent_launch(xrt_ctx* h, int32_t enabled) {
   return XRT_OK;
 }
 
+xrt_status xrt_set_vertex_block(xrt_ctx* h, uint32_t threads) {
+  if (!h) return XRT_ERR_INVALID_ARGUMENT;
+  Context& c = h->c;
+  if (threads < 64 || threads > 512 || threads % 32 != 0) {
+    c.set_error("vertex block must be 64 to 512 threads, a multiple of 32");
+    return XRT_ERR_INVALID_ARGUMENT;
+  }
+  c.vertex_block = threads;
+  c.graph_dirty = true;
+  return XRT_OK;
+}
+
 xrt_status xrt_set_tile_vertices(xrt_ctx* h, uint32_t tile_vertices) {
   if (!h) return XRT_ERR_INVALID_ARGUMENT;
   Context& c = h->c;

@@ -466,6 +466,7 @@ struct Context {
   // particle hash
   DBuf<uint32_t> hash_key, hash_val, cell_start, cell_end, neighbors;
   DBuf<float> stage3;  // packed xyz staging of the C ABI's host copies
+  uint32_t vertex_block = 256;  // threads per block of the per-vertex substep kernels
   RadixSort hash_sorter;
   // obstacle
   DBuf<float4> ox0, ox, ox1, on, on1;

@@ -179,7 +179,8 @@ void launch_hash(Context& c) {
 }
 
 void launch_collide(Context& c, const FrameConst& k) {
-  launch_k(c.pdl, k_collide, grid_for(c.nv), kBlock, 0, c.stream, c.x.p, c.x_alt.p, c.x0.p,
+  launch_k(c.pdl, k_collide, grid_for(c.nv, c.vertex_block), c.vertex_block, 0, c.stream,
+           c.x.p, c.x_alt.p, c.x0.p,
            c.neighbors.p, c.nv, (uint32_t)c.params.max_neighbor_size, c.inst_view(), k.friction,
            k.relaxation);
 }

@@ -362,6 +362,10 @@ class ClothSolver:
         start()."""
         L.check(self._lib.xrt_set_tile_vertices(self._h, int(n)), self._h, "tile vertices")
 
+    def set_vertex_block(self, threads: int):
+        """Threads per block of the per-vertex substep kernels (64 to 512, default 256)."""
+        L.check(self._lib.xrt_set_vertex_block(self._h, int(threads)), self._h, "vertex block")
+
     def set_dependent_launch(self, enabled: bool):
         """Programmatic dependent launch of the substep kernels (default on)."""
         L.check(self._lib.xrt_set_dependent_launch(self._h, int(bool(enabled))), self._h,
