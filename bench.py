@@ -214,21 +214,39 @@ def run_ours(args, rank, local_rank, world):
     p = scenes.scene_params(sc)
     if args.quality:
         _quality(p)
-    solver = ClothSolver(p, device=local_rank)
-    if args.tile_vertices is not None:
-        solver.set_tile_vertices(args.tile_vertices)
     fem = args.material == "fem" or args.quality
-    if fem:
-        solver.set_fem_material(ClothSolver.fem_material())
-    _setup(solver, sc)
-    s = solver.sizes()
-    V, S = s.num_vertices, p.num_substeps
     frames_needed = args.warmup + 2 * args.steps + 8
     tg = _targets(sc, frames_needed)
     dev_targets = None
     if tg is not None:
         dev_targets = torch.tensor(np.stack(tg), device=f"cuda:{local_rank}")
         torch.cuda.synchronize()
+
+    def make(tile):
+        q = ClothSolver(p, device=local_rank)
+        if tile is not None:
+            q.set_tile_vertices(tile)
+        if fem:
+            q.set_fem_material(ClothSolver.fem_material())
+        _setup(q, sc)
+        return q
+
+    # launch configuration of a single-garment workload: autotuned on the workload itself
+    tuned, trials, tune_s = None, [], 0.0
+    if args.tile_vertices is None and args.tune_instances > 0 and not args.quality:
+        from xrtailor_gb300 import autotune
+        t0 = time.perf_counter()
+        tuned, trials = autotune.tune(
+            make, tiles=(128, 256, 512), frames=8, warmup=3, vertex_blocks=(64, 128, 256),
+            targets=(None if dev_targets is None else
+                     (lambda k: dev_targets[k % frames_needed].data_ptr())))
+        tune_s = time.perf_counter() - t0
+    solver = make(args.tile_vertices if tuned is None else tuned["tile_vertices"])
+    if tuned is not None:
+        solver.set_dependent_launch(tuned["dependent_launch"])
+        solver.set_vertex_block(tuned["vertex_block"])
+    s = solver.sizes()
+    V, S = s.num_vertices, p.num_substeps
     _, _, stream_ptr = solver.device_state()
     stream = torch.cuda.ExternalStream(stream_ptr, device=f"cuda:{local_rank}")
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
@@ -339,6 +357,9 @@ def run_ours(args, rank, local_rank, world):
         "config": dict(_plain_config(args.workload, p, args.quality, fem),
                        parallelism="replicas" if world > 1 else "single"),
         "schedule": {"stretch_colors": s.num_stretch_colors, "bend_colors": s.num_bend_colors},
+        "launch": tuned or {"tile_vertices": args.tile_vertices or 256},
+        "autotune": {"seconds": round(tune_s, 1),
+                     "trials_ms_per_frame": [[t, d, b, round(ms, 3)] for t, d, b, ms in trials]},
         "e2e": {"value": e2e, "unit": "vertex-substeps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(out.nbytes)},
         "gpu_launches": int(s.launches_per_frame) * args.steps,
@@ -954,7 +975,8 @@ def _garment_summary(args, local_rank):
     a.workload, a.quality, a.material, a.tile_vertices = "garment", False, "swift", None
     a.steps = min(args.steps, 20)
     r = run_ours(a, 0, local_rank, 1)
-    keep = ("value", "ms_per_step", "e2e", "roofline", "frame_bandwidth_gbs", "clocks", "config")
+    keep = ("value", "ms_per_step", "e2e", "roofline", "frame_bandwidth_gbs", "clocks", "config",
+            "launch", "autotune")
     out = {k: r[k] for k in keep}
     out["steps"] = a.steps
     return out

@@ -233,7 +233,7 @@ xrt_status xrt_set_dependent_launch(xrt_ctx* ctx, int32_t enabled);
  * reference launches one kernel per color, BasicSolver.cu:131-134). */
 xrt_status xrt_set_tile_vertices(xrt_ctx* ctx, uint32_t tile_vertices);
 /* Threads per block of the per-vertex substep kernels (predict / finalize, particle collide,
- * LRA + VF and EE + ApplyDeltas): 64 to 512, a multiple of 32 (default 256).  Results are
+ * LRA + VF and EE + ApplyDeltas): 64 to 512, a multiple of 32 (default 128).  Results are
  * identical for every value.  No reference counterpart (a launch option of this library; the
  * reference launches its per-vertex kernels with fixed 256-thread blocks). */
 xrt_status xrt_set_vertex_block(xrt_ctx* ctx, uint32_t threads);

@@ -21,7 +21,7 @@ instances (see `subset`), which is what the batched benchmark does.
 import numpy as np
 
 DEFAULT_TILES = (256, 512, 768, 1024, 2048)
-DEFAULT_VERTEX_BLOCKS = (128, 256, 512)
+DEFAULT_VERTEX_BLOCKS = (64, 128, 256)
 
 
 def time_frames(solver, frames, targets=None, first=0):
@@ -52,7 +52,7 @@ def tune(make, tiles=DEFAULT_TILES, pdl=(True, False), frames=3, warmup=1, targe
          vertex_blocks=DEFAULT_VERTEX_BLOCKS):
     """Returns ({"tile_vertices": t, "dependent_launch": d, "vertex_block": b},
     [(tile, pdl, vertex block, ms_per_frame), ...]).  Tile size and launch mode are tuned at the
-    default vertex block (256), then the vertex block at the chosen pair."""
+    default vertex block (128), then the vertex block at the chosen pair."""
     trials = []
     for t in tiles:
         s = make(t)
@@ -60,13 +60,13 @@ def tune(make, tiles=DEFAULT_TILES, pdl=(True, False), frames=3, warmup=1, targe
             s.set_dependent_launch(d)
             time_frames(s, warmup, targets, first=0)
             ms = time_frames(s, frames, targets, first=warmup)
-            trials.append((t, d, 256, ms))
+            trials.append((t, d, 128, ms))
         s.close()
     t, d, _, _ = min(trials, key=lambda r: r[3])
     s = make(t)
     s.set_dependent_launch(d)
     for b in vertex_blocks:
-        if b == 256:
+        if b == 128:
             continue
         s.set_vertex_block(b)
         time_frames(s, warmup, targets, first=0)

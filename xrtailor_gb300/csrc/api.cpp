@@ -771,21 +771,34 @@ static xrt_status upload_constraints(Context& c) {
     const std::vector<uint32_t>& local = kind == 0 ? c.s_local : c.b_local;
     const std::vector<int4>& meta = c.h_tile_meta[kind];
     std::vector<uint4> rec;
-    std::vector<uint32_t> ofs(meta.size());
-    for (size_t t = 0; t < meta.size(); ++t) {
-      const uint32_t c0 = (uint32_t)meta[t].z, nc = (uint32_t)meta[t].w;
+    std::vector<uint32_t> ofs(meta.size() + 1);
+    // one segment per tile (stretch) or per local color of a tile (bend): slots [c0, c0 + nc)
+    auto segment = [&](uint32_t c0, uint32_t nc) {
       const uint32_t n16 = xrt::tile_rec16(nc, arity), ids16 = (2 * arity * nc + 15) / 16;
-      ofs[t] = (uint32_t)rec.size();
+      const size_t at = rec.size();
       rec.resize(rec.size() + n16, make_uint4(0, 0, 0, 0));
-      uint16_t* ids = reinterpret_cast<uint16_t*>(rec.data() + ofs[t]);
-      float2* vals = reinterpret_cast<float2*>(rec.data() + ofs[t] + ids16);
+      uint16_t* ids = reinterpret_cast<uint16_t*>(rec.data() + at);
+      float2* vals = reinterpret_cast<float2*>(rec.data() + at + ids16);
       for (uint32_t j = 0; j < nc; ++j) {
         const uint32_t slot = c0 + j;
         for (int a = 0; a < arity; ++a) ids[arity * j + a] = (uint16_t)local[arity * slot + a];
         vals[j] = kind == 0 ? make_float2(c.h_rest[c.s_perm[slot]], c.h_scomp[c.s_perm[slot]])
                             : btc[slot];
       }
+    };
+    const std::vector<uint32_t>& lofs = c.h_tile_lofs[kind];
+    const uint32_t L = T.num_local;
+    for (size_t t = 0; t < meta.size(); ++t) {
+      const uint32_t c0 = (uint32_t)meta[t].z, nc = (uint32_t)meta[t].w;
+      ofs[t] = (uint32_t)rec.size();
+      if (kind == 0) {
+        segment(c0, nc);
+      } else {
+        for (uint32_t l = 0; l < L; ++l)
+          segment(c0 + lofs[t * (L + 1) + l], lofs[t * (L + 1) + l + 1] - lofs[t * (L + 1) + l]);
+      }
     }
+    ofs[meta.size()] = (uint32_t)rec.size();  // the end of the last tile's block
     if (rec.size() >= (1ull << 32)) {
       c.set_error("tile record blocks exceed 2^32 x 16 bytes");
       return XRT_ERR_EDGE_CAPACITY;
@@ -887,6 +900,18 @@ static xrt_status schedule_kind(Context& c, const std::vector<uint32_t>& idx, in
   }
   T.max_rec16 = 0;  // the largest record block of the forward tile kernels (TiledSet::rec)
   for (const int4& m : K.meta) T.max_rec16 = std::max(T.max_rec16, xrt::tile_rec16((uint32_t)m.w, arity));
+  T.max_seg16 = 0;  // bend: the largest local color's segment and tile block of segments
+  T.max_tile16 = 0;
+  for (size_t tt = 0; tt + 1 < S.foot_ptr.size(); ++tt) {
+    uint32_t sum = 0;
+    for (uint32_t l = 0; l < S.num_local; ++l) {
+      const size_t k = tt * S.num_local + l;
+      const uint32_t seg = xrt::color_seg16(S.lc_ptr[k + 1] - S.lc_ptr[k]);
+      T.max_seg16 = std::max(T.max_seg16, seg);
+      sum += seg;
+    }
+    T.max_tile16 = std::max(T.max_tile16, sum);
+  }
   XRT_CUDA(&c, upload(T.foot, S.foot, c.stream));
   XRT_CUDA(&c, upload(T.meta, K.meta, c.stream));
   XRT_CUDA(&c, upload(T.lofs, K.lofs, c.stream));
@@ -980,7 +1005,9 @@ xrt_status xrt_start(xrt_ctx* h) {
     const size_t smem = std::max(
         std::max(xrt::tile_smem_bytes(c.s_tiles, sizeof(int4) + sizeof(float)),
                  xrt::tile_smem_bytes(c.b_tiles, sizeof(int4) + sizeof(float2))),
-        std::max(xrt::tile_smem_fwd(c.s_tiles, true), xrt::tile_smem_fwd(c.b_tiles, false)));
+        std::max(xrt::tile_smem_fwd(c.s_tiles, true, false),
+                 std::max(xrt::tile_smem_fwd(c.b_tiles, false, true),
+                          xrt::tile_smem_fwd(c.b_tiles, false, false))));
     if (smem > 200 * 1024) {
       c.set_error("tile schedule needs more shared memory than a block has");
       return XRT_ERR_INVALID_MESH;

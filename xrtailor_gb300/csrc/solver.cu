@@ -221,46 +221,96 @@ __global__ void k_bend(const int4* __restrict__ idx, const float2* __restrict__ 
 // PAIR: two lanes per bend element (bend_project_pair), half the dependency chain per step, for
 // launches whose tiles are all resident at once (latency-bound); otherwise one lane per element
 // (fewer instructions in total, for launches with many waves of tiles).
+// Records: the tile's record block (TiledSet::rec) holds one segment per local color (16-bit
+// footprint-local ids, then float2 values, each padded to 16 bytes).
+//   one lane (throughput regime): the segments stream in by local color, each bulk-copied into
+//     one of two shared-memory buffers on its own mbarrier, two colors ahead of its use; a buffer
+//     is refilled right after the barrier that closes the color that read it.  Only two colors'
+//     records occupy shared memory, so more tiles fit on an SM.
+//   lane pairs (latency regime, every tile of the launch resident): the whole block comes in one
+//     bulk copy before the first color, so no color waits on a copy.
 template <int NT, bool PAIR>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
     const uint4* __restrict__ rec, const uint32_t* __restrict__ rec_ofs, float4* __restrict__ x,
     const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
     const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
-    uint32_t max_foot, uint32_t max_rec16, float dt, uint32_t* err) {
+    uint32_t max_foot, uint32_t max_seg16, uint32_t buf16, float dt, uint32_t* err) {
+  if (num_local == 0) return;  // no constraint in the schedule
   extern __shared__ float4 smem[];
-  const TileSmem m = tile_smem(smem, max_foot, max_rec16, 0, num_local);
+  float4* sx = smem;
+  // buf16 uint4 of records: one lane, two buffers of max_seg16; lane pairs, the largest block
+  uint4* buf = reinterpret_cast<uint4*>(sx + max_foot);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(buf + buf16);
+  uint32_t* so = reinterpret_cast<uint32_t*>(bar + 2);
+  uint32_t* sf = so + num_local + 1;
   const uint32_t t = tile_begin + blockIdx.x;
-  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, t, num_local, m.so);
-  const uint32_t nc = (uint32_t)f.m.w;
-  tile_records_start(m, rec, rec_ofs, t, tile_rec16(nc, 4));
+  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, t, num_local, so);
+  const uint32_t* tl = lofs + (size_t)t * (num_local + 1);
+  uint32_t src = 0;  // thread 0: the next segment's first uint4
+  auto issue = [&](uint32_t l) {  // thread 0: the copy of color l's segment
+    const uint32_t n = __ldg(&tl[l + 1]) - __ldg(&tl[l]);
+    const uint32_t seg = 2 * ((n + 1) / 2);
+    uint64_t* b = bar + (l & 1);
+    if (seg)
+      bulk_load_g2s(buf + (l & 1) * max_seg16, rec + src, 16u * seg, b);
+    else
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+    src += seg;
+  };
+  if (threadIdx.x == 0) {
+    src = __ldg(&rec_ofs[t]);
+    mbar_init(bar, 1);
+    mbar_init(bar + 1, 1);
+    if (PAIR) {  // the whole block at once (barrier 1 completes without a copy)
+      const uint32_t all = __ldg(&rec_ofs[t + 1]) - src;
+      if (all)
+        bulk_load_g2s(buf, rec + src, 16u * all, bar);
+      else
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+    } else {
+      issue(0);
+      if (num_local > 1) issue(1);
+    }
+  }
   pdl_wait();
-  tile_gather<NT>(f, x, m.sx, m.sf);
-  __syncthreads();
-  if (!tile_records_ready(m, err)) return;
-  const ushort4* sid = reinterpret_cast<const ushort4*>(m.srec);
-  const float2* st = reinterpret_cast<const float2*>(m.srec + (8 * nc + 15) / 16);
-  float4* sx = m.sx;
-  const uint32_t* so = m.so;
-  if (PAIR) {
-    // the loop trip count is warp-uniform so the pair exchanges run with full warps
-    const uint32_t lane0 = threadIdx.x & ~31u;
-    for (uint32_t l = 0; l < num_local; ++l) {
-      const uint32_t cb = 2 * so[l], ce = 2 * so[l + 1];
-      for (uint32_t base = cb + lane0; base < ce; base += NT) {
+  tile_gather<NT>(f, x, sx, sf);
+  __syncthreads();  // offsets, footprint and the barriers' initialisation are visible
+  // a wait that runs out raises the error; the block waits (bounded) for its copies in flight
+  // and leaves, the same in every thread
+  auto failed = [&](bool ok, uint32_t l) {
+    if (!__syncthreads_or(!ok)) return false;
+    if (threadIdx.x == 0) {
+      raise_error(err, kErrBulkCopy);
+      if (PAIR)  // the one copy of the whole block
+        mbar_wait_bounded(bar, 0, kBulkWaitLimit);
+      else
+        for (uint32_t k = l; k < l + 2 && k < num_local; ++k)
+          mbar_wait_bounded(bar + (k & 1), (k >> 1) & 1u, kBulkWaitLimit);
+    }
+    __syncthreads();
+    return true;
+  };
+  if (failed(mbar_wait_bounded(bar, 0, kBulkWaitLimit), PAIR ? num_local : 0)) return;
+  uint32_t at = 0;  // PAIR: the color's segment in the whole block
+  for (uint32_t l = 0; l < num_local; ++l) {
+    const uint4* cur = PAIR ? buf + at : buf + (l & 1) * max_seg16;
+    const uint32_t c0 = so[l], n = so[l + 1] - c0;
+    const ushort4* sid = reinterpret_cast<const ushort4*>(cur);
+    const float2* st = reinterpret_cast<const float2*>(cur + (n + 1) / 2);
+    if (PAIR) {
+      // the loop trip count is warp-uniform so the pair exchanges run with full warps
+      const uint32_t lane0 = threadIdx.x & ~31u, ce = 2 * n;
+      for (uint32_t base = lane0; base < ce; base += NT) {
         const uint32_t s = base + (threadIdx.x & 31u);
         const bool active = s < ce;
-        const uint32_t j = active ? s >> 1 : cb >> 1;
+        const uint32_t j = active ? s >> 1 : 0;
         const ushort4 q = sid[j];
         const int4 b = make_int4(q.x, q.y, q.z, q.w);
         const float2 th = st[j];
         bend_project_pair(sx, b, th.x, th.y, dt, s & 1u, active);
       }
-      __syncthreads();
-    }
-  } else {
-    for (uint32_t l = 0; l < num_local; ++l) {
-      const uint32_t ce = so[l + 1];
-      for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
+    } else {
+      for (uint32_t j = threadIdx.x; j < n; j += NT) {
         const ushort4 b = sid[j];
         const float2 th = st[j];
         float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
@@ -270,11 +320,20 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
         sx[b.z] = a3;
         sx[b.w] = a4;
       }
-      __syncthreads();
     }
+    if (PAIR) {
+      at += color_seg16(n);
+      __syncthreads();
+      continue;
+    }
+    // the next color's records, then the barrier that closes this color
+    const bool ok = l + 1 >= num_local ||
+                    mbar_wait_bounded(bar + ((l + 1) & 1), ((l + 1) >> 1) & 1u, kBulkWaitLimit);
+    if (failed(ok, l + 1)) return;
+    if (threadIdx.x == 0 && l + 2 < num_local) issue(l + 2);  // into the buffer color l read
   }
   pdl_release();
-  tile_scatter<NT>((uint32_t)f.m.y, x, sx, m.sf);
+  tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
 }
 
 
@@ -443,14 +502,14 @@ __global__ void k_ee(const TailArgs a) {
 }  // namespace
 
 void launch_predict(Context& c, const FrameConst& k) {
-  launch_k(c.pdl, k_predict, grid_for(c.nv), kBlock, 0, c.stream, c.x.p, c.x0.p, c.v.p, c.nv, k.dt,
+  launch_k(c.pdl, k_predict, grid_for(c.nv, c.vertex_block), c.vertex_block, 0, c.stream, c.x.p, c.x0.p, c.v.p, c.nv, k.dt,
            k.gx, k.gy, k.gz);
 }
 
 void launch_finalize_predict(Context& c, const FrameConst& k, bool predict_next, bool normals) {
   auto kern = predict_next ? k_finalize<true, false>
                            : (normals ? k_finalize<false, true> : k_finalize<false, false>);
-  launch_k(c.pdl, kern, grid_for(c.nv), kBlock, 0, c.stream, c.x.p, c.x0.p, c.v.p, c.nv, k.dt,
+  launch_k(c.pdl, kern, grid_for(c.nv, c.vertex_block), c.vertex_block, 0, c.stream, c.x.p, c.x0.p, c.v.p, c.nv, k.dt,
            k.damping, k.gx, k.gy, k.gz, c.tri.p, c.vf_ptr.p, c.vf_list.p, c.n.p);
 }
 
@@ -516,12 +575,15 @@ size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes) {
          sizeof(uint32_t) * (T.num_local + 1) + sizeof(uint32_t) * T.max_foot;
 }
 
-// Shared memory of the forward tile kernels (TileSmem): footprint, record block, mbarrier slot,
-// the stretch multipliers, offsets and footprint ids.
-size_t tile_smem_fwd(const TiledSet& T, bool stretch) {
-  return sizeof(float4) * T.max_foot + 16 * (size_t)T.max_rec16 + 16 +
-         (stretch ? sizeof(float) * T.max_cons : 0) + sizeof(uint32_t) * (T.num_local + 1) +
-         sizeof(uint32_t) * T.max_foot;
+// Shared memory of the forward tile kernels: footprint, record block (stretch and paired bend:
+// the whole tile's; one-lane bend: two colors' segments), mbarrier slot(s), the stretch
+// multipliers, offsets and footprint ids.
+size_t tile_smem_fwd(const TiledSet& T, bool stretch, bool pair) {
+  const size_t records = stretch ? 16 * (size_t)T.max_rec16 + 16
+                                 : (pair ? 16 * (size_t)T.max_tile16 + 16
+                                         : 32 * (size_t)T.max_seg16 + 16);
+  return sizeof(float4) * T.max_foot + records + (stretch ? sizeof(float) * T.max_cons : 0) +
+         sizeof(uint32_t) * (T.num_local + 1) + sizeof(uint32_t) * T.max_foot;
 }
 
 // Block size of a tile set: 256 threads when the footprint fits 256 x kFootPerThread and a local
@@ -530,11 +592,14 @@ size_t tile_smem_fwd(const TiledSet& T, bool stretch) {
 cudaError_t choose_tile_block(TiledSet& T, bool bend) {
   const uint32_t lanes = bend ? 2 * T.max_step : T.max_step;
   T.block = (T.max_foot <= 256u * kFootPerThread && lanes <= 256) ? 256 : 512;
+  // one-lane bend blocks: 256 threads whenever the footprint allows (a large color takes a
+  // second pass, but twice the blocks fit on an SM)
+  T.block1 = bend && T.max_foot <= 256u * kFootPerThread ? 256 : T.block;
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
-  const size_t smem = tile_smem_fwd(T, !bend);
+  const size_t smem = tile_smem_fwd(T, !bend, true);
   const void* kern = bend ? (T.block == 256 ? (const void*)k_bend_tiles<256, true>
                                             : (const void*)k_bend_tiles<512, true>)
                           : (T.block == 256 ? (const void*)k_stretch_tiles<false, 256>
@@ -576,7 +641,7 @@ void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, boo
   const uint32_t nt = tiles.end - tiles.begin;
   if (nt == 0) return;
   const TiledSet& T = c.s_tiles;
-  const size_t smem = tile_smem_fwd(T, true);
+  const size_t smem = tile_smem_fwd(T, true, false);
   auto kern = T.block == 256 ? (reset_lambda ? k_stretch_tiles<true, 256> : k_stretch_tiles<false, 256>)
                              : (reset_lambda ? k_stretch_tiles<true, 512> : k_stretch_tiles<false, 512>);
   launch_k(c.pdl, kern, nt, T.block, smem, c.stream, T.rec.p, T.rec_ofs.p, c.s_lambda.p, c.x.p,
@@ -588,12 +653,17 @@ void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles) {
   const uint32_t nt = tiles.end - tiles.begin;
   if (nt == 0) return;
   const TiledSet& T = c.b_tiles;
-  const bool pair = nt <= T.resident;  // one wave: latency-bound, halve the chain
-  auto kern = T.block == 256 ? (pair ? k_bend_tiles<256, true> : k_bend_tiles<256, false>)
-                             : (pair ? k_bend_tiles<512, true> : k_bend_tiles<512, false>);
-  launch_k(c.pdl, kern, nt, T.block, tile_smem_fwd(T, false), c.stream, T.rec.p, T.rec_ofs.p,
-           c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin, T.num_local, T.max_foot, T.max_rec16,
-           k.dt, c.err.p);
+  // two lanes per element when the launch's tiles are all resident (latency-bound: halve the
+  // chain), or when every local color's lane pairs fit one pass of the block (the pairs then
+  // use lanes that would idle at the color's barrier)
+  const bool pair = nt <= T.resident || 2 * T.max_step <= T.block;
+  const uint32_t block = pair ? T.block : T.block1;
+  auto kern = block == 256 ? (pair ? k_bend_tiles<256, true> : k_bend_tiles<256, false>)
+                           : (pair ? k_bend_tiles<512, true> : k_bend_tiles<512, false>);
+  const uint32_t buf16 = pair ? T.max_tile16 : 2 * T.max_seg16;  // as tile_smem_fwd sizes it
+  launch_k(c.pdl, kern, nt, block, tile_smem_fwd(T, false, pair), c.stream, T.rec.p, T.rec_ofs.p,
+           c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin, T.num_local, T.max_foot, T.max_seg16,
+           buf16, k.dt, c.err.p);
 }
 
 // LRA phase with a free slot vertex: one launch per slot block in list order.  (With every slot
@@ -637,13 +707,13 @@ static TailArgs tail_args(Context& c, const FrameConst& k) {
 void launch_stage(Context& c, const FrameConst& k, bool lra, bool contacts) {
   if (!lra && !contacts) return;
   auto kern = lra ? (contacts ? k_stage<true, true> : k_stage<true, false>) : k_stage<false, true>;
-  launch_k(c.pdl, kern, grid_for(c.nv), kBlock, 0, c.stream, tail_args(c, k));
+  launch_k(c.pdl, kern, grid_for(c.nv, c.vertex_block), c.vertex_block, 0, c.stream, tail_args(c, k));
 }
 
 void launch_ee(Context& c, const FrameConst& k, bool contacts, bool bindings) {
   if (!contacts && !bindings) return;
   auto kern = contacts ? (bindings ? k_ee<true, true> : k_ee<true, false>) : k_ee<false, true>;
-  launch_k(c.pdl, kern, grid_for(c.nv), kBlock, 0, c.stream, tail_args(c, k));
+  launch_k(c.pdl, kern, grid_for(c.nv, c.vertex_block), c.vertex_block, 0, c.stream, tail_args(c, k));
 }
 
 }  // namespace xrt

@@ -363,7 +363,7 @@ class ClothSolver:
         L.check(self._lib.xrt_set_tile_vertices(self._h, int(n)), self._h, "tile vertices")
 
     def set_vertex_block(self, threads: int):
-        """Threads per block of the per-vertex substep kernels (64 to 512, default 256)."""
+        """Threads per block of the per-vertex substep kernels (64 to 512, default 128)."""
         L.check(self._lib.xrt_set_vertex_block(self._h, int(threads)), self._h, "vertex block")
 
     def set_dependent_launch(self, enabled: bool):
