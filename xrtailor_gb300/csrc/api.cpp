@@ -774,7 +774,7 @@ static xrt_status upload_constraints(Context& c) {
     std::vector<uint32_t> ofs(meta.size() + 1);
     // one segment per tile (stretch) or per local color of a tile (bend): slots [c0, c0 + nc)
     auto segment = [&](uint32_t c0, uint32_t nc) {
-      const uint32_t n16 = xrt::tile_rec16(nc, arity), ids16 = (2 * arity * nc + 15) / 16;
+      const uint32_t n16 = xrt::color_seg16(nc, arity), ids16 = (2 * arity * nc + 15) / 16;
       const size_t at = rec.size();
       rec.resize(rec.size() + n16, make_uint4(0, 0, 0, 0));
       uint16_t* ids = reinterpret_cast<uint16_t*>(rec.data() + at);
@@ -791,12 +791,9 @@ static xrt_status upload_constraints(Context& c) {
     for (size_t t = 0; t < meta.size(); ++t) {
       const uint32_t c0 = (uint32_t)meta[t].z, nc = (uint32_t)meta[t].w;
       ofs[t] = (uint32_t)rec.size();
-      if (kind == 0) {
-        segment(c0, nc);
-      } else {
-        for (uint32_t l = 0; l < L; ++l)
-          segment(c0 + lofs[t * (L + 1) + l], lofs[t * (L + 1) + l + 1] - lofs[t * (L + 1) + l]);
-      }
+      for (uint32_t l = 0; l < L; ++l)
+        segment(c0 + lofs[t * (L + 1) + l], lofs[t * (L + 1) + l + 1] - lofs[t * (L + 1) + l]);
+      (void)nc;
     }
     ofs[meta.size()] = (uint32_t)rec.size();  // the end of the last tile's block
     if (rec.size() >= (1ull << 32)) {
@@ -898,15 +895,13 @@ static xrt_status schedule_kind(Context& c, const std::vector<uint32_t>& idx, in
                                (int)c0, (int)(c1 - c0)));
     for (uint32_t l = 0; l <= S.num_local; ++l) K.lofs.push_back(S.lc_ptr[tt * S.num_local + l] - c0);
   }
-  T.max_rec16 = 0;  // the largest record block of the forward tile kernels (TiledSet::rec)
-  for (const int4& m : K.meta) T.max_rec16 = std::max(T.max_rec16, xrt::tile_rec16((uint32_t)m.w, arity));
-  T.max_seg16 = 0;  // bend: the largest local color's segment and tile block of segments
+  T.max_seg16 = 0;  // the largest local color's segment and tile block of segments
   T.max_tile16 = 0;
   for (size_t tt = 0; tt + 1 < S.foot_ptr.size(); ++tt) {
     uint32_t sum = 0;
     for (uint32_t l = 0; l < S.num_local; ++l) {
       const size_t k = tt * S.num_local + l;
-      const uint32_t seg = xrt::color_seg16(S.lc_ptr[k + 1] - S.lc_ptr[k]);
+      const uint32_t seg = xrt::color_seg16(S.lc_ptr[k + 1] - S.lc_ptr[k], (uint32_t)arity);
       T.max_seg16 = std::max(T.max_seg16, seg);
       sum += seg;
     }
@@ -1005,7 +1000,8 @@ xrt_status xrt_start(xrt_ctx* h) {
     const size_t smem = std::max(
         std::max(xrt::tile_smem_bytes(c.s_tiles, sizeof(int4) + sizeof(float)),
                  xrt::tile_smem_bytes(c.b_tiles, sizeof(int4) + sizeof(float2))),
-        std::max(xrt::tile_smem_fwd(c.s_tiles, true, false),
+        std::max(std::max(xrt::tile_smem_fwd(c.s_tiles, true, true),
+                          xrt::tile_smem_fwd(c.s_tiles, true, false)),
                  std::max(xrt::tile_smem_fwd(c.b_tiles, false, true),
                           xrt::tile_smem_fwd(c.b_tiles, false, false))));
     if (smem > 200 * 1024) {

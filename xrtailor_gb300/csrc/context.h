@@ -229,7 +229,7 @@ struct TiledSet {
   uint32_t max_cons = 0;                // most constraints in one tile
   uint32_t max_step = 0;                // most constraints in one local color of one tile
   uint32_t block = 512;                 // threads per tile block (256 or 512)
-  uint32_t block1 = 512;                // bend: threads per block of the one-lane kernel
+  uint32_t block1 = 512;                // threads per block of the streamed (one-lane) kernels
   uint32_t resident = 0;                // tile blocks the GPU holds at once (pair-mode bound)
   std::vector<ColorRange> tile_colors;  // ranges of executed tiles per tile color
   std::vector<uint32_t> tile_color_cons;  // constraints per tile color (profiling units)
@@ -240,23 +240,20 @@ struct TiledSet {
   // Records of the forward tile kernels, one 16-byte aligned block per executed tile: the
   // constraints' footprint-local vertex ids as 16-bit values (2 per stretch constraint, 4 per
   // bend element), padded to 16 bytes, then their float2 values (rest length and compliance /
-  // rest angle and compliance), padded to 16 bytes.  Stretch: one such block per tile, copied in
-  // one bulk copy; bend: one such segment per local color, in color order, copied color by
-  // color.
+  // rest angle and compliance), padded to 16 bytes: one such segment per local color, in color
+  // order, copied whole or color by color.
   DBuf<uint4> rec;
   DBuf<uint32_t> rec_ofs;               // per executed tile: first uint4 of its block; + the end
-  uint32_t max_rec16 = 0;               // largest block, in uint4
-  uint32_t max_seg16 = 0;               // bend: largest local color's segment, in uint4
-  uint32_t max_tile16 = 0;              // bend: largest tile's block of color segments, in uint4
+  uint32_t max_seg16 = 0;               // largest local color's segment, in uint4
+  uint32_t max_tile16 = 0;              // largest tile's block of color segments, in uint4
 };
 
-// uint4 units of one local color's record segment (bend): ids, then values, each padded.
-__host__ __device__ inline uint32_t color_seg16(uint32_t n) { return 2 * ((n + 1) / 2); }
-
-// uint4 units of a tile's record block: `arity` 16-bit ids and a float2 per constraint.
-__host__ __device__ inline uint32_t tile_rec16(uint32_t nc, uint32_t arity) {
-  return (2 * arity * nc + 15) / 16 + (8 * nc + 15) / 16;
+// uint4 units of one local color's record segment of n constraints: `arity` 16-bit ids each,
+// then a float2 each, both padded to 16 bytes.
+__host__ __device__ inline uint32_t color_seg16(uint32_t n, uint32_t arity) {
+  return (2 * arity * n + 15) / 16 + (8 * n + 15) / 16;
 }
+
 
 // One constraint kind of the FEM fabric: its schedule (as the stretch / bend kinds') and the
 // slot-ordered vertex ids (footprint-local when tiled).
@@ -615,7 +612,7 @@ void launch_fem(Context& c, const FrameConst& k, bool reset_lambda, int phase_st
 void fem_release(Context& c);
 size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes);
 // the forward stretch / bend kernels (bend: lane pairs or one lane)
-size_t tile_smem_fwd(const TiledSet& T, bool stretch, bool pair);
+size_t tile_smem_fwd(const TiledSet& T, bool stretch, bool whole);
 // float4 -> packed xyz (12 B per element) and back (w set to `w`), for host copies.
 void launch_pack_xyz(const float4* in, float* out, uint32_t n, cudaStream_t s);
 void launch_unpack_xyz(const float* in, float4* out, uint32_t n, float w, cudaStream_t s);

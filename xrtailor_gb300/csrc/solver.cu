@@ -100,104 +100,114 @@ __global__ void k_stretch(const int4* __restrict__ con, float* __restrict__ lamb
 // prologue / gather / scatter helpers in project_dev.cuh).  The tile's footprint is staged in
 // shared memory, its local colors run in order with a block barrier between them, and the
 // footprint is written back.  Tiles of one tile color have disjoint footprints.
-// Shared memory of a tile launch: footprint positions, the tile's record block, its mbarrier,
-// the multipliers (stretch), then the num_local + 1 local-color offsets and the footprint ids.
+// Shared memory of a tile launch: footprint positions, the tile's records (its whole block, or
+// two local colors' segments), two mbarriers, the multipliers (stretch), then the num_local + 1
+// local-color offsets and the footprint ids.
 // Prologue before pdl_wait (setup-time data only): the tile's metadata, offsets and footprint
 // vertex ids (kFootPerThread per thread in registers, so the gather and the write-back each
-// issue all their loads and stores at once), and one bulk copy of the tile's record block
+// issue all their loads and stores at once), and the first bulk copies of the tile's records
 // (TiledSet::rec: 16-bit footprint-local ids, then float2 values) into shared memory, completed
-// on an mbarrier while the predecessor grid drains and the footprint is gathered.  NT threads
-// per block: 512 for footprints up to 4,096 vertices, 256 (twice the resident blocks per SM) up
-// to 2,048.
-struct TileSmem {
-  float4* sx;
-  uint4* srec;
-  uint64_t* bar;
-  float* sl;
-  uint32_t* so;
-  uint32_t* sf;
-};
-
-__device__ __forceinline__ TileSmem tile_smem(float4* smem, uint32_t max_foot, uint32_t max_rec16,
-                                              uint32_t max_lambda, uint32_t num_local) {
-  TileSmem m;
-  m.sx = smem;
-  m.srec = reinterpret_cast<uint4*>(m.sx + max_foot);
-  m.bar = reinterpret_cast<uint64_t*>(m.srec + max_rec16);
-  m.sl = reinterpret_cast<float*>(m.bar + 2);
-  m.so = reinterpret_cast<uint32_t*>(m.sl + max_lambda);
-  m.sf = m.so + num_local + 1;
-  return m;
-}
-
-// Thread 0 starts the copy of tile t's record block (n16 uint4).
-__device__ __forceinline__ void tile_records_start(const TileSmem& m, const uint4* __restrict__ rec,
-                                                   const uint32_t* __restrict__ rec_ofs,
-                                                   uint32_t t, uint32_t n16) {
-  if (threadIdx.x != 0) return;
-  mbar_init(m.bar, 1);
-  if (n16)
-    bulk_load_g2s(m.srec, rec + __ldg(&rec_ofs[t]), 16u * n16, m.bar);
-  else
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m.bar)) : "memory");
-}
-
-// After a __syncthreads that follows tile_records_start: every thread waits for the records
-// (bounded).  False (the same in every thread) when the copy did not complete: the error is
-// raised, the copy waited for once more, and the block must leave.
-__device__ __forceinline__ bool tile_records_ready(const TileSmem& m, uint32_t* err) {
-  const bool ok = mbar_wait_bounded(m.bar, 0, kBulkWaitLimit);
-  if (__syncthreads_or(!ok)) {
-    if (threadIdx.x == 0) {
-      raise_error(err, kErrBulkCopy);
-      mbar_wait_bounded(m.bar, 0, kBulkWaitLimit);
-    }
-    __syncthreads();
-    return false;
-  }
-  return true;
-}
-
-template <bool RESET, int NT>
+// on mbarriers while the predecessor grid drains and the footprint is gathered.  Every wait on a
+// barrier is bounded; a copy that does not complete raises kErrBulkCopy and the block waits
+// (bounded) for its copies in flight and leaves.  NT threads per block: 512 for footprints up to
+// 4,096 vertices, 256 (twice the resident blocks per SM) up to 2,048.
+// Stretch tiles: the record block holds one segment per local color, as for bend (16-bit ids,
+// then float2 rest length and compliance, each padded to 16 bytes).  STREAM (throughput regime):
+// the segments stream in two colors ahead through two shared-memory buffers; otherwise the whole
+// block comes in one bulk copy.  The multipliers of the tile's constraints stay in shared memory
+// from the prologue to the write-back.
+template <bool RESET, int NT, bool STREAM>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_stretch_tiles(
     const uint4* __restrict__ rec, const uint32_t* __restrict__ rec_ofs,
     float* __restrict__ lambda, float4* __restrict__ x, const uint32_t* __restrict__ foot,
     const int4* __restrict__ meta, const uint32_t* __restrict__ lofs, uint32_t tile_begin,
-    uint32_t num_local, uint32_t max_foot, uint32_t max_rec16, uint32_t max_cons, float dt,
-    uint32_t* err) {
+    uint32_t num_local, uint32_t max_foot, uint32_t max_seg16, uint32_t buf16, uint32_t max_cons,
+    float dt, uint32_t* err) {
+  if (num_local == 0) return;  // no constraint in the schedule
   extern __shared__ float4 smem[];
-  const TileSmem m = tile_smem(smem, max_foot, max_rec16, max_cons, num_local);
+  float4* sx = smem;
+  uint4* buf = reinterpret_cast<uint4*>(sx + max_foot);  // buf16 uint4 (see the launcher)
+  uint64_t* bar = reinterpret_cast<uint64_t*>(buf + buf16);
+  float* sl = reinterpret_cast<float*>(bar + 2);
+  uint32_t* so = reinterpret_cast<uint32_t*>(sl + max_cons);
+  uint32_t* sf = so + num_local + 1;
   const uint32_t t = tile_begin + blockIdx.x;
-  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, t, num_local, m.so);
+  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, t, num_local, so);
   const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
-  tile_records_start(m, rec, rec_ofs, t, tile_rec16(nc, 2));
+  const uint32_t* tl = lofs + (size_t)t * (num_local + 1);
+  uint32_t src = 0;  // thread 0: the next segment's first uint4
+  auto issue = [&](uint32_t l) {  // thread 0: the copy of color l's segment
+    const uint32_t seg = color_seg16(__ldg(&tl[l + 1]) - __ldg(&tl[l]), 2);
+    uint64_t* b = bar + (l & 1);
+    if (seg)
+      bulk_load_g2s(buf + (l & 1) * max_seg16, rec + src, 16u * seg, b);
+    else
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+    src += seg;
+  };
+  if (threadIdx.x == 0) {
+    src = __ldg(&rec_ofs[t]);
+    mbar_init(bar, 1);
+    mbar_init(bar + 1, 1);
+    if (!STREAM) {  // the whole block at once
+      const uint32_t all = __ldg(&rec_ofs[t + 1]) - src;
+      if (all)
+        bulk_load_g2s(buf, rec + src, 16u * all, bar);
+      else
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+    } else {
+      issue(0);
+      if (num_local > 1) issue(1);
+    }
+  }
   pdl_wait();
 #pragma unroll 4
-  for (uint32_t j = threadIdx.x; j < nc; j += NT) m.sl[j] = RESET ? 0.0f : lambda[c0 + j];
-  tile_gather<NT>(f, x, m.sx, m.sf);
-  __syncthreads();
-  if (!tile_records_ready(m, err)) return;
-  const ushort2* sid = reinterpret_cast<const ushort2*>(m.srec);
-  const float2* sval = reinterpret_cast<const float2*>(m.srec + (4 * nc + 15) / 16);
-  float4* sx = m.sx;
-  float* sl = m.sl;
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) sl[j] = RESET ? 0.0f : lambda[c0 + j];
+  tile_gather<NT>(f, x, sx, sf);
+  __syncthreads();  // offsets, footprint, multipliers and the barriers' initialisation
+  auto failed = [&](bool ok, uint32_t l) {
+    if (!__syncthreads_or(!ok)) return false;
+    if (threadIdx.x == 0) {
+      raise_error(err, kErrBulkCopy);
+      if (!STREAM)
+        mbar_wait_bounded(bar, 0, kBulkWaitLimit);
+      else
+        for (uint32_t k = l; k < l + 2 && k < num_local; ++k)
+          mbar_wait_bounded(bar + (k & 1), (k >> 1) & 1u, kBulkWaitLimit);
+    }
+    __syncthreads();
+    return true;
+  };
+  if (failed(mbar_wait_bounded(bar, 0, kBulkWaitLimit), 0)) return;
+  uint32_t at = 0;  // whole block: the color's segment
   for (uint32_t l = 0; l < num_local; ++l) {
-    const uint32_t ce = m.so[l + 1];
-    for (uint32_t j = m.so[l] + threadIdx.x; j < ce; j += NT) {
+    const uint4* cur = STREAM ? buf + (l & 1) * max_seg16 : buf + at;
+    const uint32_t cb = so[l], n = so[l + 1] - cb;
+    const ushort2* sid = reinterpret_cast<const ushort2*>(cur);
+    const float2* sval = reinterpret_cast<const float2*>(cur + (4 * n + 15) / 16);
+    for (uint32_t j = threadIdx.x; j < n; j += NT) {
       const ushort2 ab = sid[j];
       const float2 rc = sval[j];
-      float lam = sl[j];
+      float lam = sl[cb + j];
       float4 a = sx[ab.x], b = sx[ab.y];
       if (stretch_project(a, b, rc.x, rc.y, dt, lam)) {
         sx[ab.x] = a;
         sx[ab.y] = b;
-        sl[j] = lam;
+        sl[cb + j] = lam;
       }
     }
-    __syncthreads();
+    if (!STREAM) {
+      at += color_seg16(n, 2);
+      __syncthreads();
+      continue;
+    }
+    const bool ok = l + 1 >= num_local ||
+                    mbar_wait_bounded(bar + ((l + 1) & 1), ((l + 1) >> 1) & 1u, kBulkWaitLimit);
+    if (failed(ok, l + 1)) return;
+    if (threadIdx.x == 0 && l + 2 < num_local) issue(l + 2);  // into the buffer color l read
   }
   pdl_release();  // late: the successor's blocks arrive as this one drains (measured faster)
-  tile_scatter<NT>((uint32_t)f.m.y, x, sx, m.sf);
+  tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
 #pragma unroll 4
   for (uint32_t j = threadIdx.x; j < nc; j += NT) lambda[c0 + j] = sl[j];
 }
@@ -248,8 +258,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
   const uint32_t* tl = lofs + (size_t)t * (num_local + 1);
   uint32_t src = 0;  // thread 0: the next segment's first uint4
   auto issue = [&](uint32_t l) {  // thread 0: the copy of color l's segment
-    const uint32_t n = __ldg(&tl[l + 1]) - __ldg(&tl[l]);
-    const uint32_t seg = 2 * ((n + 1) / 2);
+    const uint32_t seg = color_seg16(__ldg(&tl[l + 1]) - __ldg(&tl[l]), 4);
     uint64_t* b = bar + (l & 1);
     if (seg)
       bulk_load_g2s(buf + (l & 1) * max_seg16, rec + src, 16u * seg, b);
@@ -322,7 +331,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
       }
     }
     if (PAIR) {
-      at += color_seg16(n);
+      at += color_seg16(n, 4);
       __syncthreads();
       continue;
     }
@@ -555,8 +564,10 @@ cudaError_t configure_tile_kernels(size_t max_smem_bytes) {
   const int bytes = std::max(cur, (int)max_smem_bytes);
   if (bytes == cur) return cudaSuccess;
   const void* kernels[] = {
-      (const void*)k_stretch_tiles<true, 256>, (const void*)k_stretch_tiles<false, 256>,
-      (const void*)k_stretch_tiles<true, 512>, (const void*)k_stretch_tiles<false, 512>,
+      (const void*)k_stretch_tiles<true, 256, false>, (const void*)k_stretch_tiles<false, 256, false>,
+      (const void*)k_stretch_tiles<true, 512, false>, (const void*)k_stretch_tiles<false, 512, false>,
+      (const void*)k_stretch_tiles<true, 256, true>,  (const void*)k_stretch_tiles<false, 256, true>,
+      (const void*)k_stretch_tiles<true, 512, true>,  (const void*)k_stretch_tiles<false, 512, true>,
       (const void*)k_bend_tiles<256, true>,    (const void*)k_bend_tiles<256, false>,
       (const void*)k_bend_tiles<512, true>,    (const void*)k_bend_tiles<512, false>};
   for (const void* kern : kernels) {
@@ -575,13 +586,11 @@ size_t tile_smem_bytes(const TiledSet& T, size_t record_bytes) {
          sizeof(uint32_t) * (T.num_local + 1) + sizeof(uint32_t) * T.max_foot;
 }
 
-// Shared memory of the forward tile kernels: footprint, record block (stretch and paired bend:
-// the whole tile's; one-lane bend: two colors' segments), mbarrier slot(s), the stretch
-// multipliers, offsets and footprint ids.
-size_t tile_smem_fwd(const TiledSet& T, bool stretch, bool pair) {
-  const size_t records = stretch ? 16 * (size_t)T.max_rec16 + 16
-                                 : (pair ? 16 * (size_t)T.max_tile16 + 16
-                                         : 32 * (size_t)T.max_seg16 + 16);
+// Shared memory of the forward tile kernels: footprint, records (`whole`: the tile's whole block;
+// otherwise two colors' segments), two mbarriers, the stretch multipliers, offsets and footprint
+// ids.
+size_t tile_smem_fwd(const TiledSet& T, bool stretch, bool whole) {
+  const size_t records = whole ? 16 * (size_t)T.max_tile16 + 16 : 32 * (size_t)T.max_seg16 + 16;
   return sizeof(float4) * T.max_foot + records + (stretch ? sizeof(float) * T.max_cons : 0) +
          sizeof(uint32_t) * (T.num_local + 1) + sizeof(uint32_t) * T.max_foot;
 }
@@ -592,9 +601,9 @@ size_t tile_smem_fwd(const TiledSet& T, bool stretch, bool pair) {
 cudaError_t choose_tile_block(TiledSet& T, bool bend) {
   const uint32_t lanes = bend ? 2 * T.max_step : T.max_step;
   T.block = (T.max_foot <= 256u * kFootPerThread && lanes <= 256) ? 256 : 512;
-  // one-lane bend blocks: 256 threads whenever the footprint allows (a large color takes a
-  // second pass, but twice the blocks fit on an SM)
-  T.block1 = bend && T.max_foot <= 256u * kFootPerThread ? 256 : T.block;
+  // streamed (throughput-regime) blocks: 256 threads whenever the footprint allows (a large color
+  // takes a second pass, but twice the blocks fit on an SM)
+  T.block1 = T.max_foot <= 256u * kFootPerThread ? 256 : T.block;
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -602,8 +611,8 @@ cudaError_t choose_tile_block(TiledSet& T, bool bend) {
   const size_t smem = tile_smem_fwd(T, !bend, true);
   const void* kern = bend ? (T.block == 256 ? (const void*)k_bend_tiles<256, true>
                                             : (const void*)k_bend_tiles<512, true>)
-                          : (T.block == 256 ? (const void*)k_stretch_tiles<false, 256>
-                                            : (const void*)k_stretch_tiles<false, 512>);
+                          : (T.block == 256 ? (const void*)k_stretch_tiles<false, 256, false>
+                                            : (const void*)k_stretch_tiles<false, 512, false>);
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)T.block, smem);
   if (e != cudaSuccess) return e;
   T.resident = (uint32_t)std::max(per_sm, 1) * (uint32_t)sms;
@@ -641,12 +650,17 @@ void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, boo
   const uint32_t nt = tiles.end - tiles.begin;
   if (nt == 0) return;
   const TiledSet& T = c.s_tiles;
-  const size_t smem = tile_smem_fwd(T, true, false);
-  auto kern = T.block == 256 ? (reset_lambda ? k_stretch_tiles<true, 256> : k_stretch_tiles<false, 256>)
-                             : (reset_lambda ? k_stretch_tiles<true, 512> : k_stretch_tiles<false, 512>);
-  launch_k(c.pdl, kern, nt, T.block, smem, c.stream, T.rec.p, T.rec_ofs.p, c.s_lambda.p, c.x.p,
-           T.foot.p, T.meta.p, T.lofs.p, tiles.begin, T.num_local, T.max_foot, T.max_rec16,
-           T.max_cons, k.dt, c.err.p);
+  const bool stream = nt > T.resident;  // many waves of tiles: throughput regime
+  const uint32_t block = stream ? T.block1 : T.block;
+  const uint32_t buf16 = stream ? 2 * T.max_seg16 : T.max_tile16;  // as tile_smem_fwd sizes it
+  auto pick = [&](auto k256, auto k512) { return block == 256 ? k256 : k512; };
+  auto kern = stream ? (reset_lambda ? pick(k_stretch_tiles<true, 256, true>, k_stretch_tiles<true, 512, true>)
+                                     : pick(k_stretch_tiles<false, 256, true>, k_stretch_tiles<false, 512, true>))
+                     : (reset_lambda ? pick(k_stretch_tiles<true, 256, false>, k_stretch_tiles<true, 512, false>)
+                                     : pick(k_stretch_tiles<false, 256, false>, k_stretch_tiles<false, 512, false>));
+  launch_k(c.pdl, kern, nt, block, tile_smem_fwd(T, true, !stream), c.stream, T.rec.p,
+           T.rec_ofs.p, c.s_lambda.p, c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin,
+           T.num_local, T.max_foot, T.max_seg16, buf16, T.max_cons, k.dt, c.err.p);
 }
 
 void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles) {
