@@ -420,6 +420,7 @@ xrt_status xrt_destroy(xrt_ctx* h) {
   c.tri.release(); c.s_con.release(); c.b_idx.release(); c.bind_b.release(); c.otri.release();
   c.s_lambda.release(); c.lra_rest.release(); c.lra_l_rest.release(); c.b_tc.release();
   c.stage3.release();
+  c.ee_vflag.release();
   c.edge.release(); c.vf_idx.release(); c.rt_idx.release();
   c.hash_sorter.keys_tmp.release(); c.hash_sorter.vals_tmp.release(); c.hash_sorter.hist.release();
   c.hash_sorter.sums.release();
@@ -1091,6 +1092,8 @@ xrt_status xrt_start(xrt_ctx* h) {
   XRT_CUDA(&c, c.ee_a.reserve(std::max(c.ne, 1u)));
   XRT_CUDA(&c, c.ee_b.reserve(std::max(c.ne, 1u)));
   XRT_CUDA(&c, c.ee_c.reserve(std::max(c.ne, 1u)));
+  XRT_CUDA(&c, c.ee_vflag.reserve(std::max(c.nv, 1u)));
+  XRT_CUDA(&c, cudaMemsetAsync(c.ee_vflag.p, 0, std::max(c.nv, 1u), c.stream));
   XRT_CUDA(&c, cudaMemsetAsync(c.vf_idx.p, 0xFF, sizeof(int) * c.nv, c.stream));
   XRT_CUDA(&c, cudaMemsetAsync(c.rt_idx.p, 0xFF, sizeof(int) * c.nv, c.stream));
   XRT_CUDA(&c, cudaMemsetAsync(c.vf_qs.p, 0, sizeof(float4) * c.nv, c.stream));

@@ -192,7 +192,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_generate_ee(LbvhForest F, InstVie
                                                         const int4* __restrict__ otri_all,
                                                         float4* __restrict__ ee_a,
                                                         float4* __restrict__ ee_b,
-                                                        float4* __restrict__ ee_c, uint32_t* err,
+                                                        float4* __restrict__ ee_c,
+                                                        uint8_t* __restrict__ vflag, uint32_t* err,
                                                         uint32_t* counter) {
   LbvhView b{};
   TraverseState st{};
@@ -246,6 +247,11 @@ __global__ void __launch_bounds__(kBlock, 4) k_generate_ee(LbvhForest F, InstVie
         ee_a[e] = make_float4(min_dist, p2.x, p2.y, p2.z);
         ee_b[e] = make_float4(q2.x, q2.y, q2.z, s);
         ee_c[e] = make_float4(fn.x, fn.y, fn.z, t);
+        if (min_dist <= 1e6f) {  // a contact (the EE solve's test): flag both endpoints
+          const uint2 ed = edge[e];
+          vflag[ed.x] = 1;
+          vflag[ed.y] = 1;
+        }
       });
 }
 
@@ -268,12 +274,13 @@ void launch_generate_contacts(Context& c) {
   // pass the end
   const unsigned cap = (unsigned)c.num_sms * 8u;
   cudaMemsetAsync(c.gen_counter.p, 0, sizeof(uint32_t) * 3, c.stream);
+  cudaMemsetAsync(c.ee_vflag.p, 0, c.nv, c.stream);  // this pass's contacts set it
   k_generate_vf_dcd<<<std::min(grid_for(c.nv), cap), kBlock, 0, c.stream>>>(
       F, I, c.x.p, c.nv, c.vf_idx.p, c.vf_qs.p, c.err.p, c.gen_counter.p);
   k_generate_vf_ccd<<<std::min(grid_for(c.nv), cap), kBlock, 0, c.stream>>>(
       F, I, c.x.p, c.x0.p, c.nv, c.rt_idx.p, c.rt_qc.p, c.err.p, c.gen_counter.p + 1);
   k_generate_ee<<<std::min(grid_for(c.ne), cap), kBlock, 0, c.stream>>>(
-      F, I, c.x.p, c.edge.p, c.ne, c.otri.p, c.ee_a.p, c.ee_b.p, c.ee_c.p, c.err.p,
+      F, I, c.x.p, c.edge.p, c.ne, c.otri.p, c.ee_a.p, c.ee_b.p, c.ee_c.p, c.ee_vflag.p, c.err.p,
       c.gen_counter.p + 2);
 }
 

@@ -471,6 +471,7 @@ struct Context {
   // particle hash
   DBuf<uint32_t> hash_key, hash_val, cell_start, cell_end, neighbors;
   DBuf<float> stage3;  // packed xyz staging of the C ABI's host copies
+  DBuf<uint8_t> ee_vflag;  // per cloth vertex: an incident edge holds an EE contact (this pass)
   uint32_t vertex_block = 128;  // threads per block of the per-vertex substep kernels
   RadixSort hash_sorter;
   // obstacle

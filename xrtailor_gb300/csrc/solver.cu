@@ -379,6 +379,7 @@ struct TailArgs {
   const uint32_t *ve_ptr, *ve_list;
   const uint2* edge;
   const float4 *ee_a, *ee_b, *ee_c;
+  const uint8_t* ee_vflag;  // per vertex: an incident edge holds a contact
   float relaxation;
   const uint32_t* bind_ptr;
   const float4* bind_a;
@@ -452,7 +453,8 @@ __global__ void k_ee(const TailArgs a) {
   const float relaxation = a.relaxation;
   const float4 p = x_in[i];
   f3 q = mk3(p);
-  if (CONTACTS) {
+  // a vertex none of whose edges holds a contact skips the list (delta 0, count 0)
+  if (CONTACTS && a.ee_vflag[i]) {
     f3 delta = mk3(0, 0, 0);
     int count = 0;
     // The contact-flag loads of a batch of incident edges are issued together; the edges are
@@ -710,6 +712,7 @@ static TailArgs tail_args(Context& c, const FrameConst& k) {
   a.ee_a = c.ee_a.p;
   a.ee_b = c.ee_b.p;
   a.ee_c = c.ee_c.p;
+  a.ee_vflag = c.ee_vflag.p;
   a.relaxation = k.relaxation;
   a.bind_ptr = c.bind_ptr.p;
   a.bind_a = c.bind_a.p;
