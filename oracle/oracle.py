@@ -117,6 +117,10 @@ class OracleSolver:
         self.params = params
         self._l.orc_set_params(self._h, C.byref(params))
 
+    def set_params(self, params: L.SwiftParams):
+        self.params = params
+        self._l.orc_set_params(self._h, C.byref(params))
+
     def add_cloth(self, mesh, model_matrix=None, particle_diameter=0.0):
         d, keep = cloth_desc(mesh, model_matrix, particle_diameter)
         r = self._l.orc_add_cloth(self._h, C.byref(d))

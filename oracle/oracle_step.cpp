@@ -497,7 +497,7 @@ void solve_stretch(Oracle& o, uint32_t color, float dt, int iter) {
     float distance = length(diff);
     float w1 = o.w[i1], w2 = o.w[i2];
     if (distance != expected && w1 + w2 > 0.0f) {
-      V3 gradient = diff / (distance + kEps);
+      V3 gradient = diff * (1.0f / (distance + kEps));
       float alpha_tilde = o.s_comp[id] / (dt * dt);
       float constraint = distance - expected;
       float dl = (-constraint - alpha_tilde * o.s_lambda[id]) / (w1 + w2 + alpha_tilde);
@@ -530,10 +530,11 @@ void solve_bend(Oracle& o, uint32_t color, float dt) {
     float d = clampf(dot(n1, n2), 0.0f, 1.0f);
     float angle = acos_as(d);  // the reference calls acos; see oracle_math.h
     if (angle < kEps || std::isnan(d)) continue;
-    V3 q3 = (cross(p2, n2) + cross(n1, p2) * d) / (length(cross(p2, p3)) + kEps);
-    V3 q4 = (cross(p2, n1) + cross(n2, p2) * d) / (length(cross(p2, p4)) + kEps);
-    V3 q2 = -(cross(p3, n2) + cross(n1, p3) * d) / (length(cross(p2, p3)) + kEps) -
-            (cross(p4, n1) + cross(n2, p4) * d) / (length(cross(p2, p4)) + kEps);
+    float r3 = 1.0f / (length(cross(p2, p3)) + kEps);
+    float r4 = 1.0f / (length(cross(p2, p4)) + kEps);
+    V3 q3 = (cross(p2, n2) + cross(n1, p2) * d) * r3;
+    V3 q4 = (cross(p2, n1) + cross(n2, p2) * d) * r4;
+    V3 q2 = -(cross(p3, n2) + cross(n1, p3) * d) * r3 - (cross(p4, n1) + cross(n2, p4) * d) * r4;
     V3 q1 = -q2 - q3 - q4;
     float xpbd_bend = o.b_comp[id] / dt / dt;
     float denom = xpbd_bend + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) +

@@ -1,9 +1,8 @@
 """Parity of the Swift frame on the GPU against the CPU oracle.
 
-Tolerance (north-star): positions after a frame within 1e-4 of the cloth's bounding-box diagonal.
-Without bending every operation on the path is an IEEE +,-,*,/,sqrt or floor in the same order on
-both sides, so those frames must match bit for bit; with bending the device acosf and the host
-acosf may differ in the last place, so those frames are held to the tolerance."""
+Every operation on the path is an IEEE +,-,*,/,sqrt or floor in the same order on both sides (the
+bend angle's arccos is one polynomial evaluated the same way on both), so frames must match bit
+for bit; the tolerance of 1e-4 of the cloth's bounding-box diagonal is checked as well."""
 import numpy as np
 import pytest
 
@@ -98,6 +97,21 @@ def test_frame_with_bending(xrt):
     # the bend angle uses the same arccos polynomial on both sides, so bending frames are exact
     cloth, obs = small_scene(16)
     g, o = make_pair(_params(), [cloth], [obs], particle_diameter=0.02)
+    for _ in range(2):
+        g.step()
+        o.step()
+        _close(g, o, exact=True)
+
+
+def test_new_substep_dt_after_start_matches_oracle(xrt):
+    # the tile records carry compliance / dt^2 terms: a new dt after start re-evaluates them
+    cloth, obs = small_scene(16)
+    g, o = make_pair(_params(), [cloth], [obs], particle_diameter=0.02)
+    g.step()
+    o.step()
+    p = _params(num_substeps=3)
+    g.set_params(p)
+    o.set_params(p)
     for _ in range(2):
         g.step()
         o.step()

@@ -453,6 +453,8 @@ xrt_status xrt_destroy(xrt_ctx* h) {
 
 const char* xrt_last_error(const xrt_ctx* h) { return h ? h->c.last_error.c_str() : "null context"; }
 
+static xrt_status upload_constraints(Context& c);
+
 xrt_status xrt_set_params(xrt_ctx* h, const xrt_swift_params* p) {
   if (!h || !p) return XRT_ERR_INVALID_ARGUMENT;
   std::string why;
@@ -460,8 +462,15 @@ xrt_status xrt_set_params(xrt_ctx* h, const xrt_swift_params* p) {
     h->c.set_error(why);
     return XRT_ERR_INVALID_CONFIG;
   }
-  h->c.params = *p;
-  h->c.graph_dirty = true;
+  Context& c = h->c;
+  c.params = *p;
+  c.graph_dirty = true;
+  // the tile records hold compliance terms of the substep dt: a new dt re-evaluates them
+  if (c.started && (c.s_tiles.on || c.b_tiles.on) && xrt::frame_const(c).dt != c.rec_dt) {
+    cudaSetDevice(c.device);
+    XRT_CUDA(&c, cudaStreamSynchronize(c.stream));
+    return upload_constraints(c);
+  }
   return XRT_OK;
 }
 
@@ -765,6 +774,8 @@ static xrt_status upload_constraints(Context& c) {
   // the forward tile kernels' per-tile record blocks (TiledSet::rec); footprint-local ids fit
   // 16 bits
   static_assert(xrt::kTileMaxFootprint <= 65536, "16-bit footprint-local vertex ids");
+  const float dt = xrt::frame_const(c).dt;  // the compliance terms are evaluated for this dt
+  c.rec_dt = dt;
   for (int kind = 0; kind < 2; ++kind) {
     xrt::TiledSet& T = kind == 0 ? c.s_tiles : c.b_tiles;
     if (!T.on) continue;
@@ -783,8 +794,9 @@ static xrt_status upload_constraints(Context& c) {
       for (uint32_t j = 0; j < nc; ++j) {
         const uint32_t slot = c0 + j;
         for (int a = 0; a < arity; ++a) ids[arity * j + a] = (uint16_t)local[arity * slot + a];
-        vals[j] = kind == 0 ? make_float2(c.h_rest[c.s_perm[slot]], c.h_scomp[c.s_perm[slot]])
-                            : btc[slot];
+        vals[j] = kind == 0 ? make_float2(c.h_rest[c.s_perm[slot]],
+                                          xrt::stretch_alpha(c.h_scomp[c.s_perm[slot]], dt))
+                            : make_float2(btc[slot].x, xrt::bend_alpha(btc[slot].y, dt));
       }
     };
     const std::vector<uint32_t>& lofs = c.h_tile_lofs[kind];

@@ -239,9 +239,10 @@ struct TiledSet {
   DBuf<uint32_t> lofs;                  // per executed tile: num_local + 1 offsets, tile-relative
   // Records of the forward tile kernels, one 16-byte aligned block per executed tile: the
   // constraints' footprint-local vertex ids as 16-bit values (2 per stretch constraint, 4 per
-  // bend element), padded to 16 bytes, then their float2 values (rest length and compliance /
-  // rest angle and compliance), padded to 16 bytes: one such segment per local color, in color
-  // order, copied whole or color by color.
+  // bend element), padded to 16 bytes, then their float2 values (rest length and
+  // stretch_alpha(compliance, dt) / rest angle and bend_alpha(compliance, dt), for the dt of
+  // Context::rec_dt), padded to 16 bytes: one such segment per local color, in color order,
+  // copied whole or color by color.
   DBuf<uint4> rec;
   DBuf<uint32_t> rec_ofs;               // per executed tile: first uint4 of its block; + the end
   uint32_t max_seg16 = 0;               // largest local color's segment, in uint4
@@ -252,6 +253,17 @@ struct TiledSet {
 // then a float2 each, both padded to 16 bytes.
 __host__ __device__ inline uint32_t color_seg16(uint32_t n, uint32_t arity) {
   return (2 * arity * n + 15) / 16 + (8 * n + 15) / 16;
+}
+
+// The XPBD compliance terms, in the reference's order of operations: alpha~ = compliance /
+// (dt dt) of SolveStretch_Kernel (BasicSolverHelper.cu:105) and compliance / dt / dt of
+// SolveBend_Kernel (BasicSolverHelper.cu:53).  The host evaluates them into the tile records with
+// the same correctly rounded operations, so the kernels that read them get the same bits.
+__host__ __device__ inline float stretch_alpha(float compliance, float dt) {
+  return compliance / (dt * dt);
+}
+__host__ __device__ inline float bend_alpha(float compliance, float dt) {
+  return compliance / dt / dt;
 }
 
 
@@ -379,6 +391,7 @@ struct Context {
   xrt_status frame_status = XRT_OK;  // first failure of an eagerly recorded frame's host steps
   xrt_swift_params params{};
   bool started = false;
+  float rec_dt = 0.0f;  // the substep dt the tile records' compliance terms were evaluated for
   bool graph_enabled = true;
   cudaGraphExec_t graph_exec = nullptr;
   bool graph_dirty = true;

@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(NT) k_bend_tiles_tape(
         t[0] = sx[half ? b.z : b.x];
         t[1] = sx[half ? b.w : b.y];
       }
-      bend_project_pair(sx, b, th.x, th.y, dt, half, active);
+      bend_project_pair(sx, b, th.x, bend_alpha(th.y, dt), half, active);
     }
     __syncthreads();
   }

@@ -7,6 +7,7 @@
 //   prim_normal ....... face normal of an obstacle primitive's predicted vertices
 #pragma once
 #include "common.cuh"
+#include "context.h"
 
 namespace xrt {
 
@@ -59,15 +60,15 @@ __device__ __forceinline__ void tile_scatter(uint32_t nfoot, float4* __restrict_
   }
 }
 
-// XPBD distance constraint on two vertices; returns true when it moved them (lam updated).
-__device__ __forceinline__ bool stretch_project(float4& a, float4& b, float rest, float compliance,
-                                                float dt, float& lam) {
+// XPBD distance constraint on two vertices, alpha_tilde = stretch_alpha(compliance, dt); returns
+// true when it moved them (lam updated).
+__device__ __forceinline__ bool stretch_project_alpha(float4& a, float4& b, float rest,
+                                                      float alpha_tilde, float& lam) {
   const f3 diff = mk3(a) - mk3(b);
   const float distance = length(diff);
   const float w1 = a.w, w2 = b.w;
   if (!(distance != rest && w1 + w2 > 0.0f)) return false;
-  const f3 gradient = diff / (distance + kEps);
-  const float alpha_tilde = compliance / (dt * dt);
+  const f3 gradient = diff * (1.0f / (distance + kEps));
   const float constraint = distance - rest;
   const float dl = (-constraint - alpha_tilde * lam) / (w1 + w2 + alpha_tilde);
   const f3 corr = dl * gradient;
@@ -79,10 +80,16 @@ __device__ __forceinline__ bool stretch_project(float4& a, float4& b, float rest
   return true;
 }
 
+__device__ __forceinline__ bool stretch_project(float4& a, float4& b, float rest, float compliance,
+                                                float dt, float& lam) {
+  return stretch_project_alpha(a, b, rest, stretch_alpha(compliance, dt), lam);
+}
 
-// Dihedral bend projection of SolveBend_Kernel on four vertices.
-__device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3, float4& a4,
-                                             float theta, float compliance, float dt) {
+
+// Dihedral bend projection of SolveBend_Kernel on four vertices, xpbd_bend =
+// bend_alpha(compliance, dt).
+__device__ __forceinline__ void bend_project_alpha(float4& a1, float4& a2, float4& a3, float4& a4,
+                                                   float theta, float xpbd_bend) {
   const float w1 = a1.w, w2 = a2.w, w3 = a3.w, w4 = a4.w;
   const f3 p1 = mk3(a1);
   const f3 p2 = mk3(a2) - p1;
@@ -93,12 +100,12 @@ __device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3,
   const float d = tclamp(dot(n1, n2), 0.0f, 1.0f);
   const float angle = acos_as(d);  // d in [0, 1] (or NaN, rejected below)
   if (angle < kEps || isnan(d)) return;
-  const f3 q3 = (cross(p2, n2) + cross(n1, p2) * d) / (length(cross(p2, p3)) + kEps);
-  const f3 q4 = (cross(p2, n1) + cross(n2, p2) * d) / (length(cross(p2, p4)) + kEps);
-  const f3 q2 = -(cross(p3, n2) + cross(n1, p3) * d) / (length(cross(p2, p3)) + kEps) -
-                (cross(p4, n1) + cross(n2, p4) * d) / (length(cross(p2, p4)) + kEps);
+  const float r3 = 1.0f / (length(cross(p2, p3)) + kEps);
+  const float r4 = 1.0f / (length(cross(p2, p4)) + kEps);
+  const f3 q3 = (cross(p2, n2) + cross(n1, p2) * d) * r3;
+  const f3 q4 = (cross(p2, n1) + cross(n2, p2) * d) * r4;
+  const f3 q2 = -(cross(p3, n2) + cross(n1, p3) * d) * r3 - (cross(p4, n1) + cross(n2, p4) * d) * r4;
   const f3 q1 = -q2 - q3 - q4;
-  const float xpbd_bend = compliance / dt / dt;
   const float denom =
       xpbd_bend + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) + w4 * dot(q4, q4));
   if (denom < kEps) return;
@@ -114,6 +121,11 @@ __device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3,
   a4 = make_float4(a4.x + c4.x, a4.y + c4.y, a4.z + c4.z, w4);
 }
 
+__device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3, float4& a4,
+                                             float theta, float compliance, float dt) {
+  bend_project_alpha(a1, a2, a3, a4, theta, bend_alpha(compliance, dt));
+}
+
 
 // The same projection on a lane pair (lanes 2m, 2m+1 of a warp, `half` = lane & 1), for the
 // shared-memory footprint of a tile: each lane evaluates one of the two independent halves of
@@ -121,14 +133,13 @@ __device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3,
 // are exchanged by shuffles, and lane 0 writes vertices 1-2, lane 1 vertices 3-4.  Every value is
 // produced by the same operations as bend_project, so the result is identical.  All 32 lanes
 // call it; `active` is false for lanes past the color's last element (they write nothing).
-// With (nA, nB, lA) = (n1, n2, |p2 x p3| + eps) on lane 0 and (n2, n1, |p2 x p4| + eps) on
-// lane 1, and pA = p3 / p4:
-//   q3 (lane 0) and q4 (lane 1) are both (p2 x nB + (nA x p2) d) / lA,
-//   the two terms of q2 are -(pA x nB + (nA x pA) d) / lA on lane 0 and +(...) / lA on lane 1;
-// (-X) / L equals -(X / L) bit for bit, so both lanes run one instruction stream.
-__device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float theta,
-                                                  float compliance, float dt, uint32_t half,
-                                                  bool active) {
+// With (nA, nB, rA) = (n1, n2, 1 / (|p2 x p3| + eps)) on lane 0 and (n2, n1, 1 / (|p2 x p4| +
+// eps)) on lane 1, and pA = p3 / p4:
+//   q3 (lane 0) and q4 (lane 1) are both (p2 x nB + (nA x p2) d) rA,
+//   the two terms of q2 are -(pA x nB + (nA x pA) d) rA on lane 0 and +(...) rA on lane 1;
+// (-X) r equals -(X r) bit for bit, so both lanes run one instruction stream.
+__device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float theta, float xpbd_bend,
+                                                  uint32_t half, bool active) {
   constexpr unsigned kAll = 0xffffffffu;
   const float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
   const f3 p1 = mk3(a1);
@@ -138,14 +149,14 @@ __device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float thet
   const f3 pA = half ? p4 : p3;
   const f3 cA = cross(p2, pA);
   const f3 nA = normalize(cA);
-  const float lA = length(cA) + kEps;
+  const float rA = 1.0f / (length(cA) + kEps);
   const f3 nB = mk3(__shfl_xor_sync(kAll, nA.x, 1), __shfl_xor_sync(kAll, nA.y, 1),
                     __shfl_xor_sync(kAll, nA.z, 1));
   const f3 n1 = half ? nB : nA, n2 = half ? nA : nB;
   const float d = tclamp(dot(n1, n2), 0.0f, 1.0f);
   const float angle = acos_as(d);
-  const f3 qA = (cross(p2, nB) + cross(nA, p2) * d) / lA;   // q3 on lane 0, q4 on lane 1
-  const f3 vA = (cross(pA, nB) + cross(nA, pA) * d) / lA;   // |terms| of q2
+  const f3 qA = (cross(p2, nB) + cross(nA, p2) * d) * rA;   // q3 on lane 0, q4 on lane 1
+  const f3 vA = (cross(pA, nB) + cross(nA, pA) * d) * rA;   // |terms| of q2
   const f3 qB = mk3(__shfl_xor_sync(kAll, qA.x, 1), __shfl_xor_sync(kAll, qA.y, 1),
                     __shfl_xor_sync(kAll, qA.z, 1));
   const f3 vB = mk3(__shfl_xor_sync(kAll, vA.x, 1), __shfl_xor_sync(kAll, vA.y, 1),
@@ -155,7 +166,6 @@ __device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float thet
   const f3 q2 = -v23 - v24;
   const f3 q1 = -q2 - q3 - q4;
   const float w1 = a1.w, w2 = a2.w, w3 = a3.w, w4 = a4.w;
-  const float xpbd_bend = compliance / dt / dt;
   const float denom =
       xpbd_bend + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) + w4 * dot(q4, q4));
   if (!active || angle < kEps || isnan(d) || denom < kEps) return;

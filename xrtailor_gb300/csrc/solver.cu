@@ -112,7 +112,7 @@ __global__ void k_stretch(const int4* __restrict__ con, float* __restrict__ lamb
 // (bounded) for its copies in flight and leaves.  NT threads per block: 512 for footprints up to
 // 4,096 vertices, 256 (twice the resident blocks per SM) up to 2,048.
 // Stretch tiles: the record block holds one segment per local color, as for bend (16-bit ids,
-// then float2 rest length and compliance, each padded to 16 bytes).  STREAM (throughput regime):
+// then float2 rest length and stretch_alpha(compliance, dt), each padded to 16 bytes).  STREAM (throughput regime):
 // the segments stream in two colors ahead through two shared-memory buffers; otherwise the whole
 // block comes in one bulk copy.  The multipliers of the tile's constraints stay in shared memory
 // from the prologue to the write-back.
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_stretch_tiles(
     float* __restrict__ lambda, float4* __restrict__ x, const uint32_t* __restrict__ foot,
     const int4* __restrict__ meta, const uint32_t* __restrict__ lofs, uint32_t tile_begin,
     uint32_t num_local, uint32_t max_foot, uint32_t max_seg16, uint32_t buf16, uint32_t max_cons,
-    float dt, uint32_t* err) {
+    uint32_t* err) {
   if (num_local == 0) return;  // no constraint in the schedule
   extern __shared__ float4 smem[];
   float4* sx = smem;
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_stretch_tiles(
       const float2 rc = sval[j];
       float lam = sl[cb + j];
       float4 a = sx[ab.x], b = sx[ab.y];
-      if (stretch_project(a, b, rc.x, rc.y, dt, lam)) {
+      if (stretch_project_alpha(a, b, rc.x, rc.y, lam)) {
         sx[ab.x] = a;
         sx[ab.y] = b;
         sl[cb + j] = lam;
@@ -232,7 +232,8 @@ __global__ void k_bend(const int4* __restrict__ idx, const float2* __restrict__ 
 // launches whose tiles are all resident at once (latency-bound); otherwise one lane per element
 // (fewer instructions in total, for launches with many waves of tiles).
 // Records: the tile's record block (TiledSet::rec) holds one segment per local color (16-bit
-// footprint-local ids, then float2 values, each padded to 16 bytes).
+// footprint-local ids, then float2 rest angle and bend_alpha(compliance, dt), each padded to 16
+// bytes).
 //   one lane (throughput regime): the segments stream in by local color, each bulk-copied into
 //     one of two shared-memory buffers on its own mbarrier, two colors ahead of its use; a buffer
 //     is refilled right after the barrier that closes the color that read it.  Only two colors'
@@ -244,7 +245,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
     const uint4* __restrict__ rec, const uint32_t* __restrict__ rec_ofs, float4* __restrict__ x,
     const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
     const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
-    uint32_t max_foot, uint32_t max_seg16, uint32_t buf16, float dt, uint32_t* err) {
+    uint32_t max_foot, uint32_t max_seg16, uint32_t buf16, uint32_t* err) {
   if (num_local == 0) return;  // no constraint in the schedule
   extern __shared__ float4 smem[];
   float4* sx = smem;
@@ -316,14 +317,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
         const ushort4 q = sid[j];
         const int4 b = make_int4(q.x, q.y, q.z, q.w);
         const float2 th = st[j];
-        bend_project_pair(sx, b, th.x, th.y, dt, s & 1u, active);
+        bend_project_pair(sx, b, th.x, th.y, s & 1u, active);
       }
     } else {
       for (uint32_t j = threadIdx.x; j < n; j += NT) {
         const ushort4 b = sid[j];
         const float2 th = st[j];
         float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
-        bend_project(a1, a2, a3, a4, th.x, th.y, dt);
+        bend_project_alpha(a1, a2, a3, a4, th.x, th.y);
         sx[b.x] = a1;
         sx[b.y] = a2;
         sx[b.z] = a3;
@@ -662,7 +663,7 @@ void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, boo
                                      : pick(k_stretch_tiles<false, 256, false>, k_stretch_tiles<false, 512, false>));
   launch_k(c.pdl, kern, nt, block, tile_smem_fwd(T, true, !stream), c.stream, T.rec.p,
            T.rec_ofs.p, c.s_lambda.p, c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin,
-           T.num_local, T.max_foot, T.max_seg16, buf16, T.max_cons, k.dt, c.err.p);
+           T.num_local, T.max_foot, T.max_seg16, buf16, T.max_cons, c.err.p);
 }
 
 void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles) {
@@ -679,7 +680,7 @@ void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles) {
   const uint32_t buf16 = pair ? T.max_tile16 : 2 * T.max_seg16;  // as tile_smem_fwd sizes it
   launch_k(c.pdl, kern, nt, block, tile_smem_fwd(T, false, pair), c.stream, T.rec.p, T.rec_ofs.p,
            c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin, T.num_local, T.max_foot, T.max_seg16,
-           buf16, k.dt, c.err.p);
+           buf16, c.err.p);
 }
 
 // LRA phase with a free slot vertex: one launch per slot block in list order.  (With every slot
