@@ -8,7 +8,8 @@ Per substep (ClothSolverBase::SimulateSwift, ClothSolverBase.cpp:171-261, frames
 particle self-collision or bindings):
   predict (ClothSolverHelper.cu:125-137)
   per iteration: stretch colors in order (XPBD, lambda reset at iteration 0,
-    BasicSolverHelper.cu:80-132), bend colors in order (BasicSolverHelper.cu:8-72, arccos by the
+    BasicSolverHelper.cu:80-132; the library's fused multiply-adds, see _fma), bend colors in
+    order (BasicSolverHelper.cu:8-72, arccos by the
     same Abramowitz & Stegun 4.4.46 polynomial as the library), LRA with pinned slots
     (LongRangeAttachments.cu:5-26), VF-CCD then VF-DCD per vertex (PBDCollision.cu:279-298, 57-80),
     EE-DCD + ApplyDeltas as a Jacobi step (PBDCollision.cu:163-212, ClothSolverHelper.cu:139-148)
@@ -50,7 +51,7 @@ def _sqrt0(a):
 def acos_as(x):
     p = torch.full_like(x, ACOS_C[0])
     for c in ACOS_C[1:]:
-        p = p * x + c
+        p = _fma(p, x, torch.full_like(x, c))
     return _sqrt0(1.0 - x) * p
 
 
@@ -60,6 +61,20 @@ def _normalize(v):
 
 def _dot(a, b):
     return (a * b).sum(-1)
+
+
+def _fma(a, b, c):
+    """a*b + c rounded once, as the library's stretch and bend projections evaluate it (fmaf):
+    in float32 through float64 and one rounding (the fused result up to a rare double rounding),
+    in float64 the plain expression."""
+    if T == torch.float32:
+        return (a.double() * b.double() + c.double()).to(T)
+    return a * b + c
+
+
+def _fdot(a, b):
+    """The library's fused dot product fma(a.z, b.z, fma(a.y, b.y, a.x b.x))."""
+    return _fma(a[..., 2], b[..., 2], _fma(a[..., 1], b[..., 1], a[..., 0] * b[..., 0]))
 
 
 @dataclass
@@ -109,15 +124,16 @@ def _stretch(x, w, lam, p: Problem, comp, reset):
         rest = torch.as_tensor(p.rest[cid], dtype=T)
         lam_c = torch.zeros(len(cid), dtype=T) if reset else lam[idx]
         d = xa - xb
-        dist = _sqrt0(_dot(d, d))
+        dist = _sqrt0(_fdot(d, d))
         mask = (dist != rest) & (wa + wb > 0)
-        n = d / (dist + EPS)[:, None]
+        n = d * (1.0 / (dist + EPS))[:, None]
         at = comp[idx] / (p.dt * p.dt)
         C = dist - rest
-        dl = (-C - at * lam_c) / (wa + wb + at)
+        dl = _fma(-at, lam_c, -C) / (wa + wb + at)
         dl = torch.where(mask, dl, torch.zeros_like(dl))
         corr = dl[:, None] * n
-        x = x.index_copy(0, a, xa + wa[:, None] * corr).index_copy(0, b, xb - wb[:, None] * corr)
+        x = (x.index_copy(0, a, _fma(corr, wa[:, None], xa))
+              .index_copy(0, b, _fma(-corr, wb[:, None], xb)))
         lam = lam.index_copy(0, idx, torch.where(mask, lam_c + dl, lam_c))
     return x, lam
 

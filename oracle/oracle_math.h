@@ -2,7 +2,8 @@
 //
 // Restates the glm operations the reference kernels use, with glm's evaluation order, so that the
 // oracle's float results can be compared bit-for-bit with the CUDA path (both sides are compiled
-// without FMA contraction: -ffp-contract=off here, --fmad=false for the CUDA library).
+// without FMA contraction: -ffp-contract=off here, --fmad=false for the CUDA library; the stretch
+// and bend projections use explicit fused multiply-adds, the same ones on both sides).
 //   dot(a,b)      = (a.x*b.x + a.y*b.y) + a.z*b.z          (glm compute_dot for vec3)
 //   cross(x,y)    = (x.y*y.z - y.y*x.z, x.z*y.x - y.z*x.x, x.x*y.y - y.x*x.y)
 //   length(v)     = sqrt(dot(v,v));  normalize(v) = v * (1 / sqrt(dot(v,v)))
@@ -47,17 +48,29 @@ template <typename T> static inline T mabs(T x) { return x < T(0) ? -x : x; }
 static const float kEps = 1e-6f;       // EPSILON, core/Scalar.hpp:39
 static const float kScalarMax = FLT_MAX;  // SCALAR_MAX, core/Scalar.cuh:10
 
-// arccos on [0, 1]: Abramowitz & Stegun 4.4.46, |error| <= 2e-8 (the CUDA library evaluates the
-// same polynomial in its bend kernel, so both sides round identically).
+// Fused forms of the stretch and bend projections (the CUDA library's fdot / fcross / fmad): one
+// std::fma (rounded once) per product-plus-term, in the same expression tree on both sides.
+static inline float fma1(float a, float b, float c) { return std::fma(a, b, c); }
+static inline float fdot(V3 a, V3 b) { return fma1(a.z, b.z, fma1(a.y, b.y, a.x * b.x)); }
+static inline V3 fcross(V3 a, V3 b) {
+  return V3{fma1(a.y, b.z, -(b.y * a.z)), fma1(a.z, b.x, -(b.z * a.x)),
+            fma1(a.x, b.y, -(b.x * a.y))};
+}
+static inline V3 fmad(V3 a, float s, V3 b) {
+  return V3{fma1(a.x, s, b.x), fma1(a.y, s, b.y), fma1(a.z, s, b.z)};
+}
+
+// arccos on [0, 1]: Abramowitz & Stegun 4.4.46, |error| <= 2e-8, Horner steps fused (the CUDA
+// library evaluates the same polynomial in its bend kernel, so both sides round identically).
 static inline float acos_as(float x) {
   float p = -0.0012624911f;
-  p = p * x + 0.0066700901f;
-  p = p * x + -0.0170881256f;
-  p = p * x + 0.0308918810f;
-  p = p * x + -0.0501743046f;
-  p = p * x + 0.0889789874f;
-  p = p * x + -0.2145988016f;
-  p = p * x + 1.5707963050f;
+  p = fma1(p, x, 0.0066700901f);
+  p = fma1(p, x, -0.0170881256f);
+  p = fma1(p, x, 0.0308918810f);
+  p = fma1(p, x, -0.0501743046f);
+  p = fma1(p, x, 0.0889789874f);
+  p = fma1(p, x, -0.2145988016f);
+  p = fma1(p, x, 1.5707963050f);
   return std::sqrt(1.0f - x) * p;
 }
 

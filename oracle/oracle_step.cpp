@@ -494,19 +494,17 @@ void solve_stretch(Oracle& o, uint32_t color, float dt, int iter) {
     uint32_t i1 = o.edges[id * 2], i2 = o.edges[id * 2 + 1];
     float expected = o.rest[id];
     V3 diff = o.x[i1] - o.x[i2];
-    float distance = length(diff);
+    float distance = std::sqrt(fdot(diff, diff));
     float w1 = o.w[i1], w2 = o.w[i2];
     if (distance != expected && w1 + w2 > 0.0f) {
       V3 gradient = diff * (1.0f / (distance + kEps));
       float alpha_tilde = o.s_comp[id] / (dt * dt);
       float constraint = distance - expected;
-      float dl = (-constraint - alpha_tilde * o.s_lambda[id]) / (w1 + w2 + alpha_tilde);
+      float dl = fma1(-alpha_tilde, o.s_lambda[id], -constraint) / (w1 + w2 + alpha_tilde);
       V3 corr = dl * gradient;
       o.s_lambda[id] = o.s_lambda[id] + dl;
-      V3 c1 = corr * w1;
-      V3 c2 = -corr * w2;
-      o.x[i1] += c1;
-      o.x[i2] += c2;
+      o.x[i1] = fmad(corr, w1, o.x[i1]);
+      o.x[i2] = fmad(-corr, w2, o.x[i2]);
     }
   }
 }
@@ -525,31 +523,30 @@ void solve_bend(Oracle& o, uint32_t color, float dt) {
     V3 p2 = o.x[i2] - p1;
     V3 p3 = o.x[i3] - p1;
     V3 p4 = o.x[i4] - p1;
-    V3 n1 = normalize(cross(p2, p3));
-    V3 n2 = normalize(cross(p2, p4));
-    float d = clampf(dot(n1, n2), 0.0f, 1.0f);
+    V3 c23 = fcross(p2, p3), c24 = fcross(p2, p4);
+    float l23 = std::sqrt(fdot(c23, c23)), l24 = std::sqrt(fdot(c24, c24));
+    V3 n1 = c23 * (1.0f / l23);  // normalize
+    V3 n2 = c24 * (1.0f / l24);
+    float d = clampf(fdot(n1, n2), 0.0f, 1.0f);
     float angle = acos_as(d);  // the reference calls acos; see oracle_math.h
     if (angle < kEps || std::isnan(d)) continue;
-    float r3 = 1.0f / (length(cross(p2, p3)) + kEps);
-    float r4 = 1.0f / (length(cross(p2, p4)) + kEps);
-    V3 q3 = (cross(p2, n2) + cross(n1, p2) * d) * r3;
-    V3 q4 = (cross(p2, n1) + cross(n2, p2) * d) * r4;
-    V3 q2 = -(cross(p3, n2) + cross(n1, p3) * d) * r3 - (cross(p4, n1) + cross(n2, p4) * d) * r4;
+    float r3 = 1.0f / (l23 + kEps);
+    float r4 = 1.0f / (l24 + kEps);
+    V3 q3 = fmad(fcross(n1, p2), d, fcross(p2, n2)) * r3;
+    V3 q4 = fmad(fcross(n2, p2), d, fcross(p2, n1)) * r4;
+    V3 q2 = -(fmad(fcross(n1, p3), d, fcross(p3, n2)) * r3) -
+            fmad(fcross(n2, p4), d, fcross(p4, n1)) * r4;
     V3 q1 = -q2 - q3 - q4;
     float xpbd_bend = o.b_comp[id] / dt / dt;
-    float denom = xpbd_bend + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) +
-                               w4 * dot(q4, q4));
+    float denom = xpbd_bend + fma1(w4, fdot(q4, q4),
+                                   fma1(w3, fdot(q3, q3), fma1(w2, fdot(q2, q2), w1 * fdot(q1, q1))));
     if (denom < kEps) continue;
-    float lambda = std::sqrt(1.0f - d * d) * (angle - expected) / denom;
+    float lambda = std::sqrt(fma1(-d, d, 1.0f)) * (angle - expected) / denom;
     float scaling = 1.0f;
-    V3 c1 = scaling * w1 * lambda * q1;
-    V3 c2 = scaling * w2 * lambda * q2;
-    V3 c3 = scaling * w3 * lambda * q3;
-    V3 c4 = scaling * w4 * lambda * q4;
-    o.x[i1] += c1;
-    o.x[i2] += c2;
-    o.x[i3] += c3;
-    o.x[i4] += c4;
+    o.x[i1] = fmad(q1, scaling * w1 * lambda, o.x[i1]);
+    o.x[i2] = fmad(q2, scaling * w2 * lambda, o.x[i2]);
+    o.x[i3] = fmad(q3, scaling * w3 * lambda, o.x[i3]);
+    o.x[i4] = fmad(q4, scaling * w4 * lambda, o.x[i4]);
   }
 }
 

@@ -65,18 +65,16 @@ __device__ __forceinline__ void tile_scatter(uint32_t nfoot, float4* __restrict_
 __device__ __forceinline__ bool stretch_project_alpha(float4& a, float4& b, float rest,
                                                       float alpha_tilde, float& lam) {
   const f3 diff = mk3(a) - mk3(b);
-  const float distance = length(diff);
+  const float distance = sqrtf(fdot(diff, diff));
   const float w1 = a.w, w2 = b.w;
   if (!(distance != rest && w1 + w2 > 0.0f)) return false;
   const f3 gradient = diff * (1.0f / (distance + kEps));
   const float constraint = distance - rest;
-  const float dl = (-constraint - alpha_tilde * lam) / (w1 + w2 + alpha_tilde);
+  const float dl = fmaf(-alpha_tilde, lam, -constraint) / (w1 + w2 + alpha_tilde);
   const f3 corr = dl * gradient;
   lam = lam + dl;
-  const f3 c1 = corr * w1;
-  const f3 c2 = -corr * w2;
-  a = make_float4(a.x + c1.x, a.y + c1.y, a.z + c1.z, a.w);
-  b = make_float4(b.x + c2.x, b.y + c2.y, b.z + c2.z, b.w);
+  a = mk4(fmad(corr, w1, mk3(a)), a.w);
+  b = mk4(fmad(-corr, w2, mk3(b)), b.w);
   return true;
 }
 
@@ -95,30 +93,32 @@ __device__ __forceinline__ void bend_project_alpha(float4& a1, float4& a2, float
   const f3 p2 = mk3(a2) - p1;
   const f3 p3 = mk3(a3) - p1;
   const f3 p4 = mk3(a4) - p1;
-  const f3 n1 = normalize(cross(p2, p3));
-  const f3 n2 = normalize(cross(p2, p4));
-  const float d = tclamp(dot(n1, n2), 0.0f, 1.0f);
+  const f3 c23 = fcross(p2, p3), c24 = fcross(p2, p4);
+  const float l23 = sqrtf(fdot(c23, c23)), l24 = sqrtf(fdot(c24, c24));
+  const f3 n1 = c23 * (1.0f / l23);  // normalize
+  const f3 n2 = c24 * (1.0f / l24);
+  const float d = tclamp(fdot(n1, n2), 0.0f, 1.0f);
   const float angle = acos_as(d);  // d in [0, 1] (or NaN, rejected below)
   if (angle < kEps || isnan(d)) return;
-  const float r3 = 1.0f / (length(cross(p2, p3)) + kEps);
-  const float r4 = 1.0f / (length(cross(p2, p4)) + kEps);
-  const f3 q3 = (cross(p2, n2) + cross(n1, p2) * d) * r3;
-  const f3 q4 = (cross(p2, n1) + cross(n2, p2) * d) * r4;
-  const f3 q2 = -(cross(p3, n2) + cross(n1, p3) * d) * r3 - (cross(p4, n1) + cross(n2, p4) * d) * r4;
+  const float r3 = 1.0f / (l23 + kEps);
+  const float r4 = 1.0f / (l24 + kEps);
+  // q3 = (p2 x n2 + (n1 x p2) d) / (|p2 x p3| + eps), q4 likewise, q2 = -(p3 x n2 + (n1 x p3) d)
+  // / (|p2 x p3| + eps) - (p4 x n1 + (n2 x p4) d) / (|p2 x p4| + eps)
+  const f3 q3 = fmad(fcross(n1, p2), d, fcross(p2, n2)) * r3;
+  const f3 q4 = fmad(fcross(n2, p2), d, fcross(p2, n1)) * r4;
+  const f3 q2 = -(fmad(fcross(n1, p3), d, fcross(p3, n2)) * r3) -
+                fmad(fcross(n2, p4), d, fcross(p4, n1)) * r4;
   const f3 q1 = -q2 - q3 - q4;
   const float denom =
-      xpbd_bend + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) + w4 * dot(q4, q4));
+      xpbd_bend +
+      fmaf(w4, fdot(q4, q4), fmaf(w3, fdot(q3, q3), fmaf(w2, fdot(q2, q2), w1 * fdot(q1, q1))));
   if (denom < kEps) return;
-  const float lambda = sqrtf(1.0f - d * d) * (angle - theta) / denom;
+  const float lambda = sqrtf(fmaf(-d, d, 1.0f)) * (angle - theta) / denom;
   const float scaling = 1.0f;
-  const f3 c1 = scaling * w1 * lambda * q1;
-  const f3 c2 = scaling * w2 * lambda * q2;
-  const f3 c3 = scaling * w3 * lambda * q3;
-  const f3 c4 = scaling * w4 * lambda * q4;
-  a1 = make_float4(a1.x + c1.x, a1.y + c1.y, a1.z + c1.z, w1);
-  a2 = make_float4(a2.x + c2.x, a2.y + c2.y, a2.z + c2.z, w2);
-  a3 = make_float4(a3.x + c3.x, a3.y + c3.y, a3.z + c3.z, w3);
-  a4 = make_float4(a4.x + c4.x, a4.y + c4.y, a4.z + c4.z, w4);
+  a1 = mk4(fmad(q1, scaling * w1 * lambda, mk3(a1)), w1);
+  a2 = mk4(fmad(q2, scaling * w2 * lambda, mk3(a2)), w2);
+  a3 = mk4(fmad(q3, scaling * w3 * lambda, mk3(a3)), w3);
+  a4 = mk4(fmad(q4, scaling * w4 * lambda, mk3(a4)), w4);
 }
 
 __device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3, float4& a4,
@@ -131,7 +131,8 @@ __device__ __forceinline__ void bend_project(float4& a1, float4& a2, float4& a3,
 // shared-memory footprint of a tile: each lane evaluates one of the two independent halves of
 // the expression (normal n1 and gradient q3 / normal n2, gradient q4 and the angle), the halves
 // are exchanged by shuffles, and lane 0 writes vertices 1-2, lane 1 vertices 3-4.  Every value is
-// produced by the same operations as bend_project, so the result is identical.  All 32 lanes
+// produced by the same operations (fused ones included) as bend_project_alpha, so the result is
+// identical.  All 32 lanes
 // call it; `active` is false for lanes past the color's last element (they write nothing).
 // With (nA, nB, rA) = (n1, n2, 1 / (|p2 x p3| + eps)) on lane 0 and (n2, n1, 1 / (|p2 x p4| +
 // eps)) on lane 1, and pA = p3 / p4:
@@ -147,16 +148,17 @@ __device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float thet
   const f3 p3 = mk3(a3) - p1;
   const f3 p4 = mk3(a4) - p1;
   const f3 pA = half ? p4 : p3;
-  const f3 cA = cross(p2, pA);
-  const f3 nA = normalize(cA);
-  const float rA = 1.0f / (length(cA) + kEps);
+  const f3 cA = fcross(p2, pA);
+  const float lA = sqrtf(fdot(cA, cA));
+  const f3 nA = cA * (1.0f / lA);  // normalize
+  const float rA = 1.0f / (lA + kEps);
   const f3 nB = mk3(__shfl_xor_sync(kAll, nA.x, 1), __shfl_xor_sync(kAll, nA.y, 1),
                     __shfl_xor_sync(kAll, nA.z, 1));
   const f3 n1 = half ? nB : nA, n2 = half ? nA : nB;
-  const float d = tclamp(dot(n1, n2), 0.0f, 1.0f);
+  const float d = tclamp(fdot(n1, n2), 0.0f, 1.0f);
   const float angle = acos_as(d);
-  const f3 qA = (cross(p2, nB) + cross(nA, p2) * d) * rA;   // q3 on lane 0, q4 on lane 1
-  const f3 vA = (cross(pA, nB) + cross(nA, pA) * d) * rA;   // |terms| of q2
+  const f3 qA = fmad(fcross(nA, p2), d, fcross(p2, nB)) * rA;  // q3 on lane 0, q4 on lane 1
+  const f3 vA = fmad(fcross(nA, pA), d, fcross(pA, nB)) * rA;  // |terms| of q2
   const f3 qB = mk3(__shfl_xor_sync(kAll, qA.x, 1), __shfl_xor_sync(kAll, qA.y, 1),
                     __shfl_xor_sync(kAll, qA.z, 1));
   const f3 vB = mk3(__shfl_xor_sync(kAll, vA.x, 1), __shfl_xor_sync(kAll, vA.y, 1),
@@ -167,18 +169,17 @@ __device__ __forceinline__ void bend_project_pair(float4* sx, int4 b, float thet
   const f3 q1 = -q2 - q3 - q4;
   const float w1 = a1.w, w2 = a2.w, w3 = a3.w, w4 = a4.w;
   const float denom =
-      xpbd_bend + (w1 * dot(q1, q1) + w2 * dot(q2, q2) + w3 * dot(q3, q3) + w4 * dot(q4, q4));
+      xpbd_bend +
+      fmaf(w4, fdot(q4, q4), fmaf(w3, fdot(q3, q3), fmaf(w2, fdot(q2, q2), w1 * fdot(q1, q1))));
   if (!active || angle < kEps || isnan(d) || denom < kEps) return;
-  const float lambda = sqrtf(1.0f - d * d) * (angle - theta) / denom;
+  const float lambda = sqrtf(fmaf(-d, d, 1.0f)) * (angle - theta) / denom;
   const float scaling = 1.0f;
   // lane 0 moves vertices 1 and 2, lane 1 vertices 3 and 4
   const float wa = half ? w3 : w1, wb = half ? w4 : w2;
   const f3 qa = half ? q3 : q1, qb = half ? q4 : q2;
   const float4 aa = half ? a3 : a1, ab = half ? a4 : a2;
-  const f3 ca = scaling * wa * lambda * qa;
-  const f3 cb = scaling * wb * lambda * qb;
-  sx[half ? b.z : b.x] = make_float4(aa.x + ca.x, aa.y + ca.y, aa.z + ca.z, wa);
-  sx[half ? b.w : b.y] = make_float4(ab.x + cb.x, ab.y + cb.y, ab.z + cb.z, wb);
+  sx[half ? b.z : b.x] = mk4(fmad(qa, scaling * wa * lambda, mk3(aa)), wa);
+  sx[half ? b.w : b.y] = mk4(fmad(qb, scaling * wb * lambda, mk3(ab)), wb);
 }
 
 // ---- FEM fabric (FEMHelper.cu) -------------------------------------------------------------
