@@ -638,9 +638,12 @@ void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles);
 void launch_lra(Context& c, const FrameConst& k);
 // Iteration tail, each launch reads x and writes x_alt (caller swaps):
 // LRA with all slots pinned (else launch_lra runs before) + VF solve ...
-void launch_stage(Context& c, const FrameConst& k, bool lra, bool contacts);
+// `tape` (the adjoint's recorded replay): each vertex's input position is also written there.
+void launch_stage(Context& c, const FrameConst& k, bool lra, bool contacts,
+                  float4* tape = nullptr);
 // ... then EE solve + ApplyDeltas + binding.
-void launch_ee(Context& c, const FrameConst& k, bool contacts, bool bindings);
+void launch_ee(Context& c, const FrameConst& k, bool contacts, bool bindings,
+               float4* tape = nullptr);
 void launch_obstacle_pass(Context& c, int step, int num_steps);
 void launch_generate_contacts(Context& c);
 void launch_obstacle_commit(Context& c);

@@ -42,6 +42,8 @@ __global__ void k_stretch_tape(const uint32_t* __restrict__ order, uint32_t begi
                                const int2* __restrict__ gidx, const int4* __restrict__ con,
                                float* __restrict__ lambda, float4* __restrict__ x,
                                float4* __restrict__ tx, float* __restrict__ tl, float dt) {
+  pdl_release();
+  pdl_wait();
   const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= end) return;
   const uint32_t j = order[k];
@@ -64,6 +66,8 @@ __global__ void k_stretch_tape(const uint32_t* __restrict__ order, uint32_t begi
 __global__ void k_bend_tape(const uint32_t* __restrict__ order, uint32_t begin, uint32_t end,
                             const int4* __restrict__ gidx, const float2* __restrict__ tc,
                             float4* __restrict__ x, float4* __restrict__ tx, float dt) {
+  pdl_release();
+  pdl_wait();
   const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= end) return;
   const uint32_t j = order[k];
@@ -105,7 +109,7 @@ __device__ __forceinline__ bool stretch_vjp(float4 A, float4 B, float lam, float
                                             float dt, float lbo, float4& ga, float4& gb,
                                             float& lam_in_bar, float& cbar) {
   const f3 d = mk3(A) - mk3(B);
-  const float dist = length(d);  // as the forward: it decides whether the projection ran
+  const float dist = sqrtf(fdot(d, d));  // as the forward: it decides whether the projection ran
   const float wa = A.w, wb = B.w;
   if (!(dist != rest && wa + wb > 0.0f)) return false;
   const float re = frcp(dist + kEps);
@@ -145,6 +149,8 @@ __global__ void k_stretch_bwd(const uint32_t* __restrict__ order, uint32_t begin
                               const float4* __restrict__ tx, const float* __restrict__ tl,
                               float4* __restrict__ G, float* __restrict__ lam_bar,
                               float* __restrict__ comp_bar, float dt) {
+  pdl_release();
+  pdl_wait();
   const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= end) return;
   const uint32_t j = order[k];
@@ -185,11 +191,11 @@ __device__ __forceinline__ bool bend_vjp(float4 A1, float4 A2, float4 A3, float4
   const float w1 = A1.w, w2 = A2.w, w3 = A3.w, w4 = A4.w;
   const f3 p1 = mk3(A1);
   const f3 p2 = mk3(A2) - p1, p3 = mk3(A3) - p1, p4 = mk3(A4) - p1;
-  const f3 c23 = cross(p2, p3), c24 = cross(p2, p4);
-  const float d23 = dot(c23, c23), d24 = dot(c24, c24);
+  const f3 c23 = fcross(p2, p3), c24 = fcross(p2, p4);  // the forward's fused forms, exactly
+  const float d23 = fdot(c23, c23), d24 = fdot(c24, c24);
   const float i23 = 1.0f / sqrtf(d23), i24 = 1.0f / sqrtf(d24);  // normalize's, exactly
   const f3 n1 = c23 * i23, n2 = c24 * i24;
-  const float draw = dot(n1, n2);
+  const float draw = fdot(n1, n2);
   const float d = tclamp(draw, 0.0f, 1.0f);
   const float angle = acos_as(d);
   if (angle < kEps || isnan(d)) return false;  // not projected: identity
@@ -284,6 +290,8 @@ __global__ void k_bend_bwd(const uint32_t* __restrict__ order, uint32_t begin, u
                            const int4* __restrict__ gidx, const float2* __restrict__ tc,
                            const float4* __restrict__ tx, float4* __restrict__ G,
                            float* __restrict__ bcomp_bar, float dt) {
+  pdl_release();
+  pdl_wait();
   const uint32_t k = begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= end) return;
   const uint32_t j = order[k];
@@ -328,10 +336,9 @@ __global__ void __launch_bounds__(NT) k_stretch_tiles_tape(
   uint32_t* sf = so + num_local + 1;
   const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
   const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
-  for (uint32_t j = threadIdx.x; j < nc; j += NT) {
-    sc[j] = __ldg(&con[c0 + j]);
-    sl[j] = RESET ? 0.0f : lambda[c0 + j];
-  }
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) sc[j] = __ldg(&con[c0 + j]);  // setup data
+  pdl_wait();
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) sl[j] = RESET ? 0.0f : lambda[c0 + j];
   tile_gather<NT>(f, x, sx, sf);
   __syncthreads();
   for (uint32_t l = 0; l < num_local; ++l) {
@@ -351,6 +358,7 @@ __global__ void __launch_bounds__(NT) k_stretch_tiles_tape(
     }
     __syncthreads();
   }
+  pdl_release();
   tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
   for (uint32_t j = threadIdx.x; j < nc; j += NT) lambda[c0 + j] = sl[j];
 }
@@ -369,10 +377,11 @@ __global__ void __launch_bounds__(NT) k_bend_tiles_tape(
   uint32_t* sf = so + num_local + 1;
   const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
   const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
-  for (uint32_t j = threadIdx.x; j < nc; j += NT) {
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) {  // setup data
     sc[j] = __ldg(&idx[c0 + j]);
     st[j] = __ldg(&tc[c0 + j]);
   }
+  pdl_wait();
   tile_gather<NT>(f, x, sx, sf);
   __syncthreads();
   // the forward's lane-pair projection (bend_project_pair, the same bits as bend_project); each
@@ -396,6 +405,7 @@ __global__ void __launch_bounds__(NT) k_bend_tiles_tape(
     }
     __syncthreads();
   }
+  pdl_release();
   tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
 }
 
@@ -419,14 +429,15 @@ __global__ void __launch_bounds__(NT) k_stretch_tiles_bwd(
   uint32_t* sf = so + num_local + 1;
   const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
   const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) sc[j] = __ldg(&con[c0 + j]);  // setup data
+  pdl_wait();  // the tape and the adjoints are written by earlier launches of the reverse
   if (STAGE) {
     const float4* src = tx + 2 * (size_t)c0;
-    for (uint32_t k = threadIdx.x; k < 2 * nc; k += NT) stx[k] = __ldg(&src[k]);
+    for (uint32_t k = threadIdx.x; k < 2 * nc; k += NT) stx[k] = src[k];
   }
   for (uint32_t j = threadIdx.x; j < nc; j += NT) {
-    sc[j] = __ldg(&con[c0 + j]);
     slb[j] = lam_bar[c0 + j];
-    if (STAGE) stl[j] = __ldg(&tl[c0 + j]);
+    if (STAGE) stl[j] = tl[c0 + j];
   }
   tile_gather<NT>(f, G, sg, sf);
   __syncthreads();
@@ -448,6 +459,7 @@ __global__ void __launch_bounds__(NT) k_stretch_tiles_bwd(
     }
     __syncthreads();
   }
+  pdl_release();
   tile_scatter<NT>((uint32_t)f.m.y, G, sg, sf);
   for (uint32_t j = threadIdx.x; j < nc; j += NT) lam_bar[c0 + j] = slb[j];
 }
@@ -468,13 +480,14 @@ __global__ void __launch_bounds__(NT) k_bend_tiles_bwd(
   uint32_t* sf = so + num_local + 1;
   const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
   const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
-  if (STAGE) {
-    const float4* src = tx + 4 * (size_t)c0;
-    for (uint32_t k = threadIdx.x; k < 4 * nc; k += NT) stx[k] = __ldg(&src[k]);
-  }
-  for (uint32_t j = threadIdx.x; j < nc; j += NT) {
+  for (uint32_t j = threadIdx.x; j < nc; j += NT) {  // setup data
     sc[j] = __ldg(&idx[c0 + j]);
     st[j] = __ldg(&tc[c0 + j]);
+  }
+  pdl_wait();  // the tape and the adjoints are written by earlier launches of the reverse
+  if (STAGE) {
+    const float4* src = tx + 4 * (size_t)c0;
+    for (uint32_t k = threadIdx.x; k < 4 * nc; k += NT) stx[k] = src[k];
   }
   tile_gather<NT>(f, G, sg, sf);
   __syncthreads();
@@ -497,6 +510,7 @@ __global__ void __launch_bounds__(NT) k_bend_tiles_bwd(
     }
     __syncthreads();
   }
+  pdl_release();
   tile_scatter<NT>((uint32_t)f.m.y, G, sg, sf);
 }
 
@@ -512,6 +526,8 @@ __global__ void k_stage_bwd(const float4* __restrict__ X, const float4* __restri
                             const int* __restrict__ rt_idx, const float4* __restrict__ rt_qc,
                             const int* __restrict__ vf_idx, const float4* __restrict__ vf_qs,
                             const float4* __restrict__ pred, uint32_t* err) {
+  pdl_release();
+  pdl_wait();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nv) return;
   const float4 p = X[t];
@@ -582,6 +598,8 @@ __global__ void k_stage_bwd(const float4* __restrict__ X, const float4* __restri
 }
 
 __global__ void k_add_sources(float4* __restrict__ G, float4* __restrict__ Gs, uint32_t nv) {
+  pdl_release();
+  pdl_wait();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nv) return;
   const float4 s = Gs[i];
@@ -626,6 +644,8 @@ __global__ void k_ee_count(const float4* __restrict__ X, uint32_t nv,
                            const uint2* __restrict__ edge, const float4* __restrict__ ee_a,
                            const float4* __restrict__ ee_b, const float4* __restrict__ ee_c,
                            float* __restrict__ cnt) {
+  pdl_release();
+  pdl_wait();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nv) return;
   int n = 0;
@@ -642,6 +662,8 @@ __global__ void k_ee_bwd(const float4* __restrict__ X, const float4* __restrict_
                          const uint2* __restrict__ edge, const float4* __restrict__ ee_a,
                          const float4* __restrict__ ee_b, const float4* __restrict__ ee_c,
                          const float* __restrict__ cnt, float relaxation) {
+  pdl_release();
+  pdl_wait();
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nv) return;
   const float4 gj = Gin[j];
@@ -665,6 +687,8 @@ __global__ void k_ee_bwd(const float4* __restrict__ X, const float4* __restrict_
 // finalize: v' = (x_end - x0) / dt * kd, x0' = x_end.  G: x0'-bar -> x_end-bar, H: x0-bar part.
 __global__ void k_finalize_bwd(float4* __restrict__ G, float4* __restrict__ Gv,
                                float4* __restrict__ H, uint32_t nv, float dt, float kd) {
+  pdl_release();
+  pdl_wait();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nv) return;
   const float4 g = G[i];
@@ -677,6 +701,8 @@ __global__ void k_finalize_bwd(float4* __restrict__ G, float4* __restrict__ Gv,
 // predict: x_p = x0 + v_p dt, v_p = v + g dt.  G: x_p-bar -> x0-bar, Gv: v-bar.
 __global__ void k_predict_bwd(float4* __restrict__ G, float4* __restrict__ Gv,
                               const float4* __restrict__ H, uint32_t nv, float dt) {
+  pdl_release();
+  pdl_wait();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nv) return;
   const float4 g = G[i];
@@ -857,7 +883,7 @@ void stretch_tiles_tape(Context& c, float dt, bool reset, size_t ti) {
   float* tl = D.t_sl.p + ti * c.ne;
   for (const ColorRange& r : T.tile_colors)
     if (r.end > r.begin)
-      kern<<<r.end - r.begin, T.block, smem, c.stream>>>(c.s_con.p, c.s_lambda.p, c.x.p,
+      launch_k(c.pdl, kern, r.end - r.begin, T.block, smem, c.stream, c.s_con.p, c.s_lambda.p, c.x.p,
                                                          T.foot.p, T.meta.p, T.lofs.p, r.begin,
                                                          T.num_local, T.max_foot, T.max_cons, dt,
                                                          tx, tl);
@@ -871,7 +897,7 @@ void bend_tiles_tape(Context& c, float dt, size_t ti) {
   float4* tx = D.t_bx.p + 4 * ti * c.nb;
   for (const ColorRange& r : T.tile_colors)
     if (r.end > r.begin)
-      kern<<<r.end - r.begin, T.block, smem, c.stream>>>(c.b_idx.p, c.b_tc.p, c.x.p, T.foot.p,
+      launch_k(c.pdl, kern, r.end - r.begin, T.block, smem, c.stream, c.b_idx.p, c.b_tc.p, c.x.p, T.foot.p,
                                                          T.meta.p, T.lofs.p, r.begin, T.num_local,
                                                          T.max_foot, T.max_cons, dt, tx);
 }
@@ -886,7 +912,7 @@ void stretch_tiles_bwd(Context& c, float dt, bool reset, size_t ti) {
   for (int k = (int)T.tile_colors.size() - 1; k >= 0; --k) {
     const ColorRange r = T.tile_colors[k];
     if (r.end > r.begin)
-      kern<<<r.end - r.begin, D.s_block, smem, c.stream>>>(
+      launch_k(c.pdl, kern, r.end - r.begin, D.s_block, smem, c.stream,
           c.s_con.p, T.foot.p, T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot, T.max_cons,
           dt, tx, tl, D.G.p, D.lam_bar.p, D.comp_bar.p);
   }
@@ -901,7 +927,7 @@ void bend_tiles_bwd(Context& c, float dt, size_t ti) {
   for (int k = (int)T.tile_colors.size() - 1; k >= 0; --k) {
     const ColorRange r = T.tile_colors[k];
     if (r.end > r.begin)
-      kern<<<r.end - r.begin, D.b_block, smem, c.stream>>>(
+      launch_k(c.pdl, kern, r.end - r.begin, D.b_block, smem, c.stream,
           c.b_idx.p, c.b_tc.p, T.foot.p, T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot,
           T.max_cons, dt, tx, D.G.p, D.bcomp_bar.p);
   }
@@ -963,12 +989,12 @@ void record_frame_diff(Context& c) {
       else for (const ColorRange& r : D.s_colors) {
         const unsigned g = grid_for(r.end - r.begin);
         if (it == 0)
-          k_stretch_tape<true><<<g, blk, 0, c.stream>>>(D.s_order.p, r.begin, r.end, D.s_gidx.p,
+          launch_k(c.pdl, k_stretch_tape<true>, g, blk, 0, c.stream, D.s_order.p, r.begin, r.end, D.s_gidx.p,
                                                          c.s_con.p, c.s_lambda.p, c.x.p,
                                                          D.t_sx.p + 2 * ti * E, D.t_sl.p + ti * E,
                                                          k.dt);
         else
-          k_stretch_tape<false><<<g, blk, 0, c.stream>>>(D.s_order.p, r.begin, r.end, D.s_gidx.p,
+          launch_k(c.pdl, k_stretch_tape<false>, g, blk, 0, c.stream, D.s_order.p, r.begin, r.end, D.s_gidx.p,
                                                           c.s_con.p, c.s_lambda.p, c.x.p,
                                                           D.t_sx.p + 2 * ti * E,
                                                           D.t_sl.p + ti * E, k.dt);
@@ -976,17 +1002,15 @@ void record_frame_diff(Context& c) {
       if (p.solve_bending && D.b_tiled) bend_tiles_tape(c, k.dt, ti);
       else if (p.solve_bending)
         for (const ColorRange& r : D.b_colors)
-          k_bend_tape<<<grid_for(r.end - r.begin), blk, 0, c.stream>>>(
+          launch_k(c.pdl, k_bend_tape, grid_for(r.end - r.begin), blk, 0, c.stream,
               D.b_order.p, r.begin, r.end, D.b_gidx.p, c.b_tc.p, c.x.p, D.t_bx.p + 4 * ti * B,
               k.dt);
-      if (lra_fused || has_obstacle) {
-        copy_d(D.t_stage.p + ti * V, c.x.p, sizeof(float4) * V, c.stream);
-        launch_stage(c, k, lra_fused, has_obstacle);
+      if (lra_fused || has_obstacle) {  // the launches tape their input positions
+        launch_stage(c, k, lra_fused, has_obstacle, D.t_stage.p + ti * V);
         swap_x();
       }
       if (has_obstacle) {
-        copy_d(D.t_ee.p + ti * V, c.x.p, sizeof(float4) * V, c.stream);
-        launch_ee(c, k, has_obstacle, false);
+        launch_ee(c, k, has_obstacle, false, D.t_ee.p + ti * V);
         swap_x();
       }
     }
@@ -1020,7 +1044,7 @@ void backward_frame(Context& c) {
   for (int s = (int)D.S - 1; s >= 0; --s) {
     {
       Timed t(c, kAdjVertex, 1, V);
-      k_finalize_bwd<<<gv, blk, 0, c.stream>>>(D.G.p, D.Gv.p, D.H.p, V, k.dt, kd);
+      launch_k(c.pdl, k_finalize_bwd, gv, blk, 0, c.stream, D.G.p, D.Gv.p, D.H.p, V, k.dt, kd);
       cudaMemsetAsync(D.lam_bar.p, 0, sizeof(float) * std::max(E, 1u), c.stream);
     }
     for (int it = (int)D.I - 1; it >= 0; --it) {
@@ -1031,21 +1055,21 @@ void backward_frame(Context& c) {
         Timed tv(c, kAdjVertex, n_vertex_launches, V);
         if (has_obstacle) {
           const float4* X = D.t_ee.p + ti * V;
-          k_ee_count<<<gv, blk, 0, c.stream>>>(X, V, c.ve_ptr.p, c.ve_list.p, c.edge.p,
+          launch_k(c.pdl, k_ee_count, gv, blk, 0, c.stream, X, V, c.ve_ptr.p, c.ve_list.p, c.edge.p,
                                               D.t_ee_a.p + pe, D.t_ee_b.p + pe, D.t_ee_c.p + pe,
                                               D.cnt.p);
-          k_ee_bwd<<<gv, blk, 0, c.stream>>>(X, D.G.p, D.G2.p, V, c.ve_ptr.p, c.ve_list.p,
+          launch_k(c.pdl, k_ee_bwd, gv, blk, 0, c.stream, X, D.G.p, D.G2.p, V, c.ve_ptr.p, c.ve_list.p,
                                             c.edge.p, D.t_ee_a.p + pe, D.t_ee_b.p + pe,
                                             D.t_ee_c.p + pe, D.cnt.p, k.relaxation);
           std::swap(D.G.p, D.G2.p);
         }
         if (lra_fused || has_obstacle) {
-          k_stage_bwd<<<gv, blk, 0, c.stream>>>(
+          launch_k(c.pdl, k_stage_bwd, gv, blk, 0, c.stream,
               D.t_stage.p + ti * V, D.G.p, D.G2.p, D.Gs.p, V, lra_fused, c.lra_ptr.p,
               c.lra_src.p, c.lra_rest.p, k.lra_stretch, has_obstacle, D.t_rt_idx.p + pv,
               D.t_rt_qc.p + pv, D.t_vf_idx.p + pv, D.t_vf_qs.p + pv,
               D.t_pred.p + (size_t)pass * 3 * c.onf, c.err.p);
-          if (lra_fused) k_add_sources<<<gv, blk, 0, c.stream>>>(D.G2.p, D.Gs.p, V);
+          if (lra_fused) launch_k(c.pdl, k_add_sources, gv, blk, 0, c.stream, D.G2.p, D.Gs.p, V);
           std::swap(D.G.p, D.G2.p);
         }
       }
@@ -1055,7 +1079,7 @@ void backward_frame(Context& c) {
         else
           for (int ci = (int)D.b_colors.size() - 1; ci >= 0; --ci) {
             const ColorRange r = D.b_colors[ci];
-            k_bend_bwd<<<grid_for(r.end - r.begin), blk, 0, c.stream>>>(
+            launch_k(c.pdl, k_bend_bwd, grid_for(r.end - r.begin), blk, 0, c.stream,
                 D.b_order.p, r.begin, r.end, D.b_gidx.p, c.b_tc.p, D.t_bx.p + 4 * ti * B, D.G.p,
                 D.bcomp_bar.p, k.dt);
           }
@@ -1066,19 +1090,19 @@ void backward_frame(Context& c) {
         const ColorRange r = D.s_colors[ci];
         const unsigned g = grid_for(r.end - r.begin);
         if (it == 0)
-          k_stretch_bwd<true><<<g, blk, 0, c.stream>>>(D.s_order.p, r.begin, r.end, D.s_gidx.p,
+          launch_k(c.pdl, k_stretch_bwd<true>, g, blk, 0, c.stream, D.s_order.p, r.begin, r.end, D.s_gidx.p,
                                                         c.s_con.p, D.t_sx.p + 2 * ti * E,
                                                         D.t_sl.p + ti * E, D.G.p, D.lam_bar.p,
                                                         D.comp_bar.p, k.dt);
         else
-          k_stretch_bwd<false><<<g, blk, 0, c.stream>>>(D.s_order.p, r.begin, r.end, D.s_gidx.p,
+          launch_k(c.pdl, k_stretch_bwd<false>, g, blk, 0, c.stream, D.s_order.p, r.begin, r.end, D.s_gidx.p,
                                                          c.s_con.p, D.t_sx.p + 2 * ti * E,
                                                          D.t_sl.p + ti * E, D.G.p, D.lam_bar.p,
                                                          D.comp_bar.p, k.dt);
       }
     }
     Timed t(c, kAdjVertex, 1, V);
-    k_predict_bwd<<<gv, blk, 0, c.stream>>>(D.G.p, D.Gv.p, D.H.p, V, k.dt);
+    launch_k(c.pdl, k_predict_bwd, gv, blk, 0, c.stream, D.G.p, D.Gv.p, D.H.p, V, k.dt);
   }
 }
 

@@ -386,6 +386,7 @@ struct TailArgs {
   const float4* bind_a;
   const int4* bind_b;
   const float4* ox;
+  float4* tape;  // when set (the adjoint's recorded replay): each vertex's input x_in is copied here
 };
 
 // Position of vertex j after the LRA and VF phases.
@@ -426,6 +427,7 @@ __global__ void k_stage(const TailArgs a) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.nv) return;
   const float4 p = a.x_in[i];
+  if (a.tape) a.tape[i] = p;
   a.x_out[i] = mk4(tail_stage<LRA, CONTACTS>(a, i, p), p.w);
 }
 
@@ -453,6 +455,7 @@ __global__ void k_ee(const TailArgs a) {
   const uint32_t* __restrict__ ve_list = a.ve_list;
   const float relaxation = a.relaxation;
   const float4 p = x_in[i];
+  if (a.tape) a.tape[i] = p;
   f3 q = mk3(p);
   // a vertex none of whose edges holds a contact skips the list (delta 0, count 0)
   if (CONTACTS && a.ee_vflag[i]) {
@@ -719,19 +722,24 @@ static TailArgs tail_args(Context& c, const FrameConst& k) {
   a.bind_a = c.bind_a.p;
   a.bind_b = c.bind_b.p;
   a.ox = c.ox.p;
+  a.tape = nullptr;
   return a;
 }
 
-void launch_stage(Context& c, const FrameConst& k, bool lra, bool contacts) {
+void launch_stage(Context& c, const FrameConst& k, bool lra, bool contacts, float4* tape) {
   if (!lra && !contacts) return;
   auto kern = lra ? (contacts ? k_stage<true, true> : k_stage<true, false>) : k_stage<false, true>;
-  launch_k(c.pdl, kern, grid_for(c.nv, c.vertex_block), c.vertex_block, 0, c.stream, tail_args(c, k));
+  TailArgs a = tail_args(c, k);
+  a.tape = tape;
+  launch_k(c.pdl, kern, grid_for(c.nv, c.vertex_block), c.vertex_block, 0, c.stream, a);
 }
 
-void launch_ee(Context& c, const FrameConst& k, bool contacts, bool bindings) {
+void launch_ee(Context& c, const FrameConst& k, bool contacts, bool bindings, float4* tape) {
   if (!contacts && !bindings) return;
   auto kern = contacts ? (bindings ? k_ee<true, true> : k_ee<true, false>) : k_ee<false, true>;
-  launch_k(c.pdl, kern, grid_for(c.nv, c.vertex_block), c.vertex_block, 0, c.stream, tail_args(c, k));
+  TailArgs a = tail_args(c, k);
+  a.tape = tape;
+  launch_k(c.pdl, kern, grid_for(c.nv, c.vertex_block), c.vertex_block, 0, c.stream, a);
 }
 
 }  // namespace xrt
