@@ -207,7 +207,8 @@ struct DiffState {
   DBuf<float4> t_pred;                  // P x 3F (obstacle primitives of the pass)
   // adjoint
   DBuf<float4> G, G2, Gv, H, Gs;        // x-bar (+ inverse-mass bar in w), v-bar, temporaries
-  DBuf<float> cnt, lam_bar, comp_bar, bcomp_bar;
+  DBuf<float> cnt;                      // tape: per iteration, each vertex's EE contact count
+  DBuf<float> lam_bar, comp_bar, bcomp_bar;
   // one frame's replay + reverse as a CUDA graph (built per xrt_backward call), per starting
   // assignment of the G / G2 double buffer, with the assignment the frame leaves
   struct FrameGraph {
@@ -633,17 +634,22 @@ void launch_unpack_xyz(const float* in, float4* out, uint32_t n, float w, cudaSt
 // Sets T.block (256 / 512 threads) and T.resident; after configure_tile_kernels.
 cudaError_t choose_tile_block(TiledSet& T, bool bend);
 // tile-local Gauss-Seidel: all tiles of one tile color (range of executed tiles)
-void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, bool reset_lambda);
-void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles);
+// tape_x / tape_l (the adjoint's recorded replay): every projection's input positions (and
+// multiplier) are also written there, by execution slot.
+void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, bool reset_lambda,
+                          float4* tape_x = nullptr, float* tape_l = nullptr);
+void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles,
+                       float4* tape_x = nullptr);
 void launch_lra(Context& c, const FrameConst& k);
 // Iteration tail, each launch reads x and writes x_alt (caller swaps):
 // LRA with all slots pinned (else launch_lra runs before) + VF solve ...
-// `tape` (the adjoint's recorded replay): each vertex's input position is also written there.
+// `tape` (the adjoint's recorded replay): each vertex's input position is also written there;
+// `tape_cnt` (launch_ee, with `tape`): each vertex's count of applied EE contacts.
 void launch_stage(Context& c, const FrameConst& k, bool lra, bool contacts,
                   float4* tape = nullptr);
 // ... then EE solve + ApplyDeltas + binding.
 void launch_ee(Context& c, const FrameConst& k, bool contacts, bool bindings,
-               float4* tape = nullptr);
+               float4* tape = nullptr, float* tape_cnt = nullptr);
 void launch_obstacle_pass(Context& c, int step, int num_steps);
 void launch_generate_contacts(Context& c);
 void launch_obstacle_commit(Context& c);

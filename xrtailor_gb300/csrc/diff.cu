@@ -310,104 +310,16 @@ __global__ void k_bend_bwd(const uint32_t* __restrict__ order, uint32_t begin, u
 }
 
 // ---- tiled replay and reverse ---------------------------------------------------------------
-// With the tile-local schedule the replay runs the forward's tile kernels (one launch per tile
-// color, footprint in shared memory, the forward's code in the forward's order, hence its bits)
-// and tapes each projection's inputs by execution slot (a local color's slots are contiguous, so
-// the tape writes coalesce).  The reverse of a tile color launch is one block per tile, tile
+// With the tile-local schedule the replay runs the forward's own tile launches (solver.cu
+// k_stretch_tiles / k_bend_tiles with their tape pointers set: the same kernels, hence the same
+// bits), which tape each projection's inputs by execution slot (a local color's slots are
+// contiguous, so the tape writes coalesce).  The reverse of a tile color launch is one block per tile, tile
 // colors last to first: the block stages the footprint's adjoint in shared memory and walks the
 // tile's local colors backwards, reading the taped inputs.  Tiles of one tile color have
 // disjoint footprints, so the write-back of the adjoint needs no atomics.  Shared memory of the
 // reverse: adjoint (16 B) and id (4 B) per footprint vertex; record (16 B) + multiplier adjoint
 // (stretch, 4 B) or rest angle and compliance (bend, 8 B) per constraint; num_local + 1
 // offsets.
-
-template <bool RESET, int NT>
-__global__ void __launch_bounds__(NT) k_stretch_tiles_tape(
-    const int4* __restrict__ con, float* __restrict__ lambda, float4* __restrict__ x,
-    const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
-    const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
-    uint32_t max_foot, uint32_t max_cons, float dt, float4* __restrict__ tx,
-    float* __restrict__ tl) {
-  extern __shared__ float4 smem[];
-  float4* sx = smem;
-  int4* sc = reinterpret_cast<int4*>(sx + max_foot);
-  float* sl = reinterpret_cast<float*>(sc + max_cons);
-  uint32_t* so = reinterpret_cast<uint32_t*>(sl + max_cons);
-  uint32_t* sf = so + num_local + 1;
-  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
-  const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
-  for (uint32_t j = threadIdx.x; j < nc; j += NT) sc[j] = __ldg(&con[c0 + j]);  // setup data
-  pdl_wait();
-  for (uint32_t j = threadIdx.x; j < nc; j += NT) sl[j] = RESET ? 0.0f : lambda[c0 + j];
-  tile_gather<NT>(f, x, sx, sf);
-  __syncthreads();
-  for (uint32_t l = 0; l < num_local; ++l) {
-    const uint32_t ce = so[l + 1];
-    for (uint32_t j = so[l] + threadIdx.x; j < ce; j += NT) {
-      const int4 c = sc[j];
-      float lam = sl[j];
-      float4 a = sx[c.x], b = sx[c.y];
-      tx[2 * (size_t)(c0 + j)] = a;
-      tx[2 * (size_t)(c0 + j) + 1] = b;
-      tl[c0 + j] = lam;
-      if (stretch_project(a, b, __int_as_float(c.z), __int_as_float(c.w), dt, lam)) {
-        sx[c.x] = a;
-        sx[c.y] = b;
-        sl[j] = lam;
-      }
-    }
-    __syncthreads();
-  }
-  pdl_release();
-  tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
-  for (uint32_t j = threadIdx.x; j < nc; j += NT) lambda[c0 + j] = sl[j];
-}
-
-template <int NT>
-__global__ void __launch_bounds__(NT) k_bend_tiles_tape(
-    const int4* __restrict__ idx, const float2* __restrict__ tc, float4* __restrict__ x,
-    const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
-    const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
-    uint32_t max_foot, uint32_t max_cons, float dt, float4* __restrict__ tx) {
-  extern __shared__ float4 smem[];
-  float4* sx = smem;
-  int4* sc = reinterpret_cast<int4*>(sx + max_foot);
-  float2* st = reinterpret_cast<float2*>(sc + max_cons);
-  uint32_t* so = reinterpret_cast<uint32_t*>(st + max_cons);
-  uint32_t* sf = so + num_local + 1;
-  const TileFrame f = tile_prologue<NT>(foot, meta, lofs, tile_begin + blockIdx.x, num_local, so);
-  const uint32_t c0 = (uint32_t)f.m.z, nc = (uint32_t)f.m.w;
-  for (uint32_t j = threadIdx.x; j < nc; j += NT) {  // setup data
-    sc[j] = __ldg(&idx[c0 + j]);
-    st[j] = __ldg(&tc[c0 + j]);
-  }
-  pdl_wait();
-  tile_gather<NT>(f, x, sx, sf);
-  __syncthreads();
-  // the forward's lane-pair projection (bend_project_pair, the same bits as bend_project); each
-  // lane tapes the two input vertices it owns.  The loop trip count is warp-uniform.
-  const uint32_t lane0 = threadIdx.x & ~31u;
-  for (uint32_t l = 0; l < num_local; ++l) {
-    const uint32_t cb = 2 * so[l], ce = 2 * so[l + 1];
-    for (uint32_t base = cb + lane0; base < ce; base += NT) {
-      const uint32_t s = base + (threadIdx.x & 31u);
-      const bool active = s < ce;
-      const uint32_t j = active ? s >> 1 : cb >> 1;
-      const uint32_t half = s & 1u;
-      const int4 b = sc[j];
-      const float2 th = st[j];
-      if (active) {
-        float4* t = tx + 4 * (size_t)(c0 + j) + 2 * half;
-        t[0] = sx[half ? b.z : b.x];
-        t[1] = sx[half ? b.w : b.y];
-      }
-      bend_project_pair(sx, b, th.x, bend_alpha(th.y, dt), half, active);
-    }
-    __syncthreads();
-  }
-  pdl_release();
-  tile_scatter<NT>((uint32_t)f.m.y, x, sx, sf);
-}
 
 // STAGE: the tile's slice of the tape (contiguous slots c0 .. c0 + nc) is loaded into shared
 // memory up front, all loads in flight at once, instead of one dependent global load per local
@@ -639,21 +551,6 @@ __device__ __forceinline__ EeTerm ee_term(uint32_t e, const float4* __restrict__
   return r;
 }
 
-__global__ void k_ee_count(const float4* __restrict__ X, uint32_t nv,
-                           const uint32_t* __restrict__ ve_ptr, const uint32_t* __restrict__ ve_list,
-                           const uint2* __restrict__ edge, const float4* __restrict__ ee_a,
-                           const float4* __restrict__ ee_b, const float4* __restrict__ ee_c,
-                           float* __restrict__ cnt) {
-  pdl_release();
-  pdl_wait();
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nv) return;
-  int n = 0;
-  for (uint32_t k = ve_ptr[i]; k < ve_ptr[i + 1]; ++k)
-    n += ee_term(ve_list[k] >> 1, X, edge, ee_a, ee_b, ee_c).on ? 1 : 0;
-  cnt[i] = (float)n;
-}
-
 // out_i = x_i + relax / cnt_i * sum_{e active at i} -sigma_ie lambda_e fn_e, with
 // lambda_e = ((1-s) x_e.x + s x_e.y - c2) . fn - m; sigma / omega = 1-s at e.x, s at e.y.
 __global__ void k_ee_bwd(const float4* __restrict__ X, const float4* __restrict__ Gin,
@@ -845,14 +742,6 @@ cudaError_t configure_tiled_adjoint(Context& c, int smem_max) {
   };
   if (D.s_tiled) {
     const TiledSet& T = c.s_tiles;
-    const size_t ft = tile_smem_bytes(T, sizeof(int4) + sizeof(float));
-    if (T.block == 256) {
-      set((const void*)k_stretch_tiles_tape<true, 256>, ft);
-      set((const void*)k_stretch_tiles_tape<false, 256>, ft);
-    } else {
-      set((const void*)k_stretch_tiles_tape<true, 512>, ft);
-      set((const void*)k_stretch_tiles_tape<false, 512>, ft);
-    }
     if (e == cudaSuccess)
       e = choose_reverse_shape(
           c, T, +[](uint32_t b, bool s) { return stretch_bwd_kernel(b, false, s); },
@@ -861,8 +750,6 @@ cudaError_t configure_tiled_adjoint(Context& c, int smem_max) {
   }
   if (D.b_tiled) {
     const TiledSet& T = c.b_tiles;
-    set(T.block == 256 ? (const void*)k_bend_tiles_tape<256> : (const void*)k_bend_tiles_tape<512>,
-        tile_smem_bytes(T, sizeof(int4) + sizeof(float2)));
     if (e == cudaSuccess)
       e = choose_reverse_shape(
           c, T, +[](uint32_t b, bool s) { return bend_bwd_kernel(b, s); },
@@ -871,37 +758,7 @@ cudaError_t configure_tiled_adjoint(Context& c, int smem_max) {
   return e;
 }
 
-// Tiled replay of one stretch / bend phase (all tile colors, in order) and its reverse.
-void stretch_tiles_tape(Context& c, float dt, bool reset, size_t ti) {
-  DiffState& D = c.diff;
-  const TiledSet& T = c.s_tiles;
-  const size_t smem = tile_smem_bytes(T, sizeof(int4) + sizeof(float));
-  auto kern = T.block == 256
-                  ? (reset ? k_stretch_tiles_tape<true, 256> : k_stretch_tiles_tape<false, 256>)
-                  : (reset ? k_stretch_tiles_tape<true, 512> : k_stretch_tiles_tape<false, 512>);
-  float4* tx = D.t_sx.p + 2 * ti * c.ne;
-  float* tl = D.t_sl.p + ti * c.ne;
-  for (const ColorRange& r : T.tile_colors)
-    if (r.end > r.begin)
-      launch_k(c.pdl, kern, r.end - r.begin, T.block, smem, c.stream, c.s_con.p, c.s_lambda.p, c.x.p,
-                                                         T.foot.p, T.meta.p, T.lofs.p, r.begin,
-                                                         T.num_local, T.max_foot, T.max_cons, dt,
-                                                         tx, tl);
-}
-
-void bend_tiles_tape(Context& c, float dt, size_t ti) {
-  DiffState& D = c.diff;
-  const TiledSet& T = c.b_tiles;
-  const size_t smem = tile_smem_bytes(T, sizeof(int4) + sizeof(float2));
-  auto kern = T.block == 256 ? k_bend_tiles_tape<256> : k_bend_tiles_tape<512>;
-  float4* tx = D.t_bx.p + 4 * ti * c.nb;
-  for (const ColorRange& r : T.tile_colors)
-    if (r.end > r.begin)
-      launch_k(c.pdl, kern, r.end - r.begin, T.block, smem, c.stream, c.b_idx.p, c.b_tc.p, c.x.p, T.foot.p,
-                                                         T.meta.p, T.lofs.p, r.begin, T.num_local,
-                                                         T.max_foot, T.max_cons, dt, tx);
-}
-
+// Reverse of one tiled stretch / bend phase (all tile colors, last to first).
 void stretch_tiles_bwd(Context& c, float dt, bool reset, size_t ti) {
   DiffState& D = c.diff;
   const TiledSet& T = c.s_tiles;
@@ -985,7 +842,10 @@ void record_frame_diff(Context& c) {
       }
       D.it_pass[cur] = cnt - 1;
       const size_t ti = (size_t)cur;
-      if (D.s_tiled) stretch_tiles_tape(c, k.dt, it == 0, ti);
+      // tiled: the forward's tile launches, taping each projection's inputs by execution slot
+      if (D.s_tiled)
+        for (const ColorRange& r : c.s_tiles.tile_colors)
+          launch_stretch_tiles(c, k, r, it == 0, D.t_sx.p + 2 * ti * E, D.t_sl.p + ti * E);
       else for (const ColorRange& r : D.s_colors) {
         const unsigned g = grid_for(r.end - r.begin);
         if (it == 0)
@@ -999,7 +859,9 @@ void record_frame_diff(Context& c) {
                                                           D.t_sx.p + 2 * ti * E,
                                                           D.t_sl.p + ti * E, k.dt);
       }
-      if (p.solve_bending && D.b_tiled) bend_tiles_tape(c, k.dt, ti);
+      if (p.solve_bending && D.b_tiled)
+        for (const ColorRange& r : c.b_tiles.tile_colors)
+          launch_bend_tiles(c, k, r, D.t_bx.p + 4 * ti * B);
       else if (p.solve_bending)
         for (const ColorRange& r : D.b_colors)
           launch_k(c.pdl, k_bend_tape, grid_for(r.end - r.begin), blk, 0, c.stream,
@@ -1010,7 +872,7 @@ void record_frame_diff(Context& c) {
         swap_x();
       }
       if (has_obstacle) {
-        launch_ee(c, k, has_obstacle, false, D.t_ee.p + ti * V);
+        launch_ee(c, k, has_obstacle, false, D.t_ee.p + ti * V, D.cnt.p + ti * V);
         swap_x();
       }
     }
@@ -1035,7 +897,7 @@ void backward_frame(Context& c) {
   const bool lra_fused = p.geodesic_lra && c.nl && c.lra_by_target;
   const float kd = 1 - k.damping * k.dt;
   const unsigned gv = grid_for(V), blk = kBlock;
-  const uint32_t n_vertex_launches = (has_obstacle ? 2 : 0) + (lra_fused || has_obstacle ? 1 : 0) +
+  const uint32_t n_vertex_launches = (has_obstacle ? 1 : 0) + (lra_fused || has_obstacle ? 1 : 0) +
                                      (lra_fused ? 1 : 0);
   const uint32_t n_bend_launches =
       D.b_tiled ? (uint32_t)c.b_tiles.tile_colors.size() : (uint32_t)D.b_colors.size();
@@ -1055,12 +917,9 @@ void backward_frame(Context& c) {
         Timed tv(c, kAdjVertex, n_vertex_launches, V);
         if (has_obstacle) {
           const float4* X = D.t_ee.p + ti * V;
-          launch_k(c.pdl, k_ee_count, gv, blk, 0, c.stream, X, V, c.ve_ptr.p, c.ve_list.p, c.edge.p,
-                                              D.t_ee_a.p + pe, D.t_ee_b.p + pe, D.t_ee_c.p + pe,
-                                              D.cnt.p);
           launch_k(c.pdl, k_ee_bwd, gv, blk, 0, c.stream, X, D.G.p, D.G2.p, V, c.ve_ptr.p, c.ve_list.p,
                                             c.edge.p, D.t_ee_a.p + pe, D.t_ee_b.p + pe,
-                                            D.t_ee_c.p + pe, D.cnt.p, k.relaxation);
+                                            D.t_ee_c.p + pe, D.cnt.p + ti * V, k.relaxation);
           std::swap(D.G.p, D.G2.p);
         }
         if (lra_fused || has_obstacle) {
@@ -1247,7 +1106,7 @@ xrt_status diff_prepare(Context& c) {
   XRT_CUDA(&c, D.t_ee_c.reserve(P * E));
   XRT_CUDA(&c, D.t_pred.reserve(P * 3 * F));
   for (DBuf<float4>* b : {&D.G, &D.G2, &D.Gv, &D.H, &D.Gs}) XRT_CUDA(&c, b->reserve(V));
-  XRT_CUDA(&c, D.cnt.reserve(V));
+  XRT_CUDA(&c, D.cnt.reserve(c.onf ? SI * V : 1));
   XRT_CUDA(&c, D.lam_bar.reserve(E));
   XRT_CUDA(&c, D.comp_bar.reserve(E));
   XRT_CUDA(&c, D.bcomp_bar.reserve(Bn));

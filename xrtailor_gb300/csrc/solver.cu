@@ -116,13 +116,13 @@ __global__ void k_stretch(const int4* __restrict__ con, float* __restrict__ lamb
 // the segments stream in two colors ahead through two shared-memory buffers; otherwise the whole
 // block comes in one bulk copy.  The multipliers of the tile's constraints stay in shared memory
 // from the prologue to the write-back.
-template <bool RESET, int NT, bool STREAM>
+template <bool RESET, int NT, bool STREAM, bool TAPE>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_stretch_tiles(
     const uint4* __restrict__ rec, const uint32_t* __restrict__ rec_ofs,
     float* __restrict__ lambda, float4* __restrict__ x, const uint32_t* __restrict__ foot,
     const int4* __restrict__ meta, const uint32_t* __restrict__ lofs, uint32_t tile_begin,
     uint32_t num_local, uint32_t max_foot, uint32_t max_seg16, uint32_t buf16, uint32_t max_cons,
-    uint32_t* err) {
+    uint32_t* err, float4* __restrict__ tape_x, float* __restrict__ tape_l) {
   if (num_local == 0) return;  // no constraint in the schedule
   extern __shared__ float4 smem[];
   float4* sx = smem;
@@ -190,6 +190,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_stretch_tiles(
       const float2 rc = sval[j];
       float lam = sl[cb + j];
       float4 a = sx[ab.x], b = sx[ab.y];
+      if (TAPE) {  // the adjoint's replay: the projection's inputs by execution slot
+        const size_t slot = (size_t)f.m.z + cb + j;
+        tape_x[2 * slot] = a;
+        tape_x[2 * slot + 1] = b;
+        tape_l[slot] = lam;
+      }
       if (stretch_project_alpha(a, b, rc.x, rc.y, lam)) {
         sx[ab.x] = a;
         sx[ab.y] = b;
@@ -240,12 +246,13 @@ __global__ void k_bend(const int4* __restrict__ idx, const float2* __restrict__ 
 //     records occupy shared memory, so more tiles fit on an SM.
 //   lane pairs (latency regime, every tile of the launch resident): the whole block comes in one
 //     bulk copy before the first color, so no color waits on a copy.
-template <int NT, bool PAIR>
+template <int NT, bool PAIR, bool TAPE>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
     const uint4* __restrict__ rec, const uint32_t* __restrict__ rec_ofs, float4* __restrict__ x,
     const uint32_t* __restrict__ foot, const int4* __restrict__ meta,
     const uint32_t* __restrict__ lofs, uint32_t tile_begin, uint32_t num_local,
-    uint32_t max_foot, uint32_t max_seg16, uint32_t buf16, uint32_t* err) {
+    uint32_t max_foot, uint32_t max_seg16, uint32_t buf16, uint32_t* err,
+    float4* __restrict__ tape_x) {
   if (num_local == 0) return;  // no constraint in the schedule
   extern __shared__ float4 smem[];
   float4* sx = smem;
@@ -317,6 +324,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
         const ushort4 q = sid[j];
         const int4 b = make_int4(q.x, q.y, q.z, q.w);
         const float2 th = st[j];
+        if (TAPE && active) {  // the adjoint's replay: each lane tapes the two inputs it owns
+          const uint32_t half = s & 1u;
+          float4* t = tape_x + 4 * ((size_t)f.m.z + c0 + j) + 2 * half;
+          t[0] = sx[half ? b.z : b.x];
+          t[1] = sx[half ? b.w : b.y];
+        }
         bend_project_pair(sx, b, th.x, th.y, s & 1u, active);
       }
     } else {
@@ -324,6 +337,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_bend_tiles(
         const ushort4 b = sid[j];
         const float2 th = st[j];
         float4 a1 = sx[b.x], a2 = sx[b.y], a3 = sx[b.z], a4 = sx[b.w];
+        if (TAPE) {  // the adjoint's replay: the projection's inputs by execution slot
+          float4* t = tape_x + 4 * ((size_t)f.m.z + c0 + j);
+          t[0] = a1;
+          t[1] = a2;
+          t[2] = a3;
+          t[3] = a4;
+        }
         bend_project_alpha(a1, a2, a3, a4, th.x, th.y);
         sx[b.x] = a1;
         sx[b.y] = a2;
@@ -386,7 +406,8 @@ struct TailArgs {
   const float4* bind_a;
   const int4* bind_b;
   const float4* ox;
-  float4* tape;  // when set (the adjoint's recorded replay): each vertex's input x_in is copied here
+  float4* tape;     // TAPE (the adjoint's recorded replay): each vertex's input x_in
+  float* tape_cnt;  // TAPE, k_ee: each vertex's EE contact count
 };
 
 // Position of vertex j after the LRA and VF phases.
@@ -420,19 +441,19 @@ __device__ __forceinline__ f3 tail_stage(const TailArgs& a, uint32_t j, const fl
 }
 
 // LRA + VF: x_out = tail_stage(x_in), per vertex.
-template <bool LRA, bool CONTACTS>
+template <bool LRA, bool CONTACTS, bool TAPE>
 __global__ void k_stage(const TailArgs a) {
   pdl_release();
   pdl_wait();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.nv) return;
   const float4 p = a.x_in[i];
-  if (a.tape) a.tape[i] = p;
+  if (TAPE) a.tape[i] = p;
   a.x_out[i] = mk4(tail_stage<LRA, CONTACTS>(a, i, p), p.w);
 }
 
 // EE + ApplyDeltas + binding on the post-VF positions x_in.
-template <bool CONTACTS, bool BINDINGS>
+template <bool CONTACTS, bool BINDINGS, bool TAPE>
 __global__ void k_ee(const TailArgs a) {
   pdl_release();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -455,12 +476,12 @@ __global__ void k_ee(const TailArgs a) {
   const uint32_t* __restrict__ ve_list = a.ve_list;
   const float relaxation = a.relaxation;
   const float4 p = x_in[i];
-  if (a.tape) a.tape[i] = p;
+  if (TAPE) a.tape[i] = p;
   f3 q = mk3(p);
+  int count = 0;  // the EE contacts applied to this vertex
   // a vertex none of whose edges holds a contact skips the list (delta 0, count 0)
   if (CONTACTS && a.ee_vflag[i]) {
     f3 delta = mk3(0, 0, 0);
-    int count = 0;
     // The contact-flag loads of a batch of incident edges are issued together; the edges are
     // then processed one by one in list order.
     for (uint32_t base = kb; base < ke; base += kBatch) {
@@ -511,6 +532,7 @@ __global__ void k_ee(const TailArgs a) {
       q = q + (-s * p.w * nn);
     }
   }
+  if (TAPE) a.tape_cnt[i] = (float)count;
   a.x_out[i] = mk4(q, p.w);
 }
 
@@ -556,6 +578,45 @@ cudaError_t raise_smem(const void* kern, size_t bytes) {
   return e;
 }
 
+// Every instantiation of the forward tile kernels, indexed by their template flags (reset, 512
+// threads, streamed records, tape / 512 threads, lane pairs, tape).
+using StretchTilesK = decltype(&k_stretch_tiles<false, 256, false, false>);
+using BendTilesK = decltype(&k_bend_tiles<256, false, false>);
+static const StretchTilesK kStretchTiles[16] = {
+    k_stretch_tiles<false, 256, false, false>,
+    k_stretch_tiles<false, 256, false, true>,
+    k_stretch_tiles<false, 256, true, false>,
+    k_stretch_tiles<false, 256, true, true>,
+    k_stretch_tiles<false, 512, false, false>,
+    k_stretch_tiles<false, 512, false, true>,
+    k_stretch_tiles<false, 512, true, false>,
+    k_stretch_tiles<false, 512, true, true>,
+    k_stretch_tiles<true, 256, false, false>,
+    k_stretch_tiles<true, 256, false, true>,
+    k_stretch_tiles<true, 256, true, false>,
+    k_stretch_tiles<true, 256, true, true>,
+    k_stretch_tiles<true, 512, false, false>,
+    k_stretch_tiles<true, 512, false, true>,
+    k_stretch_tiles<true, 512, true, false>,
+    k_stretch_tiles<true, 512, true, true>,
+};
+static const BendTilesK kBendTiles[8] = {
+    k_bend_tiles<256, false, false>,
+    k_bend_tiles<256, false, true>,
+    k_bend_tiles<256, true, false>,
+    k_bend_tiles<256, true, true>,
+    k_bend_tiles<512, false, false>,
+    k_bend_tiles<512, false, true>,
+    k_bend_tiles<512, true, false>,
+    k_bend_tiles<512, true, true>,
+};
+static StretchTilesK stretch_tiles_kernel(bool reset, bool b512, bool stream, bool tape) {
+  return kStretchTiles[(reset ? 8 : 0) + (b512 ? 4 : 0) + (stream ? 2 : 0) + (tape ? 1 : 0)];
+}
+static BendTilesK bend_tiles_kernel(bool b512, bool pair, bool tape) {
+  return kBendTiles[(b512 ? 4 : 0) + (pair ? 2 : 0) + (tape ? 1 : 0)];
+}
+
 // The limit is a property of the kernel function on the current device, shared by every
 // context of the process, so it only ever grows: a context started later with smaller tiles
 // must not lower it under one that is already running.
@@ -569,15 +630,12 @@ cudaError_t configure_tile_kernels(size_t max_smem_bytes) {
   int& cur = configured[dev];
   const int bytes = std::max(cur, (int)max_smem_bytes);
   if (bytes == cur) return cudaSuccess;
-  const void* kernels[] = {
-      (const void*)k_stretch_tiles<true, 256, false>, (const void*)k_stretch_tiles<false, 256, false>,
-      (const void*)k_stretch_tiles<true, 512, false>, (const void*)k_stretch_tiles<false, 512, false>,
-      (const void*)k_stretch_tiles<true, 256, true>,  (const void*)k_stretch_tiles<false, 256, true>,
-      (const void*)k_stretch_tiles<true, 512, true>,  (const void*)k_stretch_tiles<false, 512, true>,
-      (const void*)k_bend_tiles<256, true>,    (const void*)k_bend_tiles<256, false>,
-      (const void*)k_bend_tiles<512, true>,    (const void*)k_bend_tiles<512, false>};
-  for (const void* kern : kernels) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  for (const StretchTilesK kern : kStretchTiles) {
+    e = cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+  }
+  for (const BendTilesK kern : kBendTiles) {
+    e = cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
   }
   cur = bytes;
@@ -615,10 +673,8 @@ cudaError_t choose_tile_block(TiledSet& T, bool bend) {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
   const size_t smem = tile_smem_fwd(T, !bend, true);
-  const void* kern = bend ? (T.block == 256 ? (const void*)k_bend_tiles<256, true>
-                                            : (const void*)k_bend_tiles<512, true>)
-                          : (T.block == 256 ? (const void*)k_stretch_tiles<false, 256, false>
-                                            : (const void*)k_stretch_tiles<false, 512, false>);
+  const void* kern = bend ? (const void*)bend_tiles_kernel(T.block != 256, true, false)
+                          : (const void*)stretch_tiles_kernel(false, T.block != 256, false, false);
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)T.block, smem);
   if (e != cudaSuccess) return e;
   T.resident = (uint32_t)std::max(per_sm, 1) * (uint32_t)sms;
@@ -652,24 +708,21 @@ void launch_unpack_xyz(const float* in, float4* out, uint32_t n, float w, cudaSt
   if (n) k_unpack_xyz<<<grid_for(n), kBlock, 0, s>>>(in, out, n, w);
 }
 
-void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, bool reset_lambda) {
+void launch_stretch_tiles(Context& c, const FrameConst& k, ColorRange tiles, bool reset_lambda,
+                          float4* tape_x, float* tape_l) {
   const uint32_t nt = tiles.end - tiles.begin;
   if (nt == 0) return;
   const TiledSet& T = c.s_tiles;
   const bool stream = nt > T.resident;  // many waves of tiles: throughput regime
   const uint32_t block = stream ? T.block1 : T.block;
   const uint32_t buf16 = stream ? 2 * T.max_seg16 : T.max_tile16;  // as tile_smem_fwd sizes it
-  auto pick = [&](auto k256, auto k512) { return block == 256 ? k256 : k512; };
-  auto kern = stream ? (reset_lambda ? pick(k_stretch_tiles<true, 256, true>, k_stretch_tiles<true, 512, true>)
-                                     : pick(k_stretch_tiles<false, 256, true>, k_stretch_tiles<false, 512, true>))
-                     : (reset_lambda ? pick(k_stretch_tiles<true, 256, false>, k_stretch_tiles<true, 512, false>)
-                                     : pick(k_stretch_tiles<false, 256, false>, k_stretch_tiles<false, 512, false>));
+  const StretchTilesK kern = stretch_tiles_kernel(reset_lambda, block != 256, stream, tape_x);
   launch_k(c.pdl, kern, nt, block, tile_smem_fwd(T, true, !stream), c.stream, T.rec.p,
            T.rec_ofs.p, c.s_lambda.p, c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin,
-           T.num_local, T.max_foot, T.max_seg16, buf16, T.max_cons, c.err.p);
+           T.num_local, T.max_foot, T.max_seg16, buf16, T.max_cons, c.err.p, tape_x, tape_l);
 }
 
-void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles) {
+void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles, float4* tape_x) {
   const uint32_t nt = tiles.end - tiles.begin;
   if (nt == 0) return;
   const TiledSet& T = c.b_tiles;
@@ -678,12 +731,11 @@ void launch_bend_tiles(Context& c, const FrameConst& k, ColorRange tiles) {
   // use lanes that would idle at the color's barrier)
   const bool pair = nt <= T.resident || 2 * T.max_step <= T.block;
   const uint32_t block = pair ? T.block : T.block1;
-  auto kern = block == 256 ? (pair ? k_bend_tiles<256, true> : k_bend_tiles<256, false>)
-                           : (pair ? k_bend_tiles<512, true> : k_bend_tiles<512, false>);
+  const BendTilesK kern = bend_tiles_kernel(block != 256, pair, tape_x);
   const uint32_t buf16 = pair ? T.max_tile16 : 2 * T.max_seg16;  // as tile_smem_fwd sizes it
   launch_k(c.pdl, kern, nt, block, tile_smem_fwd(T, false, pair), c.stream, T.rec.p, T.rec_ofs.p,
            c.x.p, T.foot.p, T.meta.p, T.lofs.p, tiles.begin, T.num_local, T.max_foot, T.max_seg16,
-           buf16, c.err.p);
+           buf16, c.err.p, tape_x);
 }
 
 // LRA phase with a free slot vertex: one launch per slot block in list order.  (With every slot
@@ -723,22 +775,31 @@ static TailArgs tail_args(Context& c, const FrameConst& k) {
   a.bind_b = c.bind_b.p;
   a.ox = c.ox.p;
   a.tape = nullptr;
+  a.tape_cnt = nullptr;
   return a;
 }
 
 void launch_stage(Context& c, const FrameConst& k, bool lra, bool contacts, float4* tape) {
   if (!lra && !contacts) return;
-  auto kern = lra ? (contacts ? k_stage<true, true> : k_stage<true, false>) : k_stage<false, true>;
+  auto kern = tape ? (lra ? (contacts ? k_stage<true, true, true> : k_stage<true, false, true>)
+                          : k_stage<false, true, true>)
+                   : (lra ? (contacts ? k_stage<true, true, false> : k_stage<true, false, false>)
+                          : k_stage<false, true, false>);
   TailArgs a = tail_args(c, k);
   a.tape = tape;
   launch_k(c.pdl, kern, grid_for(c.nv, c.vertex_block), c.vertex_block, 0, c.stream, a);
 }
 
-void launch_ee(Context& c, const FrameConst& k, bool contacts, bool bindings, float4* tape) {
+void launch_ee(Context& c, const FrameConst& k, bool contacts, bool bindings, float4* tape,
+               float* tape_cnt) {
   if (!contacts && !bindings) return;
-  auto kern = contacts ? (bindings ? k_ee<true, true> : k_ee<true, false>) : k_ee<false, true>;
+  auto kern = tape ? (contacts ? (bindings ? k_ee<true, true, true> : k_ee<true, false, true>)
+                               : k_ee<false, true, true>)
+                   : (contacts ? (bindings ? k_ee<true, true, false> : k_ee<true, false, false>)
+                               : k_ee<false, true, false>);
   TailArgs a = tail_args(c, k);
   a.tape = tape;
+  a.tape_cnt = tape_cnt;
   launch_k(c.pdl, kern, grid_for(c.nv, c.vertex_block), c.vertex_block, 0, c.stream, a);
 }
 
