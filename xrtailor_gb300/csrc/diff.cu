@@ -794,8 +794,9 @@ cudaError_t copy_d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
   return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s) : cudaSuccess;
 }
 
-// One frame, as record_frame issues it, with taping kernels for the projections and copies of
-// the inputs of the per-vertex launches and of each collision pass.
+// One frame, as record_frame issues it, with the projections' and per-vertex launches' inputs
+// taped by the launches themselves and each collision pass's contacts generated into their tape
+// slots (the obstacle primitives are copied).
 void record_frame_diff(Context& c) {
   DiffState& D = c.diff;
   const xrt_swift_params& p = c.params;
@@ -818,6 +819,13 @@ void record_frame_diff(Context& c) {
   const int frequency = (p.num_substeps * p.num_iterations) / p.num_collision_passes;
   const unsigned blk = kBlock;
   int cnt = 0;
+  int* const vf_idx = c.vf_idx.p;  // the contact buffers, redirected to tape slots per pass
+  int* const rt_idx = c.rt_idx.p;
+  float4* const vf_qs = c.vf_qs.p;
+  float4* const rt_qc = c.rt_qc.p;
+  float4* const ee_a = c.ee_a.p;
+  float4* const ee_b = c.ee_b.p;
+  float4* const ee_c = c.ee_c.p;
   D.it_pass.assign((size_t)D.S * D.I, 0);
   for (uint32_t s = 0; s < D.S; ++s) {
     if (s == 0) launch_predict(c, k);
@@ -826,15 +834,18 @@ void record_frame_diff(Context& c) {
       if ((int)cur % frequency == 0) {
         if (obstacle_updated) launch_obstacle_pass(c, cnt, p.num_collision_passes);
         if (has_obstacle) {
-          launch_generate_contacts(c);
+          // the pass's contacts are generated straight into their tape slots, which the stage
+          // and EE launches up to the next pass then read (the context's buffers are restored
+          // at the end of the frame)
           const size_t pv = (size_t)cnt * V, pe = (size_t)cnt * E;
-          copy_d(D.t_vf_idx.p + pv, c.vf_idx.p, sizeof(int) * V, c.stream);
-          copy_d(D.t_rt_idx.p + pv, c.rt_idx.p, sizeof(int) * V, c.stream);
-          copy_d(D.t_vf_qs.p + pv, c.vf_qs.p, sizeof(float4) * V, c.stream);
-          copy_d(D.t_rt_qc.p + pv, c.rt_qc.p, sizeof(float4) * V, c.stream);
-          copy_d(D.t_ee_a.p + pe, c.ee_a.p, sizeof(float4) * E, c.stream);
-          copy_d(D.t_ee_b.p + pe, c.ee_b.p, sizeof(float4) * E, c.stream);
-          copy_d(D.t_ee_c.p + pe, c.ee_c.p, sizeof(float4) * E, c.stream);
+          c.vf_idx.p = D.t_vf_idx.p + pv;
+          c.rt_idx.p = D.t_rt_idx.p + pv;
+          c.vf_qs.p = D.t_vf_qs.p + pv;
+          c.rt_qc.p = D.t_rt_qc.p + pv;
+          c.ee_a.p = D.t_ee_a.p + pe;
+          c.ee_b.p = D.t_ee_b.p + pe;
+          c.ee_c.p = D.t_ee_c.p + pe;
+          launch_generate_contacts(c);
           copy_d(D.t_pred.p + (size_t)cnt * 3 * c.onf, c.bvh.pred.p, sizeof(float4) * 3 * c.onf,
                  c.stream);
         }
@@ -880,6 +891,13 @@ void record_frame_diff(Context& c) {
     launch_finalize_predict(c, k, !last, last);
   }
   if (c.onv > 0) launch_obstacle_commit(c);
+  c.vf_idx.p = vf_idx;
+  c.rt_idx.p = rt_idx;
+  c.vf_qs.p = vf_qs;
+  c.rt_qc.p = rt_qc;
+  c.ee_a.p = ee_a;
+  c.ee_b.p = ee_b;
+  c.ee_c.p = ee_c;
   if (swaps & 1) {
     cudaMemcpyAsync(x_start, c.x.p, sizeof(float4) * c.nv, cudaMemcpyDeviceToDevice, c.stream);
     std::swap(c.x.p, c.x_alt.p);
