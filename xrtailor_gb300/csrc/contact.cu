@@ -96,26 +96,53 @@ __global__ void k_obstacle_commit(const float4* __restrict__ x, float4* __restri
 // one-thread-per-query launch left ~2 of 32 lanes of a warp busy.  Contacts record global
 // triangle ids.
 
-// VF-DCD: nearest obstacle point of the predicted vertex.
-__global__ void __launch_bounds__(kBlock, 4) k_generate_vf_dcd(LbvhForest F, InstView I,
-                                                            const float4* __restrict__ x,
-                                                            uint32_t nv, int* __restrict__ vf_idx,
-                                                            float4* __restrict__ vf_qs,
-                                                            uint32_t* err, uint32_t* counter) {
+// VF-DCD (nearest obstacle point of the predicted vertex) and VF-CCD (first obstacle hit of the
+// segment x0 -> x) of one vertex, in one walk of its instance's tree.  Each query keeps the state
+// of its own stackless traversal: where its box test fails at an internal node that the other
+// query enters, it stays off until the walk reaches that node's escape index (the first node
+// after the subtree), and it stops after its own 256th leaf.  So each query tests the same nodes
+// in the same order as alone, visits the same leaves in the same order and ends at the same cap:
+// both results are those of the two separate traversals (GenerateVF_DCD_Kernel,
+// GenerateVFCCD_Kernel), with the nodes they share fetched once.
+__global__ void __launch_bounds__(kBlock, 4) k_generate_vf(LbvhForest F, InstView I,
+                                                        const float4* __restrict__ x,
+                                                        const float4* __restrict__ x0,
+                                                        uint32_t nv, int* __restrict__ vf_idx,
+                                                        float4* __restrict__ vf_qs,
+                                                        int* __restrict__ rt_idx,
+                                                        float4* __restrict__ rt_qc, uint32_t* err,
+                                                        uint32_t* counter) {
+  constexpr int kOn = -1, kDone = -2;  // a query's state; >= 0: off until the walk reaches it
   LbvhView b{};
-  TraverseState st{};
-  f3 pred{}, hit_qs{};
-  float hit = kScalarMax;
-  int hit_idx = -1, base = 0;
-  auto overlap = [&](float4 l, float4 h) { return overlap_point(l, h, pred); };
-  auto visit = [&](uint32_t f) {
+  int node = -1, base = 0;
+  uint32_t guard = 0;
+  // DCD
+  f3 pred{}, dqs{};
+  float dhit = kScalarMax;
+  int didx = -1, dstate = kDone;
+  uint32_t dfound = 0;
+  // CCD
+  f3 p1{}, dir{}, cqc{};
+  float len = 0, chit = kScalarMax;
+  int cidx = -1, cstate = kDone;
+  uint32_t cfound = 0;
+  auto visit_dcd = [&](uint32_t f) {
     f3 qs;
     const float dist = nearest_point(pred, mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]),
                                      mk3(b.pred[3 * f + 2]), qs);
-    if (dist < hit) {
-      hit = dist;
-      hit_qs = qs;
-      hit_idx = base + (int)f;
+    if (dist < dhit) {
+      dhit = dist;
+      dqs = qs;
+      didx = base + (int)f;
+    }
+  };
+  auto visit_ccd = [&](uint32_t f) {
+    const float dist = ray_intersect(p1, dir, len, mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]),
+                                     mk3(b.pred[3 * f + 2]));
+    if (dist < chit) {
+      cqc = p1 + dist * dir;
+      chit = dist;
+      cidx = base + (int)f;
     }
   };
   work_queue(
@@ -125,63 +152,65 @@ __global__ void __launch_bounds__(kBlock, 4) k_generate_vf_dcd(LbvhForest F, Ins
         b = forest_view(F, sg);
         base = forest_rec(F, sg).x;
         pred = mk3(x[i]);
-        hit = kScalarMax;
-        hit_idx = -1;
-        hit_qs = mk3(0, 0, 0);
-        st = lbvh_begin(b);
-        return st.node != -1;
-      },
-      [&]() { return lbvh_step(b, st, overlap, visit, err); },
-      [&](uint32_t i) {
-        vf_idx[i] = hit_idx;
-        vf_qs[i] = mk4(hit_qs, 0.0f);
-      });
-}
-
-// VF-CCD: first obstacle hit of the segment x0 -> x.
-__global__ void __launch_bounds__(kBlock, 4) k_generate_vf_ccd(LbvhForest F, InstView I,
-                                                            const float4* __restrict__ x,
-                                                            const float4* __restrict__ x0,
-                                                            uint32_t nv, int* __restrict__ rt_idx,
-                                                            float4* __restrict__ rt_qc,
-                                                            uint32_t* err, uint32_t* counter) {
-  LbvhView b{};
-  TraverseState st{};
-  f3 p1{}, p2{}, d{}, qc{};
-  float len = 0, hit = kScalarMax;
-  int hit_idx = -1, base = 0;
-  auto overlap = [&](float4 l, float4 h) { return overlap_segment(l, h, p1, p2); };
-  auto visit = [&](uint32_t f) {
-    const float dist =
-        ray_intersect(p1, d, len, mk3(b.pred[3 * f]), mk3(b.pred[3 * f + 1]), mk3(b.pred[3 * f + 2]));
-    if (dist < hit) {
-      qc = p1 + dist * d;
-      hit = dist;
-      hit_idx = base + (int)f;
-    }
-  };
-  work_queue(
-      counter, nv,
-      [&](uint32_t i) {
-        const uint32_t sg = inst_index(I, i);
-        b = forest_view(F, sg);
-        base = forest_rec(F, sg).x;
+        dhit = kScalarMax;
+        didx = -1;
+        dqs = mk3(0, 0, 0);
+        dfound = 0;
         p1 = mk3(x0[i]);
-        p2 = mk3(x[i]);
-        d = p2 - p1;
-        len = length(d);
-        hit_idx = -1;
-        qc = mk3(0, 0, 0);
-        if (len < kEps) return false;
-        d = d / len;
-        hit = kScalarMax;
-        st = lbvh_begin(b);
-        return st.node != -1;
+        dir = pred - p1;
+        len = length(dir);
+        chit = kScalarMax;
+        cidx = -1;
+        cqc = mk3(0, 0, 0);
+        cfound = 0;
+        node = lbvh_begin(b).node;
+        guard = 0;
+        dstate = node != -1 ? kOn : kDone;
+        cstate = node != -1 && !(len < kEps) ? kOn : kDone;  // a still vertex casts no ray
+        if (cstate == kOn) dir = dir / len;
+        return node != -1;
       },
-      [&]() { return lbvh_step(b, st, overlap, visit, err); },
+      [&]() {
+        if (node == -1) return false;
+        if (dstate == node) dstate = kOn;  // the walk left the subtree the query skipped
+        if (cstate == node) cstate = kOn;
+        if (++guard > 2 * b.n + 2) {
+          raise_error(err, kErrTraversal);
+          node = -1;
+          return false;
+        }
+        const bool don = dstate == kOn, con = cstate == kOn;
+        const float4 l = b.lo[node], h = b.hi[node];
+        const bool od = don && overlap_point(l, h, pred);
+        const bool oc = con && overlap_segment(l, h, p1, pred);
+        const int esc = __float_as_int(h.w);
+        if ((uint32_t)node >= b.n - 1) {
+          const uint32_t f = (uint32_t)__float_as_int(l.w);
+          if (od) {
+            visit_dcd(f);
+            if (++dfound >= kMaxCandidates) dstate = kDone;
+          }
+          if (oc) {
+            visit_ccd(f);
+            if (++cfound >= kMaxCandidates) cstate = kDone;
+          }
+          node = esc;
+        } else if (od || oc) {
+          // off for the subtree (an escape of -1: for the rest of the walk)
+          if (don && !od) dstate = esc >= 0 ? esc : kDone;
+          if (con && !oc) cstate = esc >= 0 ? esc : kDone;
+          node = __float_as_int(l.w);
+        } else {
+          node = esc;
+        }
+        if (dstate == kDone && cstate == kDone) node = -1;
+        return node != -1;
+      },
       [&](uint32_t i) {
-        rt_idx[i] = hit_idx;
-        rt_qc[i] = mk4(qc, 0.0f);
+        vf_idx[i] = didx;
+        vf_qs[i] = mk4(dqs, 0.0f);
+        rt_idx[i] = cidx;
+        rt_qc[i] = mk4(cqc, 0.0f);
       });
 }
 
@@ -275,10 +304,9 @@ void launch_generate_contacts(Context& c) {
   const unsigned cap = (unsigned)c.num_sms * 8u;
   cudaMemsetAsync(c.gen_counter.p, 0, sizeof(uint32_t) * 3, c.stream);
   cudaMemsetAsync(c.ee_vflag.p, 0, c.nv, c.stream);  // this pass's contacts set it
-  k_generate_vf_dcd<<<std::min(grid_for(c.nv), cap), kBlock, 0, c.stream>>>(
-      F, I, c.x.p, c.nv, c.vf_idx.p, c.vf_qs.p, c.err.p, c.gen_counter.p);
-  k_generate_vf_ccd<<<std::min(grid_for(c.nv), cap), kBlock, 0, c.stream>>>(
-      F, I, c.x.p, c.x0.p, c.nv, c.rt_idx.p, c.rt_qc.p, c.err.p, c.gen_counter.p + 1);
+  k_generate_vf<<<std::min(grid_for(c.nv), cap), kBlock, 0, c.stream>>>(
+      F, I, c.x.p, c.x0.p, c.nv, c.vf_idx.p, c.vf_qs.p, c.rt_idx.p, c.rt_qc.p, c.err.p,
+      c.gen_counter.p);
   k_generate_ee<<<std::min(grid_for(c.ne), cap), kBlock, 0, c.stream>>>(
       F, I, c.x.p, c.edge.p, c.ne, c.otri.p, c.ee_a.p, c.ee_b.p, c.ee_c.p, c.ee_vflag.p, c.err.p,
       c.gen_counter.p + 2);
