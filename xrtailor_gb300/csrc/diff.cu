@@ -311,9 +311,9 @@ __global__ void k_bend_bwd(const uint32_t* __restrict__ order, uint32_t begin, u
 
 // ---- tiled replay and reverse ---------------------------------------------------------------
 // With the tile-local schedule the replay runs the forward's own tile launches (solver.cu
-// k_stretch_tiles / k_bend_tiles with their tape pointers set: the same kernels, hence the same
-// bits), which tape each projection's inputs by execution slot (a local color's slots are
-// contiguous, so the tape writes coalesce).  The reverse of a tile color launch is one block per tile, tile
+// k_stretch_tiles / k_bend_tiles instantiated with TAPE: the forward's code, hence its bits),
+// which tape each projection's inputs by execution slot (a local color's slots are contiguous,
+// so the tape writes coalesce).  The reverse of a tile color launch is one block per tile, tile
 // colors last to first: the block stages the footprint's adjoint in shared memory and walks the
 // tile's local colors backwards, reading the taped inputs.  Tiles of one tile color have
 // disjoint footprints, so the write-back of the adjoint needs no atomics.  Shared memory of the
@@ -769,9 +769,9 @@ void stretch_tiles_bwd(Context& c, float dt, bool reset, size_t ti) {
   for (int k = (int)T.tile_colors.size() - 1; k >= 0; --k) {
     const ColorRange r = T.tile_colors[k];
     if (r.end > r.begin)
-      launch_k(c.pdl, kern, r.end - r.begin, D.s_block, smem, c.stream,
-          c.s_con.p, T.foot.p, T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot, T.max_cons,
-          dt, tx, tl, D.G.p, D.lam_bar.p, D.comp_bar.p);
+      launch_k(c.pdl, kern, r.end - r.begin, D.s_block, smem, c.stream, c.s_con.p, T.foot.p,
+               T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot, T.max_cons, dt, tx, tl,
+               D.G.p, D.lam_bar.p, D.comp_bar.p);
   }
 }
 
@@ -784,9 +784,9 @@ void bend_tiles_bwd(Context& c, float dt, size_t ti) {
   for (int k = (int)T.tile_colors.size() - 1; k >= 0; --k) {
     const ColorRange r = T.tile_colors[k];
     if (r.end > r.begin)
-      launch_k(c.pdl, kern, r.end - r.begin, D.b_block, smem, c.stream,
-          c.b_idx.p, c.b_tc.p, T.foot.p, T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot,
-          T.max_cons, dt, tx, D.G.p, D.bcomp_bar.p);
+      launch_k(c.pdl, kern, r.end - r.begin, D.b_block, smem, c.stream, c.b_idx.p, c.b_tc.p,
+               T.foot.p, T.meta.p, T.lofs.p, r.begin, T.num_local, T.max_foot, T.max_cons, dt,
+               tx, D.G.p, D.bcomp_bar.p);
   }
 }
 
@@ -859,25 +859,17 @@ void record_frame_diff(Context& c) {
           launch_stretch_tiles(c, k, r, it == 0, D.t_sx.p + 2 * ti * E, D.t_sl.p + ti * E);
       else for (const ColorRange& r : D.s_colors) {
         const unsigned g = grid_for(r.end - r.begin);
-        if (it == 0)
-          launch_k(c.pdl, k_stretch_tape<true>, g, blk, 0, c.stream, D.s_order.p, r.begin, r.end, D.s_gidx.p,
-                                                         c.s_con.p, c.s_lambda.p, c.x.p,
-                                                         D.t_sx.p + 2 * ti * E, D.t_sl.p + ti * E,
-                                                         k.dt);
-        else
-          launch_k(c.pdl, k_stretch_tape<false>, g, blk, 0, c.stream, D.s_order.p, r.begin, r.end, D.s_gidx.p,
-                                                          c.s_con.p, c.s_lambda.p, c.x.p,
-                                                          D.t_sx.p + 2 * ti * E,
-                                                          D.t_sl.p + ti * E, k.dt);
+        launch_k(c.pdl, it == 0 ? k_stretch_tape<true> : k_stretch_tape<false>, g, blk, 0,
+                 c.stream, D.s_order.p, r.begin, r.end, D.s_gidx.p, c.s_con.p, c.s_lambda.p,
+                 c.x.p, D.t_sx.p + 2 * ti * E, D.t_sl.p + ti * E, k.dt);
       }
       if (p.solve_bending && D.b_tiled)
         for (const ColorRange& r : c.b_tiles.tile_colors)
           launch_bend_tiles(c, k, r, D.t_bx.p + 4 * ti * B);
       else if (p.solve_bending)
         for (const ColorRange& r : D.b_colors)
-          launch_k(c.pdl, k_bend_tape, grid_for(r.end - r.begin), blk, 0, c.stream,
-              D.b_order.p, r.begin, r.end, D.b_gidx.p, c.b_tc.p, c.x.p, D.t_bx.p + 4 * ti * B,
-              k.dt);
+          launch_k(c.pdl, k_bend_tape, grid_for(r.end - r.begin), blk, 0, c.stream, D.b_order.p,
+                   r.begin, r.end, D.b_gidx.p, c.b_tc.p, c.x.p, D.t_bx.p + 4 * ti * B, k.dt);
       if (lra_fused || has_obstacle) {  // the launches tape their input positions
         launch_stage(c, k, lra_fused, has_obstacle, D.t_stage.p + ti * V);
         swap_x();
@@ -935,17 +927,16 @@ void backward_frame(Context& c) {
         Timed tv(c, kAdjVertex, n_vertex_launches, V);
         if (has_obstacle) {
           const float4* X = D.t_ee.p + ti * V;
-          launch_k(c.pdl, k_ee_bwd, gv, blk, 0, c.stream, X, D.G.p, D.G2.p, V, c.ve_ptr.p, c.ve_list.p,
-                                            c.edge.p, D.t_ee_a.p + pe, D.t_ee_b.p + pe,
-                                            D.t_ee_c.p + pe, D.cnt.p + ti * V, k.relaxation);
+          launch_k(c.pdl, k_ee_bwd, gv, blk, 0, c.stream, X, D.G.p, D.G2.p, V, c.ve_ptr.p,
+                   c.ve_list.p, c.edge.p, D.t_ee_a.p + pe, D.t_ee_b.p + pe, D.t_ee_c.p + pe,
+                   D.cnt.p + ti * V, k.relaxation);
           std::swap(D.G.p, D.G2.p);
         }
         if (lra_fused || has_obstacle) {
-          launch_k(c.pdl, k_stage_bwd, gv, blk, 0, c.stream,
-              D.t_stage.p + ti * V, D.G.p, D.G2.p, D.Gs.p, V, lra_fused, c.lra_ptr.p,
-              c.lra_src.p, c.lra_rest.p, k.lra_stretch, has_obstacle, D.t_rt_idx.p + pv,
-              D.t_rt_qc.p + pv, D.t_vf_idx.p + pv, D.t_vf_qs.p + pv,
-              D.t_pred.p + (size_t)pass * 3 * c.onf, c.err.p);
+          launch_k(c.pdl, k_stage_bwd, gv, blk, 0, c.stream, D.t_stage.p + ti * V, D.G.p, D.G2.p,
+                   D.Gs.p, V, lra_fused, c.lra_ptr.p, c.lra_src.p, c.lra_rest.p, k.lra_stretch,
+                   has_obstacle, D.t_rt_idx.p + pv, D.t_rt_qc.p + pv, D.t_vf_idx.p + pv,
+                   D.t_vf_qs.p + pv, D.t_pred.p + (size_t)pass * 3 * c.onf, c.err.p);
           if (lra_fused) launch_k(c.pdl, k_add_sources, gv, blk, 0, c.stream, D.G2.p, D.Gs.p, V);
           std::swap(D.G.p, D.G2.p);
         }
@@ -956,9 +947,9 @@ void backward_frame(Context& c) {
         else
           for (int ci = (int)D.b_colors.size() - 1; ci >= 0; --ci) {
             const ColorRange r = D.b_colors[ci];
-            launch_k(c.pdl, k_bend_bwd, grid_for(r.end - r.begin), blk, 0, c.stream,
-                D.b_order.p, r.begin, r.end, D.b_gidx.p, c.b_tc.p, D.t_bx.p + 4 * ti * B, D.G.p,
-                D.bcomp_bar.p, k.dt);
+            launch_k(c.pdl, k_bend_bwd, grid_for(r.end - r.begin), blk, 0, c.stream, D.b_order.p,
+                     r.begin, r.end, D.b_gidx.p, c.b_tc.p, D.t_bx.p + 4 * ti * B, D.G.p,
+                     D.bcomp_bar.p, k.dt);
           }
       }
       Timed ts(c, kAdjStretch, n_stretch_launches, E);
@@ -966,16 +957,10 @@ void backward_frame(Context& c) {
       else for (int ci = (int)D.s_colors.size() - 1; ci >= 0; --ci) {
         const ColorRange r = D.s_colors[ci];
         const unsigned g = grid_for(r.end - r.begin);
-        if (it == 0)
-          launch_k(c.pdl, k_stretch_bwd<true>, g, blk, 0, c.stream, D.s_order.p, r.begin, r.end, D.s_gidx.p,
-                                                        c.s_con.p, D.t_sx.p + 2 * ti * E,
-                                                        D.t_sl.p + ti * E, D.G.p, D.lam_bar.p,
-                                                        D.comp_bar.p, k.dt);
-        else
-          launch_k(c.pdl, k_stretch_bwd<false>, g, blk, 0, c.stream, D.s_order.p, r.begin, r.end, D.s_gidx.p,
-                                                         c.s_con.p, D.t_sx.p + 2 * ti * E,
-                                                         D.t_sl.p + ti * E, D.G.p, D.lam_bar.p,
-                                                         D.comp_bar.p, k.dt);
+        launch_k(c.pdl, it == 0 ? k_stretch_bwd<true> : k_stretch_bwd<false>, g, blk, 0,
+                 c.stream, D.s_order.p, r.begin, r.end, D.s_gidx.p, c.s_con.p,
+                 D.t_sx.p + 2 * ti * E, D.t_sl.p + ti * E, D.G.p, D.lam_bar.p, D.comp_bar.p,
+                 k.dt);
       }
     }
     Timed t(c, kAdjVertex, 1, V);
