@@ -158,7 +158,9 @@ const char* xrt_last_error(const xrt_ctx* ctx);
 
 /* ---- setup ---------------------------------------------------------------------------- */
 /* Global::sim_params / sim_config (core/Global.hpp:22-25) -> SetSimulationParams
- * (ClothSolverHelper.cu:16-23).  May be called again between frames. */
+ * (ClothSolverHelper.cu:16-23).  May be called again between frames.  After xrt_start, a new
+ * substep time (frame_time / num_substeps) also re-evaluates the compliance terms held in the
+ * constraint records (a synchronous upload, as xrt_set_compliance). */
 xrt_status xrt_set_params(xrt_ctx* ctx, const xrt_swift_params* params);
 /* ClothSolverUniversal::AddCloth.  out_vertex_offset receives prev_num_particles. */
 xrt_status xrt_add_cloth(xrt_ctx* ctx, const xrt_cloth_desc* desc, int32_t* out_vertex_offset);
